@@ -1,0 +1,100 @@
+/* stokes_gpu.h -- additive GPU API of libstokes_gb300.
+ *
+ * These entry points have no counterpart in libstokes; they sit beside the
+ * drop-in functions of stokes_abi.h.  Every one returns an int status
+ * (STOKES_GPU_OK = 0) instead of exiting, takes plain pointers and sizes,
+ * and runs on the calling thread's current CUDA device.
+ *
+ * Device pointers ("d_" prefix) must point to memory of that device.
+ * A "stream" argument is a cudaStream_t passed as void*; NULL selects the
+ * library's own stream for that system.
+ */
+#ifndef LIBSTOKES_GB300_STOKES_GPU_H
+#define LIBSTOKES_GB300_STOKES_GPU_H
+
+#include "stokes_abi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  STOKES_GPU_OK = 0,
+  STOKES_GPU_EINVAL = 1,      /* bad argument (n, version, NULL pointer, ...) */
+  STOKES_GPU_ENOTPERIODIC = 2,/* open systems are not served by this library */
+  STOKES_GPU_ECUDA = 3,       /* a CUDA runtime call failed */
+  STOKES_GPU_ENOMEM = 4,      /* device allocation failed */
+  STOKES_GPU_ETIMEOUT = 5,    /* a bounded device wait ran out */
+  STOKES_GPU_EACCURACY = 6,   /* Chebyshev error above the requested bound */
+  STOKES_GPU_ETOOBIG = 7      /* size above a fixed capacity */
+};
+
+/* precision modes of the mobility product */
+enum {
+  STOKES_GPU_FP64 = 0,        /* IEEE FP64, the reference's image and k sets */
+  STOKES_GPU_MIXED = 1        /* FP32 real space + split-BF16 tensor-core
+                                 reciprocal space on a re-tuned Ewald split;
+                                 relative L2 error <= 1e-6 vs FP64 */
+};
+
+/* status of the last failing call on this thread and its message */
+int stokes_gpu_last_error (void);
+const char *stokes_gpu_last_error_message (void);
+/* 0 (default): a failing drop-in (void) function prints its reason and
+ * exits with status 1, like libstokes on allocation failure.
+ * 1: it records the error, fills its outputs with NaN and returns. */
+void stokes_gpu_set_error_mode (int mode);
+
+/* precision of the products of this system (default: STOKES_GPU_FP64, or
+ * the value of the LIBSTOKES_GB300_PRECISION environment variable,
+ * "fp64" or "mixed", at the first product of a system) */
+int stokes_gpu_set_precision (struct stokes *sys, int mode);
+int stokes_gpu_get_precision (const struct stokes *sys, int *mode);
+
+/* free the device state kept for sys (stokes_free does this too) */
+int stokes_gpu_release (struct stokes *sys);
+
+/* y = M x with host buffers; the status-returning form of
+ * atimes_ewald_3all */
+int stokes_gpu_atimes (struct stokes *sys, const double *x, double *y);
+
+/* y = M x with device buffers.  d_pos: positions [np*3] on the device, or
+ * NULL to upload sys->pos.  Asynchronous on `stream`. */
+int stokes_gpu_atimes_dev (struct stokes *sys, const double *d_pos,
+                           const double *d_x, double *d_y, void *stream);
+
+/* dense mobility matrix with host / device output */
+int stokes_gpu_matrix (struct stokes *sys, double *mat);
+int stokes_gpu_matrix_dev (struct stokes *sys, const double *d_pos,
+                           double *d_mat, void *stream);
+
+/* y = mat . x (extracted form for FTS) on device buffers */
+int stokes_gpu_matvec_dev (int version, int np, const double *d_mat,
+                           const double *d_x, double *d_y, void *stream);
+
+/* device milliseconds of the last product: total, real, reciprocal */
+int stokes_gpu_last_times (const struct stokes *sys, double *ms3);
+
+/* Profiling window for the device entry points: between begin and end, each
+ * product of sys (up to max_products) records CUDA events on its stream at
+ * its phase boundaries.  end waits for them and returns the summed device
+ * milliseconds (total, real space, reciprocal space) and the product count. */
+int stokes_gpu_profile_begin (struct stokes *sys, int max_products);
+int stokes_gpu_profile_end (struct stokes *sys, double *sum_ms3, int *count);
+
+/* number of kernel launches issued by the last product of sys */
+int stokes_gpu_last_launches (const struct stokes *sys, int *count);
+
+/* number of real-space (i, j, image) terms with 0 < r^2 <= rmax2 -- the
+ * unit count of the real-space roofline */
+int stokes_gpu_count_real_terms (struct stokes *sys, long long *count);
+
+/* measured FMA throughput of the current GPU in GFLOP/s (2 flops per FMA),
+ * fp64 = 1 for FP64, 0 for FP32 */
+int stokes_gpu_peak_fma (int fp64, double *gflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIBSTOKES_GB300_STOKES_GPU_H */

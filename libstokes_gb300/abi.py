@@ -1,0 +1,351 @@
+"""ctypes mirror of the libstokes_gb300 C ABI (include/stokes_abi.h,
+include/stokes_gpu.h).
+
+``StokesStruct`` is the Python image of ``struct stokes`` (src/stokes.h:27-154
+of libstokes); ``System`` wraps one struct the way a libstokes caller would:
+``stokes_init`` / ``stokes_set_np`` / ``stokes_set_l`` / ``stokes_set_xi`` and
+direct member writes, then ``atimes_ewald_3all`` / ``make_matrix_mob_ewald_3all``.
+
+There is no fallback: if libstokes_gb300.so is missing or fails to load, an
+ImportError is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib",
+                        "libstokes_gb300.so")
+
+STOKES_GPU_OK = 0
+STOKES_GPU_EINVAL = 1
+STOKES_GPU_ENOTPERIODIC = 2
+STOKES_GPU_ECUDA = 3
+STOKES_GPU_ENOMEM = 4
+STOKES_GPU_ETIMEOUT = 5
+STOKES_GPU_EACCURACY = 6
+STOKES_GPU_ETOOBIG = 7
+FP64 = 0
+MIXED = 1
+
+
+class StokesStruct(C.Structure):
+    """Byte-for-byte image of libstokes' struct stokes."""
+    _fields_ = [
+        ("version", C.c_int),
+        ("np", C.c_int),
+        ("nm", C.c_int),
+        ("pos", _dp),
+        ("a", _dp),
+        ("rmin", C.c_double),
+        ("twobody_nmax", C.c_int),
+        ("twobody_lub", C.c_int),
+        ("poly_table", _ip),
+        ("twobody_f_list", C.c_void_p),
+        ("slip", _dp),
+        ("slip_a", _dp),
+        ("slip_G32", _dp),
+        ("slip_G30", _dp),
+        ("slip_G52", _dp),
+        ("slip_table", _ip),
+        ("twobody_slip_f_list", C.c_void_p),
+        ("Ui", C.c_double * 3),
+        ("Oi", C.c_double * 3),
+        ("Ei", C.c_double * 5),
+        ("shear_mode", C.c_int),
+        ("shear_rate", C.c_double),
+        ("shear_shift", C.c_double),
+        ("periodic", C.c_int),
+        ("ewald_eps", C.c_double),
+        ("rmax2", C.c_double),
+        ("rmaxx", C.c_int), ("rmaxy", C.c_int), ("rmaxz", C.c_int),
+        ("kmax", C.c_double),
+        ("kmaxx", C.c_int), ("kmaxy", C.c_int), ("kmaxz", C.c_int),
+        ("xi", C.c_double), ("xi2", C.c_double), ("xiaspi", C.c_double),
+        ("xia2", C.c_double),
+        ("pivol", C.c_double),
+        ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
+        ("ilx", C.c_int * 27), ("ily", C.c_int * 27), ("ilz", C.c_int * 27),
+        ("self_a", C.c_double), ("self_c", C.c_double), ("self_m", C.c_double),
+        ("flag_table", C.c_int),
+        ("nr", C.c_int),
+        ("rlx", _dp), ("rly", _dp), ("rlz", _dp),
+        ("rmx", _ip), ("rmy", _ip), ("rmz", _ip),
+        ("nk", C.c_int),
+        ("ex", _dp), ("ey", _dp), ("ez", _dp),
+        ("k", _dp), ("k1", _dp), ("k2", _dp), ("k3", _dp),
+        ("ya", _dp), ("yb", _dp), ("yc", _dp), ("yg", _dp), ("yh", _dp),
+        ("ym", _dp),
+        ("lubmin2", C.c_double),
+        ("lubmax", C.c_double),
+        ("cpu1", C.c_double), ("cpu2", C.c_double), ("cpu3", C.c_double),
+        ("it", C.c_void_p),
+    ]
+
+
+_SP = C.POINTER(StokesStruct)
+ATIMES = C.CFUNCTYPE(None, C.c_int, _dp, _dp, C.c_void_p)
+FUNC1 = C.CFUNCTYPE(C.c_double, C.c_double)
+
+_SIGS = {
+    # set-up
+    "stokes_init": (_SP, []),
+    "stokes_free": (None, [_SP]),
+    "stokes_set_np": (None, [_SP, C.c_int, C.c_int]),
+    "stokes_set_Ui": (None, [_SP, C.c_double, C.c_double, C.c_double]),
+    "stokes_set_Oi": (None, [_SP, C.c_double, C.c_double, C.c_double]),
+    "stokes_set_Ei": (None, [_SP] + [C.c_double] * 5),
+    "stokes_set_shear": (None, [_SP, C.c_int, C.c_double]),
+    "stokes_get_shear_shift": (C.c_double, [_SP, C.c_double, C.c_double, C.c_double]),
+    "stokes_set_shear_shift": (None, [_SP, C.c_double, C.c_double, C.c_double]),
+    "stokes_set_l": (None, [_SP, C.c_double, C.c_double, C.c_double]),
+    "stokes_set_xi": (None, [_SP, C.c_double, C.c_double]),
+    "xi_by_tratio": (C.c_double, [_SP, C.c_double]),
+    "stokes_set_pos": (None, [_SP, _dp]),
+    "stokes_set_pos_mobile": (None, [_SP, _dp]),
+    "stokes_set_pos_fixed": (None, [_SP, _dp]),
+    "stokes_set_radius": (None, [_SP, _dp]),
+    "stokes_unset_radius": (None, [_SP]),
+    "stokes_set_slip": (None, [_SP, _dp]),
+    "stokes_unset_slip": (None, [_SP]),
+    # operators
+    "atimes_ewald_3all": (None, [C.c_int, _dp, _dp, C.c_void_p]),
+    "atimes_ewald_3all_notbl": (None, [C.c_int, _dp, _dp, C.c_void_p]),
+    "atimes_3all": (None, [C.c_int, _dp, _dp, C.c_void_p]),
+    "make_matrix_mob_ewald_3all": (None, [_SP, _dp]),
+    "make_matrix_mob_ewald_3all_notbl": (None, [_SP, _dp]),
+    "make_matrix_mob_3all": (None, [_SP, _dp]),
+    "atimes_3all_matrix": (None, [C.c_int, _dp, _dp, C.c_void_p]),
+    "atimes_ewald_3all_matrix_notbl": (None, [C.c_int, _dp, _dp, C.c_void_p]),
+    "dot_prod_matrix": (None, [_dp, C.c_int, C.c_int, _dp, _dp]),
+    "multiply_extmat_with_extvec_3fts": (None, [C.c_int, _dp, _dp, _dp]),
+    # Chebyshev
+    "chebyshev_coef": (None, [C.c_int, FUNC1, C.c_double, C.c_double, _dp]),
+    "chebyshev_eval": (C.c_double, [C.c_int, _dp, C.c_double, C.c_double, C.c_double]),
+    "chebyshev_eval_": (C.c_double, [C.c_int, _dp, C.c_double, C.c_double, C.c_double]),
+    "chebyshev_eval_atimes": (None, [C.c_int, _dp, C.c_int, _dp, _dp, C.c_double,
+                                     C.c_double, C.c_void_p, C.c_void_p]),
+    "chebyshev_error_minvsqrt": (C.c_double, [C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]),
+    "chebyshev_error_Rsqrt": (C.c_double, [C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]),
+    # additive GPU API
+    "stokes_gpu_last_error": (C.c_int, []),
+    "stokes_gpu_last_error_message": (C.c_char_p, []),
+    "stokes_gpu_set_error_mode": (None, [C.c_int]),
+    "stokes_gpu_set_precision": (C.c_int, [_SP, C.c_int]),
+    "stokes_gpu_get_precision": (C.c_int, [_SP, _ip]),
+    "stokes_gpu_release": (C.c_int, [_SP]),
+    "stokes_gpu_atimes": (C.c_int, [_SP, _dp, _dp]),
+    "stokes_gpu_atimes_dev": (C.c_int, [_SP, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "stokes_gpu_matrix": (C.c_int, [_SP, _dp]),
+    "stokes_gpu_matrix_dev": (C.c_int, [_SP, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "stokes_gpu_matvec_dev": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]),
+    "stokes_gpu_last_times": (C.c_int, [_SP, _dp]),
+    "stokes_gpu_last_launches": (C.c_int, [_SP, _ip]),
+    "stokes_gpu_profile_begin": (C.c_int, [_SP, C.c_int]),
+    "stokes_gpu_profile_end": (C.c_int, [_SP, _dp, _ip]),
+    "stokes_gpu_count_real_terms": (C.c_int, [_SP, C.POINTER(C.c_longlong)]),
+    "stokes_gpu_peak_fma": (C.c_int, [C.c_int, _dp]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libstokes_gb300.so (raises ImportError when it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"libstokes_gb300: {path} is missing; run "
+                          "`python -m libstokes_gb300.build` first")
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name, None)
+        if f is None:
+            continue
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def declared_symbols():
+    """Names of every function the public headers declare."""
+    return sorted(_SIGS)
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def ncomp(version: int) -> int:
+    return (3, 6, 11)[version]
+
+
+class GPUError(RuntimeError):
+    pass
+
+
+def raise_if_failed():
+    """After a drop-in (void) call in error mode 1: raise with the reason."""
+    lib = load()
+    rc = lib.stokes_gpu_last_error()
+    if rc != STOKES_GPU_OK:
+        raise GPUError(f"libstokes_gb300 status {rc}: "
+                       f"{lib.stokes_gpu_last_error_message().decode()}")
+
+
+def check(rc: int):
+    if rc != STOKES_GPU_OK:
+        lib = load()
+        raise GPUError(f"libstokes_gb300 status {rc}: "
+                       f"{lib.stokes_gpu_last_error_message().decode()}")
+
+
+class System:
+    """One struct stokes built through the library's own set-up calls."""
+
+    def __init__(self, version: int, pos, box, xi=None, eps=1e-12, tratio=1.0):
+        self.lib = load()
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        self.version = int(version)
+        self.np = pos.shape[0]
+        self.sp = self.lib.stokes_init()
+        s = self.sp.contents
+        s.version = self.version
+        self.lib.stokes_set_np(self.sp, self.np, self.np)
+        self.lib.stokes_set_pos(self.sp, _d(pos))
+        s.periodic = 1
+        self.lib.stokes_set_l(self.sp, *[float(b) for b in box])
+        if xi is None:
+            xi = self.lib.xi_by_tratio(self.sp, float(tratio))
+        self.lib.stokes_set_xi(self.sp, float(xi), float(eps))
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "sp", None):
+            # hand the library back the tables it allocated before it frees them
+            self.restore_table()
+            self.lib.stokes_free(self.sp)
+            self.sp = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def s(self) -> StokesStruct:
+        return self.sp.contents
+
+    @property
+    def n(self) -> int:
+        return ncomp(self.version) * self.np
+
+    def set_pos(self, pos):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        self.lib.stokes_set_pos(self.sp, _d(pos))
+
+    def set_radius(self, a):
+        if a is None:
+            self.lib.stokes_unset_radius(self.sp)
+        else:
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            self.lib.stokes_set_radius(self.sp, _d(a))
+
+    def set_slip(self, g):
+        if g is None:
+            self.lib.stokes_unset_slip(self.sp)
+        else:
+            g = np.ascontiguousarray(g, dtype=np.float64)
+            self.lib.stokes_set_slip(self.sp, _d(g))
+
+    def set_misc(self, rmin=0.0, shear_mode=0, shear_shift=0.0):
+        s = self.s
+        s.rmin = float(rmin)
+        s.shear_mode = int(shear_mode)
+        s.shear_shift = float(shear_shift)
+
+    def set_cube(self, nr_shell: int, nk_shell: int):
+        """Full image cube |m| <= nr_shell (every image taken) and full k cube
+        |m| <= nk_shell (kmax = 0): the 5-shell configuration of the N=64
+        workload.  Arrays stay owned by this object."""
+        s = self.s
+        side = 2 * nr_shell + 1
+        m = np.arange(-nr_shell, nr_shell + 1)
+        m1, m2, m3 = [a.ravel() for a in np.meshgrid(m, m, m, indexing="ij")]
+        rl = [np.ascontiguousarray(m1 * s.lx, dtype=np.float64),
+              np.ascontiguousarray(m2 * s.ly, dtype=np.float64),
+              np.ascontiguousarray(m3 * s.lz, dtype=np.float64)]
+        rm = [np.ascontiguousarray(a, dtype=np.int32) for a in (m1, m2, m3)]
+        self._keep = rl + rm
+        # the library owns (and will free) the arrays it allocated: swap them
+        # out and restore them before freeing
+        # (addresses as integers: a pointer read from a ctypes Structure
+        # aliases the member and would follow the reassignment below)
+        self._orig = (s.nr,) + tuple(C.cast(p, C.c_void_p).value
+                                     for p in (s.rlx, s.rly, s.rlz, s.rmx, s.rmy, s.rmz))
+        s.nr = side ** 3
+        s.rlx, s.rly, s.rlz = [_d(a) for a in rl]
+        s.rmx, s.rmy, s.rmz = [a.ctypes.data_as(_ip) for a in rm]
+        s.rmax2 = math.inf
+        s.kmaxx = s.kmaxy = s.kmaxz = int(nk_shell)
+        s.kmax = 0.0
+
+    def restore_table(self):
+        if getattr(self, "_orig", None):
+            s = self.s
+            nr, ax, ay, az, mx, my, mz = self._orig
+            s.nr = nr
+            s.rlx, s.rly, s.rlz = [C.cast(v, _dp) for v in (ax, ay, az)]
+            s.rmx, s.rmy, s.rmz = [C.cast(v, _ip) for v in (mx, my, mz)]
+            self._orig = None
+
+    def set_precision(self, mode: int):
+        check(self.lib.stokes_gpu_set_precision(self.sp, int(mode)))
+
+    def atimes(self, x, notbl=False):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.n)
+        f = self.lib.atimes_ewald_3all_notbl if notbl else self.lib.atimes_ewald_3all
+        f(self.n, _d(x), _d(y), C.cast(self.sp, C.c_void_p))
+        raise_if_failed()
+        return y
+
+    def atimes_checked(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.n)
+        check(self.lib.stokes_gpu_atimes(self.sp, _d(x), _d(y)))
+        return y
+
+    def matrix(self, notbl=False):
+        m = np.empty((self.n, self.n))
+        f = (self.lib.make_matrix_mob_ewald_3all_notbl if notbl
+             else self.lib.make_matrix_mob_ewald_3all)
+        f(self.sp, _d(m))
+        raise_if_failed()
+        return m
+
+    def atimes_matrix(self, x, notbl=False):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.n)
+        f = (self.lib.atimes_ewald_3all_matrix_notbl if notbl
+             else self.lib.atimes_3all_matrix)
+        f(self.n, _d(x), _d(y), C.cast(self.sp, C.c_void_p))
+        raise_if_failed()
+        return y
+
+    def times(self):
+        out = np.zeros(3)
+        check(self.lib.stokes_gpu_last_times(self.sp, _d(out)))
+        return out
+
+    def close_table_override(self):
+        self.restore_table()

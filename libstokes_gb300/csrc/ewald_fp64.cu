@@ -1,0 +1,834 @@
+// ewald_fp64.cu -- FP64 kernels of the Ewald mobility (the plain FP64 path).
+//
+//  k_real      real-space pair sum  (src/ewald.c:649-789)
+//  k_phase     e^{i k.r_j} table    (reciprocal space, both operators)
+//  k_sfac      structure factors C(k) = sum_j cos(k.r_j) x_j, S(k) likewise
+//  k_backproj  y_i += sum_k cos(k.r_i) P(k) + sin(k.r_i) Q(k)
+//              (src/ewald.c:923-1075 refactored through the structure factors)
+//  k_combine   self term + partial real-space sums + reciprocal part
+//  k_matrix    dense builder via pair moments (src/ewald.c:1092-1677)
+//  k_gemv      dense y = M z(x) (src/matrix.c:365-399, :447-478)
+//
+// The arithmetic is IEEE FP64 throughout; only the summation order differs
+// from the reference (pairs in parallel, reciprocal space factorised).
+#include "ewald_device.cuh"
+#include "engine.h"
+
+namespace lsg {
+
+// ---------------------------------------------------------------------------
+// real space
+// ---------------------------------------------------------------------------
+constexpr int RS_WARPS = 4;            // warps per CTA
+constexpr int RS_QCAP = 64;            // per-warp queue of accepted terms
+constexpr int RS_IMG_SMEM = 2048;      // images staged in shared memory
+
+template <int V, int MODE>
+__device__ __forceinline__ void
+real_term (const RealArgs &a, int i, int j, double dx, double dy, double dz,
+           double ai, GenU<V, double> &acc)
+{
+  const double rr = dx * dx + dy * dy + dz * dz;
+  double r = sqrt (rr);
+  double aj = 1.0;
+  if (MODE != MODE_MONO) aj = a.rad[j];
+  const double rm = (ai + aj) * a.rmin;
+  if (r < rm) r = rm;
+  const double ri = 1.0 / r;
+  const double e[3] = {dx * ri, dy * ri, dz * ri};
+  PairScalars<double> s;
+  if (MODE == MODE_MONO)
+    real_scalars_mono<V, double> (a.xi, a.xisp, r, s);
+  else if (MODE == MODE_POLY)
+    real_scalars_poly<V, double> (a.xi, a.xisp, r, ai, aj, ai, s);
+  else
+    real_scalars_poly<V, double> (a.xi, a.xisp, r, a.slipa[i], a.slipa[j], ai, s);
+  GenF<V, double> g;
+  load_genf<V, double> (a.x + NComp<V>::value * j, g);
+  pair_apply<V, double> (e, s, g, acc);
+}
+
+// One warp per (target i, source chunk).  Lanes test 32 images at a time;
+// accepted (j, image) terms are compacted into a per-warp queue so that every
+// evaluation of the (expensive) pair term runs with all 32 lanes busy.
+template <int V, int MODE>
+__global__ void __launch_bounds__ (RS_WARPS * 32)
+k_real (RealArgs a)
+{
+  constexpr int C = NComp<V>::value;
+  extern __shared__ Img4 s_img[];
+  __shared__ double s_qd[RS_WARPS][RS_QCAP][3];
+  __shared__ int s_qj[RS_WARPS][RS_QCAP];
+
+  const int nimg_s = a.nimg < RS_IMG_SMEM ? a.nimg : 0;
+  for (int t = threadIdx.x; t < nimg_s; t += blockDim.x) s_img[t] = a.img[t];
+  __syncthreads ();
+  const Img4 *img = nimg_s ? s_img : a.img;
+
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const long long w = (long long) blockIdx.x * RS_WARPS + wib;
+  if (w >= (long long) a.np * a.nchunk) return;
+  const int i = (int) (w % a.np);
+  const int chunk = (int) (w / a.np);
+  const int j0 = (int) ((long long) a.np * chunk / a.nchunk);
+  const int j1 = (int) ((long long) a.np * (chunk + 1) / a.nchunk);
+
+  const double pix = a.pos[3 * i], piy = a.pos[3 * i + 1], piz = a.pos[3 * i + 2];
+  const double ai = (MODE == MODE_MONO) ? 1.0 : a.rad[i];
+  GenU<V, double> acc;
+  acc.zero ();
+  int qn = 0;
+  const unsigned lt = (1u << lane) - 1u;
+
+  for (int j = j0; j < j1; j++)
+    {
+      const double djx = a.pos[3 * j] - pix;
+      const double djy = a.pos[3 * j + 1] - piy;
+      const double djz = a.pos[3 * j + 2] - piz;
+      for (int m0 = 0; m0 < a.nimg; m0 += 32)
+        {
+          const int m = m0 + lane;
+          bool ok = false;
+          double dx = 0.0, dy = 0.0, dz = 0.0;
+          if (m < a.nimg)
+            {
+              const Img4 L = img[m];
+              dx = djx + L.x;
+              dy = djy + L.y;
+              dz = djz + L.z;
+              const double rr = dx * dx + dy * dy + dz * dz;
+              ok = (rr != 0.0) && (rr <= a.rmax2);
+            }
+          const unsigned b = __ballot_sync (0xffffffffu, ok);
+          if (ok)
+            {
+              const int slot = qn + __popc (b & lt);
+              s_qd[wib][slot][0] = dx;
+              s_qd[wib][slot][1] = dy;
+              s_qd[wib][slot][2] = dz;
+              s_qj[wib][slot] = j;
+            }
+          qn += __popc (b);
+          __syncwarp ();
+          if (qn >= 32)
+            {
+              const int slot = qn - 32 + lane;
+              real_term<V, MODE> (a, i, s_qj[wib][slot], s_qd[wib][slot][0],
+                                  s_qd[wib][slot][1], s_qd[wib][slot][2], ai, acc);
+              qn -= 32;
+              __syncwarp ();
+            }
+        }
+    }
+  if (lane < qn)
+    real_term<V, MODE> (a, i, s_qj[wib][lane], s_qd[wib][lane][0],
+                        s_qd[wib][lane][1], s_qd[wib][lane][2], ai, acc);
+
+  double *out = a.partial + ((size_t) chunk * a.np + i) * C;
+#pragma unroll
+  for (int q = 0; q < C; q++)
+    {
+      const double v = warp_sum (acc.v[q]);
+      if (lane == 0) out[q] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// reciprocal space
+// ---------------------------------------------------------------------------
+// ph[k * np + j] = (cos(k.r_j), sin(k.r_j))
+__global__ void
+k_phase (const double *pos, const double *kt, int nk, int np, double2 *ph)
+{
+  const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long) nk * np) return;
+  const int k = (int) (t / np), j = (int) (t % np);
+  const double *K = kt + KT_STRIDE * k;
+  const double th = K[KT_KX] * pos[3 * j] + K[KT_KY] * pos[3 * j + 1] + K[KT_KZ] * pos[3 * j + 2];
+  double sn, cs;
+  sincos (th, &sn, &cs);
+  ph[t] = make_double2 (cs, sn);
+}
+
+// One block per k: C(k), S(k) (and the q_j-weighted pair Cq, Sq for
+// unequal radii / slip), then, for equal spheres, the per-k operators
+// P(k) = Bc C - Bs S and Q(k) = Bc S + Bs C.
+template <int V, int MODE>
+__global__ void __launch_bounds__ (256)
+k_sfac (const double *x, const double2 *ph, const double *kt, const double *qb,
+        int np, double *sf)
+{
+  constexpr int C = NComp<V>::value;
+  constexpr int NW = (MODE == MODE_MONO) ? 2 * C : 4 * C;
+  const int k = blockIdx.x;
+  double acc[NW];
+#pragma unroll
+  for (int q = 0; q < NW; q++) acc[q] = 0.0;
+  for (int j = threadIdx.x; j < np; j += blockDim.x)
+    {
+      const double2 p = ph[(size_t) k * np + j];
+      const double *xj = x + (size_t) C * j;
+#pragma unroll
+      for (int q = 0; q < C; q++)
+        {
+          acc[q] += p.x * xj[q];
+          acc[C + q] += p.y * xj[q];
+        }
+      if (MODE != MODE_MONO)
+        {
+          const double w = qb[j];
+#pragma unroll
+          for (int q = 0; q < C; q++)
+            {
+              acc[2 * C + q] += w * p.x * xj[q];
+              acc[3 * C + q] += w * p.y * xj[q];
+            }
+        }
+    }
+  __shared__ double red[8][NW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NW; q++)
+    {
+      const double v = warp_sum (acc[q]);
+      if (lane == 0) red[wid][q] = v;
+    }
+  __syncthreads ();
+  if (threadIdx.x < NW)
+    {
+      double v = 0.0;
+      for (int w = 0; w < (int) (blockDim.x >> 5); w++) v += red[w][threadIdx.x];
+      red[0][threadIdx.x] = v;
+    }
+  __syncthreads ();
+  double *out = sf + (size_t) SF_STRIDE * k;
+  if (MODE != MODE_MONO)
+    {
+      if (threadIdx.x < NW) out[threadIdx.x] = red[0][threadIdx.x];
+      return;
+    }
+  if (threadIdx.x == 0)
+    {
+      const double *K = kt + KT_STRIDE * k;
+      const double e[3] = {K[KT_EX], K[KT_EY], K[KT_EZ]};
+      GenF<V, double> c, s, ms;
+      load_genf<V, double> (red[0], c);
+      load_genf<V, double> (red[0] + C, s);
+      // -S
+      double neg[C];
+#pragma unroll
+      for (int q = 0; q < C; q++) neg[q] = -red[0][C + q];
+      load_genf<V, double> (neg, ms);
+      GenU<V, double> P, Q;
+      P.zero ();
+      Q.zero ();
+      recip_apply<V, double> (e, K[KT_YA], K[KT_YB], K[KT_YC], K[KT_YG], K[KT_YH], K[KT_YM],
+                              c, ms, P);
+      recip_apply<V, double> (e, K[KT_YA], K[KT_YB], K[KT_YC], K[KT_YG], K[KT_YH], K[KT_YM],
+                              s, c, Q);
+#pragma unroll
+      for (int q = 0; q < C; q++)
+        {
+          out[q] = P.v[q];
+          out[C + q] = Q.v[q];
+        }
+    }
+}
+
+// One warp per target i, lanes over k.
+template <int V, int MODE>
+__global__ void __launch_bounds__ (128)
+k_backproj (const double2 *ph, const double *kt, const double *sf, int nk, int np,
+            const double *arad, const double *qa, double *yrec)
+{
+  constexpr int C = NComp<V>::value;
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 4 + (threadIdx.x >> 5);
+  if (i >= np) return;
+  GenU<V, double> acc;
+  acc.zero ();
+  double aa = 1.0, qai = 1.0;
+  if (MODE != MODE_MONO) { aa = arad[i]; qai = qa[i]; }
+  for (int k = lane; k < nk; k += 32)
+    {
+      const double2 p = ph[(size_t) k * np + i];
+      const double *S = sf + (size_t) SF_STRIDE * k;
+      if (MODE == MODE_MONO)
+        {
+#pragma unroll
+          for (int q = 0; q < C; q++) acc.v[q] += p.x * S[q] + p.y * S[C + q];
+        }
+      else
+        {
+          const double *K = kt + KT_STRIDE * k;
+          const double e[3] = {K[KT_EX], K[KT_EY], K[KT_EZ]};
+          const double kk = K[KT_KK], kn = K[KT_K], kexp = K[KT_KEXP];
+          const double aa2 = aa * aa, aa3 = aa2 * aa;
+          // weights without the source radius, and their q_j coefficients
+          const double ya0 = aa * 6.0 * (1.0 - kk * qai / 6.0) * kexp;
+          const double ya1 = -aa * kk * kexp;
+          const double yb = aa2 * 3.0 * kn * kexp;
+          const double yc = aa3 * 1.5 * kk * kexp;
+          const double yg0 = aa2 * 3.0 * (1.0 - kk * qai / 10.0) * kn * kexp;
+          const double yg1 = -aa2 * 0.5 * kk * kn * kexp;
+          const double yh = aa3 * 1.5 * kk * kexp;
+          const double ym0 = aa3 * 3.0 * (1.0 - kk * qai / 10.0) * kk * kexp;
+          const double ym1 = -aa3 * 0.3 * kk * kk * kexp;
+          // v1 = c_i C + s_i S, v2 = s_i C - c_i S; same with the weighted Cq, Sq
+          double t1[C], t2[C], u1[C], u2[C];
+#pragma unroll
+          for (int q = 0; q < C; q++)
+            {
+              t1[q] = p.x * S[q] + p.y * S[C + q];
+              t2[q] = p.y * S[q] - p.x * S[C + q];
+              u1[q] = p.x * S[2 * C + q] + p.y * S[3 * C + q];
+              u2[q] = p.y * S[2 * C + q] - p.x * S[3 * C + q];
+            }
+          GenF<V, double> g1, g2, h1, h2;
+          load_genf<V, double> (t1, g1);
+          load_genf<V, double> (t2, g2);
+          load_genf<V, double> (u1, h1);
+          load_genf<V, double> (u2, h2);
+          recip_apply<V, double> (e, ya0, yb, yc, yg0, yh, ym0, g1, g2, acc);
+          recip_apply<V, double> (e, ya1, 0.0, 0.0, yg1, 0.0, ym1, h1, h2, acc);
+        }
+    }
+#pragma unroll
+  for (int q = 0; q < C; q++)
+    {
+      const double v = warp_sum (acc.v[q]);
+      if (lane == 0) yrec[(size_t) C * i + q] = v;
+    }
+}
+
+// y_i = self_i . x_i + sum_chunks partial + yrec
+template <int V>
+__global__ void
+k_combine (const double *x, const double *partial, int nchunk, const double *yrec,
+           const double *selfc, int np, double *y)
+{
+  constexpr int C = NComp<V>::value;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  PairScalars<double> s;
+  s.xa = s.ya = selfc[3 * i];
+  s.xc = s.yc = selfc[3 * i + 1];
+  s.xm = s.ym = s.zm = selfc[3 * i + 2];
+  s.yb = s.xg = s.yg = s.yh = 0.0;
+  const double e[3] = {0.0, 0.0, 0.0};
+  GenF<V, double> g;
+  load_genf<V, double> (x + (size_t) C * i, g);
+  GenU<V, double> acc;
+  acc.zero ();
+  pair_apply<V, double> (e, s, g, acc);
+#pragma unroll
+  for (int q = 0; q < C; q++)
+    {
+      double v = acc.v[q];
+      for (int c = 0; c < nchunk; c++) v += partial[((size_t) c * np + i) * C + q];
+      if (yrec) v += yrec[(size_t) C * i + q];
+      y[(size_t) C * i + q] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// dense builder: pair moments
+// ---------------------------------------------------------------------------
+// Sums over terms t (real-space images and reciprocal vectors) of
+// scalar(t) x monomial(e_t).  The c x c block of a pair is linear in these.
+template <int V> struct Moments;
+template <> struct Moments<0> { static constexpr int N = 7; };
+template <> struct Moments<1> { static constexpr int N = 17; };
+template <> struct Moments<2> { static constexpr int N = 68; };
+// layout: A0 | A2[6] | B1[3] | C0 | C2[6] | G1[3] | G2[3] | G3[10] | H2[6] |
+//         M4[15] | M2[6] | M3 | M4b[6] | M5
+enum {
+  MO_A0 = 0, MO_A2 = 1, MO_B1 = 7, MO_C0 = 10, MO_C2 = 11,
+  MO_G1 = 17, MO_G2 = 20, MO_G3 = 23, MO_H2 = 33, MO_M4 = 39, MO_M2 = 54,
+  MO_M3 = 60, MO_M4B = 61, MO_M5 = 67
+};
+
+// symmetric index tables: 2nd order (xx xy xz yy yz zz), 3rd, 4th
+__device__ __forceinline__ int sym2 (int a, int b)
+{
+  if (a > b) { int t = a; a = b; b = t; }
+  return a == 0 ? b : (a == 1 ? 2 + b : 5);
+}
+__device__ __forceinline__ int sym3 (int a, int b, int c)
+{
+  // sort a <= b <= c
+  if (a > b) { int t = a; a = b; b = t; }
+  if (b > c) { int t = b; b = c; c = t; }
+  if (a > b) { int t = a; a = b; b = t; }
+  // xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz
+  const int nx = (a == 0) + (b == 0) + (c == 0);
+  const int ny = (a == 1) + (b == 1) + (c == 1);
+  // enumerate by (nx, ny)
+  if (nx == 3) return 0;
+  if (nx == 2) return ny == 1 ? 1 : 2;
+  if (nx == 1) return ny == 2 ? 3 : (ny == 1 ? 4 : 5);
+  return ny == 3 ? 6 : (ny == 2 ? 7 : (ny == 1 ? 8 : 9));
+}
+__device__ __forceinline__ int sym4 (int a, int b, int c, int d)
+{
+  // xxxx xxxy xxxz xxyy xxyz xxzz xyyy xyyz xyzz xzzz yyyy yyyz yyzz yzzz zzzz
+  const int nx = (a == 0) + (b == 0) + (c == 0) + (d == 0);
+  const int ny = (a == 1) + (b == 1) + (c == 1) + (d == 1);
+  switch (nx)
+    {
+    case 4: return 0;
+    case 3: return ny == 1 ? 1 : 2;
+    case 2: return ny == 2 ? 3 : (ny == 1 ? 4 : 5);
+    case 1: return ny == 3 ? 6 : (ny == 2 ? 7 : (ny == 1 ? 8 : 9));
+    default: return ny == 4 ? 10 : (ny == 3 ? 11 : (ny == 2 ? 12 : (ny == 1 ? 13 : 14)));
+    }
+}
+
+template <int V>
+__device__ __forceinline__ void
+moments_add (const double e[3], const PairScalars<double> &s, double *mo)
+{
+  const double e2[6] = {e[0] * e[0], e[0] * e[1], e[0] * e[2], e[1] * e[1], e[1] * e[2], e[2] * e[2]};
+  const double a2 = s.xa - s.ya;
+  mo[MO_A0] += s.ya;
+#pragma unroll
+  for (int q = 0; q < 6; q++) mo[MO_A2 + q] += a2 * e2[q];
+  if (V == V_F) return;
+  const double c2 = s.xc - s.yc;
+#pragma unroll
+  for (int q = 0; q < 3; q++) mo[MO_B1 + q] += s.yb * e[q];
+  mo[MO_C0] += s.yc;
+#pragma unroll
+  for (int q = 0; q < 6; q++) mo[MO_C2 + q] += c2 * e2[q];
+  if (V == V_FT) return;
+  const double g1 = -s.xg / 3.0, g2 = s.yg, g3 = s.xg - 2.0 * s.yg;
+  const double m1 = 1.5 * s.xm - 2.0 * s.ym + 0.5 * s.zm;
+  const double m2 = -0.5 * s.xm + 0.5 * s.zm;
+  const double m3 = s.xm / 6.0 - 0.5 * s.zm;
+  const double m4 = 0.5 * s.ym - 0.5 * s.zm;
+  const double m5 = 0.5 * s.zm;
+#pragma unroll
+  for (int q = 0; q < 3; q++)
+    {
+      mo[MO_G1 + q] += g1 * e[q];
+      mo[MO_G2 + q] += g2 * e[q];
+    }
+  // e3: xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz
+  const double e3[10] = {e2[0] * e[0], e2[0] * e[1], e2[0] * e[2], e2[1] * e[1], e2[1] * e[2],
+                         e2[2] * e[2], e2[3] * e[1], e2[3] * e[2], e2[4] * e[2], e2[5] * e[2]};
+#pragma unroll
+  for (int q = 0; q < 10; q++) mo[MO_G3 + q] += g3 * e3[q];
+#pragma unroll
+  for (int q = 0; q < 6; q++)
+    {
+      mo[MO_H2 + q] += s.yh * e2[q];
+      mo[MO_M2 + q] += m2 * e2[q];
+      mo[MO_M4B + q] += m4 * e2[q];
+    }
+  // e4: xxxx xxxy xxxz xxyy xxyz xxzz xyyy xyyz xyzz xzzz yyyy yyyz yyzz yzzz zzzz
+  const double e4[15] = {e2[0] * e2[0], e2[0] * e2[1], e2[0] * e2[2], e2[0] * e2[3], e2[0] * e2[4],
+                         e2[0] * e2[5], e2[1] * e2[3], e2[1] * e2[4], e2[1] * e2[5], e2[2] * e2[5],
+                         e2[3] * e2[3], e2[3] * e2[4], e2[3] * e2[5], e2[4] * e2[5], e2[5] * e2[5]};
+#pragma unroll
+  for (int q = 0; q < 15; q++) mo[MO_M4 + q] += m1 * e4[q];
+  mo[MO_M3] += m3;
+  mo[MO_M5] += m5;
+}
+
+__device__ __forceinline__ double
+levi (int a, int b, int c)
+{
+  if (a == b || b == c || a == c) return 0.0;
+  return ((a == 0 && b == 1) || (a == 1 && b == 2) || (a == 2 && b == 0)) ? 1.0 : -1.0;
+}
+
+// stresslet slots (xx, xy, xz, yz, yy) -> tensor indices
+__device__ __forceinline__ void
+slot_ab (int q, int &a, int &b)
+{
+  const int A[5] = {0, 0, 0, 1, 1}, B[5] = {0, 1, 2, 2, 1};
+  a = A[q];
+  b = B[q];
+}
+
+__device__ __forceinline__ double kd (int a, int b) { return a == b ? 1.0 : 0.0; }
+
+// G_(ab)c from moments
+__device__ __forceinline__ double
+g_tensor (const double *mo, int a, int b, int c)
+{
+  return mo[MO_G1 + c] * kd (a, b) + mo[MO_G2 + a] * kd (b, c) + mo[MO_G2 + b] * kd (a, c)
+    + mo[MO_G3 + sym3 (a, b, c)];
+}
+// H_(ab)c = sum_n eps_bcn H2[an] + eps_acn H2[bn]
+__device__ __forceinline__ double
+h_tensor (const double *mo, int a, int b, int c)
+{
+  double v = 0.0;
+  for (int n = 0; n < 3; n++)
+    v += levi (b, c, n) * mo[MO_H2 + sym2 (a, n)] + levi (a, c, n) * mo[MO_H2 + sym2 (b, n)];
+  return v;
+}
+// M_(ab)(cd)
+__device__ __forceinline__ double
+m_tensor (const double *mo, int a, int b, int c, int d)
+{
+  return mo[MO_M4 + sym4 (a, b, c, d)]
+    + mo[MO_M2 + sym2 (c, d)] * kd (a, b) + mo[MO_M2 + sym2 (a, b)] * kd (c, d)
+    + mo[MO_M3] * kd (a, b) * kd (c, d)
+    + mo[MO_M4B + sym2 (a, d)] * kd (b, c) + mo[MO_M4B + sym2 (a, c)] * kd (b, d)
+    + mo[MO_M4B + sym2 (b, d)] * kd (a, c) + mo[MO_M4B + sym2 (b, c)] * kd (a, d)
+    + mo[MO_M5] * (kd (a, c) * kd (b, d) + kd (b, c) * kd (a, d));
+}
+
+// one block entry (extracted form) from the moments; same = (i == j)
+template <int V>
+__device__ __forceinline__ double
+block_entry (const double *mo, int row, int col, bool same)
+{
+  const double sgn = same ? -1.0 : 1.0;   // src/ft.c:61-75, src/fts.c:72-104
+  if (row < 3)
+    {
+      const int a = row;
+      if (col < 3)
+        return mo[MO_A0] * kd (a, col) + mo[MO_A2 + sym2 (a, col)];
+      if (col < 6)
+        {
+          const int b = col - 3;
+          double v = 0.0;
+          for (int n = 0; n < 3; n++) v += levi (a, b, n) * mo[MO_B1 + n];
+          return sgn * v;
+        }
+      int p, q;
+      slot_ab (col - 6, p, q);
+      return -sgn * g_tensor (mo, p, q, a);
+    }
+  if (row < 6)
+    {
+      const int a = row - 3;
+      if (col < 3)
+        {
+          double v = 0.0;
+          for (int n = 0; n < 3; n++) v += levi (a, col, n) * mo[MO_B1 + n];
+          return v;
+        }
+      if (col < 6)
+        return mo[MO_C0] * kd (a, col - 3) + mo[MO_C2 + sym2 (a, col - 3)];
+      int p, q;
+      slot_ab (col - 6, p, q);
+      return h_tensor (mo, p, q, a);
+    }
+  int a, b;
+  slot_ab (row - 6, a, b);
+  if (col < 3) return g_tensor (mo, a, b, col);
+  if (col < 6) return h_tensor (mo, a, b, col - 3);
+  int c, d;
+  slot_ab (col - 6, c, d);
+  return m_tensor (mo, a, b, c, d);
+}
+
+// One warp per pair (i, j): lanes share the image candidates (compacted) and
+// the reciprocal vectors, accumulate moments, reduce, and write the block.
+template <int V, int MODE>
+__global__ void __launch_bounds__ (128)
+k_matrix (MatArgs a)
+{
+  constexpr int C = NComp<V>::value;
+  constexpr int NM = Moments<V>::N;
+  __shared__ double s_qd[4][RS_QCAP][3];
+  __shared__ double s_mo[4][NM];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long w = (long long) blockIdx.x * 4 + wib;
+  if (w >= (long long) a.np * a.np) return;
+  const int i = (int) (w / a.np), j = (int) (w % a.np);
+  const bool same = (i == j);
+
+  double mo[NM];
+#pragma unroll
+  for (int q = 0; q < NM; q++) mo[q] = 0.0;
+
+  const double ai = (MODE == MODE_MONO) ? 1.0 : a.rad[i];
+  const double aj = (MODE == MODE_MONO) ? 1.0 : a.rad[j];
+  if (same && lane == 0)
+    {
+      PairScalars<double> s;
+      s.xa = s.ya = a.selfc[3 * i];
+      s.xc = s.yc = a.selfc[3 * i + 1];
+      s.xm = s.ym = s.zm = a.selfc[3 * i + 2];
+      s.yb = s.xg = s.yg = s.yh = 0.0;
+      const double e0[3] = {0.0, 0.0, 0.0};
+      moments_add<V> (e0, s, mo);
+    }
+
+  const double djx = a.pos[3 * j] - a.pos[3 * i];
+  const double djy = a.pos[3 * j + 1] - a.pos[3 * i + 1];
+  const double djz = a.pos[3 * j + 2] - a.pos[3 * i + 2];
+  const unsigned lt = (1u << lane) - 1u;
+  int qn = 0;
+  auto real_one = [&] (double dx, double dy, double dz) {
+    const double rr = dx * dx + dy * dy + dz * dz;
+    double r = sqrt (rr);
+    const double rm = (ai + aj) * a.rmin;
+    if (r < rm) r = rm;
+    const double ri = 1.0 / r;
+    const double e[3] = {dx * ri, dy * ri, dz * ri};
+    PairScalars<double> s;
+    if (MODE == MODE_MONO)
+      real_scalars_mono<V, double> (a.xi, a.xisp, r, s);
+    else if (MODE == MODE_POLY)
+      real_scalars_poly<V, double> (a.xi, a.xisp, r, ai, aj, ai, s);
+    else
+      real_scalars_poly<V, double> (a.xi, a.xisp, r, a.slipa[i], a.slipa[j], ai, s);
+    moments_add<V> (e, s, mo);
+  };
+  for (int m0 = 0; m0 < a.nimg; m0 += 32)
+    {
+      const int m = m0 + lane;
+      bool ok = false;
+      double dx = 0.0, dy = 0.0, dz = 0.0;
+      if (m < a.nimg)
+        {
+          const Img4 L = a.img[m];
+          dx = djx + L.x;
+          dy = djy + L.y;
+          dz = djz + L.z;
+          const double rr = dx * dx + dy * dy + dz * dz;
+          ok = (rr != 0.0) && (rr <= a.rmax2);
+        }
+      const unsigned b = __ballot_sync (0xffffffffu, ok);
+      if (ok)
+        {
+          const int slot = qn + __popc (b & lt);
+          s_qd[wib][slot][0] = dx;
+          s_qd[wib][slot][1] = dy;
+          s_qd[wib][slot][2] = dz;
+        }
+      qn += __popc (b);
+      __syncwarp ();
+      if (qn >= 32)
+        {
+          const int slot = qn - 32 + lane;
+          real_one (s_qd[wib][slot][0], s_qd[wib][slot][1], s_qd[wib][slot][2]);
+          qn -= 32;
+          __syncwarp ();
+        }
+    }
+  if (lane < qn) real_one (s_qd[wib][lane][0], s_qd[wib][lane][1], s_qd[wib][lane][2]);
+
+  // reciprocal vectors: cos(k.(r_j - r_i)) from the phase table
+  double qai = 1.0, qbj = 1.0;
+  if (MODE != MODE_MONO) { qai = a.qa[i]; qbj = a.qa[j]; }
+  for (int k = lane; k < a.nk; k += 32)
+    {
+      const double *K = a.kt + KT_STRIDE * k;
+      const double2 pi_ = a.ph[(size_t) k * a.np + i];
+      const double2 pj = a.ph[(size_t) k * a.np + j];
+      const double cf = pj.x * pi_.x + pj.y * pi_.y;
+      const double sf = pj.x * pi_.y - pj.y * pi_.x;
+      const double e[3] = {K[KT_EX], K[KT_EY], K[KT_EZ]};
+      double ya = K[KT_YA], yb = K[KT_YB], yc = K[KT_YC], yg = K[KT_YG], yh = K[KT_YH],
+             ym = K[KT_YM];
+      if (MODE != MODE_MONO)
+        {
+          const double kk = K[KT_KK], kn = K[KT_K], kexp = K[KT_KEXP];
+          const double aa = ai, aa2 = aa * aa, aa3 = aa2 * aa;
+          ya = aa * 6.0 * (1.0 - kk * (qai + qbj) / 6.0) * kexp;
+          yb = aa2 * 3.0 * kn * kexp;
+          yc = aa3 * 1.5 * kk * kexp;
+          yg = aa2 * 3.0 * (1.0 - kk * (qai / 10.0 + qbj / 6.0)) * kn * kexp;
+          yh = aa3 * 1.5 * kk * kexp;
+          ym = aa3 * 3.0 * (1.0 - kk * (qai + qbj) / 10.0) * kk * kexp;
+        }
+      PairScalars<double> s;
+      s.xa = 0.0; s.ya = cf * ya;
+      s.yb = sf * yb;
+      s.xc = 0.0; s.yc = cf * yc;
+      s.xg = 0.0; s.yg = sf * yg;
+      s.yh = cf * yh;
+      s.xm = 0.0; s.ym = cf * ym; s.zm = 0.0;
+      moments_add<V> (e, s, mo);
+    }
+
+  // warp reduction, then lanes write the block rows
+#pragma unroll
+  for (int q = 0; q < NM; q++)
+    {
+      const double v = warp_sum (mo[q]);
+      if (lane == 0) s_mo[wib][q] = v;
+    }
+  __syncwarp ();
+  const size_t n = (size_t) C * a.np;
+  double *blk = a.mat + (size_t) C * i * n + (size_t) C * j;
+  for (int t = lane; t < C * C; t += 32)
+    {
+      const int row = t / C, col = t % C;
+      blk[row * n + col] = block_entry<V> (s_mo[wib], row, col, same);
+    }
+}
+
+// dense y = M . z(x), one warp per row (z = extracted-form transform for FTS)
+__global__ void __launch_bounds__ (256)
+k_gemv (const double *mat, const double *z, int n, double *y)
+{
+  const int lane = threadIdx.x & 31;
+  const long long row = (long long) blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (row >= n) return;
+  const double *mr = mat + (size_t) row * n;
+  double acc = 0.0;
+  for (int j = lane; j < n; j += 32) acc += mr[j] * z[j];
+  acc = warp_sum (acc);
+  if (lane == 0) y[row] = acc;
+}
+
+// rectangular y[n1] = M[n1 x n2] . x[n2]
+__global__ void __launch_bounds__ (256)
+k_gemv_rect (const double *mat, const double *x, int n1, int n2, double *y)
+{
+  const int lane = threadIdx.x & 31;
+  const long long row = (long long) blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (row >= n1) return;
+  const double *mr = mat + (size_t) row * n2;
+  double acc = 0.0;
+  for (int j = lane; j < n2; j += 32) acc += mr[j] * x[j];
+  acc = warp_sum (acc);
+  if (lane == 0) y[row] = acc;
+}
+
+__global__ void
+k_ztransform (const double *x, int np, double *z)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= np) return;
+  const double *xj = x + 11 * (size_t) j;
+  double *zj = z + 11 * (size_t) j;
+  for (int q = 0; q < 6; q++) zj[q] = xj[q];
+  zj[6] = 2.0 * xj[6] + xj[10];
+  zj[7] = 2.0 * xj[7];
+  zj[8] = 2.0 * xj[8];
+  zj[9] = 2.0 * xj[9];
+  zj[10] = 2.0 * xj[10] + xj[6];
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <int V, int MODE>
+static cudaError_t
+launch_real_t (const RealArgs &a, cudaStream_t st)
+{
+  const long long nw = (long long) a.np * a.nchunk;
+  const int grid = (int) ((nw + RS_WARPS - 1) / RS_WARPS);
+  const size_t smem = a.nimg < RS_IMG_SMEM ? sizeof (Img4) * a.nimg : 0;
+  // static (queue) + dynamic (images) can pass the 48 KB default: opt in
+  cudaError_t e = cudaFuncSetAttribute (k_real<V, MODE>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int) (smem > 0 ? smem : 1));
+  if (e != cudaSuccess) return e;
+  k_real<V, MODE><<<grid, RS_WARPS * 32, smem, st>>> (a);
+  return cudaGetLastError ();
+}
+
+cudaError_t
+launch_real_fp64 (int version, int mode, const RealArgs &a, cudaStream_t st)
+{
+#define LSG_DISPATCH(V)                                              \
+  if (mode == MODE_MONO) return launch_real_t<V, MODE_MONO> (a, st); \
+  if (mode == MODE_POLY) return launch_real_t<V, MODE_POLY> (a, st); \
+  return launch_real_t<V, MODE_SLIP> (a, st);
+  if (version == 0) { LSG_DISPATCH (0) }
+  if (version == 1) { LSG_DISPATCH (1) }
+  LSG_DISPATCH (2)
+#undef LSG_DISPATCH
+}
+
+cudaError_t
+launch_phase_fp64 (const double *pos, const double *kt, int nk, int np, double2 *ph,
+                   cudaStream_t st)
+{
+  const long long nt = (long long) nk * np;
+  if (nt == 0) return cudaSuccess;
+  k_phase<<<(int) ((nt + 255) / 256), 256, 0, st>>> (pos, kt, nk, np, ph);
+  return cudaGetLastError ();
+}
+
+template <int V, int MODE>
+static cudaError_t
+launch_recip_t (const RecipArgs &a, cudaStream_t st)
+{
+  if (a.nk > 0)
+    {
+      k_sfac<V, MODE><<<a.nk, 256, 0, st>>> (a.x, a.ph, a.kt, a.qa, a.np, a.sf);
+      k_backproj<V, MODE><<<(a.np + 3) / 4, 128, 0, st>>> (a.ph, a.kt, a.sf, a.nk, a.np,
+                                                            a.rad, a.qa, a.yrec);
+    }
+  else
+    cudaMemsetAsync (a.yrec, 0, sizeof (double) * NCOMP (V) * a.np, st);
+  return cudaGetLastError ();
+}
+
+cudaError_t
+launch_recip_fp64 (int version, int mode, const RecipArgs &a, cudaStream_t st)
+{
+#define LSG_DISPATCH(V)                                               \
+  if (mode == MODE_MONO) return launch_recip_t<V, MODE_MONO> (a, st); \
+  if (mode == MODE_POLY) return launch_recip_t<V, MODE_POLY> (a, st); \
+  return launch_recip_t<V, MODE_SLIP> (a, st);
+  if (version == 0) { LSG_DISPATCH (0) }
+  if (version == 1) { LSG_DISPATCH (1) }
+  LSG_DISPATCH (2)
+#undef LSG_DISPATCH
+}
+
+cudaError_t
+launch_combine_fp64 (int version, const double *x, const double *partial, int nchunk,
+                     const double *yrec, const double *selfc, int np, double *y,
+                     cudaStream_t st)
+{
+  const int grid = (np + 127) / 128;
+  if (version == 0) k_combine<0><<<grid, 128, 0, st>>> (x, partial, nchunk, yrec, selfc, np, y);
+  else if (version == 1) k_combine<1><<<grid, 128, 0, st>>> (x, partial, nchunk, yrec, selfc, np, y);
+  else k_combine<2><<<grid, 128, 0, st>>> (x, partial, nchunk, yrec, selfc, np, y);
+  return cudaGetLastError ();
+}
+
+cudaError_t
+launch_matrix_fp64 (int version, int mode, const MatArgs &a, cudaStream_t st)
+{
+  const long long nw = (long long) a.np * a.np;
+  const int grid = (int) ((nw + 3) / 4);
+#define LSG_DISPATCH(V)                                                        \
+  if (mode == MODE_MONO) k_matrix<V, MODE_MONO><<<grid, 128, 0, st>>> (a);      \
+  else if (mode == MODE_POLY) k_matrix<V, MODE_POLY><<<grid, 128, 0, st>>> (a); \
+  else k_matrix<V, MODE_SLIP><<<grid, 128, 0, st>>> (a);
+  if (version == 0) { LSG_DISPATCH (0) }
+  else if (version == 1) { LSG_DISPATCH (1) }
+  else { LSG_DISPATCH (2) }
+#undef LSG_DISPATCH
+  return cudaGetLastError ();
+}
+
+cudaError_t
+launch_gemv_fp64 (int version, const double *mat, const double *x, double *zbuf, int np,
+                  double *y, cudaStream_t st)
+{
+  const int n = NCOMP (version) * np;
+  const double *z = x;
+  if (version == 2)
+    {
+      k_ztransform<<<(np + 127) / 128, 128, 0, st>>> (x, np, zbuf);
+      z = zbuf;
+    }
+  k_gemv<<<(n + 7) / 8, 256, 0, st>>> (mat, z, n, y);
+  return cudaGetLastError ();
+}
+
+cudaError_t
+launch_gemv_rect_fp64 (const double *mat, int n1, int n2, const double *x, double *y,
+                       cudaStream_t st)
+{
+  k_gemv_rect<<<(n1 + 7) / 8, 256, 0, st>>> (mat, x, n1, n2, y);
+  return cudaGetLastError ();
+}
+
+}  // namespace lsg

@@ -1,0 +1,905 @@
+// gpu_engine.cu -- host engine and C ABI of libstokes_gb300.
+//
+// Keeps one device context per struct stokes (keyed by its address):
+// a stream, timing events, grow-only device buffers and the device copies
+// of the lattice tables.  Every product re-derives the image list, the
+// reciprocal table and the per-particle constants from the struct on the
+// host (cheap, O(images + k + np)) and re-uploads only what changed, so a
+// caller may poke struct members directly between calls, as libstokes'
+// own tests do (test/check-ewald.c:73-125).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+#include <vector>
+
+#include "stokes_gpu.h"
+#include "engine.h"
+#include "gpu_engine.h"
+
+namespace lsg {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local int t_err = STOKES_GPU_OK;
+static thread_local char t_msg[512] = "";
+static int g_error_mode = 0;
+
+int
+set_error (int code, const char *fmt, ...)
+{
+  t_err = code;
+  va_list ap;
+  va_start (ap, fmt);
+  vsnprintf (t_msg, sizeof t_msg, fmt, ap);
+  va_end (ap);
+  return code;
+}
+
+int
+cuda_fail (cudaError_t e, const char *where)
+{
+  if (e == cudaErrorMemoryAllocation)
+    return set_error (STOKES_GPU_ENOMEM, "%s: %s", where, cudaGetErrorString (e));
+  return set_error (STOKES_GPU_ECUDA, "%s: %s", where, cudaGetErrorString (e));
+}
+
+// called by the void drop-in functions on failure
+void
+dropin_failed (const char *fn, double *out, size_t nout)
+{
+  fprintf (stderr, "libstokes_gb300 %s: %s\n", fn, t_msg);
+  if (g_error_mode == 0) exit (1);
+  if (out)
+    for (size_t q = 0; q < nout; q++) out[q] = NAN;
+}
+
+// ---------------------------------------------------------------------------
+// buffers and contexts
+// ---------------------------------------------------------------------------
+cudaError_t
+DevBuf::ensure (size_t bytes)
+{
+  if (bytes <= cap) return cudaSuccess;
+  if (p) cudaFree (p);
+  p = nullptr;
+  cap = 0;
+  size_t want = bytes + bytes / 4 + 256;
+  cudaError_t e = cudaMalloc (&p, want);
+  if (e != cudaSuccess) { p = nullptr; return e; }
+  cap = want;
+  return cudaSuccess;
+}
+
+void
+DevBuf::release ()
+{
+  if (p) cudaFree (p);
+  p = nullptr;
+  cap = 0;
+}
+
+static std::mutex g_mu;
+static std::unordered_map<const void *, Ctx *> g_ctx;
+
+static uint64_t
+fnv (const void *data, size_t n, uint64_t h = 1469598103934665603ull)
+{
+  const unsigned char *b = (const unsigned char *) data;
+  for (size_t q = 0; q < n; q++) { h ^= b[q]; h *= 1099511628211ull; }
+  return h;
+}
+
+Ctx *
+get_ctx (const struct stokes *sys, bool create)
+{
+  std::lock_guard<std::mutex> lk (g_mu);
+  auto it = g_ctx.find (sys);
+  if (it != g_ctx.end ()) return it->second;
+  if (!create) return nullptr;
+  Ctx *c = new Ctx ();
+  cudaGetDevice (&c->device);
+  if (cudaStreamCreateWithFlags (&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    { delete c; return nullptr; }
+  for (int q = 0; q < 4; q++) cudaEventCreate (&c->ev[q]);
+  const char *env = getenv ("LIBSTOKES_GB300_PRECISION");
+  c->precision = (env && strcmp (env, "mixed") == 0) ? STOKES_GPU_MIXED : STOKES_GPU_FP64;
+  g_ctx[sys] = c;
+  return c;
+}
+
+static void
+free_ctx (Ctx *c)
+{
+  for (cudaEvent_t e : c->prof_ev) cudaEventDestroy (e);
+  for (DevBuf *b : c->all_buffers ()) b->release ();
+  for (int q = 0; q < 4; q++) cudaEventDestroy (c->ev[q]);
+  cudaStreamDestroy (c->stream);
+  release_mixed (c);
+  delete c;
+}
+
+int
+release_ctx (const struct stokes *sys)
+{
+  Ctx *c = nullptr;
+  {
+    std::lock_guard<std::mutex> lk (g_mu);
+    auto it = g_ctx.find (sys);
+    if (it == g_ctx.end ()) return STOKES_GPU_OK;
+    c = it->second;
+    g_ctx.erase (it);
+  }
+  cudaStreamSynchronize (c->stream);
+  free_ctx (c);
+  return STOKES_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host-side tables
+// ---------------------------------------------------------------------------
+static int
+check_sys (const struct stokes *sys)
+{
+  if (sys == nullptr) return set_error (STOKES_GPU_EINVAL, "struct stokes is NULL");
+  if (sys->periodic == 0)
+    return set_error (STOKES_GPU_ENOTPERIODIC,
+                      "open (non-periodic) systems are not served by libstokes_gb300");
+  if (sys->version < 0 || sys->version > 2)
+    return set_error (STOKES_GPU_EINVAL, "invalid version %d", sys->version);
+  if (sys->np <= 0 || sys->pos == nullptr)
+    return set_error (STOKES_GPU_EINVAL, "no particles (np = %d)", sys->np);
+  if (!(sys->lx > 0.0 && sys->ly > 0.0 && sys->lz > 0.0))
+    return set_error (STOKES_GPU_EINVAL, "box size not set");
+  if (sys->xi <= 0.0) return set_error (STOKES_GPU_EINVAL, "Ewald xi not set");
+  return STOKES_GPU_OK;
+}
+
+// real-space image list.  Table form: images of sys->rl* with the shear
+// shift of src/ewald.c:678-686 folded in.  Cube form ("_notbl"): the cube
+// |m| <= rmax{x,y,z} with the running shear shift of src/ewald.c:1843-1861
+// (rlx is reset per m1 only, so the shift accumulates over m2, m3).
+static void
+build_images (const struct stokes *sys, bool cube, std::vector<Img4> &img)
+{
+  img.clear ();
+  if (!cube)
+    {
+      img.reserve (sys->nr);
+      for (int m = 0; m < sys->nr; m++)
+        {
+          double sx = 0.0;
+          if (sys->shear_mode == 1) sx = (double) sys->rmy[m] * sys->shear_shift;
+          else if (sys->shear_mode == 2) sx = (double) sys->rmz[m] * sys->shear_shift;
+          img.push_back (Img4{sys->rlx[m] + sx, sys->rly[m], sys->rlz[m], 0.0});
+        }
+      return;
+    }
+  for (int m1 = -sys->rmaxx; m1 <= sys->rmaxx; m1++)
+    {
+      double rlx = sys->lx * (double) m1;
+      for (int m2 = -sys->rmaxy; m2 <= sys->rmaxy; m2++)
+        {
+          const double rly = sys->ly * (double) m2;
+          for (int m3 = -sys->rmaxz; m3 <= sys->rmaxz; m3++)
+            {
+              const double rlz = sys->lz * (double) m3;
+              if (sys->shear_mode == 1) rlx += (double) m2 * sys->shear_shift;
+              else if (sys->shear_mode == 2) rlx += (double) m3 * sys->shear_shift;
+              img.push_back (Img4{rlx, rly, rlz, 0.0});
+            }
+        }
+    }
+}
+
+// reciprocal table: the k cube |m_i| <= kmax{x,y,z} without 0, the sphere
+// |k| <= kmax unless kmax == 0, Lees-Edwards shifted (src/ewald.c:923-958)
+static void
+build_ktable (const struct stokes *sys, std::vector<double> &kt)
+{
+  kt.clear ();
+  const double k0x = 2.0 * M_PI / sys->lx, k0y = 2.0 * M_PI / sys->ly, k0z = 2.0 * M_PI / sys->lz;
+  const double sl = sys->shear_shift / sys->lx;
+  for (int m1 = -sys->kmaxx; m1 <= sys->kmaxx; m1++)
+    for (int m2 = -sys->kmaxy; m2 <= sys->kmaxy; m2++)
+      for (int m3 = -sys->kmaxz; m3 <= sys->kmaxz; m3++)
+        {
+          if (m1 == 0 && m2 == 0 && m3 == 0) continue;
+          const double k1 = k0x * (double) m1;
+          double k2 = k0y * (double) m2;
+          double k3 = k0z * (double) m3;
+          if (sys->shear_mode == 1) k2 = k0y * ((double) m2 - sl * (double) m1);
+          else if (sys->shear_mode == 2) k3 = k0z * ((double) m3 - sl * (double) m1);
+          const double kk = k1 * k1 + k2 * k2 + k3 * k3;
+          const double k = sqrt (kk);
+          if (sys->kmax != 0.0 && k > sys->kmax) continue;
+          const double k4z = kk / 4.0 / sys->xi2;
+          const double kexp = sys->pivol * (1.0 + k4z * (1.0 + 2.0 * k4z)) / kk * exp (-k4z);
+          double row[KT_STRIDE] = {0};
+          row[KT_KX] = k1; row[KT_KY] = k2; row[KT_KZ] = k3;
+          row[KT_EX] = k1 / k; row[KT_EY] = k2 / k; row[KT_EZ] = k3 / k;
+          row[KT_K] = k; row[KT_KK] = kk; row[KT_KEXP] = kexp;
+          row[KT_YA] = 6.0 * (1.0 - kk / 3.0) * kexp;
+          row[KT_YB] = 3.0 * k * kexp;
+          row[KT_YC] = 1.5 * kk * kexp;
+          row[KT_YG] = 3.0 * (1.0 - 4.0 / 15.0 * kk) * k * kexp;
+          row[KT_YH] = 1.5 * kk * kexp;
+          row[KT_YM] = 3.0 * (1.0 - kk / 5.0) * kk * kexp;
+          kt.insert (kt.end (), row, row + KT_STRIDE);
+        }
+}
+
+// per-particle arrays: radii (1 when a == NULL), slip radii, squared
+// Laplacian radii, and self scalars (src/ewald.c:540-643)
+static void
+build_particles (const struct stokes *sys, int mode, std::vector<double> &pp)
+{
+  const int np = sys->np;
+  pp.assign ((size_t) 6 * np, 0.0);
+  double *rad = pp.data (), *slipa = rad + np, *qa = slipa + np, *selfc = qa + np;
+  for (int i = 0; i < np; i++)
+    {
+      const double a = sys->a ? sys->a[i] : 1.0;
+      rad[i] = a;
+      slipa[i] = sys->slip ? sys->slip_a[i] : a;
+      qa[i] = (mode == MODE_SLIP) ? slipa[i] * slipa[i] : a * a;
+      double sa, sc, sm;
+      if (mode == MODE_MONO)
+        { sa = sys->self_a; sc = sys->self_c; sm = sys->self_m; }
+      else
+        {
+          const double a2 = a * a, a3 = a2 * a;
+          double fa = 1.0, fc = 1.0, fm = 1.0;
+          if (sys->slip) { fa = sys->slip_G32[i]; fc = sys->slip_G30[i]; fm = sys->slip_G52[i]; }
+          sa = 1.0 * fa - a * sys->xiaspi * (6.0 - 40.0 / 3.0 * sys->xia2 * a2);
+          sc = 0.75 * fc - a3 * sys->xiaspi * sys->xia2 * 10.0;
+          sm = 0.9 * fm - a3 * sys->xiaspi * sys->xia2 * (12.0 - 30.24 * sys->xia2 * a2);
+        }
+      selfc[3 * i] = sa;
+      selfc[3 * i + 1] = sc;
+      selfc[3 * i + 2] = sm;
+    }
+}
+
+static int
+upload_if_changed (DevBuf &buf, uint64_t &fp, const void *host, size_t bytes,
+                   cudaStream_t st, const char *what)
+{
+  const uint64_t h = fnv (host, bytes, fnv (&bytes, sizeof bytes));
+  if (h == fp && buf.p) return STOKES_GPU_OK;
+  cudaError_t e = buf.ensure (bytes > 0 ? bytes : 64);
+  if (e != cudaSuccess) return cuda_fail (e, what);
+  if (bytes)
+    {
+      e = cudaMemcpyAsync (buf.p, host, bytes, cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) return cuda_fail (e, what);
+      // pageable source: make the copy complete before the host vector changes
+      e = cudaStreamSynchronize (st);
+      if (e != cudaSuccess) return cuda_fail (e, what);
+    }
+  fp = h;
+  return STOKES_GPU_OK;
+}
+
+int
+prepare (Ctx *c, const struct stokes *sys, bool cube)
+{
+  int rc = check_sys (sys);
+  if (rc) return rc;
+  if (!cube && (sys->nr > 0) && (!sys->rlx || !sys->rly || !sys->rlz))
+    return set_error (STOKES_GPU_EINVAL, "image table missing (stokes_set_xi not called?)");
+  c->version = sys->version;
+  c->np = sys->np;
+  c->mode = sys->slip ? MODE_SLIP : (sys->a ? MODE_POLY : MODE_MONO);
+  c->xi = sys->xi;
+  c->xisp = sys->xi / sqrt (M_PI);
+  c->rmax2 = sys->rmax2;
+  c->rmin = sys->rmin;
+
+  build_images (sys, cube, c->h_img);
+  c->nimg = (int) c->h_img.size ();
+  rc = upload_if_changed (c->img, c->fp_img, c->h_img.data (), sizeof (Img4) * c->h_img.size (),
+                          c->stream, "image table");
+  if (rc) return rc;
+  build_ktable (sys, c->h_kt);
+  c->nk = (int) (c->h_kt.size () / KT_STRIDE);
+  rc = upload_if_changed (c->kt, c->fp_kt, c->h_kt.data (), sizeof (double) * c->h_kt.size (),
+                          c->stream, "reciprocal table");
+  if (rc) return rc;
+  build_particles (sys, c->mode, c->h_pp);
+  rc = upload_if_changed (c->pp, c->fp_pp, c->h_pp.data (), sizeof (double) * c->h_pp.size (),
+                          c->stream, "particle table");
+  if (rc) return rc;
+  return STOKES_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 product on device buffers
+// ---------------------------------------------------------------------------
+static int
+choose_nchunk (int np)
+{
+  // about 8 warps of work per SM slot; a chunk holds at least one source
+  const int target = 152 * 32;
+  int nc = (target + np - 1) / np;
+  if (nc < 1) nc = 1;
+  if (nc > np) nc = np;
+  if (nc > 64) nc = 64;
+  return nc;
+}
+
+int
+atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
+                 cudaStream_t st, bool timed)
+{
+  const int np = c->np, C = NCOMP (c->version);
+  const int nchunk = choose_nchunk (np);
+  cudaError_t e;
+  if ((e = c->partial.ensure (sizeof (double) * (size_t) nchunk * np * C)) != cudaSuccess)
+    return cuda_fail (e, "real-space scratch");
+  if ((e = c->yrec.ensure (sizeof (double) * (size_t) np * C)) != cudaSuccess)
+    return cuda_fail (e, "reciprocal scratch");
+  if ((e = c->ph.ensure (sizeof (double2) * (size_t) (c->nk > 0 ? c->nk : 1) * np)) != cudaSuccess)
+    return cuda_fail (e, "phase table");
+  if ((e = c->sf.ensure (sizeof (double) * (size_t) SF_STRIDE * (c->nk > 0 ? c->nk : 1))) != cudaSuccess)
+    return cuda_fail (e, "structure factors");
+
+  const double *pp = (const double *) c->pp.p;
+  const double *rad = pp, *slipa = pp + np, *qa = pp + 2 * np, *selfc = pp + 3 * np;
+  int launches = 0;
+  cudaEvent_t *E = phase_events (c, timed);
+  if (E) cudaEventRecord (E[0], st);
+
+  // reciprocal space
+  if (c->nk > 0)
+    {
+      if ((e = launch_phase_fp64 (d_pos, (const double *) c->kt.p, c->nk, np,
+                                  (double2 *) c->ph.p, st)) != cudaSuccess)
+        return cuda_fail (e, "phase kernel");
+      launches++;
+    }
+  RecipArgs ra;
+  ra.x = d_x;
+  ra.ph = (const double2 *) c->ph.p;
+  ra.kt = (const double *) c->kt.p;
+  ra.rad = rad;
+  ra.qa = qa;
+  ra.nk = c->nk;
+  ra.np = np;
+  ra.sf = (double *) c->sf.p;
+  ra.yrec = (double *) c->yrec.p;
+  if ((e = launch_recip_fp64 (c->version, c->mode, ra, st)) != cudaSuccess)
+    return cuda_fail (e, "reciprocal kernels");
+  launches += c->nk > 0 ? 2 : 0;
+  if (E) cudaEventRecord (E[1], st);
+
+  // real space
+  RealArgs a;
+  a.pos = d_pos;
+  a.x = d_x;
+  a.img = (const Img4 *) c->img.p;
+  a.nimg = c->nimg;
+  a.np = np;
+  a.nchunk = nchunk;
+  a.rmax2 = c->rmax2;
+  a.rmin = c->rmin;
+  a.xi = c->xi;
+  a.xisp = c->xisp;
+  a.rad = rad;
+  a.slipa = slipa;
+  a.partial = (double *) c->partial.p;
+  if ((e = launch_real_fp64 (c->version, c->mode, a, st)) != cudaSuccess)
+    return cuda_fail (e, "real-space kernel");
+  launches++;
+  if (E) cudaEventRecord (E[2], st);
+
+  if ((e = launch_combine_fp64 (c->version, d_x, (const double *) c->partial.p, nchunk,
+                                (const double *) c->yrec.p, selfc, np, d_y, st)) != cudaSuccess)
+    return cuda_fail (e, "combine kernel");
+  launches++;
+  if (E) cudaEventRecord (E[3], st);
+  c->launches = launches;
+  c->timed = timed;
+  return STOKES_GPU_OK;
+}
+
+// Event set for one product: the context's own set for host-buffer calls
+// (read back right after), or the next slot of the profiling ring while a
+// profile window is open (read back at stokes_gpu_profile_end).
+cudaEvent_t *
+phase_events (Ctx *c, bool timed)
+{
+  if (timed) return c->ev;
+  if (c->prof_on && c->prof_n < (int) (c->prof_ev.size () / 4))
+    return &c->prof_ev[4 * (size_t) c->prof_n++];
+  return nullptr;
+}
+
+void
+collect_times (Ctx *c)
+{
+  if (!c->timed) return;
+  float t_rec = 0.f, t_real = 0.f, t_all = 0.f;
+  cudaEventElapsedTime (&t_rec, c->ev[0], c->ev[1]);
+  cudaEventElapsedTime (&t_real, c->ev[1], c->ev[2]);
+  cudaEventElapsedTime (&t_all, c->ev[0], c->ev[3]);
+  c->times[0] = t_all;
+  c->times[1] = t_real;
+  c->times[2] = t_rec;
+}
+
+int
+atimes_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y, cudaStream_t st,
+            bool timed)
+{
+  if (c->precision == STOKES_GPU_MIXED)
+    return atimes_mixed_dev (c, d_pos, d_x, d_y, st, timed);
+  return atimes_fp64_dev (c, d_pos, d_x, d_y, st, timed);
+}
+
+// host buffers in and out; positions from sys->pos
+void clear_error () { t_err = STOKES_GPU_OK; t_msg[0] = 0; }
+
+int
+atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
+{
+  clear_error ();
+  if (x == nullptr || y == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL x or y");
+  Ctx *c = get_ctx (sys, true);
+  if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  int rc = prepare (c, sys, cube);
+  if (rc) return rc;
+  const int np = sys->np, n = NCOMP (sys->version) * np;
+  cudaError_t e;
+  if ((e = c->pos.ensure (sizeof (double) * 3 * np)) != cudaSuccess) return cuda_fail (e, "pos");
+  if ((e = c->x.ensure (sizeof (double) * n)) != cudaSuccess) return cuda_fail (e, "x");
+  if ((e = c->y.ensure (sizeof (double) * n)) != cudaSuccess) return cuda_fail (e, "y");
+  cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * np, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync (c->x.p, x, sizeof (double) * n, cudaMemcpyHostToDevice, c->stream);
+  rc = atimes_dev (c, (const double *) c->pos.p, (const double *) c->x.p, (double *) c->y.p,
+                   c->stream, true);
+  if (rc) return rc;
+  e = cudaMemcpyAsync (y, c->y.p, sizeof (double) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize (c->stream);
+  if (e != cudaSuccess) return cuda_fail (e, "atimes");
+  collect_times (c);
+  sys->cpu1 = c->times[0];
+  sys->cpu2 = c->times[1];
+  sys->cpu3 = c->times[2];
+  return STOKES_GPU_OK;
+}
+
+// dense matrix on device
+int
+matrix_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st)
+{
+  if (c->precision == STOKES_GPU_MIXED)
+    return matrix_mixed_dev (c, d_pos, d_mat, st);
+  const int np = c->np;
+  cudaError_t e;
+  if ((e = c->ph.ensure (sizeof (double2) * (size_t) (c->nk > 0 ? c->nk : 1) * np)) != cudaSuccess)
+    return cuda_fail (e, "phase table");
+  int launches = 0;
+  if (c->nk > 0)
+    {
+      if ((e = launch_phase_fp64 (d_pos, (const double *) c->kt.p, c->nk, np,
+                                  (double2 *) c->ph.p, st)) != cudaSuccess)
+        return cuda_fail (e, "phase kernel");
+      launches++;
+    }
+  const double *pp = (const double *) c->pp.p;
+  MatArgs a;
+  a.pos = d_pos;
+  a.img = (const Img4 *) c->img.p;
+  a.nimg = c->nimg;
+  a.np = np;
+  a.nk = c->nk;
+  a.rmax2 = c->rmax2;
+  a.rmin = c->rmin;
+  a.xi = c->xi;
+  a.xisp = c->xisp;
+  a.rad = pp;
+  a.slipa = pp + np;
+  a.qa = pp + 2 * np;
+  a.selfc = pp + 3 * np;
+  a.kt = (const double *) c->kt.p;
+  a.ph = (const double2 *) c->ph.p;
+  a.mat = d_mat;
+  if ((e = launch_matrix_fp64 (c->version, c->mode, a, st)) != cudaSuccess)
+    return cuda_fail (e, "matrix kernel");
+  c->launches = launches + 1;
+  return STOKES_GPU_OK;
+}
+
+int
+matrix_host (struct stokes *sys, double *mat, bool cube)
+{
+  clear_error ();
+  if (mat == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL mat");
+  Ctx *c = get_ctx (sys, true);
+  if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  int rc = prepare (c, sys, cube);
+  if (rc) return rc;
+  const int np = sys->np;
+  const size_t n = (size_t) NCOMP (sys->version) * np;
+  cudaError_t e;
+  if ((e = c->pos.ensure (sizeof (double) * 3 * np)) != cudaSuccess) return cuda_fail (e, "pos");
+  if ((e = c->mat.ensure (sizeof (double) * n * n)) != cudaSuccess) return cuda_fail (e, "matrix");
+  cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * np, cudaMemcpyHostToDevice, c->stream);
+  cudaEventRecord (c->ev[0], c->stream);
+  rc = matrix_dev (c, (const double *) c->pos.p, (double *) c->mat.p, c->stream);
+  if (rc) return rc;
+  cudaEventRecord (c->ev[3], c->stream);
+  e = cudaMemcpyAsync (mat, c->mat.p, sizeof (double) * n * n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize (c->stream);
+  if (e != cudaSuccess) return cuda_fail (e, "matrix");
+  float t = 0.f;
+  cudaEventElapsedTime (&t, c->ev[0], c->ev[3]);
+  sys->cpu1 = t;
+  sys->cpu2 = t;
+  sys->cpu3 = 0.0;
+  return STOKES_GPU_OK;
+}
+
+// build the matrix on the device and apply it there (src/ewald.c:484-505)
+int
+atimes_matrix_host (struct stokes *sys, const double *x, double *y, bool cube)
+{
+  clear_error ();
+  if (x == nullptr || y == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL x or y");
+  Ctx *c = get_ctx (sys, true);
+  if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  int rc = prepare (c, sys, cube);
+  if (rc) return rc;
+  const int np = sys->np;
+  const size_t n = (size_t) NCOMP (sys->version) * np;
+  cudaError_t e;
+  if ((e = c->pos.ensure (sizeof (double) * 3 * np)) != cudaSuccess) return cuda_fail (e, "pos");
+  if ((e = c->mat.ensure (sizeof (double) * n * n)) != cudaSuccess) return cuda_fail (e, "matrix");
+  if ((e = c->x.ensure (sizeof (double) * n)) != cudaSuccess) return cuda_fail (e, "x");
+  if ((e = c->y.ensure (sizeof (double) * n)) != cudaSuccess) return cuda_fail (e, "y");
+  if ((e = c->zbuf.ensure (sizeof (double) * n)) != cudaSuccess) return cuda_fail (e, "z");
+  cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * np, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync (c->x.p, x, sizeof (double) * n, cudaMemcpyHostToDevice, c->stream);
+  rc = matrix_dev (c, (const double *) c->pos.p, (double *) c->mat.p, c->stream);
+  if (rc) return rc;
+  if ((e = launch_gemv_fp64 (sys->version, (const double *) c->mat.p, (const double *) c->x.p,
+                             (double *) c->zbuf.p, np, (double *) c->y.p, c->stream)) != cudaSuccess)
+    return cuda_fail (e, "gemv");
+  e = cudaMemcpyAsync (y, c->y.p, sizeof (double) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize (c->stream);
+  if (e != cudaSuccess) return cuda_fail (e, "atimes_3all_matrix");
+  return STOKES_GPU_OK;
+}
+
+}  // namespace lsg
+
+using namespace lsg;
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int stokes_gpu_last_error (void) { return t_err; }
+const char *stokes_gpu_last_error_message (void) { return t_msg; }
+void stokes_gpu_set_error_mode (int mode) { g_error_mode = mode; }
+
+int
+stokes_gpu_set_precision (struct stokes *sys, int mode)
+{
+  if (sys == nullptr) return set_error (STOKES_GPU_EINVAL, "struct stokes is NULL");
+  if (mode != STOKES_GPU_FP64 && mode != STOKES_GPU_MIXED)
+    return set_error (STOKES_GPU_EINVAL, "invalid precision mode %d", mode);
+  Ctx *c = get_ctx (sys, true);
+  if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  c->precision = mode;
+  return STOKES_GPU_OK;
+}
+
+int
+stokes_gpu_get_precision (const struct stokes *sys, int *mode)
+{
+  if (sys == nullptr || mode == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL argument");
+  Ctx *c = get_ctx (sys, true);
+  if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  *mode = c->precision;
+  return STOKES_GPU_OK;
+}
+
+int stokes_gpu_release (struct stokes *sys) { return release_ctx (sys); }
+
+int
+stokes_gpu_atimes (struct stokes *sys, const double *x, double *y)
+{
+  return atimes_host (sys, x, y, false);
+}
+
+int
+stokes_gpu_atimes_dev (struct stokes *sys, const double *d_pos, const double *d_x,
+                       double *d_y, void *stream)
+{
+  clear_error ();
+  if (d_x == nullptr || d_y == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL x or y");
+  Ctx *c = get_ctx (sys, true);
+  if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  int rc = prepare (c, sys, false);
+  if (rc) return rc;
+  cudaStream_t st = stream ? (cudaStream_t) stream : c->stream;
+  if (d_pos == nullptr)
+    {
+      cudaError_t e = c->pos.ensure (sizeof (double) * 3 * sys->np);
+      if (e != cudaSuccess) return cuda_fail (e, "pos");
+      cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * sys->np,
+                       cudaMemcpyHostToDevice, st);
+      d_pos = (const double *) c->pos.p;
+    }
+  return atimes_dev (c, d_pos, d_x, d_y, st, false);
+}
+
+int
+stokes_gpu_matrix (struct stokes *sys, double *mat)
+{
+  return matrix_host (sys, mat, false);
+}
+
+int
+stokes_gpu_matrix_dev (struct stokes *sys, const double *d_pos, double *d_mat, void *stream)
+{
+  clear_error ();
+  if (d_mat == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL mat");
+  Ctx *c = get_ctx (sys, true);
+  if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  int rc = prepare (c, sys, false);
+  if (rc) return rc;
+  cudaStream_t st = stream ? (cudaStream_t) stream : c->stream;
+  if (d_pos == nullptr)
+    {
+      cudaError_t e = c->pos.ensure (sizeof (double) * 3 * sys->np);
+      if (e != cudaSuccess) return cuda_fail (e, "pos");
+      cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * sys->np,
+                       cudaMemcpyHostToDevice, st);
+      d_pos = (const double *) c->pos.p;
+    }
+  return matrix_dev (c, d_pos, d_mat, st);
+}
+
+int
+stokes_gpu_matvec_dev (int version, int np, const double *d_mat, const double *d_x,
+                       double *d_y, void *stream)
+{
+  if (version < 0 || version > 2 || np <= 0 || !d_mat || !d_x || !d_y)
+    return set_error (STOKES_GPU_EINVAL, "bad matvec arguments");
+  static thread_local DevBuf zb;
+  cudaError_t e = zb.ensure (sizeof (double) * NCOMP (version) * (size_t) np);
+  if (e != cudaSuccess) return cuda_fail (e, "z buffer");
+  e = launch_gemv_fp64 (version, d_mat, d_x, (double *) zb.p, np, d_y, (cudaStream_t) stream);
+  if (e != cudaSuccess) return cuda_fail (e, "gemv");
+  return STOKES_GPU_OK;
+}
+
+int
+stokes_gpu_last_times (const struct stokes *sys, double *ms3)
+{
+  if (!sys || !ms3) return set_error (STOKES_GPU_EINVAL, "NULL argument");
+  Ctx *c = get_ctx (sys, false);
+  if (!c) return set_error (STOKES_GPU_EINVAL, "no product run for this system yet");
+  ms3[0] = c->times[0];
+  ms3[1] = c->times[1];
+  ms3[2] = c->times[2];
+  return STOKES_GPU_OK;
+}
+
+int
+stokes_gpu_profile_begin (struct stokes *sys, int max_products)
+{
+  if (!sys || max_products <= 0) return set_error (STOKES_GPU_EINVAL, "bad profile window");
+  Ctx *c = get_ctx (sys, true);
+  if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  const size_t want = 4 * (size_t) max_products;
+  while (c->prof_ev.size () < want)
+    {
+      cudaEvent_t e;
+      if (cudaEventCreate (&e) != cudaSuccess)
+        return set_error (STOKES_GPU_ECUDA, "cannot create events");
+      c->prof_ev.push_back (e);
+    }
+  c->prof_on = true;
+  c->prof_n = 0;
+  return STOKES_GPU_OK;
+}
+
+int
+stokes_gpu_profile_end (struct stokes *sys, double *sum_ms3, int *count)
+{
+  if (!sys || !sum_ms3 || !count) return set_error (STOKES_GPU_EINVAL, "NULL argument");
+  Ctx *c = get_ctx (sys, false);
+  if (!c) return set_error (STOKES_GPU_EINVAL, "no profile window open");
+  c->prof_on = false;
+  sum_ms3[0] = sum_ms3[1] = sum_ms3[2] = 0.0;
+  for (int q = 0; q < c->prof_n; q++)
+    {
+      cudaEvent_t *E = &c->prof_ev[4 * (size_t) q];
+      cudaError_t e = cudaEventSynchronize (E[3]);
+      if (e != cudaSuccess) return cuda_fail (e, "profile events");
+      float t_all = 0.f, t_real = 0.f, t_rec = 0.f;
+      cudaEventElapsedTime (&t_rec, E[0], E[1]);
+      cudaEventElapsedTime (&t_real, E[1], E[2]);
+      cudaEventElapsedTime (&t_all, E[0], E[3]);
+      sum_ms3[0] += t_all;
+      sum_ms3[1] += t_real;
+      sum_ms3[2] += t_rec;
+    }
+  *count = c->prof_n;
+  return STOKES_GPU_OK;
+}
+
+int
+stokes_gpu_last_launches (const struct stokes *sys, int *count)
+{
+  if (!sys || !count) return set_error (STOKES_GPU_EINVAL, "NULL argument");
+  Ctx *c = get_ctx (sys, false);
+  if (!c) return set_error (STOKES_GPU_EINVAL, "no product run for this system yet");
+  *count = c->launches;
+  return STOKES_GPU_OK;
+}
+
+// ---- drop-in replacements of src/ewald.c ----------------------------------
+
+static int
+check_n (const struct stokes *sys, int n)
+{
+  clear_error ();
+  if (sys == nullptr) return set_error (STOKES_GPU_EINVAL, "user_data is NULL");
+  if (sys->version < 0 || sys->version > 2)
+    return set_error (STOKES_GPU_EINVAL, "invalid version %d", sys->version);
+  if (n != NCOMP (sys->version) * sys->np)
+    return set_error (STOKES_GPU_EINVAL, "n = %d but np * %d = %d", n, NCOMP (sys->version),
+                      NCOMP (sys->version) * sys->np);
+  return STOKES_GPU_OK;
+}
+
+void
+atimes_ewald_3all (int n, const double *x, double *y, void *user_data)
+{
+  struct stokes *sys = (struct stokes *) user_data;
+  if (check_n (sys, n) || atimes_host (sys, x, y, false))
+    dropin_failed ("atimes_ewald_3all", y, n > 0 ? (size_t) n : 0);
+}
+
+void
+atimes_ewald_3all_notbl (int n, const double *x, double *y, void *user_data)
+{
+  struct stokes *sys = (struct stokes *) user_data;
+  if (check_n (sys, n) || atimes_host (sys, x, y, true))
+    dropin_failed ("atimes_ewald_3all_notbl", y, n > 0 ? (size_t) n : 0);
+}
+
+void
+atimes_3all (int n, const double *x, double *y, void *user_data)
+{
+  struct stokes *sys = (struct stokes *) user_data;
+  if (check_n (sys, n) || atimes_host (sys, x, y, false))
+    dropin_failed ("atimes_3all", y, n > 0 ? (size_t) n : 0);
+}
+
+void
+make_matrix_mob_ewald_3all (struct stokes *sys, double *mat)
+{
+  if (matrix_host (sys, mat, false))
+    {
+      size_t n = sys && sys->version >= 0 && sys->version <= 2
+        ? (size_t) NCOMP (sys->version) * (sys->np > 0 ? sys->np : 0) : 0;
+      dropin_failed ("make_matrix_mob_ewald_3all", mat, n * n);
+    }
+}
+
+void
+make_matrix_mob_ewald_3all_notbl (struct stokes *sys, double *mat)
+{
+  if (matrix_host (sys, mat, true))
+    {
+      size_t n = sys && sys->version >= 0 && sys->version <= 2
+        ? (size_t) NCOMP (sys->version) * (sys->np > 0 ? sys->np : 0) : 0;
+      dropin_failed ("make_matrix_mob_ewald_3all_notbl", mat, n * n);
+    }
+}
+
+void
+make_matrix_mob_3all (struct stokes *sys, double *mat)
+{
+  if (matrix_host (sys, mat, false))
+    {
+      size_t n = sys && sys->version >= 0 && sys->version <= 2
+        ? (size_t) NCOMP (sys->version) * (sys->np > 0 ? sys->np : 0) : 0;
+      dropin_failed ("make_matrix_mob_3all", mat, n * n);
+    }
+}
+
+void
+atimes_3all_matrix (int n, const double *x, double *y, void *user_data)
+{
+  struct stokes *sys = (struct stokes *) user_data;
+  if (check_n (sys, n) || atimes_matrix_host (sys, x, y, false))
+    dropin_failed ("atimes_3all_matrix", y, n > 0 ? (size_t) n : 0);
+}
+
+void
+atimes_ewald_3all_matrix_notbl (int n, const double *x, double *y, void *user_data)
+{
+  struct stokes *sys = (struct stokes *) user_data;
+  if (check_n (sys, n) || atimes_matrix_host (sys, x, y, true))
+    dropin_failed ("atimes_ewald_3all_matrix_notbl", y, n > 0 ? (size_t) n : 0);
+}
+
+}  // extern "C"
+
+// ---- dense helpers (replace src/matrix.c:365-399 and :447-478) ------------
+// The matrix, x and y are host arrays; the product runs on the device.
+namespace lsg {
+static int
+dense_host (int version, int n1, int n2, int np, const double *mat, const double *x, double *y)
+{
+  static thread_local DevBuf dm, dx, dy, dz;
+  static thread_local cudaStream_t st = nullptr;
+  if (!st && cudaStreamCreateWithFlags (&st, cudaStreamNonBlocking) != cudaSuccess)
+    return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  cudaError_t e;
+  if ((e = dm.ensure (sizeof (double) * (size_t) n1 * n2)) != cudaSuccess) return cuda_fail (e, "mat");
+  if ((e = dx.ensure (sizeof (double) * (size_t) n2)) != cudaSuccess) return cuda_fail (e, "x");
+  if ((e = dy.ensure (sizeof (double) * (size_t) n1)) != cudaSuccess) return cuda_fail (e, "y");
+  if ((e = dz.ensure (sizeof (double) * (size_t) n2)) != cudaSuccess) return cuda_fail (e, "z");
+  cudaMemcpyAsync (dm.p, mat, sizeof (double) * (size_t) n1 * n2, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync (dx.p, x, sizeof (double) * (size_t) n2, cudaMemcpyHostToDevice, st);
+  if (version == 2)
+    e = launch_gemv_fp64 (2, (const double *) dm.p, (const double *) dx.p, (double *) dz.p, np,
+                          (double *) dy.p, st);
+  else
+    e = launch_gemv_rect_fp64 ((const double *) dm.p, n1, n2, (const double *) dx.p,
+                               (double *) dy.p, st);
+  if (e != cudaSuccess) return cuda_fail (e, "gemv");
+  e = cudaMemcpyAsync (y, dy.p, sizeof (double) * (size_t) n1, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize (st);
+  if (e != cudaSuccess) return cuda_fail (e, "gemv");
+  return STOKES_GPU_OK;
+}
+}  // namespace lsg
+
+extern "C" {
+
+void
+dot_prod_matrix (const double *mat, int n1, int n2, const double *x, double *y)
+{
+  if (n1 <= 0 || n2 <= 0) return;
+  if (!mat || !x || !y)
+    {
+      set_error (STOKES_GPU_EINVAL, "NULL argument");
+      dropin_failed ("dot_prod_matrix", y, y ? (size_t) n1 : 0);
+      return;
+    }
+  if (dense_host (0, n1, n2, 0, mat, x, y)) dropin_failed ("dot_prod_matrix", y, (size_t) n1);
+}
+
+void
+multiply_extmat_with_extvec_3fts (int np, const double *m, const double *x, double *y)
+{
+  if (np <= 0) return;
+  const int n = 11 * np;
+  if (!m || !x || !y)
+    {
+      set_error (STOKES_GPU_EINVAL, "NULL argument");
+      dropin_failed ("multiply_extmat_with_extvec_3fts", y, y ? (size_t) n : 0);
+      return;
+    }
+  if (dense_host (2, n, n, np, m, x, y))
+    dropin_failed ("multiply_extmat_with_extvec_3fts", y, (size_t) n);
+}
+
+}  // extern "C"

@@ -1,0 +1,79 @@
+// gpu_engine.h -- per-system device context shared by the host engine files.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <array>
+#include <vector>
+
+#include "stokes_abi.h"
+#include "engine.h"
+
+namespace lsg {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure (size_t bytes);
+  void release ();
+};
+
+struct MixedState;   // mixed-precision state (mixed.cu)
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {};
+  int precision = 0;
+
+  // geometry of the last prepared system
+  int version = 0, np = 0, mode = 0;
+  double xi = 0, xisp = 0, rmax2 = 0, rmin = 0;
+  int nimg = 0, nk = 0;
+  uint64_t fp_img = 0, fp_kt = 0, fp_pp = 0;
+  std::vector<Img4> h_img;
+  std::vector<double> h_kt, h_pp;
+
+  DevBuf pos, x, y, img, kt, pp, ph, sf, yrec, partial, mat, zbuf;
+
+  double times[3] = {0, 0, 0};
+  int launches = 0;
+  bool timed = false;
+
+  // profiling window: 4 events per product (start, reciprocal done,
+  // real space done, end), read back by stokes_gpu_profile_end
+  bool prof_on = false;
+  int prof_n = 0;
+  std::vector<cudaEvent_t> prof_ev;
+
+  MixedState *mixed = nullptr;
+
+  std::array<DevBuf *, 12> all_buffers ()
+  {
+    return {&pos, &x, &y, &img, &kt, &pp, &ph, &sf, &yrec, &partial, &mat, &zbuf};
+  }
+};
+
+int set_error (int code, const char *fmt, ...);
+void clear_error ();
+int cuda_fail (cudaError_t e, const char *where);
+void dropin_failed (const char *fn, double *out, size_t nout);
+
+Ctx *get_ctx (const struct stokes *sys, bool create);
+int release_ctx (const struct stokes *sys);
+int prepare (Ctx *c, const struct stokes *sys, bool cube);
+int atimes_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
+                cudaStream_t st, bool timed);
+int atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
+                     cudaStream_t st, bool timed);
+void collect_times (Ctx *c);
+cudaEvent_t *phase_events (Ctx *c, bool timed);
+
+// mixed-precision path (mixed.cu)
+int atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
+                      cudaStream_t st, bool timed);
+int matrix_mixed_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st);
+void release_mixed (Ctx *c);
+
+}  // namespace lsg

@@ -1,0 +1,228 @@
+"""Generate the golden fixtures of tests/golden/ from the reference library.
+
+Runs only where the reference checkout exists (it compiles the reference's
+own sources with oracle/Makefile.ref into oracle/_ref/ and calls them through
+oracle/ref_driver.c).  The fixtures it writes are small .npz/.json files that
+travel with the repository, so the tests never need the reference itself:
+
+  struct_stokes_layout.json  member offsets / size of libstokes' struct stokes
+  setup.npz                  Ewald split, cutoffs and image tables
+  products.npz               atimes_ewald_3all / make_matrix_mob_ewald_3all
+                             outputs (F, FT, FTS; equal, unequal radii, slip,
+                             both shear modes, rmin clamp, _notbl variants,
+                             the 8-sphere simple-cubic test of
+                             test/check-ewald.c, the N=64 5-shell workload)
+  chebyshev.npz              chebyshev_coef / chebyshev_eval /
+                             chebyshev_eval_atimes outputs
+
+    python tests/golden/make_golden.py [/path/to/libstokes]
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.oracle import Reference, build_reference  # noqa: E402
+from libstokes_gb300.workloads import rsa_positions  # noqa: E402
+
+STRUCT_FIELDS = [
+    "version", "np", "nm", "pos", "a", "rmin", "twobody_nmax", "twobody_lub",
+    "poly_table", "twobody_f_list", "slip", "slip_a", "slip_G32", "slip_G30",
+    "slip_G52", "slip_table", "twobody_slip_f_list", "Ui", "Oi", "Ei",
+    "shear_mode", "shear_rate", "shear_shift", "periodic", "ewald_eps", "rmax2",
+    "rmaxx", "rmaxy", "rmaxz", "kmax", "kmaxx", "kmaxy", "kmaxz", "xi", "xi2",
+    "xiaspi", "xia2", "pivol", "lx", "ly", "lz", "ilx", "ily", "ilz", "self_a",
+    "self_c", "self_m", "flag_table", "nr", "rlx", "rly", "rlz", "rmx", "rmy",
+    "rmz", "nk", "ex", "ey", "ez", "k", "k1", "k2", "k3", "ya", "yb", "yc", "yg",
+    "yh", "ym", "lubmin2", "lubmax", "cpu1", "cpu2", "cpu3", "it",
+]
+
+
+def layout(ref_root: str) -> dict:
+    src = ["#include <stdio.h>", "#include <stddef.h>", '#include "stokes.h"',
+           "int main(void){", 'printf("{\\"sizeof\\": %zu", sizeof(struct stokes));']
+    for f in STRUCT_FIELDS:
+        src.append(f'printf(", \\"{f}\\": %zu", offsetof(struct stokes, {f}));')
+    src += ['printf("}\\n");', "return 0;}"]
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "lay.c")
+        exe = os.path.join(d, "lay")
+        open(c, "w").write("\n".join(src))
+        subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "oracle", "ref_stubs", "inc"),
+                               "-I", os.path.join(ref_root, "src"), c, "-o", exe])
+        return json.loads(subprocess.check_output([exe]).decode())
+
+
+def mk(version, pos, box, tratio=1.0, eps=1e-12, a=None, slip=None, shear=(0, 0.0),
+       rmin=0.0, cube=None):
+    r = Reference(version, pos, box)
+    if a is not None:
+        r.set_radius(a)
+    if slip is not None:
+        r.set_slip(slip)
+    r.set_split(r.xi_by_tratio(tratio), eps)
+    if cube is not None:
+        r.set_cube(*cube)
+    r.set_misc(rmin, shear[0], shear[1])
+    return r
+
+
+def main(ref_root: str = "/root/reference"):
+    if build_reference(ref_root) is None:
+        raise SystemExit(f"reference checkout not found under {ref_root}")
+    json.dump(layout(ref_root), open(os.path.join(HERE, "struct_stokes_layout.json"), "w"),
+              indent=1)
+
+    # ---- set-up: splits and image tables --------------------------------
+    setup = {}
+    boxes = [((5.0, 5.0, 5.0), 1.0, 1e-12), ((8.0, 9.0, 10.0), 1.0, 1e-12),
+             ((24.07, 24.07, 24.07), 1.0, 1e-12), ((10.0, 5.0, 5.0), 4.0, 1e-10),
+             ((6.0, 6.0, 12.0), 0.5, 1e-6)]
+    for q, (box, tr, eps) in enumerate(boxes):
+        r = mk(0, np.zeros((1, 3)), box, tratio=tr, eps=eps)
+        sp = r.split()
+        rl, rm = r.table()
+        setup[f"c{q}_box"] = np.array(box)
+        setup[f"c{q}_tr_eps"] = np.array([tr, eps])
+        setup[f"c{q}_split"] = np.array([sp["xi"], sp["rmax2"], sp["kmax"], sp["self_a"],
+                                         sp["self_c"], sp["self_m"], sp["pivol"], sp["nr"]]
+                                        + list(sp["kmaxxyz"]))
+        setup[f"c{q}_rl"] = rl
+        setup[f"c{q}_rm"] = rm
+    np.savez_compressed(os.path.join(HERE, "setup.npz"), **setup)
+
+    # ---- products --------------------------------------------------------
+    prod = {}
+    rng = np.random.default_rng(2024)
+
+    def record(name, r, x, with_matrix=True, notbl=False):
+        prod[f"{name}/x"] = x
+        prod[f"{name}/y"] = r.atimes(x)
+        if with_matrix:
+            prod[f"{name}/mat"] = r.matrix()
+        if notbl:
+            prod[f"{name}/y_notbl"] = r.atimes_notbl(x)
+            if with_matrix:
+                prod[f"{name}/mat_notbl"] = r.matrix_notbl()
+
+    # simple-cubic 8 spheres of test/check-ewald.c:46-195 (phi 0.2, tr 1, eps 1e-12)
+    phi = 0.2
+    l = (np.pi / 0.75 / phi) ** (1.0 / 3.0)
+    sc = np.array([[0, 0, 0], [l, 0, 0], [0, l, 0], [0, 0, l], [l, l, 0], [l, 0, l],
+                   [0, l, l], [l, l, l]], dtype=float)
+    for v in (0, 1, 2):
+        name = f"sc8_v{v}"
+        r = mk(v, sc, (2 * l,) * 3)
+        prod[f"{name}/meta"] = np.array([v, 2 * l, 2 * l, 2 * l, 1.0, 1e-12, 0, 0.0, 0.0])
+        prod[f"{name}/pos"] = sc
+        record(name, r, np.ones(r.n))
+
+    # random 12 spheres in a rectangular box: every branch
+    N = 12
+    box = (8.0, 9.0, 10.0)
+    pos = rng.uniform(0.0, 1.0, (N, 3)) * np.array(box)
+    arad = rng.uniform(0.5, 1.5, N)
+    aslip_r = rng.uniform(0.7, 1.3, N)
+    gslip = rng.uniform(0.0, 0.5, N)
+    cases = {
+        "mono": {}, "poly": dict(a=arad), "slip": dict(a=aslip_r, slip=gslip),
+        "slipmono": dict(slip=gslip), "shear1": dict(shear=(1, 1.7)),
+        "shear2": dict(shear=(2, -2.3)), "rmin": dict(rmin=1.5),
+    }
+    for v in (0, 1, 2):
+        for cname, kw in cases.items():
+            name = f"r12_v{v}_{cname}"
+            r = mk(v, pos, box, **kw)
+            sh = kw.get("shear", (0, 0.0))
+            prod[f"{name}/meta"] = np.array([v, *box, 1.0, 1e-12, sh[0], sh[1],
+                                             kw.get("rmin", 0.0)])
+            prod[f"{name}/pos"] = pos
+            if "a" in kw:
+                prod[f"{name}/a"] = kw["a"]
+            if "slip" in kw:
+                prod[f"{name}/slip"] = kw["slip"]
+            record(name, r, rng.standard_normal(r.n), notbl=True)
+
+    # the 5-shell N=64 F workload (phi 0.10, xi = sqrt(pi)/L)
+    pos64, L64 = rsa_positions(64, 0.10, seed=42)
+    r = mk(0, pos64, (L64,) * 3, cube=(5, 5))
+    name = "n64_5shell_v0"
+    prod[f"{name}/meta"] = np.array([0, L64, L64, L64, 1.0, 1e-12, 0, 0.0, 0.0])
+    prod[f"{name}/pos"] = pos64
+    prod[f"{name}/cube"] = np.array([5, 5])
+    record(name, r, np.random.default_rng(7).standard_normal(r.n), with_matrix=False)
+
+    # a larger FTS case (N=40, phi 0.3) for the product only
+    pos40, L40 = rsa_positions(40, 0.30, seed=5)
+    r = mk(2, pos40, (L40,) * 3)
+    name = "n40_fts_phi0.30"
+    prod[f"{name}/meta"] = np.array([2, L40, L40, L40, 1.0, 1e-12, 0, 0.0, 0.0])
+    prod[f"{name}/pos"] = pos40
+    record(name, r, rng.standard_normal(r.n), with_matrix=False)
+    np.savez_compressed(os.path.join(HERE, "products.npz"), **prod)
+
+    # ---- Chebyshev -------------------------------------------------------
+    lib = Reference.lib()
+    import ctypes as C
+    dp = C.POINTER(C.c_double)
+    ch = {}
+    for q, (nc, which, x0, x1) in enumerate([(30, 0, 0.05, 2.0), (50, 0, 0.1, 10.0),
+                                             (20, 1, 0.5, 3.0), (100, 0, 0.01, 1.0)]):
+        a = np.zeros(nc)
+        lib.ref_cheb_coef(nc, which, x0, x1, a.ctypes.data_as(dp))
+        xs = np.linspace(x0, x1, 17)
+        ev = np.array([lib.ref_cheb_eval(nc, a.ctypes.data_as(dp), x0, x1, float(t)) for t in xs])
+        ch[f"c{q}_args"] = np.array([nc, which, x0, x1])
+        ch[f"c{q}_a"] = a
+        ch[f"c{q}_xs"] = xs
+        ch[f"c{q}_eval"] = ev
+    # Chebyshev M^{-1/2} y on a dense SPD matrix
+    n = 24
+    A = rng.standard_normal((n, n))
+    M = A @ A.T / n + np.eye(n)
+    w = np.linalg.eigvalsh(M)
+    e0, e1 = w[0] * 0.95, w[-1] * 1.05
+    nc = 40
+    a = np.zeros(nc)
+    lib.ref_cheb_coef(nc, 0, e0, e1, a.ctypes.data_as(dp))
+    y = rng.standard_normal(n)
+    z = np.zeros(n)
+    err = np.zeros(1)
+    Mc = np.ascontiguousarray(M)
+    lib.ref_cheb_eval_dense(nc, a.ctypes.data_as(dp), n, Mc.ctypes.data_as(dp),
+                            y.ctypes.data_as(dp), z.ctypes.data_as(dp), e0, e1,
+                            err.ctypes.data_as(dp))
+    ch.update(dense_M=M, dense_y=y, dense_z=z, dense_err=err.copy(), dense_a=a,
+              dense_e=np.array([e0, e1]))
+    # Chebyshev on the reference's own Ewald operator (F, 20 non-overlapping
+    # spheres, so that M is positive definite)
+    pos, L20 = rsa_positions(20, 0.2, seed=9)
+    box = (L20,) * 3
+    r = mk(0, pos, box)
+    Mfull = r.matrix()
+    w = np.linalg.eigvalsh(0.5 * (Mfull + Mfull.T))
+    e0, e1 = w[0] * 0.9, w[-1] * 1.1
+    nc = 30
+    a = np.zeros(nc)
+    lib.ref_cheb_coef(nc, 0, e0, e1, a.ctypes.data_as(dp))
+    y = rng.standard_normal(r.n)
+    z = np.zeros(r.n)
+    lib.ref_cheb_eval_ewald(C.c_void_p(r.h), nc, a.ctypes.data_as(dp), y.ctypes.data_as(dp),
+                            z.ctypes.data_as(dp), e0, e1, err.ctypes.data_as(dp))
+    ch.update(ewald_pos=pos, ewald_box=np.array(box), ewald_y=y, ewald_z=z,
+              ewald_err=err.copy(), ewald_a=a, ewald_e=np.array([e0, e1]))
+    np.savez_compressed(os.path.join(HERE, "chebyshev.npz"), **ch)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])
