@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""Benchmark of the Ewald mobility product on GB300.
+
+Workload (the configuration the headline metric is quoted on): FTS mobility
+product y = M x of N = 1000 equal spheres (a = 1) at volume fraction 0.30,
+random-sequential-addition placement (seed 42), cubic periodic box,
+x ~ N(0, 1) (seed 7), Ewald split xi = sqrt(pi)/L with libstokes' own
+cutoffs for eps = 1e-12.  A step is one product over the whole system.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--precision fp64|mixed]
+
+Prints one JSON line.  ``value`` is products per second with inputs resident
+in HBM (device-timed, CUDA events on the launching stream); ``e2e`` is the
+same metric through the drop-in C ABI (atimes_ewald_3all) with pinned host
+buffers, host<->device copies inside the timed region.  Under torchrun each
+rank runs an independent replica (the path is replicated, not sharded).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "mobility matvecs/s & BD steps/s, mixed vs FP64 on 1 GB300 at ≤1e-6 rel err"
+UNIT = "matvecs/s"
+WORKLOAD = dict(name="mob_fts_n1000_phi0.30", version=2, n=1000, phi=0.30, pos_seed=42,
+                x_seed=7, tratio=1.0, eps=1e-12)
+# reference-as-written flop count of one real-space pair term (F, FT, FTS)
+FLOPS_PER_TERM = {0: 89, 1: 184, 2: 754}
+L2_FLUSH_BYTES = 256 << 20
+
+
+def make_inputs():
+    from libstokes_gb300.workloads import forces, rsa_positions
+    pos, L = rsa_positions(WORKLOAD["n"], WORKLOAD["phi"], seed=WORKLOAD["pos_seed"])
+    c = (3, 6, 11)[WORKLOAD["version"]]
+    x = forces(c * WORKLOAD["n"], seed=WORKLOAD["x_seed"])
+    return pos, L, x
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+               "-lms", "200"]
+        if self.gpu_id is not None:
+            cmd += ["-i", self.gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            p = [v.strip() for v in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names[1:], p[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gpu_pci_id(dev: int):
+    try:
+        import torch
+        p = torch.cuda.get_device_properties(dev)
+        return f"{p.pci_domain_id:08X}:{p.pci_bus_id:02X}:{p.pci_device_id:02X}.0"
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (C restatement of the reference), all host cores
+# ---------------------------------------------------------------------------
+def cpu_baseline(pos, L, x, budget_s: float = 3.0):
+    from oracle.oracle import Oracle
+    o = Oracle(WORKLOAD["version"], pos, (L, L, L))
+    o.set_split(o.xi_by_tratio(WORKLOAD["tratio"]), WORKLOAD["eps"])
+    threads = os.cpu_count() or 1
+    o.set_threads(threads)
+    n = WORKLOAD["n"]
+    rows, chunk = 0, max(threads, 8)
+    t0 = time.perf_counter()
+    while rows < n and time.perf_counter() - t0 < budget_s:
+        o.atimes_rows(x, rows, min(n, rows + chunk))
+        rows = min(n, rows + chunk)
+    dt = time.perf_counter() - t0
+    value = (rows / n) / dt
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{rows} of {n} target rows of one FTS product "
+                      f"(real + reciprocal space), {dt:.2f} s wall on {threads} threads; "
+                      f"value = (rows/N)/time"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU algorithm (the oracle port; the
+    reference sources themselves are not on this machine) on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    pos, L, x = make_inputs()
+    from oracle.oracle import Oracle
+    o = Oracle(WORKLOAD["version"], pos, (L, L, L))
+    o.set_split(o.xi_by_tratio(WORKLOAD["tratio"]), WORKLOAD["eps"])
+    threads = os.cpu_count() or 1
+    o.set_threads(threads)
+    n = WORKLOAD["n"]
+    rows_per_step = max(threads, 16)
+    times = []
+    for k in range(args.warmup + args.steps):
+        i0 = (k * rows_per_step) % n
+        t0 = time.perf_counter()
+        o.atimes_rows(x, i0, min(n, i0 + rows_per_step))
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt * n / (min(n, i0 + rows_per_step) - i0))
+    ms = 1000.0 * sum(times) / len(times)
+    value = 1000.0 / ms
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD["name"], "n_particles": n, "phi": WORKLOAD["phi"],
+                       "version": "FTS", "ewald_eps": WORKLOAD["eps"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"each step: {rows_per_step} of {n} target rows of one "
+                                       "FTS product, scaled to a whole product"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    import libstokes_gb300 as L
+    from libstokes_gb300 import abi
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    lib = L.load()
+    pos, Lbox, x = make_inputs()
+    version, n = WORKLOAD["version"], WORKLOAD["n"]
+    sysm = L.System(version, pos, (Lbox,) * 3, tratio=WORKLOAD["tratio"], eps=WORKLOAD["eps"])
+    prec = abi.MIXED if args.precision == "mixed" else abi.FP64
+    sysm.set_precision(prec)
+
+    d_pos = torch.tensor(pos, dtype=torch.float64, device=dev).contiguous()
+    d_x = torch.tensor(x, dtype=torch.float64, device=dev)
+    d_y = torch.empty_like(d_x)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    # a dedicated stream: the library's kernels, the flush and the timing
+    # events all go to it (the legacy default stream would not order them)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def product():
+        abi.check(lib.stokes_gpu_atimes_dev(sysm.sp, C.c_void_p(d_pos.data_ptr()),
+                                            C.c_void_p(d_x.data_ptr()),
+                                            C.c_void_p(d_y.data_ptr()), sp))
+
+    for _ in range(args.warmup):
+        product()
+    torch.cuda.synchronize(dev)
+
+    # accuracy of this precision against the FP64 path on the same inputs
+    y_this = d_y.double().cpu().numpy()
+    if prec != abi.FP64:
+        ref = L.System(version, pos, (Lbox,) * 3, tratio=WORKLOAD["tratio"], eps=WORKLOAD["eps"])
+        y64 = ref.atimes(x)
+        ref.close()
+    else:
+        y64 = y_this
+    rel_err = float(np.linalg.norm(y_this - y64) / np.linalg.norm(y64))
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    abi.check(lib.stokes_gpu_profile_begin(sysm.sp, args.steps))
+    barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(gpu_pci_id(local)) as clk:
+        t_wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)            # evict L2 between steps (not timed)
+            starts[k].record(stream)
+            product()
+            ends[k].record(stream)
+        torch.cuda.synchronize(dev)
+        t_wall = time.perf_counter() - t_wall0
+        barrier()
+    prof = np.zeros(3)
+    cnt = C.c_int()
+    abi.check(lib.stokes_gpu_profile_end(sysm.sp, prof.ctypes.data_as(C.POINTER(C.c_double)),
+                                         C.byref(cnt)))
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1000.0 / ms
+    launches = C.c_int()
+    abi.check(lib.stokes_gpu_last_launches(sysm.sp, C.byref(launches)))
+
+    # end to end through the drop-in ABI with pinned host buffers
+    hx = torch.from_numpy(x).pin_memory()
+    hy = torch.empty(x.size, dtype=torch.float64).pin_memory()
+    px = C.cast(C.c_void_p(hx.data_ptr()), abi._dp)
+    py = C.cast(C.c_void_p(hy.data_ptr()), abi._dp)
+    nvec = x.size
+    for _ in range(max(1, args.warmup)):
+        lib.atimes_ewald_3all(nvec, px, py, C.cast(sysm.sp, C.c_void_p))
+    barrier()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lib.atimes_ewald_3all(nvec, px, py, C.cast(sysm.sp, C.c_void_p))
+    torch.cuda.synchronize(dev)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    abi.raise_if_failed()
+
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    # roofline of the dominant kernel (real space)
+    P = C.c_longlong()
+    abi.check(lib.stokes_gpu_count_real_terms(sysm.sp, C.byref(P)))
+    real_ms = prof[1] / max(cnt.value, 1)
+    recip_ms = prof[2] / max(cnt.value, 1)
+    total_ms = prof[0] / max(cnt.value, 1)
+    fp64 = prec == abi.FP64
+    peak = C.c_double()
+    abi.check(lib.stokes_gpu_peak_fma(1 if fp64 else 0, C.byref(peak)))
+    achieved = P.value * FLOPS_PER_TERM[version] / (real_ms * 1e-3) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        tt = json.load(open(tpath)).get(f"{WORKLOAD['name']}:{args.precision}:real")
+        traffic = tt
+    roof = {"kernel": "k_real (real-space pair sum)",
+            "bound": "fp64-pipe" if fp64 else "fp32-pipe",
+            "achieved": achieved, "peak": peak.value / 1e3, "unit": "TFLOP/s",
+            "frac": achieved / (peak.value / 1e3), "traffic": traffic,
+            "peak_source": ("measured in this run by an FMA-chain kernel "
+                            f"({'FP64' if fp64 else 'FP32'}); MEASURED_PEAKS.json holds only "
+                            "HBM copy and bf16 GEMM figures"),
+            "algorithmic": {"real_terms_per_launch": P.value,
+                            "flops_per_term": FLOPS_PER_TERM[version],
+                            "kernel_ms": real_ms}}
+    c = (3, 6, 11)[version]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if fp64 else "f32+bf16x3",
+        "data": "synthetic (seeded RSA placement, N(0,1) forces)",
+        "config": {"workload": WORKLOAD["name"], "version": "FTS", "n_particles": n,
+                   "phi": WORKLOAD["phi"], "box": Lbox, "xi": sysm.s.xi,
+                   "ewald_eps": WORKLOAD["eps"], "precision": args.precision,
+                   "n_images": sysm.s.nr, "real_terms": P.value,
+                   "l2": "flushed between steps by a 256 MiB write outside the per-step events",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "rel_err_vs_fp64": rel_err,
+        "phases_ms": {"total": total_ms, "real": real_ms, "reciprocal": recip_ms},
+        "wall_s_timed_region": t_wall,
+        "gpu_launches": launches.value * args.steps,
+        "e2e": {"value": world / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": 8 * (3 * n + c * n),
+                "d2h_bytes_per_step": 8 * c * n},
+        "roofline": roof,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(pos, Lbox, x)
+    sysm.close()
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n", type=int, default=None,
+                    help="override N (smaller cases for profiler captures)")
+    args = ap.parse_args()
+    if args.n is not None:
+        WORKLOAD["n"] = args.n
+        WORKLOAD["name"] = f"mob_fts_n{args.n}_phi{WORKLOAD['phi']:.2f}"
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -89,6 +89,10 @@ int stokes_gpu_last_launches (const struct stokes *sys, int *count);
  * unit count of the real-space roofline */
 int stokes_gpu_count_real_terms (struct stokes *sys, long long *count);
 
+/* split chosen by the mixed path for sys (after its first mixed product):
+ * xi, rc, kc, eta = xi V^(1/3), eps, half-space k count, max |m| per axis */
+int stokes_gpu_mixed_split (struct stokes *sys, double *info9);
+
 /* measured FMA throughput of the current GPU in GFLOP/s (2 flops per FMA),
  * fp64 = 1 for FP64, 0 for FP32 */
 int stokes_gpu_peak_fma (int fp64, double *gflops);

@@ -151,6 +151,7 @@ _SIGS = {
     "stokes_gpu_profile_end": (C.c_int, [_SP, _dp, _ip]),
     "stokes_gpu_count_real_terms": (C.c_int, [_SP, C.POINTER(C.c_longlong)]),
     "stokes_gpu_peak_fma": (C.c_int, [C.c_int, _dp]),
+    "stokes_gpu_mixed_split": (C.c_int, [_SP, _dp]),
 }
 
 _lib = None

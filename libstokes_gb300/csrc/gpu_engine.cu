@@ -295,6 +295,7 @@ prepare (Ctx *c, const struct stokes *sys, bool cube)
   if (rc) return rc;
   if (!cube && (sys->nr > 0) && (!sys->rlx || !sys->rly || !sys->rlz))
     return set_error (STOKES_GPU_EINVAL, "image table missing (stokes_set_xi not called?)");
+  c->sys = sys;
   c->version = sys->version;
   c->np = sys->np;
   c->mode = sys->slip ? MODE_SLIP : (sys->a ? MODE_POLY : MODE_MONO);

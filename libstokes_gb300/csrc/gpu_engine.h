@@ -28,6 +28,7 @@ struct Ctx {
   int precision = 0;
 
   // geometry of the last prepared system
+  const struct stokes *sys = nullptr;
   int version = 0, np = 0, mode = 0;
   double xi = 0, xisp = 0, rmax2 = 0, rmin = 0;
   int nimg = 0, nk = 0;

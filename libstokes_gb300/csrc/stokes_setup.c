@@ -210,6 +210,25 @@ est_recip (double k, double xi)
     * (1.0 + u2 * (1.0 / 4.0 + u2 / 8.0));
 }
 
+/* Cutoffs of the reference's search for a given split xi and tolerance eps
+ * (same estimators and shrink rule as stokes_set_xi).  Internal: the mixed
+ * path uses it to size its own, re-tuned split. */
+void
+lsg_ewald_cutoffs (double xi, double eps, double lmin, double lmax, double *rmax_out,
+                   double *kmax_out)
+{
+  const double shrink = 0.99;
+  double rmax = 10.0 * sqrt (-log (eps)) / xi;
+  while (est_real (rmax * shrink, xi) + 6.0 * est_real (rmax * shrink + lmin, xi) < eps)
+    rmax *= shrink;
+  const double dk = 2.0 * M_PI / lmax;
+  double kmax = 10.0 * sqrt (-log (eps)) * 2.0 * xi;
+  while (est_recip (kmax * shrink, xi) + 6.0 * est_recip (kmax * shrink + dk, xi) < eps)
+    kmax *= shrink;
+  *rmax_out = rmax;
+  *kmax_out = kmax;
+}
+
 /* The reciprocal table (ex..ym, src/stokes.c:236-307) is filled as in the
  * reference for callers that read it; the GPU product does not. */
 static void

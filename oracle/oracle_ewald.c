@@ -431,18 +431,64 @@ store_out (int version, const double *U, const double *W, double E[3][3],
   y[9] += E[1][2]; y[10] += E[1][1];
 }
 
-/* one pair term on vectors: y_i += block(e, s) . x_j */
+/* one pair term on vectors: y_i += block(e, s) . x_j.  Same algebra as
+ * pair_apply, unrolled for the symmetric S' of the product so that the CPU
+ * cost per term stays close to the reference's. */
 static void
 pair_vec (int version, const double *e, const double *s, const double *xj,
           double *yi)
 {
-  double U[3] = {0, 0, 0}, W[3] = {0, 0, 0}, E[3][3] = {{0}};
-  double T0[3] = {0, 0, 0};
-  double S[3][3] = {{0}};
-  const double *T = (version >= 1) ? xj + 3 : T0;
-  if (version == 2) stress_full (xj + 6, S);
-  pair_apply (version, e, s, xj, T, S, U, W, E, 1.0, 1.0);
-  store_out (version, U, W, E, yi);
+  const double *F = xj;
+  double eF = dot3 (e, F);
+  double a2 = s[XA] - s[YA];
+  yi[0] += s[YA] * F[0] + a2 * eF * e[0];
+  yi[1] += s[YA] * F[1] + a2 * eF * e[1];
+  yi[2] += s[YA] * F[2] + a2 * eF * e[2];
+  if (version == 0) return;
+
+  const double *T = xj + 3;
+  double Fxe[3], Txe[3];
+  cross3 (F, e, Fxe);
+  cross3 (T, e, Txe);
+  double eT = dot3 (e, T);
+  double c2 = s[XC] - s[YC];
+  for (int a = 0; a < 3; a++)
+    {
+      yi[a] += s[YB] * Txe[a];
+      yi[3 + a] += s[YB] * Fxe[a] + s[YC] * T[a] + c2 * eT * e[a];
+    }
+  if (version == 1) return;
+
+  double S[3][3];
+  stress_full (xj + 6, S);
+  double Se[3];
+  for (int a = 0; a < 3; a++) Se[a] = S[a][0] * e[0] + S[a][1] * e[1] + S[a][2] * e[2];
+  double eSe = dot3 (e, Se), trS = S[0][0] + S[1][1];
+  double g1 = -s[XG] / 3.0, g2 = s[YG], g3 = s[XG] - 2.0 * s[YG];
+  double m1 = 1.5 * s[XM] - 2.0 * s[YM] + 0.5 * s[ZM];
+  double m2 = -0.5 * s[XM] + 0.5 * s[ZM];
+  double m3 = s[XM] / 6.0 - 0.5 * s[ZM];
+  double m4 = 0.5 * s[YM] - 0.5 * s[ZM];
+  double m5 = 0.5 * s[ZM];
+  double v[3];
+  cross3 (e, Se, v);
+  double gu = g1 * trS + g3 * eSe;
+  double d = g1 * eF + m2 * eSe + m3 * trS;     /* delta_ab coefficient */
+  double q = g3 * eF + m1 * eSe + m2 * trS;     /* e_a e_b coefficient */
+  double V[3];                                  /* e_a V_b + e_b V_a */
+  for (int a = 0; a < 3; a++)
+    {
+      yi[a] -= gu * e[a] + 2.0 * g2 * Se[a];
+      yi[3 + a] += 2.0 * s[YH] * v[a];
+      V[a] = g2 * F[a] + s[YH] * Txe[a] + 2.0 * m4 * Se[a];
+    }
+  static const int ia[5] = {0, 0, 0, 1, 1}, ib[5] = {0, 1, 2, 2, 1};
+  for (int k = 0; k < 5; k++)
+    {
+      int a = ia[k], b = ib[k];
+      yi[6 + k] += (a == b ? d : 0.0) + q * e[a] * e[b] + e[a] * V[b] + e[b] * V[a]
+        + 2.0 * m5 * S[a][b];
+    }
 }
 
 /* one pair term on the dense matrix: block (i, j) += block(e, s), written
