@@ -63,6 +63,20 @@ int stokes_gpu_atimes (struct stokes *sys, const double *x, double *y);
 int stokes_gpu_atimes_dev (struct stokes *sys, const double *d_pos,
                            const double *d_x, double *d_y, void *stream);
 
+/* y = M x in FP64 without allocating device memory.  No counterpart in
+ * libstokes.  For callers that may not allocate on the device while they
+ * run (a fixed memory budget owned by another framework, steps that must
+ * never enter the driver's allocator): all scratch lives in one fixed
+ * 5.05 MiB device array per GPU, reserved when the library is loaded.
+ * Limits: np <= 512, at most 2048 real-space images and 512 reciprocal
+ * vectors; larger systems get STOKES_GPU_ETOOBIG.  d_pos [np*3], d_x, d_y
+ * [np*{3,6,11}] are device buffers of the caller; stream may be NULL (the
+ * default stream).  The first call on a device looks up the array's
+ * address; make it before any stream capture.  All calls share the array:
+ * calls that overlap on one GPU race on it. */
+int stokes_gpu_atimes_noalloc (struct stokes *sys, const double *d_pos,
+                               const double *d_x, double *d_y, void *stream);
+
 /* dense mobility matrix with host / device output */
 int stokes_gpu_matrix (struct stokes *sys, double *mat);
 int stokes_gpu_matrix_dev (struct stokes *sys, const double *d_pos,

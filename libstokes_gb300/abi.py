@@ -141,6 +141,8 @@ _SIGS = {
     "stokes_gpu_release": (C.c_int, [_SP]),
     "stokes_gpu_atimes": (C.c_int, [_SP, _dp, _dp]),
     "stokes_gpu_atimes_dev": (C.c_int, [_SP, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "stokes_gpu_atimes_noalloc": (C.c_int, [_SP, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p]),
     "stokes_gpu_matrix": (C.c_int, [_SP, _dp]),
     "stokes_gpu_matrix_dev": (C.c_int, [_SP, C.c_void_p, C.c_void_p, C.c_void_p]),
     "stokes_gpu_matvec_dev": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p,
