@@ -107,6 +107,11 @@ int stokes_gpu_count_real_terms (struct stokes *sys, long long *count);
  * xi, rc, kc, eta = xi V^(1/3), eps, half-space k count, max |m| per axis */
 int stokes_gpu_mixed_split (struct stokes *sys, double *info9);
 
+/* known-answer test of the tensor-core (tcgen05, 3xTF32) path on the
+ * current GPU: largest error of a 128x16x32 product relative to the sum of
+ * absolute products (expect ~1e-7) */
+int stokes_gpu_selftest_tensor (double *max_rel_err);
+
 /* measured FMA throughput of the current GPU in GFLOP/s (2 flops per FMA),
  * fp64 = 1 for FP64, 0 for FP32 */
 int stokes_gpu_peak_fma (int fp64, double *gflops);

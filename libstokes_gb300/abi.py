@@ -88,6 +88,19 @@ class StokesStruct(C.Structure):
     ]
 
 
+class BDParams(C.Structure):
+    """struct stokes_gpu_bd_params (include/stokes_bd.h)."""
+    _fields_ = [("peclet", C.c_double), ("dt", C.c_double), ("n_cheb", C.c_int),
+                ("n_lanczos", C.c_int), ("cheb_eps", C.c_double), ("check_every", C.c_int),
+                ("lj_e", C.c_double), ("lj_r0", C.c_double), ("seed", C.c_ulonglong),
+                ("precision", C.c_int)]
+
+
+class KIrandStruct(C.Structure):
+    _fields_ = [("mt", C.c_ulong * 624), ("mti", C.c_int), ("Gaussian_has_saved", C.c_int),
+                ("Gaussian_saved", C.c_double)]
+
+
 _SP = C.POINTER(StokesStruct)
 ATIMES = C.CFUNCTYPE(None, C.c_int, _dp, _dp, C.c_void_p)
 FUNC1 = C.CFUNCTYPE(C.c_double, C.c_double)
@@ -154,6 +167,26 @@ _SIGS = {
     "stokes_gpu_count_real_terms": (C.c_int, [_SP, C.POINTER(C.c_longlong)]),
     "stokes_gpu_peak_fma": (C.c_int, [C.c_int, _dp]),
     "stokes_gpu_mixed_split": (C.c_int, [_SP, _dp]),
+    "stokes_gpu_selftest_tensor": (C.c_int, [_dp]),
+    # Brownian dynamics
+    "KIrand_init": (C.POINTER(KIrandStruct), []),
+    "KIrand_free": (None, [C.POINTER(KIrandStruct)]),
+    "KIrand_init_genrand": (None, [C.POINTER(KIrandStruct), C.c_ulong]),
+    "KIrand_genrand_int32": (C.c_ulong, [C.POINTER(KIrandStruct)]),
+    "KIrand_genrand_res53": (C.c_double, [C.POINTER(KIrandStruct)]),
+    "KIrand_genrand_real2": (C.c_double, [C.POINTER(KIrandStruct)]),
+    "KIrand_Gaussian": (C.c_double, [C.POINTER(KIrandStruct)]),
+    "stokes_gpu_bd_create": (C.c_int, [_SP, C.POINTER(BDParams), C.POINTER(C.c_void_p)]),
+    "stokes_gpu_bd_destroy": (C.c_int, [C.c_void_p]),
+    "stokes_gpu_bd_set_positions": (C.c_int, [C.c_void_p, _dp]),
+    "stokes_gpu_bd_get_positions": (C.c_int, [C.c_void_p, _dp]),
+    "stokes_gpu_bd_set_force": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "stokes_gpu_bd_estimate_bounds": (C.c_int, [C.c_void_p, _dp]),
+    "stokes_gpu_bd_set_bounds": (C.c_int, [C.c_void_p, _dp]),
+    "stokes_gpu_bd_noise": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "stokes_gpu_bd_step_noise": (C.c_int, [C.c_void_p, C.c_double, _dp]),
+    "stokes_gpu_bd_run": (C.c_int, [C.c_void_p, C.c_double, C.c_int]),
+    "stokes_gpu_bd_stats": (C.c_int, [C.c_void_p, _dp]),
 }
 
 _lib = None

@@ -25,20 +25,13 @@
 
 #include "ewald_device.cuh"
 #include "gpu_engine.h"
+#include "mixed.h"
 #include "stokes_gpu.h"
 
 extern "C" void lsg_ewald_cutoffs (double xi, double eps, double lmin, double lmax,
                                    double *rmax_out, double *kmax_out);
 
 namespace lsg {
-
-// one half-space reciprocal vector (64 bytes)
-struct __align__ (16) MixK {
-  int m1, m2, m3, pad;
-  float ex, ey, ez;
-  float ya, yb, yc, yg, yh, ym;
-  float f0, f1, f2;
-};
 
 struct MixedState {
   uint64_t fp = 0;
@@ -48,7 +41,9 @@ struct MixedState {
   int nk_split = 0;      // rows of the re-tuned split; the rest: reference G term
   double selfc[3] = {0, 0, 0};
   std::vector<MixK> h_k;
-  DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf;
+  DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf, status;
+  int *h_status = nullptr;      // pinned copy of the kernels' status word
+  bool tensor = true;           // reciprocal space on the tensor cores
   uint64_t self_fp = 0;
   int self_np = 0;
   int nchunk_r = 1, nchunk_k = 1;
@@ -600,9 +595,37 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   const int np = c->np, C = NCOMP (c->version);
   const int ntab = (m->M[0] + 1) + (m->M[1] + 1) + (m->M[2] + 1);
   m->nchunk_r = std::max (1, std::min (64, (152 * 48 + np - 1) / np));
-  m->nchunk_k = std::max (1, std::min (64, (152 * 48 + np - 1) / np));
-  if (m->nchunk_k * 32 > m->nkh) m->nchunk_k = std::max (1, m->nkh / 32);
+  {
+    const char *ks = getenv ("LIBSTOKES_GB300_KSPACE");
+    m->tensor = (ks && strcmp (ks, "tc") == 0);
+  }
+  if (m->tensor)
+    {
+      m->nchunk_k = backproj_splits (np, m->nkh);
+      if (ntab > 150)
+        return set_error (STOKES_GPU_ETOOBIG, "mixed split: %d phase-table rows (at most 150)", ntab);
+    }
+  else
+    {
+      m->nchunk_k = std::max (1, std::min (64, (152 * 48 + np - 1) / np));
+      if (m->nchunk_k * 32 > m->nkh) m->nchunk_k = std::max (1, m->nkh / 32);
+    }
+  // a status word raised by a bounded device wait of the previous product
+  if (m->h_status && *m->h_status)
+    {
+      *m->h_status = 0;
+      cudaMemsetAsync (m->status.p, 0, sizeof (int), st);
+      return set_error (STOKES_GPU_ETIMEOUT,
+                        "a tensor-core wait of the previous mixed product ran out");
+    }
   cudaError_t e;
+  if (!m->h_status)
+    {
+      if ((e = cudaMallocHost (&m->h_status, sizeof (int))) != cudaSuccess) return cuda_fail (e, "status");
+      *m->h_status = 0;
+      if ((e = m->status.ensure (sizeof (int))) != cudaSuccess) return cuda_fail (e, "status");
+      cudaMemsetAsync (m->status.p, 0, sizeof (int), st);
+    }
   if ((e = m->qpos.ensure (sizeof (uint32_t) * 4 * np)) != cudaSuccess) return cuda_fail (e, "qpos");
   if ((e = m->tab.ensure (sizeof (float2) * (size_t) ntab * np)) != cudaSuccess) return cuda_fail (e, "phase tables");
   if ((e = m->xf.ensure (sizeof (float) * (size_t) C * np)) != cudaSuccess) return cuda_fail (e, "xf");
@@ -633,7 +656,17 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   ba.off1 = off1; ba.off2 = off2; ba.partial = (float *) m->part_rec.p;
   const int gk = (m->nkh + MX_WARPS - 1) / MX_WARPS;
   const int gb = (int) (((long long) np * m->nchunk_k + MX_WARPS - 1) / MX_WARPS);
-  if (m->nkh > 0)
+  if (m->nkh > 0 && m->tensor)
+    {
+      PhaseTables pt{(const float2 *) m->tab.p, off1, off2, m->M[0], m->M[1], m->M[2], np};
+      if ((e = launch_sfac_tc (c->version, ka.kt, m->nkh, pt, ka.xf, ka.pq, (int *) m->status.p,
+                               st)) != cudaSuccess)
+        return cuda_fail (e, "reciprocal forward (tensor cores)");
+      if ((e = launch_backproj_tc (c->version, ka.kt, m->nkh, pt, ka.pq, m->nchunk_k,
+                                   (float *) m->part_rec.p, (int *) m->status.p, st)) != cudaSuccess)
+        return cuda_fail (e, "reciprocal back-projection (tensor cores)");
+    }
+  else if (m->nkh > 0)
     {
       if (c->version == 0) { mk_sfac<0><<<gk, MX_WARPS * 32, 0, st>>> (ka); mk_backproj<0><<<gb, MX_WARPS * 32, 0, st>>> (ba); }
       else if (c->version == 1) { mk_sfac<1><<<gk, MX_WARPS * 32, 0, st>>> (ka); mk_backproj<1><<<gb, MX_WARPS * 32, 0, st>>> (ba); }
@@ -689,6 +722,8 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   else if (c->version == 1) mk_combine<1><<<gc, 128, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
   else mk_combine<2><<<gc, 128, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
   if (E) cudaEventRecord (E[3], st);
+  if (m->tensor)
+    cudaMemcpyAsync (m->h_status, m->status.p, sizeof (int), cudaMemcpyDeviceToHost, st);
   e = cudaGetLastError ();
   if (e != cudaSuccess) return cuda_fail (e, "mixed kernels");
   c->launches = (m->nkh > 0 ? 5 : 3);
@@ -708,8 +743,9 @@ release_mixed (Ctx *c)
   if (!c->mixed) return;
   MixedState *m = c->mixed;
   for (DevBuf *b : {&m->kt, &m->qpos, &m->tab, &m->xf, &m->pq, &m->part_real, &m->part_rec,
-                    &m->selfbuf})
+                    &m->selfbuf, &m->status})
     b->release ();
+  if (m->h_status) cudaFreeHost (m->h_status);
   delete m;
   c->mixed = nullptr;
 }

@@ -187,6 +187,12 @@ class Oracle(_Backend):
             lib.oracle_count_k.argtypes = [C.c_void_p]
             lib.oracle_xi_by_tratio.restype = C.c_double
             lib.oracle_xi_by_tratio.argtypes = [C.c_double] * 4
+            lib.oracle_cheb_eval.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, C.c_double,
+                                             C.c_double, _dp, _dp]
+            lib.oracle_bd_step.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double,
+                                           C.c_double, C.c_double, C.c_double, C.c_int, _dp,
+                                           C.c_double, C.c_double, _dp, _dp, C.c_double,
+                                           C.c_double, _dp, _dp]
         return cls._lib
 
     def set_threads(self, n):
@@ -204,6 +210,28 @@ class Oracle(_Backend):
         y = np.zeros(self.n)
         self._L.oracle_atimes_rows(self.h, _d(x), _d(y), int(i0), int(i1))
         return y
+
+    def cheb_eval(self, a, e0, e1, y):
+        """z = sum_k a_k T_k(M~) y by Clenshaw (src/chebyshev.c:163-228)."""
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        z = np.zeros(self.n)
+        self._L.oracle_cheb_eval(self.h, self.n, len(a), _d(a), float(e0), float(e1), _d(y),
+                                 _d(z))
+        return z
+
+    def bd_step(self, x, dt, peclet, a, e0, e1, y, F=None, lj_e=0.0, lj_r0=2.0):
+        """One mid-point step from positions x with noise y; returns (x_new, z)."""
+        x = np.array(x, dtype=np.float64).reshape(-1).copy()
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        Fp = None if F is None else np.ascontiguousarray(F, dtype=np.float64)
+        z = np.zeros(self.n)
+        self._L.oracle_bd_step(self.h, self.version, self.np, *self.box, float(dt),
+                               float(peclet), len(a), _d(a), float(e0), float(e1), _d(y),
+                               None if Fp is None else _d(Fp), float(lj_e), float(lj_r0),
+                               _d(x), _d(z))
+        return x, z
 
     def count_real_terms(self):
         return int(self._L.oracle_count_real_terms(self.h))

@@ -62,6 +62,34 @@ def layout(ref_root: str) -> dict:
         return json.loads(subprocess.check_output([exe]).decode())
 
 
+BD_FIELDS = ["sys", "rng", "F", "T", "E", "uf", "of", "ef", "flag_noHI", "flag_mat",
+             "flag_lub", "flag_lub_B", "t0", "s0", "st", "br", "bonds", "groups", "gamma", "ev",
+             "ang", "ev_dh", "ev_LJ", "cf", "flag_Q", "peclet", "eps", "n_minv", "eig_minv",
+             "a_minv", "n_lub", "eig_lub", "a_lub", "scheme", "BB_n", "rmin", "dt_lim"]
+
+
+def bd_layouts(ref_root: str) -> dict:
+    src = ["#include <stdio.h>", "#include <stddef.h>", '#include "stokes.h"',
+           '#include "KIrand.h"', '#include "ev-LJ.h"', '#include "brownian.h"',
+           "int main(void){", 'printf("{");']
+    items = [("BD_params", f) for f in BD_FIELDS]
+    items += [("KIrand", f) for f in ("mt", "mti", "Gaussian_has_saved", "Gaussian_saved")]
+    items += [("EV_LJ", f) for f in ("n", "flag", "e", "r0")]
+    for k, (st, f) in enumerate(items):
+        sep = "" if k == 0 else ", "
+        src.append(f'printf("{sep}\\"{st}.{f}\\": %zu", offsetof(struct {st}, {f}));')
+    for st in ("BD_params", "KIrand", "EV_LJ"):
+        src.append(f'printf(", \\"{st}.sizeof\\": %zu", sizeof(struct {st}));')
+    src += ['printf("}\\n");', "return 0;}"]
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "lay.c")
+        exe = os.path.join(d, "lay")
+        open(c, "w").write("\n".join(src))
+        subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "oracle", "ref_stubs", "inc"),
+                               "-I", os.path.join(ref_root, "src"), c, "-o", exe])
+        return json.loads(subprocess.check_output([exe]).decode())
+
+
 def mk(version, pos, box, tratio=1.0, eps=1e-12, a=None, slip=None, shear=(0, 0.0),
        rmin=0.0, cube=None):
     r = Reference(version, pos, box)
@@ -221,6 +249,29 @@ def main(ref_root: str = "/root/reference"):
     ch.update(ewald_pos=pos, ewald_box=np.array(box), ewald_y=y, ewald_z=z,
               ewald_err=err.copy(), ewald_a=a, ewald_e=np.array([e0, e1]))
     np.savez_compressed(os.path.join(HERE, "chebyshev.npz"), **ch)
+
+    # ---- KIrand (MT19937 + polar Box-Muller) ------------------------------
+    ki = {}
+    for seed in (1, 1234, 4357):
+        st = lib.KIrand_init
+        st.restype = C.c_void_p
+        r = C.c_void_p(st())
+        lib.KIrand_init_genrand.argtypes = [C.c_void_p, C.c_ulong]
+        lib.KIrand_genrand_int32.argtypes = [C.c_void_p]
+        lib.KIrand_genrand_int32.restype = C.c_ulong
+        lib.KIrand_genrand_res53.argtypes = [C.c_void_p]
+        lib.KIrand_genrand_res53.restype = C.c_double
+        lib.KIrand_Gaussian.argtypes = [C.c_void_p]
+        lib.KIrand_Gaussian.restype = C.c_double
+        lib.KIrand_init_genrand(r, seed)
+        ki[f"s{seed}_int32"] = np.array([lib.KIrand_genrand_int32(r) for _ in range(700)],
+                                        dtype=np.uint64)
+        ki[f"s{seed}_res53"] = np.array([lib.KIrand_genrand_res53(r) for _ in range(50)])
+        ki[f"s{seed}_gauss"] = np.array([lib.KIrand_Gaussian(r) for _ in range(101)])
+    np.savez_compressed(os.path.join(HERE, "kirand.npz"), **ki)
+
+    # ---- struct layouts of the Brownian-dynamics interface ---------------
+    json.dump(bd_layouts(ref_root), open(os.path.join(HERE, "bd_layouts.json"), "w"), indent=1)
     print("golden fixtures written to", HERE)
 
 
