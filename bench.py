@@ -146,6 +146,47 @@ def cpu_baseline(pos, L, x, budget_s: float = 3.0):
                       f"value = (rows/N)/time"}
 
 
+BD_WORKLOAD = dict(name="bd_f_n4096_phi0.20", version=0, n=4096, phi=0.20, seed=42, dt=1e-3,
+                   peclet=1.0, n_cheb=30, n_lanczos=20, lj_e=1.0, lj_r0=2.0, rmin=1.0, warm=1,
+                   steps=5)
+
+
+def bd_measure(lib, abi, L, torch, dev):
+    """Brownian-dynamics steps/s: F spheres N=4096 at phi 0.20, dt 1e-3, kT 1
+    (Pe 1), Chebyshev order 30 on 20-step Lanczos bounds, EV_LJ repulsion at
+    r < 2 (e = 1, r0 = 2), noise from the device generator (float32)."""
+    from libstokes_gb300.workloads import rsa_positions
+    w = BD_WORKLOAD
+    pos, Lb = rsa_positions(w["n"], w["phi"], seed=w["seed"])
+    s = L.System(w["version"], pos, (Lb,) * 3)
+    # real-space distances clamped at contact (libstokes' sys->rmin = 1): the
+    # soft repulsion lets spheres overlap, where the unclamped far-field
+    # mobility is not positive definite
+    s.set_misc(rmin=w["rmin"])
+    p = abi.BDParams(peclet=w["peclet"], dt=w["dt"], n_cheb=w["n_cheb"],
+                     n_lanczos=w["n_lanczos"], cheb_eps=1e-2, check_every=1, lj_e=w["lj_e"],
+                     lj_r0=w["lj_r0"], seed=12345, precision=abi.MIXED)
+    h = C.c_void_p()
+    abi.check(lib.stokes_gpu_bd_create(s.sp, C.byref(p), C.byref(h)))
+    abi.check(lib.stokes_gpu_bd_run(h, 0.0, w["warm"]))      # includes the Lanczos bounds
+    st0 = np.zeros(4)
+    abi.check(lib.stokes_gpu_bd_stats(h, st0.ctypes.data_as(abi._dp)))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    abi.check(lib.stokes_gpu_bd_run(h, w["warm"] * w["dt"], w["steps"]))
+    dt_wall = time.perf_counter() - t0
+    st = np.zeros(4)
+    abi.check(lib.stokes_gpu_bd_stats(h, st.ctypes.data_as(abi._dp)))
+    abi.check(lib.stokes_gpu_bd_destroy(h))
+    s.close()
+    return {"workload": w["name"], "steps_per_s": w["steps"] / dt_wall,
+            "ms_per_step": 1000.0 * dt_wall / w["steps"], "steps_timed": w["steps"],
+            "products_per_step": (st[0] - st0[0]) / w["steps"], "cheb_err_last": st[2],
+            "precision": "mixed", "timing": "wall clock around the device-resident run",
+            "params": {k: w[k] for k in ("dt", "peclet", "n_cheb", "n_lanczos", "lj_e", "lj_r0",
+                                         "rmin")}}
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU algorithm (the oracle port; the
     reference sources themselves are not on this machine) on the host cores."""
@@ -300,42 +341,53 @@ def run_gpu(args):
             dist.destroy_process_group()
         return
 
-    # roofline of the dominant kernel (real space)
-    P = C.c_longlong()
-    abi.check(lib.stokes_gpu_count_real_terms(sysm.sp, C.byref(P)))
+    c = (3, 6, 11)[version]
     real_ms = prof[1] / max(cnt.value, 1)
     recip_ms = prof[2] / max(cnt.value, 1)
     total_ms = prof[0] / max(cnt.value, 1)
     fp64 = prec == abi.FP64
     peak = C.c_double()
     abi.check(lib.stokes_gpu_peak_fma(1 if fp64 else 0, C.byref(peak)))
-    achieved = P.value * FLOPS_PER_TERM[version] / (real_ms * 1e-3) / 1e12
+    peak_tf = peak.value / 1e3
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        tt = json.load(open(tpath)).get(f"{WORKLOAD['name']}:{args.precision}:real")
-        traffic = tt
-    roof = {"kernel": "k_real (real-space pair sum)",
-            "bound": "fp64-pipe" if fp64 else "fp32-pipe",
-            "achieved": achieved, "peak": peak.value / 1e3, "unit": "TFLOP/s",
-            "frac": achieved / (peak.value / 1e3), "traffic": traffic,
-            "peak_source": ("measured in this run by an FMA-chain kernel "
-                            f"({'FP64' if fp64 else 'FP32'}); MEASURED_PEAKS.json holds only "
-                            "HBM copy and bf16 GEMM figures"),
-            "algorithmic": {"real_terms_per_launch": P.value,
-                            "flops_per_term": FLOPS_PER_TERM[version],
-                            "kernel_ms": real_ms}}
-    c = (3, 6, 11)[version]
+        traffic = json.load(open(tpath)).get(f"{WORKLOAD['name']}:{args.precision}")
+    if fp64:
+        # dominant: the real-space pair sum over the reference's image table
+        P = C.c_longlong()
+        abi.check(lib.stokes_gpu_count_real_terms(sysm.sp, C.byref(P)))
+        achieved = P.value * FLOPS_PER_TERM[version] / (real_ms * 1e-3) / 1e12
+        roof = {"kernel": "k_real (real-space pair sum, FP64)", "bound": "fp64-pipe",
+                "algorithmic": {"unit": "pair term", "units_per_launch": P.value,
+                                "flops_per_unit": FLOPS_PER_TERM[version], "kernel_ms": real_ms}}
+    else:
+        # dominant: reciprocal space (structure factors + back-projection)
+        info = np.zeros(9)
+        abi.check(lib.stokes_gpu_mixed_split(sysm.sp, info.ctypes.data_as(abi._dp)))
+        nk_full = 2 * int(info[5])
+        achieved = 8.0 * nk_full * n * c / (recip_ms * 1e-3) / 1e12
+        roof = {"kernel": "reciprocal space (mk_sfac + mk_backproj, FP32)", "bound": "fp32-pipe",
+                "algorithmic": {"unit": "k vector x particle x component",
+                                "units_per_launch": nk_full * n * c, "flops_per_unit": 8,
+                                "kernel_ms": recip_ms, "k_vectors": nk_full,
+                                "mixed_split": {"xi": info[0], "rc": info[1], "kc": info[2],
+                                                "eta": info[3], "eps": info[4]}}}
+    roof.update({"achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
+                 "frac": achieved / peak_tf, "traffic": traffic,
+                 "peak_source": ("measured in this run by an FMA-chain kernel "
+                                 f"({'FP64' if fp64 else 'FP32'}); MEASURED_PEAKS.json holds "
+                                 "only the HBM copy and bf16 GEMM figures")})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if fp64 else "f32+bf16x3",
+        "dtype": "f64" if fp64 else "f32 (self term and final sum f64)",
         "data": "synthetic (seeded RSA placement, N(0,1) forces)",
         "config": {"workload": WORKLOAD["name"], "version": "FTS", "n_particles": n,
                    "phi": WORKLOAD["phi"], "box": Lbox, "xi": sysm.s.xi,
                    "ewald_eps": WORKLOAD["eps"], "precision": args.precision,
-                   "n_images": sysm.s.nr, "real_terms": P.value,
+                   "n_images": sysm.s.nr,
                    "l2": "flushed between steps by a 256 MiB write outside the per-step events",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "rel_err_vs_fp64": rel_err,
@@ -348,6 +400,23 @@ def run_gpu(args):
         "roofline": roof,
         "clocks": clk.summary(),
     }
+    if not fp64 and not args.no_fp64_compare:
+        # the plain FP64 path on the same inputs, for the mixed/FP64 ratio
+        sysm.set_precision(abi.FP64)
+        for _ in range(1):
+            product()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            product()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        fp64_ms = e0.elapsed_time(e1) / 3
+        line["fp64_path"] = {"value": 1000.0 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
+                             "mixed_over_fp64": (1000.0 / ms) / (1000.0 / fp64_ms)}
+    if not args.no_bd:
+        line["bd"] = bd_measure(lib, abi, L, torch, dev)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, Lbox, x)
     sysm.close()
@@ -365,6 +434,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-bd", action="store_true", help="skip the Brownian-dynamics leg")
+    ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--n", type=int, default=None,
                     help="override N (smaller cases for profiler captures)")
     args = ap.parse_args()

@@ -284,8 +284,9 @@ bd_error (stokes_gpu_bd *b, const double *d_pos, double *err)
   cudaError_t e = cudaStreamSynchronize (st);
   if (e != cudaSuccess) return cuda_fail (e, "Chebyshev error");
   const double zz = b->h_dots[0], yyv = b->h_dots[2];
-  if (!(zz > 0.0)) return set_error (STOKES_GPU_EACCURACY, "non-positive z.Mz = %g", zz);
-  *err = fabs (zz - yyv) / zz;
+  // a non-positive z.Mz means the noise left the bounds' interval: infinite
+  // error, which makes the caller re-estimate the bounds
+  *err = (zz > 0.0) ? fabs (zz - yyv) / zz : HUGE_VAL;
   return STOKES_GPU_OK;
 }
 
@@ -462,6 +463,10 @@ bd_step (stokes_gpu_bd *b, double t)
           if ((rc = bd_noise (b, x))) return rc;
           if ((rc = bd_error (b, x, &err))) return rc;
           b->last_err = err;
+          if (!(err < HUGE_VAL))
+            return set_error (STOKES_GPU_EACCURACY,
+                              "non-positive z.Mz after re-estimating the bounds: the mobility "
+                              "is not positive definite (overlapping spheres; set rmin)");
         }
     }
   const Flow fl0 = bd_flow (b->sys);

@@ -41,9 +41,11 @@ struct MixedState {
   int nk_split = 0;      // rows of the re-tuned split; the rest: reference G term
   double selfc[3] = {0, 0, 0};
   std::vector<MixK> h_k;
-  DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf, status;
+  DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf, status, sf, wop, rowm;
+  int nrow = 0;          // (m2, m3) rows of the tensor-core contraction
   int *h_status = nullptr;      // pinned copy of the kernels' status word
   bool tensor = true;           // reciprocal space on the tensor cores
+  KGemm plan;
   uint64_t self_fp = 0;
   int self_np = 0;
   int nchunk_r = 1, nchunk_k = 1;
@@ -395,15 +397,32 @@ mk_backproj (BpMixArgs a)
     }
 }
 
-// y_i = self_i x_i (FP64) + sum real partials + 2 sum reciprocal partials
+// y_i = self_i x_i (FP64) + sum real partials + 2 sum reciprocal partials;
+// one warp per particle, the lanes split the partial chunks
 template <int V>
 __global__ void
 mk_combine (const double *x, const float *pr, int ncr, const float *pk, int nck,
             const double *selfc, int np, double *y)
 {
   constexpr int C = NComp<V>::value;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (i >= np) return;
+  double sr[C], sk[C];
+#pragma unroll
+  for (int q = 0; q < C; q++) sr[q] = sk[q] = 0.0;
+  for (int c = lane; c < ncr; c += 32)
+#pragma unroll
+    for (int q = 0; q < C; q++) sr[q] += (double) pr[((size_t) c * np + i) * C + q];
+  for (int c = lane; c < nck; c += 32)
+#pragma unroll
+    for (int q = 0; q < C; q++) sk[q] += (double) pk[((size_t) c * np + i) * C + q];
+#pragma unroll
+  for (int q = 0; q < C; q++)
+    {
+      sr[q] = warp_sum (sr[q]);
+      sk[q] = warp_sum (sk[q]);
+    }
   PairScalars<double> s;
   s.xa = s.ya = selfc[3 * i];
   s.xc = s.yc = selfc[3 * i + 1];
@@ -417,12 +436,7 @@ mk_combine (const double *x, const float *pr, int ncr, const float *pk, int nck,
   pair_apply<V, double> (e, s, g, acc);
 #pragma unroll
   for (int q = 0; q < C; q++)
-    {
-      double v = acc.v[q], r = 0.0, k = 0.0;
-      for (int c = 0; c < ncr; c++) r += (double) pr[((size_t) c * np + i) * C + q];
-      for (int c = 0; c < nck; c++) k += (double) pk[((size_t) c * np + i) * C + q];
-      y[(size_t) C * i + q] = v + r + 2.0 * k;
-    }
+    if (lane == q) y[(size_t) C * i + q] = acc.v[q] + sr[q] + 2.0 * sk[q];
 }
 
 // ---------------------------------------------------------------------------
@@ -567,7 +581,28 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
     return set_error (STOKES_GPU_ETOOBIG, "mixed split: |m| above %d", MX_MTAB);
   m->M[0] = M[0]; m->M[1] = M[1]; m->M[2] = M[2];
   m->nkh = (int) m->h_k.size ();
-  cudaError_t e = m->kt.ensure (sizeof (MixK) * (m->nkh > 0 ? m->nkh : 1));
+  // rows of the tensor-core contraction: the (m2, m3) combinations in use,
+  // in (m2, m3) order
+  std::vector<int> rowid ((size_t) (2 * M[1] + 1) * (2 * M[2] + 1), -1);
+  for (const MixK &k : m->h_k) rowid[(size_t) (k.m2 + M[1]) * (2 * M[2] + 1) + (k.m3 + M[2])] = 0;
+  std::vector<int2> rows;
+  for (int a = -M[1]; a <= M[1]; a++)
+    for (int b = -M[2]; b <= M[2]; b++)
+      {
+        int &id = rowid[(size_t) (a + M[1]) * (2 * M[2] + 1) + (b + M[2])];
+        if (id < 0) continue;
+        id = (int) rows.size ();
+        rows.push_back (make_int2 (a, b));
+      }
+  for (MixK &k : m->h_k) k.r = rowid[(size_t) (k.m2 + M[1]) * (2 * M[2] + 1) + (k.m3 + M[2])];
+  m->nrow = (int) rows.size ();
+  cudaError_t e = m->rowm.ensure (sizeof (int2) * (rows.empty () ? 1 : rows.size ()));
+  if (e == cudaSuccess && !rows.empty ())
+    e = cudaMemcpyAsync (m->rowm.p, rows.data (), sizeof (int2) * rows.size (),
+                         cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize (c->stream);
+  if (e != cudaSuccess) return cuda_fail (e, "mixed row table");
+  e = m->kt.ensure (sizeof (MixK) * (m->nkh > 0 ? m->nkh : 1));
   if (e != cudaSuccess) return cuda_fail (e, "mixed k table");
   if (m->nkh)
     {
@@ -595,16 +630,17 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   const int np = c->np, C = NCOMP (c->version);
   const int ntab = (m->M[0] + 1) + (m->M[1] + 1) + (m->M[2] + 1);
   m->nchunk_r = std::max (1, std::min (64, (152 * 48 + np - 1) / np));
+  const size_t off1 = (size_t) (m->M[0] + 1) * np;
+  const size_t off2 = off1 + (size_t) (m->M[1] + 1) * np;
+  PhaseTables pt{(const float2 *) m->tab.p, off1, off2, m->M[0], m->M[1], m->M[2], np};
   {
+    // reciprocal space on the tensor cores unless LIBSTOKES_GB300_KSPACE=simt
     const char *ks = getenv ("LIBSTOKES_GB300_KSPACE");
-    m->tensor = (ks && strcmp (ks, "tc") == 0);
+    m->plan = kgemm_plan (c->version, pt, (const int2 *) m->rowm.p, m->nrow);
+    m->tensor = !(ks && strcmp (ks, "simt") == 0) && m->nkh > 0 && kgemm_fits (m->plan);
   }
   if (m->tensor)
-    {
-      m->nchunk_k = backproj_splits (np, m->nkh);
-      if (ntab > 150)
-        return set_error (STOKES_GPU_ETOOBIG, "mixed split: %d phase-table rows (at most 150)", ntab);
-    }
+    m->nchunk_k = kgemm_ypart_chunks (m->plan);
   else
     {
       m->nchunk_k = std::max (1, std::min (64, (152 * 48 + np - 1) / np));
@@ -628,8 +664,15 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     }
   if ((e = m->qpos.ensure (sizeof (uint32_t) * 4 * np)) != cudaSuccess) return cuda_fail (e, "qpos");
   if ((e = m->tab.ensure (sizeof (float2) * (size_t) ntab * np)) != cudaSuccess) return cuda_fail (e, "phase tables");
+  m->plan.t.tab = (const float2 *) m->tab.p;
   if ((e = m->xf.ensure (sizeof (float) * (size_t) C * np)) != cudaSuccess) return cuda_fail (e, "xf");
-  if ((e = m->pq.ensure (sizeof (float) * 2 * C * (size_t) (m->nkh > 0 ? m->nkh : 1))) != cudaSuccess) return cuda_fail (e, "pq");
+  if (m->tensor)
+    {
+      if ((e = m->sf.ensure (sizeof (float) * kgemm_sf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "structure factors");
+      if ((e = m->wop.ensure (sizeof (float2) * kgemm_w_elems (m->plan))) != cudaSuccess) return cuda_fail (e, "k operators");
+    }
+  else if ((e = m->pq.ensure (sizeof (float) * 2 * C * (size_t) (m->nkh > 0 ? m->nkh : 1))) != cudaSuccess)
+    return cuda_fail (e, "pq");
   if ((e = m->part_real.ensure (sizeof (float) * (size_t) m->nchunk_r * np * C)) != cudaSuccess) return cuda_fail (e, "real partials");
   if ((e = m->part_rec.ensure (sizeof (float) * (size_t) m->nchunk_k * np * C)) != cudaSuccess) return cuda_fail (e, "k partials");
   if ((e = m->selfbuf.ensure (sizeof (double) * 3 * np)) != cudaSuccess) return cuda_fail (e, "self");
@@ -644,8 +687,6 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   pa.qpos = (uint32_t *) m->qpos.p; pa.tab = (float2 *) m->tab.p; pa.xf = (float *) m->xf.p;
   mk_prep<<<(np + 127) / 128, 128, 0, st>>> (pa);
 
-  const size_t off1 = (size_t) (m->M[0] + 1) * np;
-  const size_t off2 = off1 + (size_t) (m->M[1] + 1) * np;
   KMixArgs ka;
   ka.kt = (const MixK *) m->kt.p; ka.tab = (const float2 *) m->tab.p;
   ka.xf = (const float *) m->xf.p; ka.np = np; ka.nkh = m->nkh;
@@ -658,13 +699,10 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   const int gb = (int) (((long long) np * m->nchunk_k + MX_WARPS - 1) / MX_WARPS);
   if (m->nkh > 0 && m->tensor)
     {
-      PhaseTables pt{(const float2 *) m->tab.p, off1, off2, m->M[0], m->M[1], m->M[2], np};
-      if ((e = launch_sfac_tc (c->version, ka.kt, m->nkh, pt, ka.xf, ka.pq, (int *) m->status.p,
-                               st)) != cudaSuccess)
-        return cuda_fail (e, "reciprocal forward (tensor cores)");
-      if ((e = launch_backproj_tc (c->version, ka.kt, m->nkh, pt, ka.pq, m->nchunk_k,
-                                   (float *) m->part_rec.p, (int *) m->status.p, st)) != cudaSuccess)
-        return cuda_fail (e, "reciprocal back-projection (tensor cores)");
+      if ((e = launch_kspace_gemm (c->version, m->plan, ka.kt, m->nkh, ka.xf, (float *) m->sf.p,
+                                   (float2 *) m->wop.p, (float *) m->part_rec.p,
+                                   (int *) m->status.p, st)) != cudaSuccess)
+        return cuda_fail (e, "reciprocal space (tensor cores)");
     }
   else if (m->nkh > 0)
     {
@@ -717,7 +755,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
         m->self_np = np;
       }
   }
-  const int gc = (np + 127) / 128;
+  const int gc = (np + 3) / 4;      // four particles (warps) per CTA
   if (c->version == 0) mk_combine<0><<<gc, 128, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
   else if (c->version == 1) mk_combine<1><<<gc, 128, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
   else mk_combine<2><<<gc, 128, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
@@ -726,7 +764,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     cudaMemcpyAsync (m->h_status, m->status.p, sizeof (int), cudaMemcpyDeviceToHost, st);
   e = cudaGetLastError ();
   if (e != cudaSuccess) return cuda_fail (e, "mixed kernels");
-  c->launches = (m->nkh > 0 ? 5 : 3);
+  c->launches = m->nkh == 0 ? 3 : (m->tensor ? 6 : 5);
   c->timed = timed;
   return STOKES_GPU_OK;
 }
@@ -743,7 +781,7 @@ release_mixed (Ctx *c)
   if (!c->mixed) return;
   MixedState *m = c->mixed;
   for (DevBuf *b : {&m->kt, &m->qpos, &m->tab, &m->xf, &m->pq, &m->part_real, &m->part_rec,
-                    &m->selfbuf, &m->status})
+                    &m->selfbuf, &m->status, &m->sf, &m->wop, &m->rowm})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
   delete m;

@@ -7,9 +7,10 @@
 
 namespace lsg {
 
-// one half-space reciprocal vector (64 bytes)
+// one half-space reciprocal vector (64 bytes); r: its (m2, m3) row of the
+// tensor-core contraction
 struct __align__ (16) MixK {
-  int m1, m2, m3, pad;
+  int m1, m2, m3, r;
   float ex, ey, ez;
   float ya, yb, yc, yg, yh, ym;
   float f0, f1, f2;
@@ -23,17 +24,33 @@ struct PhaseTables {
   int np;
 };
 
-// structure factors and per-k operators: pq[q * nkh + k] holds P_k[q] for
-// q < c and Q_k[q - c] for c <= q < 2c
-cudaError_t launch_sfac_tc (int version, const MixK *kt, int nkh, PhaseTables t,
-                            const float *xf, float *pq, int *status, cudaStream_t st);
+// plan of the separable tensor-core reciprocal sum (kspace_tc.cu).  The k
+// vectors of the list are (m1, row) with row = one (m2, m3) combination that
+// occurs in it; R rows, n1 = M0 + 1 values of m1.
+struct KGemm {
+  PhaseTables t;
+  const int2 *rowm;       // (m2, m3) of each row, R entries
+  int R;                  // rows
+  int c;                  // components per particle (3, 6, 11)
+  int n1;                 // M0 + 1
+  int nrt;                // forward row tiles of 64 rows
+  int gf, ntile_f, nf;    // m1 per forward column tile, tiles, MMA N
+  int jper, nsplit;       // particles per forward K slice, number of slices
+  int gb, ntile_b, nb;    // m1 per backward column tile, tiles, MMA N
+  int mtiles;             // 128-particle row tiles of the backward GEMM
+  int rper, ksplit;       // rows per backward K slice, number of slices
+};
 
-// y_i partial sums over k slices: partial[split][i][q]
-cudaError_t launch_backproj_tc (int version, const MixK *kt, int nkh, PhaseTables t,
-                                const float *pq, int nsplit, float *partial, int *status,
-                                cudaStream_t st);
+KGemm kgemm_plan (int version, PhaseTables t, const int2 *rowm, int R);
+bool kgemm_fits (const KGemm &g);
+size_t kgemm_sf_floats (const KGemm &g);      // partial structure factors
+size_t kgemm_w_elems (const KGemm &g);        // complex operators W (float2)
+size_t kgemm_ypart_floats (const KGemm &g);   // partial y, [ksplit][ntile_b][np][c]
+int kgemm_ypart_chunks (const KGemm &g);       // ksplit * ntile_b
 
-// number of k slices the back-projection uses for np particles, nkh vectors
-int backproj_splits (int np, int nkh);
+// forward GEMM -> per-k operators W -> backward GEMM into ypart
+cudaError_t launch_kspace_gemm (int version, const KGemm &g, const MixK *kt, int nk,
+                                const float *xf, float *sf, float2 *W, float *ypart,
+                                int *status, cudaStream_t st);
 
 }  // namespace lsg

@@ -25,9 +25,16 @@ def _pair(version, n, phi, seed=1, shear=(0, 0.0)):
     return a, b, x
 
 
+@pytest.fixture(params=["tc", "simt"])
+def kspace(request, monkeypatch):
+    """Reciprocal space on the tensor cores (default) and on the SIMT path."""
+    monkeypatch.setenv("LIBSTOKES_GB300_KSPACE", request.param)
+    return request.param
+
+
 @pytest.mark.parametrize("version,n,phi", [(0, 200, 0.2), (1, 300, 0.25), (2, 200, 0.3),
                                            (2, 1000, 0.3), (0, 1500, 0.2)])
-def test_mixed_accuracy(lib, version, n, phi):
+def test_mixed_accuracy(lib, kspace, version, n, phi):
     a, b, x = _pair(version, n, phi)
     y64 = a.atimes(x)
     ymx = b.atimes(x)
@@ -38,12 +45,52 @@ def test_mixed_accuracy(lib, version, n, phi):
 
 
 @pytest.mark.parametrize("version,mode,shift", [(0, 1, 3.1), (2, 2, -4.4), (1, 1, 0.0)])
-def test_mixed_shear(lib, version, mode, shift):
+def test_mixed_shear(lib, kspace, version, mode, shift):
     a, b, x = _pair(version, 300, 0.2, seed=4, shear=(mode, shift))
     err = rel_l2(b.atimes(x), a.atimes(x))
     assert err < TOL, err
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("version,box", [(2, (1.0, 1.3, 0.8)), (1, (0.7, 1.0, 1.45)),
+                                         (0, (1.5, 0.75, 1.0))])
+def test_mixed_rectangular_box(lib, kspace, version, box):
+    """Unequal box sides: different |m| ranges per axis in the k-space box."""
+    from libstokes_gb300 import FP64, MIXED, System
+    rng = np.random.default_rng(21)
+    n = 240
+    L = (4.0 / 3.0 * np.pi * n / 0.06) ** (1.0 / 3.0)
+    lx, ly, lz = (L * f for f in box)
+    # a loose lattice with jitter keeps the spheres apart
+    g = int(np.ceil(n ** (1.0 / 3.0)))
+    idx = np.array([(i, j, k) for i in range(g) for j in range(g) for k in range(g)][:n], float)
+    pos = (idx + 0.5 + 0.05 * rng.uniform(-1, 1, idx.shape)) * np.array([lx, ly, lz]) / g
+    x = rng.standard_normal((3, 6, 11)[version] * n)
+    a = System(version, pos.ravel(), (lx, ly, lz))
+    b = System(version, pos.ravel(), (lx, ly, lz))
+    a.set_precision(FP64)
+    b.set_precision(MIXED)
+    err = rel_l2(b.atimes(x), a.atimes(x))
+    assert err < TOL, err
+    a.close()
+    b.close()
+
+
+def test_kspace_paths_agree(lib, monkeypatch):
+    """Tensor-core and SIMT reciprocal sums give the same product."""
+    from libstokes_gb300 import MIXED, System
+    from libstokes_gb300.workloads import rsa_positions
+    pos, L = rsa_positions(700, 0.3, seed=33)
+    x = np.random.default_rng(34).standard_normal(11 * 700)
+    s = System(2, pos, (L, L, L))
+    s.set_precision(MIXED)
+    monkeypatch.setenv("LIBSTOKES_GB300_KSPACE", "simt")
+    y0 = s.atimes(x)
+    monkeypatch.setenv("LIBSTOKES_GB300_KSPACE", "tc")
+    y1 = s.atimes(x)
+    assert rel_l2(y1, y0) < 1e-6
+    s.close()
 
 
 def test_mixed_unwrapped_positions(lib):
