@@ -57,6 +57,12 @@ struct EV_LJ {
   double *r0;     /* potential-minimum distance per particle */
 };
 
+/* src/ev-LJ.c:35-81: zero-initialised per-particle coefficients; the scale
+ * turns e into e / (peclet r0) for entries with flag 0 and sets their flag */
+struct EV_LJ *EV_LJ_init (int np);
+void EV_LJ_free (struct EV_LJ *ev_LJ);
+void EV_LJ_scale (struct EV_LJ *ev_LJ, double peclet);
+
 /* ---- Brownian dynamics parameters (src/brownian.h:28-96) ------------------ */
 
 struct BeadRod;
@@ -118,6 +124,19 @@ struct BD_params {
 
 /* ---- drop-in routines (replace src/brownian.c) ---------------------------- */
 
+/* src/brownian.c:105-260: the RNG is seeded with `seed`, a_minv / a_lub are
+ * zeroed and eig_minv = eig_lub = {0, 0} (bounds not set yet) */
+struct BD_params *
+BD_params_init (struct stokes *sys, unsigned long seed, double *F, double *T, double *E,
+                double *uf, double *of, double *ef, int flag_noHI, int flag_lub, int flag_mat,
+                double st, struct BeadRod *br, struct BONDS *bonds, double gamma, struct EV *ev,
+                struct angles *ang, struct EV_DH *ev_dh, struct EV_LJ *ev_LJ,
+                struct confinement *cf, int flag_Q, double peclet, double eps, int n_minv,
+                int n_lub, int scheme, double BB_n, double rmin, double dt_lim);
+/* src/brownian.c:262-277 (F, T, E, uf, of, ef stay the caller's); also
+ * releases the device state the BD routines keep for this BD */
+void BD_params_free (struct BD_params *BD);
+
 /* src/brownian.c:2177-2187: sqrt(2 / (Pe dt)), 0 without Brownian force */
 double BD_params_get_fact (struct BD_params *BD, double dt);
 /* src/brownian.c:2033-2058: nm*3 (F) or nm*6 (FT, FTS) */
@@ -128,9 +147,11 @@ int BD_get_n (struct stokes *sys);
  * estimated first (20-step FP64 Lanczos on the device, in place of ARPACK)
  * and a_minv is fitted.  Unsupported branches exit with a message. */
 void BD_calc_FB (struct BD_params *BD, double *z);
-/* src/brownian.c:2352-2560 (scheme 0, F and FT without orientation, external
- * force F/T, EV_LJ repulsion, dt halving on overlap): one mid-point step,
- * returns the dt done. */
+/* src/brownian.c:2352-2560 (scheme 0, F and FT, quaternions q when given,
+ * constant force F/T, EV_LJ repulsion, imposed flow and shear, dt halving on
+ * overlap when sys->rmin == 0 and BD->rmin > 0): one mid-point step with
+ * noise from BD_calc_FB; returns the dt done.  The products run on the GPU
+ * in the precision set for sys (stokes_gpu_set_precision). */
 double BD_evolve_mid (double t, struct BD_params *BD, double *x, double *q, double dt);
 
 /* ---- device-resident engine (no counterpart in libstokes) ----------------- */

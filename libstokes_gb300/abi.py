@@ -101,6 +101,27 @@ class KIrandStruct(C.Structure):
                 ("Gaussian_saved", C.c_double)]
 
 
+class EVLJStruct(C.Structure):
+    """struct EV_LJ (src/ev-LJ.h:26-51)."""
+    _fields_ = [("n", C.c_int), ("flag", C.POINTER(C.c_int)), ("e", _dp), ("r0", _dp)]
+
+
+class BDStruct(C.Structure):
+    """struct BD_params (src/brownian.h:28-96)."""
+    _fields_ = [("sys", C.c_void_p), ("rng", C.POINTER(KIrandStruct)), ("F", _dp), ("T", _dp),
+                ("E", _dp), ("uf", _dp), ("of", _dp), ("ef", _dp), ("flag_noHI", C.c_int),
+                ("flag_mat", C.c_int), ("flag_lub", C.c_int), ("flag_lub_B", C.c_int),
+                ("t0", C.c_double), ("s0", C.c_double), ("st", C.c_double),
+                ("br", C.c_void_p), ("bonds", C.c_void_p), ("groups", C.c_void_p),
+                ("gamma", C.c_double), ("ev", C.c_void_p), ("ang", C.c_void_p),
+                ("ev_dh", C.c_void_p), ("ev_LJ", C.POINTER(EVLJStruct)), ("cf", C.c_void_p),
+                ("flag_Q", C.c_int), ("peclet", C.c_double), ("eps", C.c_double),
+                ("n_minv", C.c_int), ("eig_minv", C.c_double * 2), ("a_minv", _dp),
+                ("n_lub", C.c_int), ("eig_lub", C.c_double * 2), ("a_lub", _dp),
+                ("scheme", C.c_int), ("BB_n", C.c_double), ("rmin", C.c_double),
+                ("dt_lim", C.c_double)]
+
+
 _SP = C.POINTER(StokesStruct)
 ATIMES = C.CFUNCTYPE(None, C.c_int, _dp, _dp, C.c_void_p)
 FUNC1 = C.CFUNCTYPE(C.c_double, C.c_double)
@@ -187,6 +208,21 @@ _SIGS = {
     "stokes_gpu_bd_step_noise": (C.c_int, [C.c_void_p, C.c_double, _dp]),
     "stokes_gpu_bd_run": (C.c_int, [C.c_void_p, C.c_double, C.c_int]),
     "stokes_gpu_bd_stats": (C.c_int, [C.c_void_p, _dp]),
+    # libstokes' BD routines
+    "EV_LJ_init": (C.POINTER(EVLJStruct), [C.c_int]),
+    "EV_LJ_free": (None, [C.POINTER(EVLJStruct)]),
+    "EV_LJ_scale": (None, [C.POINTER(EVLJStruct), C.c_double]),
+    "BD_params_init": (C.POINTER(BDStruct),
+                       [_SP, C.c_ulong, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int,
+                        C.c_double, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
+                        C.c_void_p, C.POINTER(EVLJStruct), C.c_void_p, C.c_int, C.c_double,
+                        C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                        C.c_double]),
+    "BD_params_free": (None, [C.POINTER(BDStruct)]),
+    "BD_params_get_fact": (C.c_double, [C.POINTER(BDStruct), C.c_double]),
+    "BD_get_n": (C.c_int, [_SP]),
+    "BD_calc_FB": (None, [C.POINTER(BDStruct), _dp]),
+    "BD_evolve_mid": (C.c_double, [C.c_double, C.POINTER(BDStruct), _dp, _dp, C.c_double]),
 }
 
 _lib = None

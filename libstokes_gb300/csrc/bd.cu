@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "engine.h"
@@ -134,7 +135,8 @@ k_bd_force (int nm, int np, int c, double fact, const double *z, const double *f
 // overlap; the candidates are redone exactly in FP64.
 __global__ void
 k_bd_lj (int nm, int np, int c, const double *pos, double lx, double ly, double lz,
-         int shear_mode, double shift, const double *rad, double e, double r0, double *f)
+         int shear_mode, double shift, const double *rad, double e_all, double r0_all,
+         const double *lje, const double *ljr0, double *f)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nm) return;
@@ -157,6 +159,10 @@ k_bd_lj (int nm, int np, int c, const double *pos, double lx, double ly, double 
       const bool far_raw = fabsf (sx) > 1.4f * flx || fabsf (sy) > 1.4f * fly
         || fabsf (sz) > 1.4f * flz || shear_mode != 0;
       if (!far_raw && wx * wx + wy * wy + wz * wz > lim * lim) continue;
+      // pair coefficients (src/ev-LJ.c:131-137): geometric mean of e,
+      // arithmetic mean of r0
+      const double e = lje ? sqrt (lje[i] * lje[j]) : e_all;
+      const double r0 = ljr0 ? 0.5 * (ljr0[i] + ljr0[j]) : r0_all;
       for (int kx = -1; kx <= 1; kx++)
         for (int ky = -1; ky <= 1; ky++)
           for (int kz = -1; kz <= 1; kz++)
@@ -233,6 +239,36 @@ k_bd_zcompress (int nm, int c, const double *x, double *z)
   for (int q = 0; q < zc; q++) z[(size_t) i * zc + q] = x[(size_t) i * c + q];
 }
 
+// number of pairs i <= j < nm closer than sqrt(rmin) (a_i + a_j) in the
+// primary cell (i != j) or in one of the 26 neighbour cells
+// (src/brownian.c:299-375)
+__global__ void
+k_bd_overlap (int nm, const double *pos, double lx, double ly, double lz, int shear_mode,
+              double shift, const double *rad, double rmin, int *count)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nm) return;
+  int cnt = 0;
+  const double ai = rad ? rad[i] : 1.0;
+  for (int j = i; j < nm; j++)
+    {
+      const double x = pos[3 * i] - pos[3 * j], y = pos[3 * i + 1] - pos[3 * j + 1],
+                   z = pos[3 * i + 2] - pos[3 * j + 2];
+      const double s = ai + (rad ? rad[j] : 1.0), a2 = s * s;
+      for (int kx = -1; kx <= 1; kx++)
+        for (int ky = -1; ky <= 1; ky++)
+          for (int kz = -1; kz <= 1; kz++)
+            {
+              if (kx == 0 && ky == 0 && kz == 0 && i == j) continue;
+              double xx = x + kx * lx, yy = y + ky * ly, zz = z + kz * lz;
+              if (shear_mode == 1) xx += ky * shift;
+              else if (shear_mode == 2) xx += kz * shift;
+              if (xx * xx + yy * yy + zz * zz < rmin * a2) cnt++;
+            }
+    }
+  if (cnt) atomicAdd (count, cnt);
+}
+
 // ---------------------------------------------------------------------------
 // engine
 // ---------------------------------------------------------------------------
@@ -246,6 +282,8 @@ struct stokes_gpu_bd {
   stokes_gpu_bd_params p{};
   int nm = 0, np = 0, C = 3, n = 0;   // n = BD_get_n (noise length)
   lsg::DevBuf x, xmid, y, z, f, u, fext, work, lan, tmp, dots, pos_fixed;
+  lsg::DevBuf xnew, lje, ljr0, ovl;    // drop-in BD_evolve_mid
+  bool lj_arrays = false;              // per-particle EV_LJ coefficients in lje, ljr0
   double eig[2] = {0, 0};
   std::vector<double> coef;
   bool have_bounds = false;
@@ -421,11 +459,14 @@ bd_forces (stokes_gpu_bd *b, const double *d_pos, double fact)
   k_bd_force<<<gridn (b->np), 256, 0, st>>> (b->nm, b->np, b->C, fact, (const double *) b->z.p,
                                              b->fext.p ? (const double *) b->fext.p : nullptr,
                                              (double *) b->f.p);
-  if (b->p.lj_e != 0.0)
+  if (b->p.lj_e != 0.0 || b->lj_arrays)
     k_bd_lj<<<gridn (b->nm), 128, 0, st>>> (b->nm, b->np, b->C, d_pos, s->lx, s->ly, s->lz,
                                             s->shear_mode, s->shear_shift,
                                             s->a ? (const double *) b->c->pp.p : nullptr,
-                                            b->p.lj_e, b->p.lj_r0, (double *) b->f.p);
+                                            b->p.lj_e, b->p.lj_r0,
+                                            b->lj_arrays ? (const double *) b->lje.p : nullptr,
+                                            b->lj_arrays ? (const double *) b->ljr0.p : nullptr,
+                                            (double *) b->f.p);
   cudaError_t e = cudaGetLastError ();
   return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "BD forces");
 }
@@ -557,7 +598,7 @@ stokes_gpu_bd_destroy (stokes_gpu_bd *b)
   if (!b) return STOKES_GPU_OK;
   if (b->c) cudaStreamSynchronize (b->c->stream);
   for (DevBuf *d : {&b->x, &b->xmid, &b->y, &b->z, &b->f, &b->u, &b->fext, &b->work, &b->lan,
-                    &b->tmp, &b->dots, &b->pos_fixed})
+                    &b->tmp, &b->dots, &b->pos_fixed, &b->xnew, &b->lje, &b->ljr0, &b->ovl})
     d->release ();
   if (b->h_dots) cudaFreeHost (b->h_dots);
   delete b;
@@ -694,6 +735,458 @@ stokes_gpu_bd_stats (stokes_gpu_bd *b, double *out4)
   out4[2] = b->last_err;
   out4[3] = b->steps;
   return STOKES_GPU_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// libstokes' own BD routines on the engine (src/brownian.c)
+// ---------------------------------------------------------------------------
+namespace lsg {
+
+// one engine per BD_params, re-created when the system behind it changes
+struct DropinKey {
+  struct BD_params *bd;
+  struct stokes *sys;
+  int np, version, n_minv, precision;
+};
+
+static std::mutex g_dropin_mu;
+static std::vector<std::pair<DropinKey, stokes_gpu_bd *>> g_dropin;
+
+[[noreturn]] static void
+dropin_die (const char *fn, const char *why)
+{
+  fprintf (stderr, "libstokes_gb300 %s: %s\n", fn, why);
+  exit (1);
+}
+
+static int
+ctx_precision (struct stokes *sys)
+{
+  int p = STOKES_GPU_FP64;
+  return stokes_gpu_get_precision (sys, &p) == STOKES_GPU_OK ? p : STOKES_GPU_FP64;
+}
+
+// the engine of BD (created or refreshed); exits like the reference on
+// configurations outside the supported branch
+static stokes_gpu_bd *
+dropin_engine (struct BD_params *BD, const char *fn)
+{
+  struct stokes *sys = BD->sys;
+  if (!sys) dropin_die (fn, "BD->sys is NULL");
+  if (sys->version < 0 || sys->version > 1)
+    dropin_die (fn, "the device BD serves the F and FT versions");
+  if (sys->np != sys->nm) dropin_die (fn, "the device BD serves systems without fixed particles");
+  if (BD->flag_lub || BD->flag_lub_B || BD->flag_mat)
+    dropin_die (fn, "lubrication and matrix noise are not on the device path");
+  if (BD->n_minv <= 0) dropin_die (fn, "n_minv <= 0 (matrix noise) is not on the device path");
+  if (BD->br || BD->bonds || BD->ev || BD->ang || BD->ev_dh || BD->cf)
+    dropin_die (fn, "only EV_LJ among the interactions is on the device path");
+  const DropinKey key{BD, sys, sys->np, sys->version, BD->n_minv, ctx_precision (sys)};
+  std::lock_guard<std::mutex> lk (g_dropin_mu);
+  for (auto &e : g_dropin)
+    if (e.first.bd == BD)
+      {
+        if (!memcmp (&e.first, &key, sizeof key)) return e.second;
+        stokes_gpu_bd_destroy (e.second);
+        e = g_dropin.back ();
+        g_dropin.pop_back ();
+        break;
+      }
+  stokes_gpu_bd_params p{};
+  p.peclet = BD->peclet;
+  p.dt = 1.0;                     // per call
+  p.n_cheb = BD->n_minv;
+  p.n_lanczos = 40;
+  p.cheb_eps = BD->eps;
+  p.check_every = 1;
+  p.precision = key.precision;
+  stokes_gpu_bd *b = nullptr;
+  if (stokes_gpu_bd_create (sys, &p, &b) != STOKES_GPU_OK)
+    dropin_die (fn, stokes_gpu_last_error_message ());
+  g_dropin.push_back ({key, b});
+  return b;
+}
+
+static void
+check_rc (int rc, const char *fn)
+{
+  if (rc != STOKES_GPU_OK) dropin_die (fn, stokes_gpu_last_error_message ());
+}
+
+static void
+upload (DevBuf &d, const double *h, size_t n, cudaStream_t st, const char *fn)
+{
+  cudaError_t e = d.ensure (sizeof (double) * (n ? n : 1));
+  if (e == cudaSuccess && n)
+    e = cudaMemcpyAsync (d.p, h, sizeof (double) * n, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+}
+
+// per-particle EV_LJ and the constant force/torque of BD
+static void
+dropin_interactions (stokes_gpu_bd *b, struct BD_params *BD, const char *fn)
+{
+  cudaStream_t st = b->c->stream;
+  b->lj_arrays = BD->ev_LJ != nullptr;
+  if (b->lj_arrays)
+    {
+      if (BD->ev_LJ->n < b->np) dropin_die (fn, "EV_LJ has fewer entries than particles");
+      upload (b->lje, BD->ev_LJ->e, (size_t) b->np, st, fn);
+      upload (b->ljr0, BD->ev_LJ->r0, (size_t) b->np, st, fn);
+    }
+  std::vector<double> h ((size_t) b->C * b->np, 0.0);
+  for (int i = 0; i < b->nm; i++)
+    for (int q = 0; q < 3; q++)
+      {
+        if (BD->F) h[(size_t) i * b->C + q] = BD->F[3 * i + q];
+        if (BD->T && b->C >= 6) h[(size_t) i * b->C + 3 + q] = BD->T[3 * i + q];
+      }
+  upload (b->fext, h.data (), h.size (), st, fn);
+}
+
+// BD_calc_FB's Chebyshev branch on the device: y from BD->rng, z = M^{-1/2} y
+// in b->z (particle order) at positions d_pos; bounds and coefficients are
+// BD's own (estimated first when eig_minv[0] == eig_minv[1], re-estimated
+// when the error exceeds BD->eps), src/brownian.c:1597-1728
+static void
+dropin_noise (stokes_gpu_bd *b, struct BD_params *BD, const double *d_pos, const char *fn)
+{
+  std::vector<double> y ((size_t) b->n);
+  for (double &v : y) v = KIrand_Gaussian (BD->rng);
+  cudaError_t e = cudaMemcpyAsync (b->y.p, y.data (), sizeof (double) * b->n,
+                                   cudaMemcpyHostToDevice, b->c->stream);
+  if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+  b->p.n_cheb = BD->n_minv;
+  auto take_bounds = [&] () {
+    BD->eig_minv[0] = b->eig[0];
+    BD->eig_minv[1] = b->eig[1];
+    for (int k = 0; k < BD->n_minv; k++) BD->a_minv[k] = b->coef[k];
+  };
+  if (BD->eig_minv[0] == BD->eig_minv[1])
+    {
+      check_rc (bd_lanczos (b, d_pos, b->p.n_lanczos, 0.8, 1.05), fn);
+      take_bounds ();
+    }
+  b->eig[0] = BD->eig_minv[0];
+  b->eig[1] = BD->eig_minv[1];
+  b->coef.assign (BD->a_minv, BD->a_minv + BD->n_minv);
+  check_rc (bd_noise (b, d_pos), fn);
+  double err = 0.0;
+  check_rc (bd_error (b, d_pos, &err), fn);
+  if (err > BD->eps)
+    {
+      check_rc (bd_lanczos (b, d_pos, b->p.n_lanczos, 0.8, 1.05), fn);
+      take_bounds ();
+      check_rc (bd_noise (b, d_pos), fn);
+      check_rc (bd_error (b, d_pos, &err), fn);
+      if (!(err < HUGE_VAL))
+        dropin_die (fn, "non-positive z.Mz after re-estimating the bounds (overlapping spheres?)");
+    }
+  b->last_err = err;
+}
+
+static int
+dropin_overlap (stokes_gpu_bd *b, const double *d_pos, double rmin, const char *fn)
+{
+  const struct stokes *s = b->sys;
+  cudaStream_t st = b->c->stream;
+  cudaError_t e = b->ovl.ensure (sizeof (int));
+  if (e == cudaSuccess) e = cudaMemsetAsync (b->ovl.p, 0, sizeof (int), st);
+  if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+  k_bd_overlap<<<gridn (b->nm), 128, 0, st>>> (b->nm, d_pos, s->lx, s->ly, s->lz, s->shear_mode,
+                                               s->shear_shift,
+                                               s->a ? (const double *) b->c->pp.p : nullptr, rmin,
+                                               (int *) b->ovl.p);
+  int cnt = 0;
+  e = cudaMemcpyAsync (&cnt, b->ovl.p, sizeof (int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize (st);
+  if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+  return cnt;
+}
+
+// q += h dQ/dt(q, o) (src/ode-quaternion.c:60-105 with the inverse of the
+// quaternion rate matrix written out)
+static void
+quaternion_step (int nm, const double *o, double h, const double *q0, double *q)
+{
+  for (int i = 0; i < nm; i++)
+    {
+      const double *Q = q0 + 4 * i, *O = o + 3 * i;
+      const double den = Q[0] * Q[0] + Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3];
+      const double W[4][3] = {{Q[3], -Q[2], Q[1]},
+                              {Q[2], Q[3], -Q[0]},
+                              {-Q[1], Q[0], Q[3]},
+                              {-Q[0], -Q[1], -Q[2]}};
+      for (int r = 0; r < 4; r++)
+        {
+          double d = 0.0;
+          for (int j = 0; j < 3; j++) d += 0.5 * (W[r][j] / den) * O[j];
+          q[4 * i + r] = Q[r] + h * d;
+        }
+    }
+}
+
+}  // namespace lsg
+
+extern "C" {
+
+double
+BD_params_get_fact (struct BD_params *BD, double dt)
+{
+  return BD->peclet > 0.0 ? sqrt (2.0 / (BD->peclet * dt)) : 0.0;
+}
+
+int
+BD_get_n (struct stokes *sys)
+{
+  if (sys->version == 0) return sys->nm * 3;
+  if (sys->version == 1 || sys->version == 2) return sys->nm * 6;
+  fprintf (stderr, "invalid version %d\n", sys->version);
+  exit (1);
+}
+
+void
+BD_calc_FB (struct BD_params *BD, double *z)
+{
+  static const char *fn = "BD_calc_FB";
+  struct stokes *sys = BD->sys;
+  const int n = BD_get_n (sys);
+  if (BD->flag_noHI == 1)
+    {
+      // free-draining noise (src/brownian.c:1552-1595)
+      for (int i = 0; i < sys->nm; i++)
+        {
+          const double as = sys->a ? sqrt (sys->a[i]) : 1.0;
+          if (sys->version == 0)
+            for (int q = 0; q < 3; q++) z[3 * i + q] = KIrand_Gaussian (BD->rng) * as;
+          else
+            {
+              const double as3 = as * as * as / sqrt (0.75);
+              for (int q = 0; q < 3; q++) z[6 * i + q] = KIrand_Gaussian (BD->rng) * as;
+              for (int q = 0; q < 3; q++) z[6 * i + 3 + q] = KIrand_Gaussian (BD->rng) * as3;
+            }
+        }
+      return;
+    }
+  stokes_gpu_bd *b = dropin_engine (BD, fn);
+  check_rc (prepare (b->c, sys, false), fn);
+  upload (b->x, sys->pos, 3 * (size_t) sys->np, b->c->stream, fn);
+  dropin_noise (b, BD, (const double *) b->x.p, fn);
+  std::vector<double> zp ((size_t) n);
+  cudaError_t e = cudaMemcpyAsync (zp.data (), b->z.p, sizeof (double) * n,
+                                   cudaMemcpyDeviceToHost, b->c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize (b->c->stream);
+  if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+  // particle order -> [F part, T part] (src/brownian.c:1851-1871)
+  const int nm = sys->nm;
+  if (sys->version == 0)
+    for (int i = 0; i < n; i++) z[i] = zp[i];
+  else
+    for (int i = 0; i < nm; i++)
+      for (int q = 0; q < 3; q++)
+        {
+          z[3 * i + q] = zp[6 * i + q];
+          z[3 * nm + 3 * i + q] = zp[6 * i + 3 + q];
+        }
+}
+
+double
+BD_evolve_mid (double t, struct BD_params *BD, double *x, double *q, double dt)
+{
+  static const char *fn = "BD_evolve_mid";
+  struct stokes *sys = BD->sys;
+  stokes_gpu_bd *b = dropin_engine (BD, fn);
+  cudaStream_t st = b->c->stream;
+  const int nm = sys->nm, np = sys->np, C = b->C;
+  const bool rot = sys->version > 0 && q != nullptr;
+  cudaError_t e = b->xnew.ensure (sizeof (double) * 3 * np);
+  if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+  dropin_interactions (b, BD, fn);
+  double *dx = (double *) b->x.p, *dmid = (double *) b->xmid.p, *dnew = (double *) b->xnew.p;
+  std::vector<double> o ((size_t) 3 * nm), uh ((size_t) C * np), qmid;
+  if (rot) qmid.assign (q, q + 4 * (size_t) nm);
+
+  double dt_local = dt;
+  double fact = BD_params_get_fact (BD, dt_local);
+  const double *cur = dx;            // the configuration sys->pos holds
+  // the overlap checks run only without the real-space clamp
+  const bool check = sys->rmin == 0.0 && BD->rmin > 0.0;
+
+redo:
+  upload (b->x, x, 3 * (size_t) np, st, fn);
+  memcpy (sys->pos, x, sizeof (double) * 3 * nm);
+  cur = dx;
+  stokes_set_shear_shift (sys, t, BD->t0, BD->s0);
+  check_rc (prepare (b->c, sys, false), fn);
+redo_fb:
+  dropin_noise (b, BD, cur, fn);
+redo_scale:
+  {
+    // 1: velocity at the current configuration, Euler half step from x
+    const Flow fl = bd_flow (sys);
+    check_rc (bd_forces (b, cur, fact), fn);
+    check_rc (bd_prod (b, cur, (const double *) b->f.p, (double *) b->u.p), fn);
+    k_bd_euler<<<gridn (nm), 256, 0, st>>> (nm, C, dx, (const double *) b->u.p, cur, fl,
+                                            0.5 * dt_local, dmid);
+    if (check && dropin_overlap (b, dmid, BD->rmin, fn) > 0)
+      {
+        dt_local *= 0.5;
+        if (dt_local < BD->dt_lim)
+          {
+            fprintf (stderr, "# mid-point: overlap in 1st step. dt = %e < %e => reconstruct FB\n",
+                     dt_local, BD->dt_lim);
+            dt_local = dt;
+            goto redo_fb;
+          }
+        fact = BD_params_get_fact (BD, dt_local);
+        fprintf (stderr, "# mid-point: overlap in 1st step. dt = %e > %e\n", dt_local, BD->dt_lim);
+        goto redo_scale;
+      }
+    // 2: velocity at the mid point, full step from x
+    cur = dmid;
+    e = cudaMemcpyAsync (sys->pos, dmid, sizeof (double) * 3 * nm, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+    stokes_set_shear_shift (sys, t + 0.5 * dt_local, BD->t0, BD->s0);
+    check_rc (prepare (b->c, sys, false), fn);
+    const Flow fm = bd_flow (sys);
+    check_rc (bd_forces (b, dmid, fact), fn);
+    check_rc (bd_prod (b, dmid, (const double *) b->f.p, (double *) b->u.p), fn);
+    k_bd_euler<<<gridn (nm), 256, 0, st>>> (nm, C, dx, (const double *) b->u.p, dmid, fm,
+                                            dt_local, dnew);
+    if (check && dropin_overlap (b, dnew, BD->rmin, fn) > 0)
+      {
+        dt_local *= 0.5;
+        if (dt_local < BD->dt_lim)
+          {
+            fprintf (stderr, "# mid-point: overlap in 2nd step. dt = %e < %e => reconstruct FB\n",
+                     dt_local, BD->dt_lim);
+            dt_local = dt;
+            goto redo;
+          }
+        fact = BD_params_get_fact (BD, dt_local);
+        fprintf (stderr, "# mid-point: overlap in 2nd step. dt = %e > %e\n", dt_local, BD->dt_lim);
+        // as in the reference, the redo of the first stage starts from the
+        // configuration and shear shift the system holds now (the mid point)
+        goto redo_scale;
+      }
+    if (rot)
+      {
+        e = cudaMemcpyAsync (uh.data (), b->u.p, sizeof (double) * C * np, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize (st);
+        if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+        for (int i = 0; i < nm; i++)
+          for (int k = 0; k < 3; k++) o[3 * i + k] = uh[(size_t) i * C + 3 + k] + sys->Oi[k];
+        quaternion_step (nm, o.data (), dt_local, q, qmid.data ());
+        memcpy (q, qmid.data (), sizeof (double) * 4 * nm);
+      }
+  }
+  e = cudaMemcpyAsync (x, dnew, sizeof (double) * 3 * nm, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize (st);
+  if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+  b->steps += 1;
+  return dt_local;
+}
+
+// src/brownian.c:105-260 (no bead-rod, bond-group or lubrication set-up on
+// the device path; those pointers are kept for the caller)
+struct BD_params *
+BD_params_init (struct stokes *sys, unsigned long seed, double *F, double *T, double *E,
+                double *uf, double *of, double *ef, int flag_noHI, int flag_lub, int flag_mat,
+                double st, struct BeadRod *br, struct BONDS *bonds, double gamma, struct EV *ev,
+                struct angles *ang, struct EV_DH *ev_dh, struct EV_LJ *ev_LJ,
+                struct confinement *cf, int flag_Q, double peclet, double eps, int n_minv,
+                int n_lub, int scheme, double BB_n, double rmin, double dt_lim)
+{
+  struct BD_params *BD = (struct BD_params *) calloc (1, sizeof (struct BD_params));
+  if (!BD) dropin_die ("BD_params_init", "out of memory");
+  BD->sys = sys;
+  BD->rng = KIrand_init ();
+  KIrand_init_genrand (BD->rng, seed);
+  BD->F = F; BD->T = T; BD->E = E;
+  BD->uf = uf; BD->of = of; BD->ef = ef;
+  BD->flag_noHI = flag_noHI;
+  BD->flag_mat = flag_mat;
+  BD->flag_lub = flag_lub;
+  BD->flag_lub_B = 0;
+  BD->st = st;
+  BD->br = br;
+  BD->bonds = bonds;
+  BD->groups = nullptr;
+  BD->gamma = gamma;
+  BD->ev = ev; BD->ang = ang; BD->ev_dh = ev_dh; BD->ev_LJ = ev_LJ; BD->cf = cf;
+  BD->flag_Q = flag_Q;
+  BD->peclet = peclet;
+  BD->eps = eps;
+  BD->n_minv = n_minv;
+  BD->a_minv = n_minv > 0 ? (double *) calloc ((size_t) n_minv, sizeof (double)) : nullptr;
+  BD->n_lub = n_lub;
+  BD->a_lub = n_lub > 0 ? (double *) calloc ((size_t) n_lub, sizeof (double)) : nullptr;
+  BD->scheme = scheme;
+  BD->BB_n = BB_n;
+  BD->rmin = rmin;
+  BD->dt_lim = dt_lim;
+  return BD;
+}
+
+// src/brownian.c:262-277; also releases the device engine of BD
+void
+BD_params_free (struct BD_params *BD)
+{
+  if (!BD) return;
+  {
+    std::lock_guard<std::mutex> lk (g_dropin_mu);
+    for (size_t k = 0; k < g_dropin.size (); k++)
+      if (g_dropin[k].first.bd == BD)
+        {
+          stokes_gpu_bd_destroy (g_dropin[k].second);
+          g_dropin[k] = g_dropin.back ();
+          g_dropin.pop_back ();
+          break;
+        }
+  }
+  if (BD->rng) KIrand_free (BD->rng);
+  free (BD->a_minv);
+  free (BD->a_lub);
+  free (BD);
+}
+
+// src/ev-LJ.c:35-81
+struct EV_LJ *
+EV_LJ_init (int np)
+{
+  struct EV_LJ *lj = (struct EV_LJ *) malloc (sizeof (struct EV_LJ));
+  if (!lj) dropin_die ("EV_LJ_init", "out of memory");
+  lj->n = np;
+  lj->flag = (int *) calloc ((size_t) np, sizeof (int));
+  lj->e = (double *) calloc ((size_t) np, sizeof (double));
+  lj->r0 = (double *) calloc ((size_t) np, sizeof (double));
+  if (!lj->flag || !lj->e || !lj->r0) dropin_die ("EV_LJ_init", "out of memory");
+  return lj;
+}
+
+void
+EV_LJ_free (struct EV_LJ *lj)
+{
+  if (!lj) return;
+  free (lj->flag);
+  free (lj->e);
+  free (lj->r0);
+  free (lj);
+}
+
+// e -> e / (peclet r0) for the entries not scaled yet
+void
+EV_LJ_scale (struct EV_LJ *lj, double peclet)
+{
+  if (!lj) return;
+  for (int i = 0; i < lj->n; i++)
+    if (lj->flag[i] == 0)
+      {
+        lj->flag[i] = 1;
+        lj->e[i] /= peclet * lj->r0[i];
+      }
 }
 
 }  // extern "C"

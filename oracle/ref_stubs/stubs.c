@@ -47,3 +47,20 @@ ORACLE_ABORT_STUB (dcopy_)
 ORACLE_ABORT_STUB (dgetrf_)
 ORACLE_ABORT_STUB (dgetri_)
 ORACLE_ABORT_STUB (dgetrs_)
+
+/* ARPACK, the LAPACK/BLAS routines of the matrix-noise branch and the
+ * bead-rod constraints: linked by the reference's Brownian-dynamics sources,
+ * never reached when the Chebyshev bounds are preset and no constraints are
+ * given. */
+ORACLE_ABORT_STUB (dnaupd_)
+ORACLE_ABORT_STUB (dneupd_)
+ORACLE_ABORT_STUB (dsaupd_)
+ORACLE_ABORT_STUB (dseupd_)
+ORACLE_ABORT_STUB (dgeev_)
+ORACLE_ABORT_STUB (dpotrf_)
+ORACLE_ABORT_STUB (dpotf2_)
+ORACLE_ABORT_STUB (dgemv_)
+ORACLE_ABORT_STUB (dgemm_)
+ORACLE_ABORT_STUB (BeadRod_set_coefs)
+ORACLE_ABORT_STUB (BeadRod_adjust_by_constraints)
+ORACLE_ABORT_STUB (BeadRod_bead_to_connector)

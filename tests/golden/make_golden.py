@@ -14,6 +14,9 @@ travel with the repository, so the tests never need the reference itself:
                              test/check-ewald.c, the N=64 5-shell workload)
   chebyshev.npz              chebyshev_coef / chebyshev_eval /
                              chebyshev_eval_atimes outputs
+  bd.npz                     BD_calc_FB noise and BD_evolve_mid trajectories
+                             (F and FT, EV_LJ, quaternions, shear, dt halving)
+                             of the reference's own brownian.c
 
     python tests/golden/make_golden.py [/path/to/libstokes]
 """
@@ -102,6 +105,91 @@ def mk(version, pos, box, tratio=1.0, eps=1e-12, a=None, slip=None, shear=(0, 0.
         r.set_cube(*cube)
     r.set_misc(rmin, shear[0], shear[1])
     return r
+
+
+BD_CASES = [
+    # name, version, N, phi, pos seed, rng seed, Pe, dt, steps, n_minv,
+    # LJ (e, r0) or None, BD->rmin, dt_lim, shear (mode, rate), with F/T, with q
+    ("f_lj", 0, 27, 0.20, 3, 42, 1.0, 1e-3, 3, 20, (1.0, 2.0), 0.0, 1e-12, (0, 0.0), False, False),
+    ("f_halving", 0, 27, 0.20, 5, 43, 1.0, 1e-2, 3, 20, (1.0, 2.0), 0.9, 1e-4, (0, 0.0), True, False),
+    ("ft_q", 1, 20, 0.15, 6, 44, 2.0, 1e-3, 2, 24, (0.5, 2.0), 0.0, 1e-12, (0, 0.0), True, True),
+    ("f_shear", 0, 24, 0.20, 7, 45, 1.0, 1e-3, 2, 20, None, 0.0, 1e-12, (1, 2.0), False, False),
+]
+
+
+def bd_fixtures() -> dict:
+    """BD_calc_FB / BD_evolve_mid of the reference on small periodic systems.
+    ARPACK is absent, so the bounds are the extreme eigenvalues of the
+    reference's dense mobility matrix widened by (0.8, 1.05); BD->eps = 10
+    keeps the re-estimate branch off."""
+    import ctypes as C
+    so = os.path.join(ROOT, "oracle", "_ref", "libstokes_ref_bd.so")
+    lib = C.CDLL(so)
+    dp = C.POINTER(C.c_double)
+    d = lambda a: None if a is None else a.ctypes.data_as(dp)  # noqa: E731
+    lib.ref_new.restype = C.c_void_p
+    lib.ref_new.argtypes = [C.c_int, C.c_int, dp, C.c_double, C.c_double, C.c_double]
+    lib.ref_free.argtypes = [C.c_void_p]
+    lib.ref_xi_by_tratio.restype = C.c_double
+    lib.ref_xi_by_tratio.argtypes = [C.c_void_p, C.c_double]
+    lib.ref_set_split.argtypes = [C.c_void_p, C.c_double, C.c_double]
+    lib.ref_matrix.argtypes = [C.c_void_p, dp]
+    lib.refbd_set_shear.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    lib.refbd_calc_fb.argtypes = [C.c_void_p, C.c_ulong, C.c_double, C.c_int, C.c_double,
+                                  C.c_double, C.c_double, dp]
+    lib.refbd_run.argtypes = [C.c_void_p, C.c_ulong, C.c_double, C.c_double, C.c_int, C.c_int,
+                              C.c_double, C.c_double, C.c_double, dp, dp, C.c_int, C.c_double,
+                              C.c_double, C.c_double, C.c_double, dp, dp, dp, dp, dp, dp]
+    out = {}
+    for (name, ver, n, phi, pseed, rseed, pe, dt, steps, nminv, lj, bdrmin, dtlim, shear,
+         with_ft, with_q) in BD_CASES:
+        pos, L = rsa_positions(n, phi, seed=pseed)
+        c = (3, 6, 11)[ver]
+        h = lib.ref_new(ver, n, d(pos), L, L, L)
+        lib.ref_set_split(h, lib.ref_xi_by_tratio(h, 1.0), 1e-12)
+        if shear[0]:
+            lib.refbd_set_shear(h, shear[0], shear[1])
+        M = np.zeros((c * n, c * n))
+        lib.ref_matrix(h, d(M))
+        ev = np.linalg.eigvalsh(0.5 * (M + M.T))
+        eig = np.array([0.8 * ev[0], 1.05 * ev[-1]])
+        rng = np.random.default_rng(pseed + 1000)
+        F = 0.3 * rng.standard_normal(3 * n) if with_ft else None
+        T = 0.3 * rng.standard_normal(3 * n) if (with_ft and ver > 0) else None
+        q = None
+        if with_q:
+            q = rng.standard_normal((n, 4))
+            q /= np.linalg.norm(q, axis=1, keepdims=True)
+            q = q.ravel().copy()
+        lje = lj0 = None
+        if lj is not None:
+            lje = np.full(n, lj[0])
+            lj0 = np.full(n, lj[1])
+        nb = (3 if ver == 0 else 6) * n
+        z = np.zeros(nb)
+        lib.refbd_calc_fb(h, rseed + 100, pe, nminv, eig[0], eig[1], 10.0, d(z))
+        x = pos.ravel().copy()
+        traj = np.zeros((steps, 3 * n))
+        dts = np.zeros(steps)
+        q0 = None if q is None else q.copy()
+        lib.refbd_run(h, rseed, pe, dt, steps, nminv, eig[0], eig[1], 10.0, d(lje), d(lj0), 1,
+                      bdrmin, dtlim, 0.0, 0.0, d(F), d(T), d(x), d(q), d(traj), d(dts))
+        lib.ref_free(h)
+        rec = dict(version=ver, pos=pos.ravel(), box=L, eig=eig, z_fb=z, fb_seed=rseed + 100,
+                   seed=rseed, peclet=pe, dt=dt, n_minv=nminv, bd_rmin=bdrmin, dt_lim=dtlim,
+                   shear=np.array(shear, float), traj=traj, dts=dts,
+                   lj=np.array(lj if lj is not None else (0.0, 0.0)))
+        if F is not None:
+            rec["F"] = F
+        if T is not None:
+            rec["T"] = T
+        if q is not None:
+            rec["q0"] = q0
+            rec["q1"] = q
+        for k, v in rec.items():
+            out[f"{name}:{k}"] = np.asarray(v)
+        print(f"bd {name}: dts {dts}, max displacement {np.abs(traj[-1] - pos.ravel()).max():.3e}")
+    return out
 
 
 def main(ref_root: str = "/root/reference"):
@@ -269,6 +357,9 @@ def main(ref_root: str = "/root/reference"):
         ki[f"s{seed}_res53"] = np.array([lib.KIrand_genrand_res53(r) for _ in range(50)])
         ki[f"s{seed}_gauss"] = np.array([lib.KIrand_Gaussian(r) for _ in range(101)])
     np.savez_compressed(os.path.join(HERE, "kirand.npz"), **ki)
+
+    # ---- Brownian dynamics (the reference's brownian.c) -------------------
+    np.savez_compressed(os.path.join(HERE, "bd.npz"), **bd_fixtures())
 
     # ---- struct layouts of the Brownian-dynamics interface ---------------
     json.dump(bd_layouts(ref_root), open(os.path.join(HERE, "bd_layouts.json"), "w"), indent=1)
