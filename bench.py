@@ -228,6 +228,67 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    return json.load(open(path)) if os.path.exists(path) else {}
+
+
+def roofline(lib, abi, sysm, version, n, c, kernels_ms, precision) -> dict:
+    """Roofline of the dominant kernel of one product: algorithmic flops of
+    that kernel per launch over its CUDA-event time (events on the product's
+    own stream), against the peak of the pipe that bounds it."""
+    name = max(kernels_ms, key=kernels_ms.get)
+    ms = kernels_ms[name]
+    peaks = measured_peaks()
+    if name in ("k_sfac_gemm", "k_bp_gemm", "mk_sfac", "mk_backproj"):
+        # reciprocal space: the forward sum or the back-projection, 4 Nk N c
+        # flops each (Nk: the full k sphere of the split)
+        info = np.zeros(9)
+        abi.check(lib.stokes_gpu_mixed_split(sysm.sp, info.ctypes.data_as(abi._dp)))
+        nk_full = 2 * int(info[5])
+        units = nk_full * n * c
+        algo = {"unit": "k vector x particle x component (full k sphere)",
+                "units_per_launch": units, "flops_per_unit": 4, "k_vectors": nk_full,
+                "mixed_split": {"xi": info[0], "rc": info[1], "kc": info[2], "eta": info[3],
+                                "eps": info[4]}}
+        flops = 4.0 * units
+        if name.startswith("k_"):
+            bound = "tensor"
+            peak = peaks.get("bf16_tflops", 1900.0) / 2.0
+            psrc = ("TF32 dense rate taken as half the measured bf16 GEMM rate "
+                    "(MEASURED_PEAKS.json bf16_tflops / 2); the 3xTF32 split executes 3x "
+                    "the algorithmic count and the m1 >= 0 box about 2x more")
+        else:
+            bound = "fp32-pipe"
+            pk = C.c_double()
+            abi.check(lib.stokes_gpu_peak_fma(0, C.byref(pk)))
+            peak = pk.value / 1e3
+            psrc = "FP32 FMA rate measured in this run by an FMA-chain kernel"
+    elif name == "k_real":
+        P = C.c_longlong()
+        abi.check(lib.stokes_gpu_count_real_terms(sysm.sp, C.byref(P)))
+        flops = float(P.value) * FLOPS_PER_TERM[version]
+        algo = {"unit": "pair-image interaction", "units_per_launch": P.value,
+                "flops_per_unit": FLOPS_PER_TERM[version]}
+        bound = "fp64-pipe"
+        pk = C.c_double()
+        abi.check(lib.stokes_gpu_peak_fma(1, C.byref(pk)))
+        peak = pk.value / 1e3
+        psrc = "FP64 FMA rate measured in this run by an FMA-chain kernel"
+    else:
+        return {"kernel": name, "kernel_ms": ms, "achieved": None, "peak": None,
+                "frac": None, "traffic": None, "note": "no algorithmic count for this kernel"}
+    achieved = flops / (ms * 1e-3) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(f"{WORKLOAD['name']}:{precision}:{name}")
+    return {"kernel": name, "bound": bound, "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+            "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
+            "kernel_ms": ms, "algorithmic": algo, "peak_source": psrc}
+
+
 def run_gpu(args):
     import torch
     import libstokes_gb300 as L
@@ -286,6 +347,7 @@ def run_gpu(args):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     abi.check(lib.stokes_gpu_profile_begin(sysm.sp, args.steps))
+    abi.check(lib.stokes_gpu_kprof_begin(sysm.sp, 16 * args.steps))
     barrier()
     torch.cuda.synchronize(dev)
     with ClockSampler(gpu_pci_id(local)) as clk:
@@ -298,6 +360,7 @@ def run_gpu(args):
         torch.cuda.synchronize(dev)
         t_wall = time.perf_counter() - t_wall0
         barrier()
+    kprof = abi.kernel_profile(lib, sysm.sp)
     prof = np.zeros(3)
     cnt = C.c_int()
     abi.check(lib.stokes_gpu_profile_end(sysm.sp, prof.ctypes.data_as(C.POINTER(C.c_double)),
@@ -346,38 +409,8 @@ def run_gpu(args):
     recip_ms = prof[2] / max(cnt.value, 1)
     total_ms = prof[0] / max(cnt.value, 1)
     fp64 = prec == abi.FP64
-    peak = C.c_double()
-    abi.check(lib.stokes_gpu_peak_fma(1 if fp64 else 0, C.byref(peak)))
-    peak_tf = peak.value / 1e3
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get(f"{WORKLOAD['name']}:{args.precision}")
-    if fp64:
-        # dominant: the real-space pair sum over the reference's image table
-        P = C.c_longlong()
-        abi.check(lib.stokes_gpu_count_real_terms(sysm.sp, C.byref(P)))
-        achieved = P.value * FLOPS_PER_TERM[version] / (real_ms * 1e-3) / 1e12
-        roof = {"kernel": "k_real (real-space pair sum, FP64)", "bound": "fp64-pipe",
-                "algorithmic": {"unit": "pair term", "units_per_launch": P.value,
-                                "flops_per_unit": FLOPS_PER_TERM[version], "kernel_ms": real_ms}}
-    else:
-        # dominant: reciprocal space (structure factors + back-projection)
-        info = np.zeros(9)
-        abi.check(lib.stokes_gpu_mixed_split(sysm.sp, info.ctypes.data_as(abi._dp)))
-        nk_full = 2 * int(info[5])
-        achieved = 8.0 * nk_full * n * c / (recip_ms * 1e-3) / 1e12
-        roof = {"kernel": "reciprocal space (mk_sfac + mk_backproj, FP32)", "bound": "fp32-pipe",
-                "algorithmic": {"unit": "k vector x particle x component",
-                                "units_per_launch": nk_full * n * c, "flops_per_unit": 8,
-                                "kernel_ms": recip_ms, "k_vectors": nk_full,
-                                "mixed_split": {"xi": info[0], "rc": info[1], "kc": info[2],
-                                                "eta": info[3], "eps": info[4]}}}
-    roof.update({"achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
-                 "frac": achieved / peak_tf, "traffic": traffic,
-                 "peak_source": ("measured in this run by an FMA-chain kernel "
-                                 f"({'FP64' if fp64 else 'FP32'}); MEASURED_PEAKS.json holds "
-                                 "only the HBM copy and bf16 GEMM figures")})
+    kernels_ms = {k: v[0] / max(v[1], 1) for k, v in kprof.items()}
+    roof = roofline(lib, abi, sysm, version, n, c, kernels_ms, args.precision)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -392,6 +425,7 @@ def run_gpu(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "rel_err_vs_fp64": rel_err,
         "phases_ms": {"total": total_ms, "real": real_ms, "reciprocal": recip_ms},
+        "kernels_ms": kernels_ms,
         "wall_s_timed_region": t_wall,
         "gpu_launches": launches.value * args.steps,
         "e2e": {"value": world / e2e_s, "unit": UNIT,

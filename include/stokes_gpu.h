@@ -96,6 +96,16 @@ int stokes_gpu_last_times (const struct stokes *sys, double *ms3);
 int stokes_gpu_profile_begin (struct stokes *sys, int max_products);
 int stokes_gpu_profile_end (struct stokes *sys, double *sum_ms3, int *count);
 
+/* Kernel profiling window: between begin and end, every product of sys
+ * records a CUDA event on its own stream after each kernel it launches (at
+ * most max_marks events in all).  end waits for them and returns, per kernel
+ * name (32-byte slots in names, at most max_kernels), the summed device
+ * milliseconds between the kernel's event and the previous one and the
+ * number of launches; *nkernels is the number of names filled. */
+int stokes_gpu_kprof_begin (struct stokes *sys, int max_marks);
+int stokes_gpu_kprof_end (struct stokes *sys, int max_kernels, char *names, double *sum_ms,
+                          int *count, int *nkernels);
+
 /* number of kernel launches issued by the last product of sys */
 int stokes_gpu_last_launches (const struct stokes *sys, int *count);
 

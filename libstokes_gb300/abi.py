@@ -184,6 +184,8 @@ _SIGS = {
     "stokes_gpu_last_times": (C.c_int, [_SP, _dp]),
     "stokes_gpu_last_launches": (C.c_int, [_SP, _ip]),
     "stokes_gpu_profile_begin": (C.c_int, [_SP, C.c_int]),
+    "stokes_gpu_kprof_begin": (C.c_int, [_SP, C.c_int]),
+    "stokes_gpu_kprof_end": (C.c_int, [_SP, C.c_int, C.c_char_p, _dp, _ip, _ip]),
     "stokes_gpu_profile_end": (C.c_int, [_SP, _dp, _ip]),
     "stokes_gpu_count_real_terms": (C.c_int, [_SP, C.POINTER(C.c_longlong)]),
     "stokes_gpu_peak_fma": (C.c_int, [C.c_int, _dp]),
@@ -258,6 +260,22 @@ def _d(a):
 
 def ncomp(version: int) -> int:
     return (3, 6, 11)[version]
+
+
+def kernel_profile(lib, sp, max_kernels: int = 16) -> dict:
+    """Close the kernel profiling window of a system: {name: (ms, launches)}."""
+    names = C.create_string_buffer(32 * max_kernels)
+    ms = np.zeros(max_kernels)
+    cnt = np.zeros(max_kernels, dtype=np.int32)
+    nk = C.c_int()
+    check(lib.stokes_gpu_kprof_end(sp, max_kernels, names, ms.ctypes.data_as(_dp),
+                                   cnt.ctypes.data_as(_ip), C.byref(nk)))
+    raw = names.raw
+    out = {}
+    for k in range(nk.value):
+        nm = raw[32 * k:32 * k + 32].split(b"\0", 1)[0].decode()
+        out[nm] = (float(ms[k]), int(cnt[k]))
+    return out
 
 
 class GPUError(RuntimeError):

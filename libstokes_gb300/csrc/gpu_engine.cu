@@ -119,6 +119,7 @@ static void
 free_ctx (Ctx *c)
 {
   for (cudaEvent_t e : c->prof_ev) cudaEventDestroy (e);
+  for (cudaEvent_t e : c->kprof_ev) cudaEventDestroy (e);
   for (DevBuf *b : c->all_buffers ()) b->release ();
   for (int q = 0; q < 4; q++) cudaEventDestroy (c->ev[q]);
   cudaStreamDestroy (c->stream);
@@ -357,6 +358,7 @@ atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   int launches = 0;
   cudaEvent_t *E = phase_events (c, timed);
   if (E) cudaEventRecord (E[0], st);
+  kmark (c, st, nullptr);
 
   // reciprocal space
   if (c->nk > 0)
@@ -365,6 +367,7 @@ atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                                   (double2 *) c->ph.p, st)) != cudaSuccess)
         return cuda_fail (e, "phase kernel");
       launches++;
+      kmark (c, st, "k_phase");
     }
   RecipArgs ra;
   ra.x = d_x;
@@ -379,6 +382,7 @@ atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   if ((e = launch_recip_fp64 (c->version, c->mode, ra, st)) != cudaSuccess)
     return cuda_fail (e, "reciprocal kernels");
   launches += c->nk > 0 ? 2 : 0;
+  if (c->nk > 0) kmark (c, st, "k_sfac+k_backproj");
   if (E) cudaEventRecord (E[1], st);
 
   // real space
@@ -399,12 +403,14 @@ atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   if ((e = launch_real_fp64 (c->version, c->mode, a, st)) != cudaSuccess)
     return cuda_fail (e, "real-space kernel");
   launches++;
+  kmark (c, st, "k_real");
   if (E) cudaEventRecord (E[2], st);
 
   if ((e = launch_combine_fp64 (c->version, d_x, (const double *) c->partial.p, nchunk,
                                 (const double *) c->yrec.p, selfc, np, d_y, st)) != cudaSuccess)
     return cuda_fail (e, "combine kernel");
   launches++;
+  kmark (c, st, "k_combine");
   if (E) cudaEventRecord (E[3], st);
   c->launches = launches;
   c->timed = timed;
@@ -421,6 +427,15 @@ phase_events (Ctx *c, bool timed)
   if (c->prof_on && c->prof_n < (int) (c->prof_ev.size () / 4))
     return &c->prof_ev[4 * (size_t) c->prof_n++];
   return nullptr;
+}
+
+void
+kmark (Ctx *c, cudaStream_t st, const char *name)
+{
+  if (!c || !c->kprof_on || c->kprof_n >= c->kprof_ev.size ()) return;
+  cudaEventRecord (c->kprof_ev[c->kprof_n], st);
+  c->kprof_name[c->kprof_n] = name;
+  c->kprof_n++;
 }
 
 void
@@ -488,12 +503,14 @@ matrix_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st)
   if ((e = c->ph.ensure (sizeof (double2) * (size_t) (c->nk > 0 ? c->nk : 1) * np)) != cudaSuccess)
     return cuda_fail (e, "phase table");
   int launches = 0;
+  kmark (c, st, nullptr);
   if (c->nk > 0)
     {
       if ((e = launch_phase_fp64 (d_pos, (const double *) c->kt.p, c->nk, np,
                                   (double2 *) c->ph.p, st)) != cudaSuccess)
         return cuda_fail (e, "phase kernel");
       launches++;
+      kmark (c, st, "k_phase");
     }
   const double *pp = (const double *) c->pp.p;
   MatArgs a;
@@ -515,6 +532,7 @@ matrix_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st)
   a.mat = d_mat;
   if ((e = launch_matrix_fp64 (c->version, c->mode, a, st)) != cudaSuccess)
     return cuda_fail (e, "matrix kernel");
+  kmark (c, st, "k_matrix");
   c->launches = launches + 1;
   return STOKES_GPU_OK;
 }
@@ -739,6 +757,63 @@ stokes_gpu_profile_end (struct stokes *sys, double *sum_ms3, int *count)
       sum_ms3[2] += t_rec;
     }
   *count = c->prof_n;
+  return STOKES_GPU_OK;
+}
+
+int
+stokes_gpu_kprof_begin (struct stokes *sys, int max_marks)
+{
+  if (!sys || max_marks <= 0) return set_error (STOKES_GPU_EINVAL, "bad profile window");
+  Ctx *c = get_ctx (sys, true);
+  if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  while (c->kprof_ev.size () < (size_t) max_marks)
+    {
+      cudaEvent_t e;
+      if (cudaEventCreate (&e) != cudaSuccess)
+        return set_error (STOKES_GPU_ECUDA, "cannot create events");
+      c->kprof_ev.push_back (e);
+    }
+  c->kprof_name.assign (c->kprof_ev.size (), nullptr);
+  c->kprof_n = 0;
+  c->kprof_on = true;
+  return STOKES_GPU_OK;
+}
+
+int
+stokes_gpu_kprof_end (struct stokes *sys, int max_kernels, char *names, double *sum_ms,
+                      int *count, int *nkernels)
+{
+  if (!sys || !names || !sum_ms || !count || !nkernels || max_kernels <= 0)
+    return set_error (STOKES_GPU_EINVAL, "NULL argument");
+  Ctx *c = get_ctx (sys, false);
+  if (!c || !c->kprof_on) return set_error (STOKES_GPU_EINVAL, "no kernel profile window open");
+  c->kprof_on = false;
+  int nk = 0;
+  for (int k = 0; k < max_kernels; k++) { sum_ms[k] = 0.0; count[k] = 0; }
+  if (c->kprof_n > 0)
+    {
+      cudaError_t e = cudaEventSynchronize (c->kprof_ev[c->kprof_n - 1]);
+      if (e != cudaSuccess) return cuda_fail (e, "kernel profile events");
+    }
+  for (size_t m = 1; m < c->kprof_n; m++)
+    {
+      const char *nm = c->kprof_name[m];
+      if (!nm) continue;
+      int k = 0;
+      while (k < nk && strncmp (names + 32 * k, nm, 31) != 0) k++;
+      if (k == nk)
+        {
+          if (nk == max_kernels) continue;
+          strncpy (names + 32 * k, nm, 31);
+          names[32 * k + 31] = 0;
+          nk++;
+        }
+      float ms = 0.f;
+      cudaEventElapsedTime (&ms, c->kprof_ev[m - 1], c->kprof_ev[m]);
+      sum_ms[k] += ms;
+      count[k] += 1;
+    }
+  *nkernels = nk;
   return STOKES_GPU_OK;
 }
 

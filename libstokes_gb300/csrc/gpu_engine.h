@@ -48,6 +48,13 @@ struct Ctx {
   int prof_n = 0;
   std::vector<cudaEvent_t> prof_ev;
 
+  // kernel profiling window: one event after each launch, tagged with the
+  // kernel's name (nullptr marks the start of a product)
+  bool kprof_on = false;
+  size_t kprof_n = 0;
+  std::vector<cudaEvent_t> kprof_ev;
+  std::vector<const char *> kprof_name;
+
   MixedState *mixed = nullptr;
 
   std::array<DevBuf *, 12> all_buffers ()
@@ -70,6 +77,8 @@ int atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y
                      cudaStream_t st, bool timed);
 void collect_times (Ctx *c);
 cudaEvent_t *phase_events (Ctx *c, bool timed);
+// record a kernel-profiling mark on st when the window is open
+void kmark (Ctx *c, cudaStream_t st, const char *name);
 
 // mixed-precision path (mixed.cu)
 int atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,

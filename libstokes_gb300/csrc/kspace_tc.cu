@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include "ewald_device.cuh"
+#include "gpu_engine.h"
 #include "mixed.h"
 #include "tc_umma.cuh"
 
@@ -306,19 +307,20 @@ k_kop (KGemm g, const MixK *kt, int nk, const float *sf, float2 *W)
   const size_t Rp = (size_t) g.nrt * 64;
   float cs[C], sn[C], ns[C];
 #pragma unroll
-  for (int q = 0; q < C; q++)
+  for (int q = 0; q < C; q++) cs[q] = sn[q] = 0.f;
+  // one slice at a time, its 2C loads issued together
+  for (int s = 0; s < g.nsplit; s++)
     {
-      float a = 0.f, b = 0.f;
-      for (int s = 0; s < g.nsplit; s++)
+      const float *base = sf + (((size_t) s * g.n1 + K.m1) * C * 2) * Rp + K.r;
+#pragma unroll
+      for (int q = 0; q < C; q++)
         {
-          const size_t o = ((((size_t) s * g.n1 + K.m1) * C + q) * 2) * Rp + K.r;
-          a += sf[o];
-          b += sf[o + Rp];
+          cs[q] += base[(size_t) (2 * q) * Rp];
+          sn[q] += base[(size_t) (2 * q + 1) * Rp];
         }
-      cs[q] = a;
-      sn[q] = b;
-      ns[q] = -b;
     }
+#pragma unroll
+  for (int q = 0; q < C; q++) ns[q] = -sn[q];
   const float e[3] = {K.ex, K.ey, K.ez};
   GenF<V, float> gc, gs, gms;
   load_genf<V, float> (cs, gc);
@@ -511,7 +513,7 @@ size_t kgemm_ypart_floats (const KGemm &g) { return (size_t) kgemm_ypart_chunks 
 template <int V>
 static cudaError_t
 launch_v (const KGemm &g, const MixK *kt, int nk, const float *xf, float *sf, float2 *W,
-          float *ypart, int *status, cudaStream_t st)
+          float *ypart, int *status, cudaStream_t st, Ctx *prof)
 {
   cudaError_t e;
   if ((e = cudaFuncSetAttribute (k_sfac_gemm<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -521,20 +523,23 @@ launch_v (const KGemm &g, const MixK *kt, int nk, const float *xf, float *sf, fl
                                  (int) SMEM_DYN)) != cudaSuccess)
     return e;
   k_sfac_gemm<V><<<dim3 (g.nrt, g.ntile_f, g.nsplit), NT, SMEM_DYN, st>>> (g, xf, sf, status);
+  kmark (prof, st, "k_sfac_gemm");
   if ((e = cudaMemsetAsync (W, 0, sizeof (float2) * kgemm_w_elems (g), st)) != cudaSuccess)
     return e;
   k_kop<V><<<(nk + 127) / 128, 128, 0, st>>> (g, kt, nk, sf, W);
+  kmark (prof, st, "k_kop");
   k_bp_gemm<V><<<dim3 (g.mtiles, g.ntile_b, g.ksplit), NT, SMEM_DYN, st>>> (g, W, ypart, status);
+  kmark (prof, st, "k_bp_gemm");
   return cudaGetLastError ();
 }
 
 cudaError_t
 launch_kspace_gemm (int version, const KGemm &g, const MixK *kt, int nk, const float *xf,
-                    float *sf, float2 *W, float *ypart, int *status, cudaStream_t st)
+                    float *sf, float2 *W, float *ypart, int *status, cudaStream_t st, Ctx *prof)
 {
-  if (version == 0) return launch_v<0> (g, kt, nk, xf, sf, W, ypart, status, st);
-  if (version == 1) return launch_v<1> (g, kt, nk, xf, sf, W, ypart, status, st);
-  return launch_v<2> (g, kt, nk, xf, sf, W, ypart, status, st);
+  if (version == 0) return launch_v<0> (g, kt, nk, xf, sf, W, ypart, status, st, prof);
+  if (version == 1) return launch_v<1> (g, kt, nk, xf, sf, W, ypart, status, st, prof);
+  return launch_v<2> (g, kt, nk, xf, sf, W, ypart, status, st, prof);
 }
 
 }  // namespace lsg

@@ -71,11 +71,13 @@ struct PrepArgs {
 };
 
 // wrap to the primary cell (Lees-Edwards aware), fixed-point positions,
-// phase tables e^{2 pi i m u_d}, m = 0..M_d, and x in FP32
+// phase tables e^{2 pi i m u_d}, m = 0..M_d, and x in FP32; one thread per
+// (particle, axis blockIdx.y) so that the FP64 recurrences spread over the SMs
 __global__ void
 mk_prep (PrepArgs a)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int d = blockIdx.y;
   if (j >= a.np) return;
   double x = a.pos[3 * j], y = a.pos[3 * j + 1], z = a.pos[3 * j + 2];
   if (a.shear_mode == 1)
@@ -91,43 +93,43 @@ mk_prep (PrepArgs a)
       x -= w * a.shift;
     }
   double s[3] = {x / a.lx, y / a.ly, z / a.lz};
-  for (int d = 0; d < 3; d++)
+  for (int k = 0; k < 3; k++)
     {
-      s[d] -= floor (s[d]);
-      if (s[d] >= 1.0) s[d] = 0.0;
+      s[k] -= floor (s[k]);
+      if (s[k] >= 1.0) s[k] = 0.0;
     }
-  const double two32 = 4294967296.0;
-  for (int d = 0; d < 3; d++)
+  if (d == 0)
     {
-      double q = floor (s[d] * two32);
-      if (q >= two32) q -= two32;
-      a.qpos[4 * j + d] = (uint32_t) q;
+      const double two32 = 4294967296.0;
+      for (int k = 0; k < 3; k++)
+        {
+          double q = floor (s[k] * two32);
+          if (q >= two32) q -= two32;
+          a.qpos[4 * j + k] = (uint32_t) q;
+        }
+      a.qpos[4 * j + 3] = 0u;
+      for (int q = 0; q < a.c; q++) a.xf[(size_t) j * a.c + q] = (float) a.x[(size_t) j * a.c + q];
     }
-  a.qpos[4 * j + 3] = 0u;
   // phases in turns; the shear-shifted k couples the flow axis to the
   // gradient axis: k.r = 2 pi (m1 (sx - sl sg) + m2 sy + m3 sz)
   const double sl = a.shift / a.lx;
-  double u[3] = {s[0], s[1], s[2]};
-  if (a.shear_mode == 1) u[0] = s[0] - sl * s[1];
-  else if (a.shear_mode == 2) u[0] = s[0] - sl * s[2];
-  const int Md[3] = {a.M0, a.M1, a.M2};
-  size_t off = 0;
-  for (int d = 0; d < 3; d++)
+  double u = s[d];
+  if (d == 0 && a.shear_mode == 1) u = s[0] - sl * s[1];
+  else if (d == 0 && a.shear_mode == 2) u = s[0] - sl * s[2];
+  const int Md = d == 0 ? a.M0 : (d == 1 ? a.M1 : a.M2);
+  const size_t off = d == 0 ? 0 : (d == 1 ? (size_t) (a.M0 + 1) * a.np
+                                          : (size_t) (a.M0 + a.M1 + 2) * a.np);
+  double sb, cb;
+  sincospi (2.0 * u, &sb, &cb);
+  double pr = 1.0, pi = 0.0;
+  for (int m = 0; m <= Md; m++)
     {
-      double sb, cb;
-      sincospi (2.0 * u[d], &sb, &cb);
-      double pr = 1.0, pi = 0.0;
-      for (int m = 0; m <= Md[d]; m++)
-        {
-          a.tab[off + (size_t) m * a.np + j] = make_float2 ((float) pr, (float) pi);
-          const double nr = pr * cb - pi * sb;
-          const double ni = pr * sb + pi * cb;
-          pr = nr;
-          pi = ni;
-        }
-      off += (size_t) (Md[d] + 1) * a.np;
+      a.tab[off + (size_t) m * a.np + j] = make_float2 ((float) pr, (float) pi);
+      const double nr = pr * cb - pi * sb;
+      const double ni = pr * sb + pi * cb;
+      pr = nr;
+      pi = ni;
     }
-  for (int q = 0; q < a.c; q++) a.xf[(size_t) j * a.c + q] = (float) a.x[(size_t) j * a.c + q];
 }
 
 __device__ __forceinline__ float2
@@ -397,32 +399,38 @@ mk_backproj (BpMixArgs a)
     }
 }
 
-// y_i = self_i x_i (FP64) + sum real partials + 2 sum reciprocal partials;
-// one warp per particle, the lanes split the partial chunks
+// y_i = self_i x_i (FP64) + sum real partials + 2 sum reciprocal partials.
+// One thread per particle in small blocks (the FP64 self term spreads over
+// all SMs); the FP32 partials are summed with Kahan compensation.
 template <int V>
 __global__ void
 mk_combine (const double *x, const float *pr, int ncr, const float *pk, int nck,
             const double *selfc, int np, double *y)
 {
   constexpr int C = NComp<V>::value;
-  const int lane = threadIdx.x & 31;
-  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= np) return;
-  double sr[C], sk[C];
+  float sr[C], cr[C], sk[C], ck[C];
 #pragma unroll
-  for (int q = 0; q < C; q++) sr[q] = sk[q] = 0.0;
-  for (int c = lane; c < ncr; c += 32)
+  for (int q = 0; q < C; q++) sr[q] = cr[q] = sk[q] = ck[q] = 0.f;
+  for (int c = 0; c < ncr; c++)
 #pragma unroll
-    for (int q = 0; q < C; q++) sr[q] += (double) pr[((size_t) c * np + i) * C + q];
-  for (int c = lane; c < nck; c += 32)
+    for (int q = 0; q < C; q++)
+      {
+        const float v = pr[((size_t) c * np + i) * C + q] - cr[q];
+        const float t = sr[q] + v;
+        cr[q] = (t - sr[q]) - v;
+        sr[q] = t;
+      }
+  for (int c = 0; c < nck; c++)
 #pragma unroll
-    for (int q = 0; q < C; q++) sk[q] += (double) pk[((size_t) c * np + i) * C + q];
-#pragma unroll
-  for (int q = 0; q < C; q++)
-    {
-      sr[q] = warp_sum (sr[q]);
-      sk[q] = warp_sum (sk[q]);
-    }
+    for (int q = 0; q < C; q++)
+      {
+        const float v = pk[((size_t) c * np + i) * C + q] - ck[q];
+        const float t = sk[q] + v;
+        ck[q] = (t - sk[q]) - v;
+        sk[q] = t;
+      }
   PairScalars<double> s;
   s.xa = s.ya = selfc[3 * i];
   s.xc = s.yc = selfc[3 * i + 1];
@@ -436,7 +444,8 @@ mk_combine (const double *x, const float *pr, int ncr, const float *pk, int nck,
   pair_apply<V, double> (e, s, g, acc);
 #pragma unroll
   for (int q = 0; q < C; q++)
-    if (lane == q) y[(size_t) C * i + q] = acc.v[q] + sr[q] + 2.0 * sk[q];
+    y[(size_t) C * i + q] = acc.v[q] + ((double) sr[q] - (double) cr[q])
+                            + 2.0 * ((double) sk[q] - (double) ck[q]);
 }
 
 // ---------------------------------------------------------------------------
@@ -679,13 +688,15 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
 
   cudaEvent_t *E = phase_events (c, timed);
   if (E) cudaEventRecord (E[0], st);
+  kmark (c, st, nullptr);
   PrepArgs pa;
   pa.pos = d_pos; pa.x = d_x; pa.np = np; pa.c = C;
   pa.lx = sys->lx; pa.ly = sys->ly; pa.lz = sys->lz; pa.shift = sys->shear_shift;
   pa.shear_mode = sys->shear_mode;
   pa.M0 = m->M[0]; pa.M1 = m->M[1]; pa.M2 = m->M[2];
   pa.qpos = (uint32_t *) m->qpos.p; pa.tab = (float2 *) m->tab.p; pa.xf = (float *) m->xf.p;
-  mk_prep<<<(np + 127) / 128, 128, 0, st>>> (pa);
+  mk_prep<<<dim3 ((np + 15) / 16, 3), 16, 0, st>>> (pa);
+  kmark (c, st, "mk_prep");
 
   KMixArgs ka;
   ka.kt = (const MixK *) m->kt.p; ka.tab = (const float2 *) m->tab.p;
@@ -701,14 +712,19 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     {
       if ((e = launch_kspace_gemm (c->version, m->plan, ka.kt, m->nkh, ka.xf, (float *) m->sf.p,
                                    (float2 *) m->wop.p, (float *) m->part_rec.p,
-                                   (int *) m->status.p, st)) != cudaSuccess)
+                                   (int *) m->status.p, st, c)) != cudaSuccess)
         return cuda_fail (e, "reciprocal space (tensor cores)");
     }
   else if (m->nkh > 0)
     {
-      if (c->version == 0) { mk_sfac<0><<<gk, MX_WARPS * 32, 0, st>>> (ka); mk_backproj<0><<<gb, MX_WARPS * 32, 0, st>>> (ba); }
-      else if (c->version == 1) { mk_sfac<1><<<gk, MX_WARPS * 32, 0, st>>> (ka); mk_backproj<1><<<gb, MX_WARPS * 32, 0, st>>> (ba); }
-      else { mk_sfac<2><<<gk, MX_WARPS * 32, 0, st>>> (ka); mk_backproj<2><<<gb, MX_WARPS * 32, 0, st>>> (ba); }
+      if (c->version == 0) mk_sfac<0><<<gk, MX_WARPS * 32, 0, st>>> (ka);
+      else if (c->version == 1) mk_sfac<1><<<gk, MX_WARPS * 32, 0, st>>> (ka);
+      else mk_sfac<2><<<gk, MX_WARPS * 32, 0, st>>> (ka);
+      kmark (c, st, "mk_sfac");
+      if (c->version == 0) mk_backproj<0><<<gb, MX_WARPS * 32, 0, st>>> (ba);
+      else if (c->version == 1) mk_backproj<1><<<gb, MX_WARPS * 32, 0, st>>> (ba);
+      else mk_backproj<2><<<gb, MX_WARPS * 32, 0, st>>> (ba);
+      kmark (c, st, "mk_backproj");
     }
   else
     cudaMemsetAsync (m->part_rec.p, 0, sizeof (float) * (size_t) m->nchunk_k * np * C, st);
@@ -737,6 +753,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   if (c->version == 0) mk_real<0, MODE_MONO><<<gr, MX_WARPS * 32, 0, st>>> (ra);
   else if (c->version == 1) mk_real<1, MODE_MONO><<<gr, MX_WARPS * 32, 0, st>>> (ra);
   else mk_real<2, MODE_MONO><<<gr, MX_WARPS * 32, 0, st>>> (ra);
+  kmark (c, st, "mk_real");
   if (E) cudaEventRecord (E[2], st);
 
   // self constants of the mixed split (equal spheres)
@@ -755,10 +772,11 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
         m->self_np = np;
       }
   }
-  const int gc = (np + 3) / 4;      // four particles (warps) per CTA
-  if (c->version == 0) mk_combine<0><<<gc, 128, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
-  else if (c->version == 1) mk_combine<1><<<gc, 128, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
-  else mk_combine<2><<<gc, 128, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
+  const int gc = (np + 7) / 8;      // eight particles per CTA
+  if (c->version == 0) mk_combine<0><<<gc, 8, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
+  else if (c->version == 1) mk_combine<1><<<gc, 8, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
+  else mk_combine<2><<<gc, 8, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
+  kmark (c, st, "mk_combine");
   if (E) cudaEventRecord (E[3], st);
   if (m->tensor)
     cudaMemcpyAsync (m->h_status, m->status.p, sizeof (int), cudaMemcpyDeviceToHost, st);

@@ -49,8 +49,9 @@ size_t kgemm_ypart_floats (const KGemm &g);   // partial y, [ksplit][ntile_b][np
 int kgemm_ypart_chunks (const KGemm &g);       // ksplit * ntile_b
 
 // forward GEMM -> per-k operators W -> backward GEMM into ypart
+struct Ctx;
 cudaError_t launch_kspace_gemm (int version, const KGemm &g, const MixK *kt, int nk,
                                 const float *xf, float *sf, float2 *W, float *ypart,
-                                int *status, cudaStream_t st);
+                                int *status, cudaStream_t st, Ctx *prof);
 
 }  // namespace lsg
