@@ -41,7 +41,7 @@ struct MixedState {
   int nk_split = 0;      // rows of the re-tuned split; the rest: reference G term
   double selfc[3] = {0, 0, 0};
   std::vector<MixK> h_k;
-  DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf, status, sf, wop, rowm;
+  DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf, status, sf, wop, rowm, tbuf;
   int nrow = 0;          // (m2, m3) rows of the tensor-core contraction
   int *h_status = nullptr;      // pinned copy of the kernels' status word
   bool tensor = true;           // reciprocal space on the tensor cores
@@ -679,6 +679,8 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     {
       if ((e = m->sf.ensure (sizeof (float) * kgemm_sf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "structure factors");
       if ((e = m->wop.ensure (sizeof (float2) * kgemm_w_elems (m->plan))) != cudaSuccess) return cuda_fail (e, "k operators");
+      if ((e = m->tbuf.ensure (sizeof (float2) * kgemm_t_elems (m->plan))) != cudaSuccess) return cuda_fail (e, "row phase table");
+      m->plan.T = (float2 *) m->tbuf.p;
     }
   else if ((e = m->pq.ensure (sizeof (float) * 2 * C * (size_t) (m->nkh > 0 ? m->nkh : 1))) != cudaSuccess)
     return cuda_fail (e, "pq");
@@ -782,7 +784,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     cudaMemcpyAsync (m->h_status, m->status.p, sizeof (int), cudaMemcpyDeviceToHost, st);
   e = cudaGetLastError ();
   if (e != cudaSuccess) return cuda_fail (e, "mixed kernels");
-  c->launches = m->nkh == 0 ? 3 : (m->tensor ? 6 : 5);
+  c->launches = m->nkh == 0 ? 3 : (m->tensor ? 7 : 5);
   c->timed = timed;
   return STOKES_GPU_OK;
 }
@@ -799,7 +801,7 @@ release_mixed (Ctx *c)
   if (!c->mixed) return;
   MixedState *m = c->mixed;
   for (DevBuf *b : {&m->kt, &m->qpos, &m->tab, &m->xf, &m->pq, &m->part_real, &m->part_rec,
-                    &m->selfbuf, &m->status, &m->sf, &m->wop, &m->rowm})
+                    &m->selfbuf, &m->status, &m->sf, &m->wop, &m->rowm, &m->tbuf})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
   delete m;

@@ -39,12 +39,15 @@ struct KGemm {
   int gb, ntile_b, nb;    // m1 per backward column tile, tiles, MMA N
   int mtiles;             // 128-particle row tiles of the backward GEMM
   int rper, ksplit;       // rows per backward K slice, number of slices
+  float2 *T;              // T_r(j) = t1[m2](j) t2[m3](j), [R][ldT]
+  int ldT;                // particles padded to a multiple of 16
 };
 
 KGemm kgemm_plan (int version, PhaseTables t, const int2 *rowm, int R);
 bool kgemm_fits (const KGemm &g);
 size_t kgemm_sf_floats (const KGemm &g);      // partial structure factors
 size_t kgemm_w_elems (const KGemm &g);        // complex operators W (float2)
+size_t kgemm_t_elems (const KGemm &g);        // row phase table T (float2)
 size_t kgemm_ypart_floats (const KGemm &g);   // partial y, [ksplit][ntile_b][np][c]
 int kgemm_ypart_chunks (const KGemm &g);       // ksplit * ntile_b
 

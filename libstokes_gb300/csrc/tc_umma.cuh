@@ -139,6 +139,40 @@ mbar_wait (uint64_t *mbar, uint32_t parity, uint32_t limit)
   return false;
 }
 
+// one arrival on an mbarrier (release at CTA scope)
+__device__ __forceinline__ void
+mbar_arrive (uint64_t *mbar)
+{
+  asm volatile ("{\n\t.reg .b64 st;\n\t"
+                "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}"
+                :: "r"(smem_u32 (mbar)) : "memory");
+}
+
+// wait for phase `parity`, giving up early when *abort (a CTA-wide error flag
+// in shared memory) becomes non-zero; returns false when the wait did not
+// complete.  Each poll lets the thread sleep until the phase completes or
+// about 20 us pass (the try_wait suspend-time hint), so waiting warps do not
+// take issue slots from working ones; `limit` polls bound the wait to about
+// limit x 20 us.
+__device__ __forceinline__ bool
+mbar_wait_or_abort (uint64_t *mbar, uint32_t parity, uint32_t limit, volatile int *abort)
+{
+  const uint32_t a = smem_u32 (mbar);
+  for (uint32_t it = 0; it < limit; it++)
+    {
+      uint32_t done;
+      asm volatile (
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done) : "r"(a), "r"(parity), "r"(20000u) : "memory");
+      if (done) return true;
+      if (*abort) return false;
+    }
+  *abort = 1;
+  return false;
+}
+
 // generic-proxy smem writes -> visible to the tensor core (async proxy)
 __device__ __forceinline__ void
 fence_async_smem ()
