@@ -187,6 +187,44 @@ def bd_measure(lib, abi, L, torch, dev):
                                          "rmin")}}
 
 
+ADJ_WORKLOAD = dict(name="vjp_ft_n2048_phi0.25", version=1, n=2048, phi=0.25, seed=42)
+
+
+def adjoint_measure(lib, abi, L):
+    """Vector-Jacobian product of L = g . M(r) f (FT, N = 2048, phi 0.25,
+    g, f ~ N(0,1)) against one forward product on the same system, both
+    FP64 through the host API (wall clock, copies included)."""
+    from libstokes_gb300.workloads import rsa_positions
+    w = ADJ_WORKLOAD
+    pos, Lb = rsa_positions(w["n"], w["phi"], seed=w["seed"])
+    s = L.System(w["version"], pos, (Lb,) * 3)
+    c = (3, 6, 11)[w["version"]]
+    rng = np.random.default_rng(1)
+    g = rng.standard_normal(c * w["n"])
+    f = rng.standard_normal(c * w["n"])
+    dr = np.zeros(3 * w["n"])
+    db = np.zeros(3)
+    Lv = C.c_double()
+    dp = abi._dp
+
+    def vjp():
+        abi.check(lib.stokes_gpu_vjp(s.sp, g.ctypes.data_as(dp), f.ctypes.data_as(dp),
+                                     dr.ctypes.data_as(dp), db.ctypes.data_as(dp), None))
+
+    s.atimes(f)
+    vjp()
+    t0 = time.perf_counter()
+    s.atimes(f)
+    fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    vjp()
+    adj = time.perf_counter() - t0
+    s.close()
+    return {"workload": w["name"], "precision": "fp64", "forward_s": fwd, "vjp_s": adj,
+            "vjp_over_forward": adj / fwd, "outputs": "dL/dr (6144) and dL/dl (3)",
+            "timing": "wall clock around one call each, host buffers"}
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU algorithm (the oracle port; the
     reference sources themselves are not on this machine) on the host cores."""
@@ -451,6 +489,8 @@ def run_gpu(args):
                              "mixed_over_fp64": (1000.0 / ms) / (1000.0 / fp64_ms)}
     if not args.no_bd:
         line["bd"] = bd_measure(lib, abi, L, torch, dev)
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_measure(lib, abi, L)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, Lbox, x)
     sysm.close()
@@ -470,6 +510,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-bd", action="store_true", help="skip the Brownian-dynamics leg")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (VJP) leg")
     ap.add_argument("--n", type=int, default=None,
                     help="override N (smaller cases for profiler captures)")
     args = ap.parse_args()

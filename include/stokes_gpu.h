@@ -96,6 +96,16 @@ int stokes_gpu_last_times (const struct stokes *sys, double *ms3);
 int stokes_gpu_profile_begin (struct stokes *sys, int max_products);
 int stokes_gpu_profile_end (struct stokes *sys, double *sum_ms3, int *count);
 
+/* Vector-Jacobian product of the mobility product (FP64): for
+ * L = g . M(r, box) f (g, f: host vectors in the product's layout), the
+ * gradient dLdr[3 np] with respect to the positions and, when dLdbox is not
+ * NULL, dLdbox[3] = dL/dl_x, dL/dl_y, dL/dl_z with the particles held fixed,
+ * both at the system's image and k sets and its xi.  Lval (optional)
+ * receives L.  F and FT versions, equal spheres without slip; the box
+ * derivatives need shear_mode 0.  No counterpart in libstokes. */
+int stokes_gpu_vjp (struct stokes *sys, const double *g, const double *f, double *dLdr,
+                    double *dLdbox, double *Lval);
+
 /* Kernel profiling window: between begin and end, every product of sys
  * records a CUDA event on its own stream after each kernel it launches (at
  * most max_marks events in all).  end waits for them and returns, per kernel

@@ -27,14 +27,23 @@ _ip = C.POINTER(C.c_int)
 
 
 def build_oracle(force: bool = False) -> str:
-    """Compile oracle/oracle_ewald.c (and oracle_bd.c) into liboracle.so."""
-    srcs = [os.path.join(HERE, f) for f in ("oracle_ewald.c", "oracle_bd.c")
+    """Compile oracle/oracle_ewald.c, oracle_bd.c and oracle_adjoint.cpp into
+    liboracle.so."""
+    srcs = [os.path.join(HERE, f) for f in ("oracle_ewald.c", "oracle_bd.c", "oracle_adjoint.cpp")
             if os.path.exists(os.path.join(HERE, f))]
     if (not force and os.path.exists(ORACLE_SO)
             and all(os.path.getmtime(ORACLE_SO) >= os.path.getmtime(s) for s in srcs)):
         return ORACLE_SO
-    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-o", ORACLE_SO] + srcs + ["-lm"]
-    subprocess.check_call(cmd)
+    objs = []
+    for src in srcs:
+        obj = ORACLE_SO + "." + os.path.basename(src) + ".o"
+        cc = "g++" if src.endswith(".cpp") else "gcc"
+        std = ["-std=c++17"] if src.endswith(".cpp") else []
+        subprocess.check_call([cc, "-O2", "-fPIC", "-fopenmp"] + std + ["-c", src, "-o", obj])
+        objs.append(obj)
+    subprocess.check_call(["g++", "-shared", "-fopenmp", "-o", ORACLE_SO] + objs + ["-lm"])
+    for obj in objs:
+        os.remove(obj)
     return ORACLE_SO
 
 
@@ -155,6 +164,25 @@ class _Backend:
         self._f("atimes")(self.h, _d(x), _d(y))
         return y
 
+    def vjp(self, pos, g, f, rmin=0.0):
+        """(L, dL/dr, dL/dbox) of L = g . M f (oracle/oracle_adjoint.cpp), on
+        this system's split and image table (F, FT; equal spheres, no shear)."""
+        sp = self.split()
+        rl, rm = self.table()
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        dr = np.zeros(3 * self.np)
+        db = np.zeros(3)
+        L = C.c_double()
+        kx, ky, kz = sp["kmaxxyz"]
+        lib = Oracle.lib()
+        lib.oracle_vjp(self.version, self.np, _d(pos), *self.box, sp["xi"], sp["rmax2"],
+                       float(rmin), sp["nr"], _d(np.ascontiguousarray(rl)),
+                       np.ascontiguousarray(rm).ctypes.data_as(_ip), kx, ky, kz, sp["kmax"],
+                       sp["self_a"], sp["self_c"], _d(g), _d(f), _d(dr), _d(db), C.byref(L))
+        return L.value, dr, db
+
     def matrix(self):
         m = np.zeros((self.n, self.n))
         self._f("matrix")(self.h, _d(m))
@@ -179,6 +207,11 @@ class Oracle(_Backend):
             build_oracle()
             lib = super().lib()
             lib.oracle_set_threads.argtypes = [C.c_void_p, C.c_int]
+            lib.oracle_vjp.restype = None
+            lib.oracle_vjp.argtypes = ([C.c_int, C.c_int, _dp] + [C.c_double] * 6
+                                       + [C.c_int, _dp, _ip, C.c_int, C.c_int, C.c_int,
+                                          C.c_double, C.c_double, C.c_double, _dp, _dp, _dp,
+                                          _dp, C.POINTER(C.c_double)])
             lib.oracle_atimes_part.argtypes = [C.c_void_p, _dp, _dp, C.c_int]
             lib.oracle_atimes_rows.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int]
             lib.oracle_count_real_terms.restype = C.c_longlong
