@@ -225,6 +225,77 @@ def adjoint_measure(lib, abi, L):
             "timing": "wall clock around one call each, host buffers"}
 
 
+BATCH_WORKLOAD = dict(name="ensemble_512_n16-512_phi0.05-0.35_F_FT", nsys=512, nmin=16,
+                      nmax=512, phimin=0.05, phimax=0.35, seed=2024, bd_steps=10, n_cheb=30)
+
+
+def batch_measure(lib, abi, L, nsys=None):
+    """Ensemble of independent periodic systems (N ~ U{16..512}, phi ~
+    U[0.05, 0.35], F and FT alternating, forces N(0,1) float32): one batched
+    mixed product of all systems and 10 batched BD steps (Chebyshev 30 on
+    20-step Lanczos bounds, device noise), against a host loop of
+    single-system mixed products over the first 32 systems."""
+    from libstokes_gb300.workloads import rsa_positions
+    w = BATCH_WORKLOAD
+    ns = nsys or w["nsys"]
+    rng = np.random.default_rng(w["seed"])
+    systems = []
+    for s in range(ns):
+        n = int(rng.integers(w["nmin"], w["nmax"] + 1))
+        phi = float(rng.uniform(w["phimin"], w["phimax"]))
+        pos, Lb = rsa_positions(n, phi, seed=w["seed"] + s)
+        systems.append(L.System(s % 2, pos, (Lb,) * 3))
+    arr = (C.POINTER(abi.StokesStruct) * ns)(*[sy.sp for sy in systems])
+    h = C.c_void_p()
+    t0 = time.perf_counter()
+    abi.check(lib.stokes_gpu_batch_create(arr, ns, abi.MIXED, C.byref(h)))
+    t_create = time.perf_counter() - t0
+    npt, nt = C.c_int(), C.c_int()
+    lib.stokes_gpu_batch_size(h, C.byref(npt), C.byref(nt))
+    x = rng.standard_normal(nt.value).astype(np.float32).astype(np.float64)
+    y = np.zeros(nt.value)
+    dp = abi._dp
+    t0 = time.perf_counter()
+    abi.check(lib.stokes_gpu_batch_atimes(h, x.ctypes.data_as(dp), y.ctypes.data_as(dp)))
+    t_tune = time.perf_counter() - t0
+    reps, dev_ms = 5, []
+    st = np.zeros(4)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        abi.check(lib.stokes_gpu_batch_atimes(h, x.ctypes.data_as(dp), y.ctypes.data_as(dp)))
+        lib.stokes_gpu_batch_stats(h, st.ctypes.data_as(dp))
+        dev_ms.append(st[0])
+    t_prod = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    abi.check(lib.stokes_gpu_batch_bd(h, 1.0, 1e-3, w["n_cheb"], 20, None, None, 11,
+                                      w["bd_steps"], None))
+    t_bd = time.perf_counter() - t0
+    abi.check(lib.stokes_gpu_batch_destroy(h))
+    # the per-system alternative: a host loop of single-system products
+    loop = systems[:32]
+    xs = [rng.standard_normal(sy.n) for sy in loop]
+    for sy, xv in zip(loop, xs):
+        sy.set_precision(abi.MIXED)
+        sy.atimes(xv)
+    t0 = time.perf_counter()
+    for sy, xv in zip(loop, xs):
+        sy.atimes(xv)
+    t_loop = (time.perf_counter() - t0) / len(loop) * ns
+    for sy in systems:
+        sy.close()
+    return {"workload": w["name"], "systems": ns, "particles": npt.value, "precision": "mixed",
+            "batch_product_ms_device": float(np.median(dev_ms)),
+            "batch_product_ms_wall": 1000.0 * t_prod,
+            "system_products_per_s": ns / t_prod,
+            "bd_steps": w["bd_steps"], "bd_wall_s": t_bd,
+            "systems_per_s_product_plus_bd": ns / (t_prod + t_bd),
+            "host_loop_product_ms_extrapolated": 1000.0 * t_loop,
+            "batch_over_host_loop": t_loop / t_prod,
+            "autotuned": {"chunk_mult": st[1], "real_warps_per_cta": st[2]},
+            "create_s": t_create, "first_product_with_autotune_s": t_tune,
+            "k_vectors_total": st[3]}
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU algorithm (the oracle port; the
     reference sources themselves are not on this machine) on the host cores."""
@@ -491,6 +562,8 @@ def run_gpu(args):
         line["bd"] = bd_measure(lib, abi, L, torch, dev)
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measure(lib, abi, L)
+    if not args.no_batch:
+        line["batch"] = batch_measure(lib, abi, L)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, Lbox, x)
     sysm.close()
@@ -511,6 +584,7 @@ def main():
     ap.add_argument("--no-bd", action="store_true", help="skip the Brownian-dynamics leg")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (VJP) leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the ensemble (batch) leg")
     ap.add_argument("--n", type=int, default=None,
                     help="override N (smaller cases for profiler captures)")
     args = ap.parse_args()

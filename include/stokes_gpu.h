@@ -106,6 +106,44 @@ int stokes_gpu_profile_end (struct stokes *sys, double *sum_ms3, int *count);
 int stokes_gpu_vjp (struct stokes *sys, const double *g, const double *f, double *dLdr,
                     double *dLdbox, double *Lval);
 
+/* Batches: many independent periodic systems (each a struct stokes set up
+ * as for atimes_ewald_3all) whose products run together, a few launches for
+ * the whole batch replayed from a CUDA graph.  Vectors are packed: the
+ * systems' vectors in libstokes' per-particle layout, one after the other
+ * (offsets from stokes_gpu_batch_offsets).  STOKES_GPU_FP64 batches use each
+ * system's own split (parity with atimes_ewald_3all); STOKES_GPU_MIXED
+ * batches (F and FT equal spheres) re-split every system as the mixed
+ * product does and tune their launch shapes on the first product.  The
+ * positions are read at creation (and by stokes_gpu_batch_set_positions);
+ * the box, split and version of every system are fixed for the batch's life.
+ * No counterpart in libstokes (there: a loop over systems). */
+typedef struct stokes_gpu_batch stokes_gpu_batch;
+int stokes_gpu_batch_create (struct stokes **systems, int nsys, int precision,
+                             stokes_gpu_batch **out);
+int stokes_gpu_batch_destroy (stokes_gpu_batch *b);
+/* particles and vector length over the whole batch */
+int stokes_gpu_batch_size (const stokes_gpu_batch *b, int *np_total, int *n_total);
+/* per system: first particle (p_off[s]) and first vector element (x_off[s]) */
+int stokes_gpu_batch_offsets (const stokes_gpu_batch *b, int *p_off, int *x_off);
+/* packed positions (3 per particle) of every system; also written back to
+ * each system's pos */
+int stokes_gpu_batch_set_positions (stokes_gpu_batch *b, const double *pos_packed);
+/* y = M x for every system, packed host vectors */
+int stokes_gpu_batch_atimes (stokes_gpu_batch *b, const double *x, double *y);
+/* device ms of the last batch product, chosen real-space chunking and warps
+ * per CTA, total k vectors (mixed) */
+int stokes_gpu_batch_stats (const stokes_gpu_batch *b, double *out4);
+/* nsteps Brownian-dynamics mid-point steps of every system of the batch
+ * (no repulsion, no imposed flow): f = sqrt(2 / (peclet dt)) z with
+ * z = M^{-1/2} y by an n_cheb-term Chebyshev series on per-system bounds
+ * eig[2 s], eig[2 s + 1] (NULL: FP64 Lanczos on the batch products,
+ * n_lanczos steps, widened by 0.8 and 1.05); y read from y_host (n_total
+ * values per step) or, when y_host is NULL, drawn on the device (Philox,
+ * seed).  pos_out (optional) receives the packed positions. */
+int stokes_gpu_batch_bd (stokes_gpu_batch *b, double peclet, double dt, int n_cheb,
+                         int n_lanczos, const double *eig, const double *y_host,
+                         unsigned long long seed, int nsteps, double *pos_out);
+
 /* Kernel profiling window: between begin and end, every product of sys
  * records a CUDA event on its own stream after each kernel it launches (at
  * most max_marks events in all).  end waits for them and returns, per kernel

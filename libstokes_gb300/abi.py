@@ -210,6 +210,17 @@ _SIGS = {
     "stokes_gpu_bd_step_noise": (C.c_int, [C.c_void_p, C.c_double, _dp]),
     "stokes_gpu_bd_run": (C.c_int, [C.c_void_p, C.c_double, C.c_int]),
     "stokes_gpu_bd_stats": (C.c_int, [C.c_void_p, _dp]),
+    # batches
+    "stokes_gpu_batch_create": (C.c_int, [C.POINTER(_SP), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "stokes_gpu_batch_destroy": (C.c_int, [C.c_void_p]),
+    "stokes_gpu_batch_size": (C.c_int, [C.c_void_p, _ip, _ip]),
+    "stokes_gpu_batch_offsets": (C.c_int, [C.c_void_p, _ip, _ip]),
+    "stokes_gpu_batch_set_positions": (C.c_int, [C.c_void_p, _dp]),
+    "stokes_gpu_batch_atimes": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "stokes_gpu_batch_stats": (C.c_int, [C.c_void_p, _dp]),
+    "stokes_gpu_batch_bd": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int, _dp,
+                                      _dp, C.c_ulonglong, C.c_int, _dp]),
+    "stokes_gpu_vjp": (C.c_int, [_SP, _dp, _dp, _dp, _dp, _dp]),
     # libstokes' BD routines
     "EV_LJ_init": (C.POINTER(EVLJStruct), [C.c_int]),
     "EV_LJ_free": (None, [C.POINTER(EVLJStruct)]),

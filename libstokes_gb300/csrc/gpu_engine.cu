@@ -146,7 +146,7 @@ release_ctx (const struct stokes *sys)
 // ---------------------------------------------------------------------------
 // host-side tables
 // ---------------------------------------------------------------------------
-static int
+int
 check_sys (const struct stokes *sys)
 {
   if (sys == nullptr) return set_error (STOKES_GPU_EINVAL, "struct stokes is NULL");
@@ -167,7 +167,7 @@ check_sys (const struct stokes *sys)
 // shift of src/ewald.c:678-686 folded in.  Cube form ("_notbl"): the cube
 // |m| <= rmax{x,y,z} with the running shear shift of src/ewald.c:1843-1861
 // (rlx is reset per m1 only, so the shift accumulates over m2, m3).
-static void
+void
 build_images (const struct stokes *sys, bool cube, std::vector<Img4> &img)
 {
   img.clear ();
@@ -202,7 +202,7 @@ build_images (const struct stokes *sys, bool cube, std::vector<Img4> &img)
 
 // reciprocal table: the k cube |m_i| <= kmax{x,y,z} without 0, the sphere
 // |k| <= kmax unless kmax == 0, Lees-Edwards shifted (src/ewald.c:923-958)
-static void
+void
 build_ktable (const struct stokes *sys, std::vector<double> &kt)
 {
   kt.clear ();
@@ -239,7 +239,7 @@ build_ktable (const struct stokes *sys, std::vector<double> &kt)
 
 // per-particle arrays: radii (1 when a == NULL), slip radii, squared
 // Laplacian radii, and self scalars (src/ewald.c:540-643)
-static void
+void
 build_particles (const struct stokes *sys, int mode, std::vector<double> &pp)
 {
   const int np = sys->np;

@@ -69,6 +69,11 @@ int cuda_fail (cudaError_t e, const char *where);
 void dropin_failed (const char *fn, double *out, size_t nout);
 
 Ctx *get_ctx (const struct stokes *sys, bool create);
+// host tables of one system (gpu_engine.cu)
+int check_sys (const struct stokes *sys);
+void build_images (const struct stokes *sys, bool cube, std::vector<Img4> &img);
+void build_ktable (const struct stokes *sys, std::vector<double> &kt);
+void build_particles (const struct stokes *sys, int mode, std::vector<double> &pp);
 int release_ctx (const struct stokes *sys);
 int prepare (Ctx *c, const struct stokes *sys, bool cube);
 int atimes_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
