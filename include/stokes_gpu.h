@@ -170,6 +170,13 @@ int stokes_gpu_mixed_split (struct stokes *sys, double *info9);
  * absolute products (expect ~1e-7) */
 int stokes_gpu_selftest_tensor (double *max_rel_err);
 
+/* known-answer test of the TMA path of the reciprocal-space GEMMs: operand
+ * images (TF32 hi/lo planes) loaded by 3-d TMA boxes with 128-byte swizzle
+ * (including zero-filled rows past the end), a 128 x 32 x 64 product in
+ * 3xTF32 on the swizzled descriptors; largest error relative to the sum of
+ * absolute products (expect ~1e-7) */
+int stokes_gpu_selftest_tma (double *max_rel_err);
+
 /* measured FMA throughput of the current GPU in GFLOP/s (2 flops per FMA),
  * fp64 = 1 for FP64, 0 for FP32 */
 int stokes_gpu_peak_fma (int fp64, double *gflops);

@@ -191,6 +191,7 @@ _SIGS = {
     "stokes_gpu_peak_fma": (C.c_int, [C.c_int, _dp]),
     "stokes_gpu_mixed_split": (C.c_int, [_SP, _dp]),
     "stokes_gpu_selftest_tensor": (C.c_int, [_dp]),
+    "stokes_gpu_selftest_tma": (C.c_int, [_dp]),
     # Brownian dynamics
     "KIrand_init": (C.POINTER(KIrandStruct), []),
     "KIrand_free": (None, [C.POINTER(KIrandStruct)]),

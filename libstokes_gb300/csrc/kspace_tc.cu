@@ -1,108 +1,86 @@
 // kspace_tc.cu -- reciprocal space of the mixed product as tensor-core GEMMs.
 //
-// With per-axis phase tables t_d[m](j) = e^{2 pi i m u_d(j)}, the phase of a
-// k vector factorises, e^{ik.r_j} = t0[m1](j) T_r(j) with T_r = t1[m2] t2[m3]
-// for the row r = (m2, m3).  So the structure factors of every k vector of the
-// list come out of ONE complex GEMM over the particles,
+// With the fixed-point fractional coordinates u_d(j) of the particles, the
+// phase of k = (m1, m2, m3) factorises, e^{ik.r_j} = t0[m1](j) T_r(j) with
+// t0[m1] = e^{2 pi i m1 u_x} and T_r = e^{2 pi i (m2 u_y + m3 u_z)} for the
+// row r = (m2, m3).  So the structure factors of every k vector of the list
+// come out of ONE complex GEMM over the particles and the back-projection
+// out of another:
 //
-//   forward   S[r, (m1, q)] = sum_j T_r(j) Z_(m1,q)(j),  Z = t0[m1] x_q
-//             real rows (r, re|im), K = (j, u|v) with a, b = Re, Im T and
-//             u, v = Re, Im Z:  A[(r,re),(j,u|v)] = (a, -b), A[(r,im),.] = (b, a)
-//   operator  W_k = P_k + i Q_k from S(k) for every k of the half-space list
-//   backward  H[i, (m1, re|im, q)] = sum_(r, u|v) conj(T_r)(i) W[r, (m1, q)]
-//             A'[i,(r,u|v)] = (a, b), B' columns Re H <- (Re W, Im W),
-//             Im H <- (Im W, -Re W);  y_i[q] += Re(conj(t0[m1])(i) H) summed
-//             over m1 in the epilogue.
+//   forward   S[r, (m1, q)] = sum_j T_r(j) Z_(m1,q)(j),   Z = t0[m1] x_q
+//             real rows r; columns (m1, re|im, q); K = (j, a|b) with
+//             (a, b) = (Re, Im) T_r(j):  A = TF[r][(j, a|b)];
+//             B row (m1, re, q) = (u, -v), row (m1, im, q) = (v, u) with
+//             (u, v) = Z  (ZF)
+//   operator  W_k = P_k + i Q_k for every k of the half-space list (k_kop)
+//   backward  H[i, (m1, re|im, q)] = sum_r conj(T_r)(i) W[r, (m1, q)]:
+//             A' = TB[i][(r, a|b)]; B' row (m1, re, q) = (U, V), row
+//             (m1, im, q) = (V, -U) with (U, V) = W  (WB);
+//             y_i[q] += Re(conj(t0[m1])(i) H) over m1 in the epilogue.
 //
-// The rows r are the (m2, m3) combinations that occur in the k list; T_r(j)
-// is tabulated once per product (k_tprep) for both GEMMs.  Both are tcgen05
-// kind::tf32 MMAs (M = 128, N <= 128, K = 8 per instruction) in 3xTF32:
-// x = hi + lo, products hi*hi + hi*lo + lo*hi.  The tensor core's FP32
-// accumulation truncates at the accumulator's magnitude, so the chains are
-// kept short: every 32-wide K tile starts fresh accumulators (hi*hi in one,
-// the two corrections in another) that are drained into FP32 registers
-// (round to nearest).
+// Each operand is written once per product as an IMAGE: an FP32 array
+// [2][rows][K] (plane 0 the TF32-rounded value, plane 1 the TF32-rounded
+// remainder, x = hi + lo), K contiguous and already in the sign pattern
+// above.  A GEMM tile is then four TMA loads (A hi, A lo, B hi, B lo, 32 K
+// values = 128 bytes per row, 128-byte swizzle) with no operand arithmetic in
+// the GEMM kernel.  The products are tcgen05 kind::tf32 MMAs (M = 128,
+// N <= 128, K = 8 per instruction) in 3xTF32: hi*hi + hi*lo + lo*hi.  The
+// tensor core's FP32 accumulation truncates at the accumulator's magnitude,
+// so every 32-wide K tile starts fresh accumulators (hi*hi in one, the two
+// corrections in another) that are drained into FP32 registers (round to
+// nearest).
 //
-// Warp roles (512 threads, one CTA per SM):
+// Warp roles (320 threads, one CTA per SM):
 //   warps 0-7   drain: double-buffered TMEM accumulators (2 x (main +
 //               correction) x 128 columns = 512 columns); warp w reads TMEM
 //               lanes 32 (w % 4) and columns 64 (w / 4) of each buffer
-//   warps 8-14  builders: fill a 3-stage ring of shared-memory operand tiles
-//               (K-major, no swizzle, hi and lo), whole 8-row core matrices
-//               per warp with 8-byte stores
-//   warp 15     one lane issues the MMAs of a tile when its stage is full
+//   warp 8      one lane issues the TMA loads of a 3-stage ring
+//   warp 9      one lane issues the MMAs of a tile when its stage is full
 //               and its accumulator buffer has been drained
 // The roles meet only at mbarriers; every wait is bounded and watches a CTA
-// error flag, so a wait that runs out ends every role, raises *status, and
-// the MMA lane waits for its MMAs in flight before the TMEM is freed.
+// error flag, so a wait that runs out ends every role and raises *status;
+// the TMA lane waits for its loads in flight and the MMA lane for its MMAs
+// before the CTA frees its TMEM and exits.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "ewald_device.cuh"
 #include "gpu_engine.h"
 #include "mixed.h"
 #include "tc_umma.cuh"
+#include "tma_host.h"
 
 namespace lsg {
 namespace {
 
-constexpr int NT = 512;                 // threads per CTA (16 warps)
+constexpr int NT = 320;                 // threads per CTA (10 warps)
 constexpr int NDRAIN = 8;               // drain warps 0..7
-constexpr int BW0 = 8, NBW = 7;         // builder warps 8..14
-constexpr int MMA_WARP = 15;
+constexpr int TMA_WARP = 8;
+constexpr int MMA_WARP = 9;
 constexpr int TM = 128;                 // MMA M
 constexpr int TN = 128;                 // largest MMA N (columns per tile)
-constexpr int KT = 32;                  // K per shared-memory tile
+constexpr int KT = 32;                  // K values per tile (128 bytes per row)
+constexpr int PT = KT / 2;              // complex entries per K tile
 constexpr int STAGES = 3;
 constexpr int CPT = TN / 2;             // accumulator columns per drain thread (64)
-constexpr int PT = 16;                  // particles (forward) or rows (backward) per K tile
 constexpr uint32_t A_BYTES = TM * KT * 4;
 constexpr uint32_t B_BYTES = TN * KT * 4;
 constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;   // 64 KB: hi + lo of A and B
-constexpr uint32_t SMEM_DYN = STAGES * STAGE_BYTES;
+constexpr uint32_t SMEM_DYN = STAGES * STAGE_BYTES + 1024;    // + room to align to 1 KB
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t WAIT_LIMIT = 1u << 18;   // polls of up to ~20 us each
-constexpr int UF = (32 + 64 + NBW - 1) / NBW;    // forward units per builder warp per tile
-constexpr int UB = (64 + 64 + NBW - 1) / NBW;    // backward units per builder warp per tile
-
-__device__ __forceinline__ float2
-cmulf (float2 a, float2 b)
-{
-  return make_float2 (a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-
-// the two K-adjacent values (v0, v1) at an even k, split into hi and lo
-__device__ __forceinline__ void
-put2 (unsigned char *hi, unsigned char *lo, uint32_t o, float v0, float v1)
-{
-  uint32_t h0, l0, h1, l1;
-  umma::split_tf32 (v0, h0, l0);
-  umma::split_tf32 (v1, h1, l1);
-  *reinterpret_cast<uint2 *> (hi + o) = make_uint2 (h0, h1);
-  *reinterpret_cast<uint2 *> (lo + o) = make_uint2 (l0, l1);
-}
-
-// a warp fills one 8-row group x one K step (8 values) of a 128-row tile:
-// lane -> row 8 g + (lane & 7), K pair lane >> 3 (k = 8 step + 2 (lane >> 3))
-__device__ __forceinline__ uint32_t
-pair_off (int g, int step, int lane)
-{
-  return umma::off ((uint32_t) (8 * g + (lane & 7)), (uint32_t) (8 * step + 2 * (lane >> 3)),
-                    (uint32_t) TM);
-}
-
-// phase-table value t_d[m](j) for any sign of m (rows m = 0..M_d stored)
-__device__ __forceinline__ float2
-tval (const float2 *row0, int m, size_t stride, size_t j)
-{
-  const float2 v = row0[(size_t) (m < 0 ? -m : m) * stride + j];
-  return m < 0 ? make_float2 (v.x, -v.y) : v;
-}
 
 struct Sync {
   uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], done;
   uint32_t tslot;
   int err;
 };
+
+__device__ __forceinline__ unsigned char *
+align1k (unsigned char *p)
+{
+  return p + ((1024u - (umma::smem_u32 (p) & 1023u)) & 1023u);
+}
 
 __device__ __forceinline__ void
 cta_setup (Sync &s)
@@ -113,7 +91,7 @@ cta_setup (Sync &s)
     {
       for (int k = 0; k < STAGES; k++)
         {
-          umma::mbar_init (&s.full[k], NBW * 32);
+          umma::mbar_init (&s.full[k], 1);
           umma::mbar_init (&s.empty[k], 1);
         }
       for (int b = 0; b < 2; b++)
@@ -128,6 +106,38 @@ cta_setup (Sync &s)
   umma::fence_before_sync ();
   __syncthreads ();
   umma::fence_after_sync ();
+}
+
+// the TMA lane: tile t (K values k0 + 32 t ..) into stage t % STAGES; A rows
+// from arow, B rows from brow, hi and lo planes of both
+__device__ __forceinline__ void
+tma_role (Sync &s, unsigned char *smem, const CUtensorMap *ta, const CUtensorMap *tb, int arow,
+          int brow, int k0, int ntiles, uint32_t b_bytes)
+{
+  volatile int *err = &s.err;
+  const uint32_t tx = 2 * A_BYTES + 2 * b_bytes;
+  umma::tma_prefetch_desc (ta);
+  umma::tma_prefetch_desc (tb);
+  int issued = 0;
+  for (int t = 0; t < ntiles; t++)
+    {
+      const int st = t % STAGES;
+      if (t >= STAGES
+          && !umma::mbar_wait_or_abort (&s.empty[st], ((t / STAGES) - 1) & 1, WAIT_LIMIT, err))
+        break;
+      unsigned char *sb = smem + (size_t) st * STAGE_BYTES;
+      const int kx = k0 + KT * t;
+      umma::mbar_expect_tx (&s.full[st], tx);
+      umma::tma_load_3d (sb, ta, kx, arow, 0, &s.full[st]);
+      umma::tma_load_3d (sb + A_BYTES, ta, kx, arow, 1, &s.full[st]);
+      umma::tma_load_3d (sb + 2 * A_BYTES, tb, kx, brow, 0, &s.full[st]);
+      umma::tma_load_3d (sb + 2 * A_BYTES + B_BYTES, tb, kx, brow, 1, &s.full[st]);
+      issued = t + 1;
+    }
+  // the last load of each stage must land before the shared memory goes away
+  volatile int never = 0;
+  for (int t = issued > STAGES ? issued - STAGES : 0; t < issued; t++)
+    umma::mbar_wait_or_abort (&s.full[t % STAGES], (t / STAGES) & 1, WAIT_LIMIT, &never);
 }
 
 // the MMA lane: tile t in stage t % STAGES, accumulator buffer t & 1
@@ -149,10 +159,10 @@ mma_role (Sync &s, const unsigned char *smem, uint32_t tmem, uint32_t idesc, int
 #pragma unroll
       for (int k = 0; k < KT / 8; k++)
         {
-          const uint64_t dah = umma::smem_desc (ahi + k * TM * 32, 128, 256);
-          const uint64_t dal = umma::smem_desc (alo + k * TM * 32, 128, 256);
-          const uint64_t dbh = umma::smem_desc (bhi + k * TN * 32, 128, 256);
-          const uint64_t dbl = umma::smem_desc (blo + k * TN * 32, 128, 256);
+          const uint64_t dah = umma::smem_desc_sw128 (ahi + 32 * k);
+          const uint64_t dal = umma::smem_desc_sw128 (alo + 32 * k);
+          const uint64_t dbh = umma::smem_desc_sw128 (bhi + 32 * k);
+          const uint64_t dbl = umma::smem_desc_sw128 (blo + 32 * k);
           umma::mma_tf32 (dm, dah, dbh, idesc, k ? 1u : 0u);
           umma::mma_tf32 (dc, dah, dbl, idesc, k ? 1u : 0u);
           umma::mma_tf32 (dc, dal, dbh, idesc, 1u);
@@ -195,46 +205,79 @@ drain_role (Sync &s, uint32_t tmem, int ntiles, float acc[CPT])
   return true;
 }
 
-// builders: a ring of tiles; the loads of tile t + 1 are issued right after
-// tile t is stored, before waiting for tile t + 1's stage to come free
-template <typename Load, typename Store>
+// a complex value as TF32 hi and lo parts (FP32 bit patterns)
 __device__ __forceinline__ void
-build_role (Sync &s, unsigned char *smem, int ntiles, Load load, Store store)
+split2 (float2 v, float2 &hi, float2 &lo)
 {
-  volatile int *err = &s.err;
-  if (ntiles > 0) load (0);
-  for (int t = 0; t < ntiles; t++)
-    {
-      const int st = t % STAGES;
-      if (t >= STAGES
-          && !umma::mbar_wait_or_abort (&s.empty[st], ((t / STAGES) - 1) & 1, WAIT_LIMIT, err))
-        return;
-      unsigned char *sb = smem + (size_t) st * STAGE_BYTES;
-      store (t, sb, sb + A_BYTES, sb + 2 * A_BYTES, sb + 2 * A_BYTES + B_BYTES);
-      umma::fence_async_smem ();
-      umma::mbar_arrive (&s.full[st]);
-      if (t + 1 < ntiles) load (t + 1);
-    }
+  uint32_t hx, lx, hy, ly;
+  umma::split_tf32 (v.x, hx, lx);
+  umma::split_tf32 (v.y, hy, ly);
+  hi = make_float2 (__uint_as_float (hx), __uint_as_float (hy));
+  lo = make_float2 (__uint_as_float (lx), __uint_as_float (ly));
 }
 
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// T_r(j) = t1[m2](j) t2[m3](j) for every row r and particle j
+// images TF[r][(j, a|b)] and TB[j][(r, a|b)] of T_r(j) = e^{2 pi i (m2 u_y(j)
+// + m3 u_z(j))}, straight from the fixed-point coordinates (m2 q_y + m3 q_z
+// mod 2^32 is the exact phase in turns x 2^32).  CTA: 32 rows x 32
+// particles; the tile passes through shared memory so that both images are
+// written with coalesced 8-byte stores.  Padding (particles np..ldT of TF,
+// rows R..Rk of TB) is written as zeros.
 // ---------------------------------------------------------------------------
-__global__ void
+__global__ void __launch_bounds__ (256)
 k_tprep (KGemm g)
 {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int r = blockIdx.y;
-  if (j >= g.ldT) return;
-  float2 v = make_float2 (0.f, 0.f);
-  if (j < g.t.np)
+  __shared__ float2 s_t[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int jb = blockIdx.x * 32, rb = blockIdx.y * 32;
+  const int np = g.t.np;
+  {
+    const int j = jb + tx;
+    uint32_t qy = 0, qz = 0;
+    const bool live = j < np;
+    if (live)
+      {
+        const uint4 q = g.t.qpos[j];
+        qy = q.y;
+        qz = q.z;
+      }
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      {
+        const int rl = ty + 8 * k, r = rb + rl;
+        float2 v = make_float2 (0.f, 0.f);
+        if (live && r < g.R)
+          {
+            const int2 mm = g.rowm[r];
+            v = phase_of (g.t.rot, (uint32_t) mm.x * qy + (uint32_t) mm.y * qz);
+          }
+        s_t[rl][tx] = v;
+        if (r < g.R && j < g.ldT)
+          {
+            float2 hi, lo;
+            split2 (v, hi, lo);
+            float2 *o = reinterpret_cast<float2 *> (g.TF + (size_t) r * g.KF) + j;
+            o[0] = hi;
+            o[g.pTF / 2] = lo;
+          }
+      }
+  }
+  __syncthreads ();
+  const int r = rb + tx;
+  if (r >= g.Rk) return;
+#pragma unroll
+  for (int k = 0; k < 4; k++)
     {
-      const int2 mm = g.rowm[r];
-      v = cmulf (tval (g.t.tab + g.t.off1, mm.x, g.t.np, j), tval (g.t.tab + g.t.off2, mm.y, g.t.np, j));
+      const int jl = ty + 8 * k, j = jb + jl;
+      if (j >= np) break;
+      float2 hi, lo;
+      split2 (s_t[tx][jl], hi, lo);
+      float2 *o = reinterpret_cast<float2 *> (g.TB + (size_t) j * g.KB) + r;
+      o[0] = hi;
+      o[g.pTB / 2] = lo;
     }
-  g.T[(size_t) r * g.ldT + j] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -242,101 +285,29 @@ k_tprep (KGemm g)
 // ---------------------------------------------------------------------------
 template <int V>
 __global__ void __launch_bounds__ (NT, 1)
-k_sfac_gemm (KGemm g, const float *xf, float *sf, int *status)
+k_sfac_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+             KGemm g, float *sf, int *status)
 {
   constexpr int C = NComp<V>::value;
-  extern __shared__ __align__ (1024) unsigned char smem[];
+  extern __shared__ unsigned char dsm[];
   __shared__ Sync s;
+  unsigned char *smem = align1k (dsm);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int np = g.t.np;
-  const int r0 = blockIdx.x * 64;
+  const int r0 = blockIdx.x * TM;
   const int m1b = blockIdx.y * g.gf, nm1 = min (g.gf, g.n1 - m1b);
   const int split = blockIdx.z;
-  const int jb = split * g.jper, je = min (np, jb + g.jper);
+  const int jb = split * g.jper, je = min (g.t.np, jb + g.jper);
   const int ntiles = (je > jb) ? (je - jb + PT - 1) / PT : 0;
-  const int ncol = nm1 * C;
-  const float2 *t0 = g.t.tab;
+  const int ncol = nm1 * 2 * C;
 
   cta_setup (s);
   const uint32_t tmem = s.tslot;
 
-  if (warp >= BW0 && warp < BW0 + NBW)
+  if (warp == TMA_WARP)
     {
-      const int bw = warp - BW0;
-      const int ngb = (ncol + 7) >> 3;           // B row groups in use
-      // unit u < 32: A, 8 groups of complex rows x 4 K steps, (a, -b) to row
-      // rl and (b, a) to row 64 + rl; unit u >= 32: B, rows n = (m1, q),
-      // pair (u, v) = Z = t0[m1] x_q.  Per unit, fixed over the tiles: the
-      // shared-memory offset with the unit's particle offset jj in bits
-      // 20-23 (sof), the element offsets of its inputs for tile 0 (e0, e1;
-      // -1: no input).  va/vx: the tile's loaded inputs.
-      uint32_t sof[UF];
-      int e0[UF], e1[UF];
-#pragma unroll
-      for (int k = 0; k < UF; k++)
-        {
-          const int u = bw + k * NBW;
-          e0[k] = e1[k] = -1;
-          sof[k] = 0;
-          if (u < 32)
-            {
-              const int gg = u >> 2, step = u & 3, rl = 8 * gg + (lane & 7);
-              const int jj = 4 * step + (lane >> 3);
-              sof[k] = pair_off (gg, step, lane) | ((uint32_t) jj << 20);
-              if (r0 + rl < g.R) e0[k] = (r0 + rl) * g.ldT + jb + jj;
-            }
-          else if (u - 32 < ngb * 4)
-            {
-              const int v = u - 32, gg = v >> 2, step = v & 3, n = 8 * gg + (lane & 7);
-              const int jj = 4 * step + (lane >> 3);
-              sof[k] = pair_off (gg, step, lane) | ((uint32_t) jj << 20);
-              if (n < ncol)
-                {
-                  const int m = n / C, q = n - m * C;
-                  e0[k] = (m1b + m) * np + jb + jj;
-                  e1[k] = (jb + jj) * C + q;
-                }
-            }
-        }
-      float2 va[UF];
-      float vx[UF];
-      auto load = [&] (int t) {
-        const int lim = je - jb - PT * t;          // particles left in the slice
-#pragma unroll
-        for (int k = 0; k < UF; k++)
-          {
-            const int u = bw + k * NBW;
-            const bool in = e0[k] >= 0 && (int) (sof[k] >> 20) < lim;
-            va[k] = make_float2 (0.f, 0.f);
-            vx[k] = 0.f;
-            if (u < 32)
-              {
-                if (in) va[k] = g.T[e0[k] + PT * t];
-              }
-            else if (in)
-              {
-                va[k] = t0[e0[k] + PT * t];
-                vx[k] = xf[e1[k] + PT * C * t];
-              }
-          }
-      };
-      auto store = [&] (int, unsigned char *Ahi, unsigned char *Alo, unsigned char *Bhi,
-                        unsigned char *Blo) {
-#pragma unroll
-        for (int k = 0; k < UF; k++)
-          {
-            const int u = bw + k * NBW;
-            const uint32_t o = sof[k] & 0xFFFFFu;
-            if (u < 32)
-              {
-                put2 (Ahi, Alo, o, va[k].x, -va[k].y);
-                put2 (Ahi, Alo, o + 2048u, va[k].y, va[k].x);   // row + 64
-              }
-            else if (u - 32 < ngb * 4)
-              put2 (Bhi, Blo, o, va[k].x * vx[k], va[k].y * vx[k]);
-          }
-      };
-      build_role (s, smem, ntiles, load, store);
+      if (lane == 0)
+        tma_role (s, smem, &tmA, &tmB, r0, m1b * 2 * C, 2 * jb, ntiles, (uint32_t) g.nf * KT * 4);
+      __syncwarp ();
     }
   else if (warp == MMA_WARP)
     {
@@ -349,22 +320,22 @@ k_sfac_gemm (KGemm g, const float *xf, float *sf, int *status)
 #pragma unroll
       for (int u = 0; u < CPT; u++) acc[u] = 0.f;
       if (drain_role (s, tmem, ntiles, acc) && !s.err)
-    {
-      // this thread: TMEM lane = D row, 64 columns from (warp >> 2) * 64;
-      // sf[split][m1][q][re|im][row], rows padded to nrt * 64
-      const int row = (warp & 3) * 32 + lane;
-      const int rl = row & 63, part = row >> 6;
-      const int cb = (warp >> 2) * CPT;
-      const size_t Rp = (size_t) g.nrt * 64;
-#pragma unroll
-      for (int u = 0; u < CPT; u++)
         {
-          const int n = cb + u;
-          if (n >= ncol) break;
-          const int m = n / C, q = n - m * C;
-          sf[((((size_t) split * g.n1 + m1b + m) * C + q) * 2 + part) * Rp + r0 + rl] = acc[u];
+          // this thread: TMEM lane = row r, 64 columns (m1, re|im, q) from
+          // (warp >> 2) * 64; sf[split][m1][q][re|im][Rp]
+          const int r = r0 + (warp & 3) * 32 + lane;
+          const int cb = (warp >> 2) * CPT;
+          if (r < g.R)
+#pragma unroll
+            for (int u = 0; u < CPT; u++)
+              {
+                const int n = cb + u;
+                if (n >= ncol) break;
+                const int m = n / (2 * C), rem = n - m * 2 * C, part = rem >= C ? 1 : 0;
+                const int q = rem - part * C;
+                sf[((((size_t) split * g.n1 + m1b + m) * C + q) * 2 + part) * g.Rp + r] = acc[u];
+              }
         }
-    }
     }
   __syncthreads ();
   if (tid == 0 && s.err) atomicExch (status, 1);
@@ -374,49 +345,96 @@ k_sfac_gemm (KGemm g, const float *xf, float *sf, int *status)
 }
 
 // ---------------------------------------------------------------------------
-// per-k operators: W[r][m1][q] += P_k + i Q_k from the summed structure factors
+// per-k operators: W_k = P_k + i Q_k from the summed structure factors,
+// written into the image WB (each (row, m1) belongs to at most one k)
 // ---------------------------------------------------------------------------
+constexpr int KOP_K = 64;    // k vectors per CTA
+constexpr int KOP_G = 4;     // particle-slice groups per k
+
+// CTA of KOP_K x KOP_G threads: thread (kk, sg) sums the slices sg, sg + 4,
+// ... of the forward partials of k = blockIdx.x * KOP_K + kk (the loads of
+// neighbouring k are neighbouring rows, so they coalesce); the four sums meet
+// in shared memory; group 0 forms P_k and group 1 Q_k; then the four groups
+// write the (re | im row) x (hi | lo plane) entries of the image.
 template <int V>
-__global__ void
-k_kop (KGemm g, const MixK *kt, int nk, const float *sf, float2 *W)
+__global__ void __launch_bounds__ (KOP_K * KOP_G)
+k_kop (KGemm g, const MixK *kt, int nk, const float *sf)
 {
   constexpr int C = NComp<V>::value;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nk) return;
-  const MixK K = kt[k];
-  const size_t Rp = (size_t) g.nrt * 64;
-  float cs[C], sn[C], ns[C];
+  __shared__ float s_v[KOP_G][2 * C][KOP_K];
+  const int kk = threadIdx.x % KOP_K, sg = threadIdx.x / KOP_K;
+  const int k = blockIdx.x * KOP_K + kk;
+  const size_t Rp = (size_t) g.Rp;
+  MixK K;
+  float cs[C], sn[C];
 #pragma unroll
   for (int q = 0; q < C; q++) cs[q] = sn[q] = 0.f;
-  // one slice at a time, its 2C loads issued together
-  for (int s = 0; s < g.nsplit; s++)
+  if (k < nk)
     {
-      const float *base = sf + (((size_t) s * g.n1 + K.m1) * C * 2) * Rp + K.r;
-#pragma unroll
-      for (int q = 0; q < C; q++)
+      K = kt[k];
+      for (int s = sg; s < g.nsplit; s += KOP_G)
         {
-          cs[q] += base[(size_t) (2 * q) * Rp];
-          sn[q] += base[(size_t) (2 * q + 1) * Rp];
+          const float *base = sf + (((size_t) s * g.n1 + K.m1) * C * 2) * Rp + K.r;
+#pragma unroll
+          for (int q = 0; q < C; q++)
+            {
+              cs[q] += base[(size_t) (2 * q) * Rp];
+              sn[q] += base[(size_t) (2 * q + 1) * Rp];
+            }
         }
     }
 #pragma unroll
-  for (int q = 0; q < C; q++) ns[q] = -sn[q];
-  const float e[3] = {K.ex, K.ey, K.ez};
-  GenF<V, float> gc, gs, gms;
-  load_genf<V, float> (cs, gc);
-  load_genf<V, float> (sn, gs);
-  load_genf<V, float> (ns, gms);
-  GenU<V, float> P, Q;
+  for (int q = 0; q < C; q++)
+    {
+      s_v[sg][2 * q][kk] = cs[q];
+      s_v[sg][2 * q + 1][kk] = sn[q];
+    }
+  __syncthreads ();
+  GenU<V, float> P;
   P.zero ();
-  Q.zero ();
-  recip_apply<V, float> (e, K.ya, K.yb, K.yc, K.yg, K.yh, K.ym, gc, gms, P);
-  recip_apply<V, float> (e, K.ya, K.yb, K.yc, K.yg, K.yh, K.ym, gs, gc, Q);
-  float2 *w = W + ((size_t) K.r * g.n1 + K.m1) * C;
+  if (k < nk && sg < 2)
+    {
+#pragma unroll
+      for (int q = 0; q < C; q++)
+        {
+          cs[q] = (s_v[0][2 * q][kk] + s_v[1][2 * q][kk]) + (s_v[2][2 * q][kk] + s_v[3][2 * q][kk]);
+          sn[q] = (s_v[0][2 * q + 1][kk] + s_v[1][2 * q + 1][kk])
+                  + (s_v[2][2 * q + 1][kk] + s_v[3][2 * q + 1][kk]);
+        }
+      const float e[3] = {K.ex, K.ey, K.ez};
+      GenF<V, float> ga, gb;
+      if (sg == 0)
+        {
+          // P = A(k) C - B(k) S with the sine part entering negated
+#pragma unroll
+          for (int q = 0; q < C; q++) sn[q] = -sn[q];
+          load_genf<V, float> (cs, ga);
+          load_genf<V, float> (sn, gb);
+        }
+      else
+        {
+          load_genf<V, float> (sn, ga);
+          load_genf<V, float> (cs, gb);
+        }
+      recip_apply<V, float> (e, K.ya, K.yb, K.yc, K.yg, K.yh, K.ym, ga, gb, P);
+    }
+  __syncthreads ();
+  if (sg < 2)
+#pragma unroll
+    for (int q = 0; q < C; q++) s_v[sg][q][kk] = P.v[q];
+  __syncthreads ();
+  if (k >= nk) return;
+  // group sg: image row (m1, re) for sg even, (m1, im) for odd; plane sg / 2
+  const int part = sg & 1, plane = sg >> 1;
+  float *img = g.WB + (size_t) plane * g.pWB;
 #pragma unroll
   for (int q = 0; q < C; q++)
     {
-      atomicAdd (&w[q].x, P.v[q]);
-      atomicAdd (&w[q].y, Q.v[q]);
+      const float U = s_v[0][q][kk], Vv = s_v[1][q][kk];
+      float2 hi, lo;
+      split2 (part ? make_float2 (Vv, -U) : make_float2 (U, Vv), hi, lo);
+      const size_t row = ((size_t) K.m1 * 2 + part) * C + q;
+      reinterpret_cast<float2 *> (img + row * g.KB)[K.r] = plane ? lo : hi;
     }
 }
 
@@ -425,12 +443,14 @@ k_kop (KGemm g, const MixK *kt, int nk, const float *sf, float2 *W)
 // ---------------------------------------------------------------------------
 template <int V>
 __global__ void __launch_bounds__ (NT, 1)
-k_bp_gemm (KGemm g, const float2 *W, float *ypart, int *status)
+k_bp_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+           KGemm g, float *ypart, int *status)
 {
   constexpr int C = NComp<V>::value;
-  extern __shared__ __align__ (1024) unsigned char smem[];
+  extern __shared__ unsigned char dsm[];
   __shared__ Sync s;
   __shared__ float s_y[TM][C];
+  unsigned char *smem = align1k (dsm);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int np = g.t.np;
   const int i0 = blockIdx.x * TM;
@@ -446,73 +466,11 @@ k_bp_gemm (KGemm g, const float2 *W, float *ypart, int *status)
   for (int e = tid; e < TM * C; e += NT) s_y[e / C][e % C] = 0.f;
   __syncthreads ();
 
-  if (warp >= BW0 && warp < BW0 + NBW)
+  if (warp == TMA_WARP)
     {
-      const int bw = warp - BW0;
-      const int ngb = (ncol + 7) >> 3;
-      // unit u < 64: A', rows = particles, K pair = (a, b) of T_r(i); unit
-      // u >= 64: B', rows n = (m1, re|im, q), K pair from W[r][m1][q].  Per
-      // unit, fixed over the tiles: the shared-memory offset with the unit's
-      // row offset rr in bits 20-23 and the im flag in bit 24 (sof), the
-      // element offset of its input for tile 0 (e0; -1: no input).
-      uint32_t sof[UB];
-      int e0[UB];
-#pragma unroll
-      for (int k = 0; k < UB; k++)
-        {
-          const int u = bw + k * NBW;
-          e0[k] = -1;
-          sof[k] = 0;
-          if (u < 64)
-            {
-              const int gg = u >> 2, step = u & 3, i = i0 + 8 * gg + (lane & 7);
-              const int rr = 4 * step + (lane >> 3);
-              sof[k] = pair_off (gg, step, lane) | ((uint32_t) rr << 20);
-              if (i < np) e0[k] = (rb + rr) * g.ldT + i;
-            }
-          else if (u - 64 < ngb * 4)
-            {
-              const int v = u - 64, gg = v >> 2, step = v & 3, n = 8 * gg + (lane & 7);
-              const int rr = 4 * step + (lane >> 3);
-              const int m = n / (2 * C), rem = n - m * 2 * C, im = rem >= C, q = rem - im * C;
-              sof[k] = pair_off (gg, step, lane) | ((uint32_t) rr << 20) | ((uint32_t) im << 24);
-              if (n < ncol) e0[k] = ((rb + rr) * g.n1 + m1b + m) * C + q;
-            }
-        }
-      float2 va[UB];
-      auto load = [&] (int t) {
-        const int lim = re_ - rb - PT * t;          // rows left in the slice
-#pragma unroll
-        for (int k = 0; k < UB; k++)
-          {
-            const int u = bw + k * NBW;
-            const bool in = e0[k] >= 0 && (int) ((sof[k] >> 20) & 15u) < lim;
-            va[k] = make_float2 (0.f, 0.f);
-            if (u < 64)
-              {
-                if (in) va[k] = g.T[e0[k] + PT * g.ldT * t];
-              }
-            else if (in)
-              va[k] = W[e0[k] + PT * g.n1 * C * t];
-          }
-      };
-      auto store = [&] (int, unsigned char *Ahi, unsigned char *Alo, unsigned char *Bhi,
-                        unsigned char *Blo) {
-#pragma unroll
-        for (int k = 0; k < UB; k++)
-          {
-            const int u = bw + k * NBW;
-            const uint32_t o = sof[k] & 0xFFFFFu;
-            if (u < 64)
-              put2 (Ahi, Alo, o, va[k].x, va[k].y);
-            else if (u - 64 < ngb * 4)
-              {
-                const bool im = (sof[k] >> 24) & 1u;
-                put2 (Bhi, Blo, o, im ? va[k].y : va[k].x, im ? -va[k].x : va[k].y);
-              }
-          }
-      };
-      build_role (s, smem, ntiles, load, store);
+      if (lane == 0)
+        tma_role (s, smem, &tmA, &tmB, i0, m1b * 2 * C, 2 * rb, ntiles, (uint32_t) g.nb * KT * 4);
+      __syncwarp ();
     }
   else if (warp == MMA_WARP)
     {
@@ -525,38 +483,38 @@ k_bp_gemm (KGemm g, const float2 *W, float *ypart, int *status)
 #pragma unroll
       for (int u = 0; u < CPT; u++) acc[u] = 0.f;
       if (drain_role (s, tmem, ntiles, acc) && !s.err)
-    {
-      const int row = (warp & 3) * 32 + lane;
-      const int i = i0 + row;
-      if (i < np)
         {
-          // y_i[q] += Re(conj(t0[m1])(i) H) over this thread's columns
-          float yq[C];
-#pragma unroll
-          for (int q = 0; q < C; q++) yq[q] = 0.f;
-          const int cb = (warp >> 2) * CPT;
-          int cur = -1;
-          float2 ph = make_float2 (0.f, 0.f);
-#pragma unroll
-          for (int u = 0; u < CPT; u++)
+          const int row = (warp & 3) * 32 + lane;
+          const int i = i0 + row;
+          if (i < np)
             {
-              const int n = cb + u;
-              if (n >= ncol) break;
-              const int m = n / (2 * C), rem = n - m * 2 * C, im = rem >= C, q = rem - im * C;
-              if (m != cur)
+              // y_i[q] += Re(conj(t0[m1])(i) H) over this thread's columns
+              float yq[C];
+#pragma unroll
+              for (int q = 0; q < C; q++) yq[q] = 0.f;
+              const int cb = (warp >> 2) * CPT;
+              int cur = -1;
+              float2 ph = make_float2 (0.f, 0.f);
+#pragma unroll
+              for (int u = 0; u < CPT; u++)
                 {
-                  ph = t0[(size_t) (m1b + m) * np + i];
-                  cur = m;
+                  const int n = cb + u;
+                  if (n >= ncol) break;
+                  const int m = n / (2 * C), rem = n - m * 2 * C, im = rem >= C, q = rem - im * C;
+                  if (m != cur)
+                    {
+                      ph = t0[(size_t) (m1b + m) * np + i];
+                      cur = m;
+                    }
+                  const float c = (im ? ph.y : ph.x) * acc[u];
+#pragma unroll
+                  for (int qq = 0; qq < C; qq++)
+                    if (qq == q) yq[qq] += c;
                 }
-              const float c = (im ? ph.y : ph.x) * acc[u];
 #pragma unroll
-              for (int qq = 0; qq < C; qq++)
-                if (qq == q) yq[qq] += c;
+              for (int q = 0; q < C; q++) atomicAdd (&s_y[row][q], yq[q]);
             }
-#pragma unroll
-          for (int q = 0; q < C; q++) atomicAdd (&s_y[row][q], yq[q]);
         }
-    }
     }
   __syncthreads ();
   if (tid == 0 && s.err) atomicExch (status, 1);
@@ -574,7 +532,7 @@ k_bp_gemm (KGemm g, const float2 *W, float *ypart, int *status)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static int round16 (int n) { return (n + 15) / 16 * 16; }
+static int round_up (int n, int m) { return (n + m - 1) / m * m; }
 
 KGemm
 kgemm_plan (int version, PhaseTables t, const int2 *rowm, int R)
@@ -583,63 +541,81 @@ kgemm_plan (int version, PhaseTables t, const int2 *rowm, int R)
   g.t = t;
   g.rowm = rowm;
   g.R = R;
+  g.Rk = round_up (R > 0 ? R : 1, 16);
+  g.Rp = round_up (R > 0 ? R : 1, 32);
   g.c = NCOMP (version);
   g.n1 = t.M0 + 1;
-  g.nrt = (R + 63) / 64;
-  g.ldT = round16 (t.np);
-  // forward columns (m1, q), at most TN per tile, balanced over the tiles
-  g.ntile_f = (g.n1 * g.c + TN - 1) / TN;
+  g.ldT = round_up (t.np, 16);
+  g.KF = 2 * g.ldT;
+  g.KB = 2 * g.Rk;
+  g.NZ = g.n1 * 2 * g.c;
+  g.nrt = (R + TM - 1) / TM;
+  // columns (m1, re|im, q), at most TN per tile, balanced over the tiles;
+  // both GEMMs use the same column tiling
+  const int per = 2 * g.c;
+  const int g0 = TN / per;
+  g.ntile_f = (g.n1 + g0 - 1) / g0;
   g.gf = (g.n1 + g.ntile_f - 1) / g.ntile_f;
-  while (g.gf * g.c > TN) g.gf--;
-  g.ntile_f = (g.n1 + g.gf - 1) / g.gf;
-  g.nf = round16 (g.gf * g.c);
+  g.nf = round_up (g.gf * per, 16);
+  g.gb = g.gf;
+  g.ntile_b = g.ntile_f;
+  g.nb = g.nf;
   // particle slices: about one wave of CTAs
   const int base = g.nrt * g.ntile_f;
-  int ns = 152 / base;            // never a second, partial wave
+  int ns = base > 0 ? 152 / base : 1;        // never a second, partial wave
   const int maxns = (t.np + PT - 1) / PT;
   if (ns > maxns) ns = maxns;
   if (ns < 1) ns = 1;
   g.jper = ((t.np + ns - 1) / ns + PT - 1) / PT * PT;
   g.nsplit = (t.np + g.jper - 1) / g.jper;
-  // backward columns (m1, re|im, q), at most TN per tile
-  g.ntile_b = (g.n1 * 2 * g.c + TN - 1) / TN;
-  g.gb = (g.n1 + g.ntile_b - 1) / g.ntile_b;
-  while (g.gb * 2 * g.c > TN) g.gb--;
-  g.ntile_b = (g.n1 + g.gb - 1) / g.gb;
-  g.nb = round16 (g.gb * 2 * g.c);
   g.mtiles = (t.np + TM - 1) / TM;
   // row slices of the backward K: about one wave of CTAs
   const int bb = g.mtiles * g.ntile_b;
-  int kss = 152 / bb;
+  int kss = bb > 0 ? 152 / bb : 1;
   const int maxk = (R + PT - 1) / PT;
   if (kss > maxk) kss = maxk;
   if (kss < 1) kss = 1;
   g.rper = ((R + kss - 1) / kss + PT - 1) / PT * PT;
   g.ksplit = R > 0 ? (R + g.rper - 1) / g.rper : 1;
+  g.pTF = (size_t) R * g.KF;
+  g.pTB = (size_t) t.np * g.KB;
+  g.pZF = (size_t) g.NZ * g.KF;
+  g.pWB = (size_t) g.NZ * g.KB;
   return g;
 }
 
 bool
 kgemm_fits (const KGemm &g)
 {
-  return g.R > 0 && g.t.np > 0 && g.c <= 11 && g.gf >= 1 && g.gb >= 1 && g.nf <= TN
-         && g.nb <= TN;
+  return g.R > 0 && g.t.np > 0 && g.c <= 11 && g.gf >= 1 && g.nf <= TN && g.nf >= 16;
 }
 
 size_t
 kgemm_sf_floats (const KGemm &g)
 {
-  return (size_t) g.nsplit * g.n1 * g.c * 2 * ((size_t) g.nrt * 64);
+  return (size_t) g.nsplit * g.n1 * g.c * 2 * (size_t) g.Rp;
 }
-size_t kgemm_w_elems (const KGemm &g) { return (size_t) g.R * g.n1 * g.c; }
-size_t kgemm_t_elems (const KGemm &g) { return (size_t) g.R * g.ldT; }
+size_t kgemm_tf_floats (const KGemm &g) { return 2 * g.pTF; }
+size_t kgemm_tb_floats (const KGemm &g) { return 2 * g.pTB; }
+size_t kgemm_zf_floats (const KGemm &g) { return 2 * g.pZF; }
+size_t kgemm_wb_floats (const KGemm &g) { return 2 * g.pWB; }
 int kgemm_ypart_chunks (const KGemm &g) { return g.ksplit * g.ntile_b; }
 size_t kgemm_ypart_floats (const KGemm &g) { return (size_t) kgemm_ypart_chunks (g) * g.t.np * g.c; }
 
+int
+kgemm_maps (const KGemm &g, KMaps *m)
+{
+  int e = encode_planes_sw128 (&m->tf, g.TF, 2, (unsigned long long) g.R, g.KF, TM);
+  if (!e) e = encode_planes_sw128 (&m->zf, g.ZF, 2, (unsigned long long) g.NZ, g.KF, g.nf);
+  if (!e) e = encode_planes_sw128 (&m->tb, g.TB, 2, (unsigned long long) g.t.np, g.KB, TM);
+  if (!e) e = encode_planes_sw128 (&m->wb, g.WB, 2, (unsigned long long) g.NZ, g.KB, g.nb);
+  return e;
+}
+
 template <int V>
 static cudaError_t
-launch_v (const KGemm &g, const MixK *kt, int nk, const float *xf, float *sf, float2 *W,
-          float *ypart, int *status, cudaStream_t st, Ctx *prof)
+launch_v (const KGemm &g, const KMaps &mp, const MixK *kt, int nk, float *sf, float *ypart,
+          int *status, cudaStream_t st, Ctx *prof)
 {
   cudaError_t e;
   if ((e = cudaFuncSetAttribute (k_sfac_gemm<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -648,26 +624,24 @@ launch_v (const KGemm &g, const MixK *kt, int nk, const float *xf, float *sf, fl
   if ((e = cudaFuncSetAttribute (k_bp_gemm<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int) SMEM_DYN)) != cudaSuccess)
     return e;
-  k_tprep<<<dim3 ((g.ldT + 127) / 128, g.R), 128, 0, st>>> (g);
+  k_tprep<<<dim3 ((g.ldT + 31) / 32, (g.Rk + 31) / 32), 256, 0, st>>> (g);
   kmark (prof, st, "k_tprep");
-  k_sfac_gemm<V><<<dim3 (g.nrt, g.ntile_f, g.nsplit), NT, SMEM_DYN, st>>> (g, xf, sf, status);
+  k_sfac_gemm<V><<<dim3 (g.nrt, g.ntile_f, g.nsplit), NT, SMEM_DYN, st>>> (mp.tf, mp.zf, g, sf, status);
   kmark (prof, st, "k_sfac_gemm");
-  if ((e = cudaMemsetAsync (W, 0, sizeof (float2) * kgemm_w_elems (g), st)) != cudaSuccess)
-    return e;
-  k_kop<V><<<(nk + 127) / 128, 128, 0, st>>> (g, kt, nk, sf, W);
+  k_kop<V><<<(nk + KOP_K - 1) / KOP_K, KOP_K * KOP_G, 0, st>>> (g, kt, nk, sf);
   kmark (prof, st, "k_kop");
-  k_bp_gemm<V><<<dim3 (g.mtiles, g.ntile_b, g.ksplit), NT, SMEM_DYN, st>>> (g, W, ypart, status);
+  k_bp_gemm<V><<<dim3 (g.mtiles, g.ntile_b, g.ksplit), NT, SMEM_DYN, st>>> (mp.tb, mp.wb, g, ypart, status);
   kmark (prof, st, "k_bp_gemm");
   return cudaGetLastError ();
 }
 
 cudaError_t
-launch_kspace_gemm (int version, const KGemm &g, const MixK *kt, int nk, const float *xf,
-                    float *sf, float2 *W, float *ypart, int *status, cudaStream_t st, Ctx *prof)
+launch_kspace_gemm (int version, const KGemm &g, const KMaps &maps, const MixK *kt, int nk,
+                    float *sf, float *ypart, int *status, cudaStream_t st, Ctx *prof)
 {
-  if (version == 0) return launch_v<0> (g, kt, nk, xf, sf, W, ypart, status, st, prof);
-  if (version == 1) return launch_v<1> (g, kt, nk, xf, sf, W, ypart, status, st, prof);
-  return launch_v<2> (g, kt, nk, xf, sf, W, ypart, status, st, prof);
+  if (version == 0) return launch_v<0> (g, maps, kt, nk, sf, ypart, status, st, prof);
+  if (version == 1) return launch_v<1> (g, maps, kt, nk, sf, ypart, status, st, prof);
+  return launch_v<2> (g, maps, kt, nk, sf, ypart, status, st, prof);
 }
 
 }  // namespace lsg

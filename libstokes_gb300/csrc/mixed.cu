@@ -21,12 +21,14 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <unordered_map>
 #include <vector>
 
 #include "ewald_device.cuh"
 #include "gpu_engine.h"
 #include "mixed.h"
 #include "stokes_gpu.h"
+#include "tc_umma.cuh"
 
 extern "C" void lsg_ewald_cutoffs (double xi, double eps, double lmin, double lmax,
                                    double *rmax_out, double *kmax_out);
@@ -41,7 +43,10 @@ struct MixedState {
   int nk_split = 0;      // rows of the re-tuned split; the rest: reference G term
   double selfc[3] = {0, 0, 0};
   std::vector<MixK> h_k;
-  DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf, status, sf, wop, rowm, tbuf;
+  DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf, status, sf, rowm, rot;
+  DevBuf img_tf, img_tb, img_zf, img_wb;   // GEMM operand images (kspace_tc.cu)
+  KMaps maps;
+  uint64_t img_key = 0;         // buffers and plan the maps and zeroed pads belong to
   int nrow = 0;          // (m2, m3) rows of the tensor-core contraction
   int *h_status = nullptr;      // pinned copy of the kernels' status word
   bool tensor = true;           // reciprocal space on the tensor cores
@@ -62,73 +67,114 @@ struct PrepArgs {
   const double *pos;
   const double *x;
   int np, c;
-  double lx, ly, lz, shift;
+  double sx, sy, sz;    // 2^32 / L_d
+  double shift;         // Lees-Edwards shift (flow axis x)
+  double sl;            // shift / lx
   int shear_mode;
-  int M0, M1, M2;
-  uint32_t *qpos;      // [np][4] fixed-point x, y, z (+ pad)
-  float2 *tab;         // [3][M+1][np]
-  float *xf;           // [np*c]
+  int ntab;             // (M0 + 1) + (M1 + 1) + (M2 + 1) table rows
+  int m0end, m1end;     // first row of the y and z tables
+  const float4 *rot;    // e^{2 pi i h / 1024}, h = 0..1023: (hi.re, hi.im, lo.re, lo.im)
+  uint32_t *qpos;       // [np][4] fixed-point x, y, z (+ pad)
+  float2 *tab;          // [ntab][np]
+  float *xf;            // [np*c]
+  float *zf;            // forward GEMM image ZF (tensor-core path) or NULL
+  size_t zplane;        // floats per ZF plane
+  int kf;               // floats per ZF row
 };
 
-// wrap to the primary cell (Lees-Edwards aware), fixed-point positions,
-// phase tables e^{2 pi i m u_d}, m = 0..M_d, and x in FP32; one thread per
-// (particle, axis blockIdx.y) so that the FP64 recurrences spread over the SMs
-__global__ void
+constexpr int PREP_P = 32;       // particles per mk_prep CTA
+constexpr int PREP_ROWS = 16;    // table rows per mk_prep CTA
+constexpr int PREP_CMAX = 11;    // components per particle at most
+
+// floor(v) mod 2^32 for |v| < 2^62: the 32-bit fixed-point coordinate, the
+// periodic wrap being the modulo
+__device__ __forceinline__ uint32_t
+fixq (double v)
+{
+  return (uint32_t) (unsigned long long) __double2ll_rd (v);
+}
+
+// Fixed-point positions (wrapped to the primary cell, Lees-Edwards aware),
+// x in FP32 and the per-axis phase tables tab[m][j] = e^{2 pi i m u_d(j)}.
+// u_d is the particle's fractional coordinate on axis d as a 32-bit fixed
+// point q_d, so m u_d mod 1 is the exact integer product m q_d mod 2^32; on
+// a sheared lattice the flow-axis phase coordinate is u_x - (shift/lx) u_g.
+// With a ZF image (the tensor-core path) the threads of the flow-axis rows
+// m1 also write Z = t0[m1] x_q as TF32 hi/lo pairs in the forward GEMM's
+// sign pattern: image row (m1, re, q) = (Re Z, -Im Z), (m1, im, q) =
+// (Im Z, Re Z) at column pair j.
+// CTA (blockIdx.x, blockIdx.y): PREP_P particles x PREP_ROWS table rows; the
+// few FP64 operations per particle are repeated by each row group.
+__global__ void __launch_bounds__ (128)
 mk_prep (PrepArgs a)
 {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int d = blockIdx.y;
-  if (j >= a.np) return;
-  double x = a.pos[3 * j], y = a.pos[3 * j + 1], z = a.pos[3 * j + 2];
-  if (a.shear_mode == 1)
+  __shared__ uint32_t s_q[4][PREP_P];
+  __shared__ float s_x[PREP_P * PREP_CMAX];
+  const int t = threadIdx.x;
+  const int jb = blockIdx.x * PREP_P;
+  {
+    const size_t e0 = (size_t) jb * a.c;
+    const int nx = PREP_P * a.c;
+    for (int e = t; e < nx; e += blockDim.x)
+      {
+        const float v = (e0 + e < (size_t) a.np * a.c) ? (float) a.x[e0 + e] : 0.f;
+        s_x[e] = v;
+        if (blockIdx.y == 0 && e0 + e < (size_t) a.np * a.c) a.xf[e0 + e] = v;
+      }
+  }
+  if (t < PREP_P)
     {
-      const double w = floor (y / a.ly);
-      y -= w * a.ly;
-      x -= w * a.shift;
-    }
-  else if (a.shear_mode == 2)
-    {
-      const double w = floor (z / a.lz);
-      z -= w * a.lz;
-      x -= w * a.shift;
-    }
-  double s[3] = {x / a.lx, y / a.ly, z / a.lz};
-  for (int k = 0; k < 3; k++)
-    {
-      s[k] -= floor (s[k]);
-      if (s[k] >= 1.0) s[k] = 0.0;
-    }
-  if (d == 0)
-    {
-      const double two32 = 4294967296.0;
-      for (int k = 0; k < 3; k++)
+      const int j = jb + t;
+      uint32_t q0 = 0, q1 = 0, q2 = 0, qu = 0;
+      if (j < a.np)
         {
-          double q = floor (s[k] * two32);
-          if (q >= two32) q -= two32;
-          a.qpos[4 * j + k] = (uint32_t) q;
+          double x = a.pos[3 * j];
+          const double y = a.pos[3 * j + 1], z = a.pos[3 * j + 2];
+          if (a.shear_mode == 1 || a.shear_mode == 2)
+            {
+              // wraps along the gradient axis shift the flow coordinate
+              const long long G = __double2ll_rd ((a.shear_mode == 1 ? y * a.sy : z * a.sz));
+              const double w = (double) (G >> 32);
+              x = fma (-w, a.shift, x);
+            }
+          q0 = fixq (x * a.sx);
+          q1 = fixq (y * a.sy);
+          q2 = fixq (z * a.sz);
+          qu = q0;
+          if (a.shear_mode == 1) qu = q0 - fixq (a.sl * (double) q1);
+          else if (a.shear_mode == 2) qu = q0 - fixq (a.sl * (double) q2);
+          if (blockIdx.y == 0)
+            reinterpret_cast<uint4 *> (a.qpos)[j] = make_uint4 (q0, q1, q2, 0u);
         }
-      a.qpos[4 * j + 3] = 0u;
-      for (int q = 0; q < a.c; q++) a.xf[(size_t) j * a.c + q] = (float) a.x[(size_t) j * a.c + q];
+      s_q[0][t] = qu; s_q[1][t] = q1; s_q[2][t] = q2;
     }
-  // phases in turns; the shear-shifted k couples the flow axis to the
-  // gradient axis: k.r = 2 pi (m1 (sx - sl sg) + m2 sy + m3 sz)
-  const double sl = a.shift / a.lx;
-  double u = s[d];
-  if (d == 0 && a.shear_mode == 1) u = s[0] - sl * s[1];
-  else if (d == 0 && a.shear_mode == 2) u = s[0] - sl * s[2];
-  const int Md = d == 0 ? a.M0 : (d == 1 ? a.M1 : a.M2);
-  const size_t off = d == 0 ? 0 : (d == 1 ? (size_t) (a.M0 + 1) * a.np
-                                          : (size_t) (a.M0 + a.M1 + 2) * a.np);
-  double sb, cb;
-  sincospi (2.0 * u, &sb, &cb);
-  double pr = 1.0, pi = 0.0;
-  for (int m = 0; m <= Md; m++)
+  __syncthreads ();
+  const int r0 = blockIdx.y * PREP_ROWS, r1 = min (a.ntab, r0 + PREP_ROWS);
+  for (int e = t; e < (r1 - r0) * PREP_P; e += blockDim.x)
     {
-      a.tab[off + (size_t) m * a.np + j] = make_float2 ((float) pr, (float) pi);
-      const double nr = pr * cb - pi * sb;
-      const double ni = pr * sb + pi * cb;
-      pr = nr;
-      pi = ni;
+      const int row = r0 + e / PREP_P, jl = e % PREP_P, j = jb + jl;
+      if (j >= a.np) continue;
+      const int d = row < a.m0end ? 0 : (row < a.m1end ? 1 : 2);
+      const uint32_t m = (uint32_t) (row - (d == 0 ? 0 : (d == 1 ? a.m0end : a.m1end)));
+      const float2 ph = phase_of (a.rot, m * s_q[d][jl]);
+      a.tab[(size_t) row * a.np + j] = ph;
+      if (d == 0 && a.zf)
+        for (int q = 0; q < a.c; q++)
+          {
+            const float xq = s_x[jl * a.c + q];
+            const float u = ph.x * xq, v = ph.y * xq;
+            for (int part = 0; part < 2; part++)
+              {
+                const float p0 = part ? v : u, p1 = part ? u : -v;
+                uint32_t h0, l0, h1, l1;
+                umma::split_tf32 (p0, h0, l0);
+                umma::split_tf32 (p1, h1, l1);
+                float2 *o = reinterpret_cast<float2 *> (
+                              a.zf + (((size_t) m * 2 + part) * a.c + q) * a.kf) + j;
+                o[0] = make_float2 (__uint_as_float (h0), __uint_as_float (h1));
+                o[a.zplane / 2] = make_float2 (__uint_as_float (l0), __uint_as_float (l1));
+              }
+          }
     }
 }
 
@@ -399,53 +445,72 @@ mk_backproj (BpMixArgs a)
     }
 }
 
-// y_i = self_i x_i (FP64) + sum real partials + 2 sum reciprocal partials.
-// One thread per particle in small blocks (the FP64 self term spreads over
-// all SMs); the FP32 partials are summed with Kahan compensation.
+// The self term of equal spheres as a C x C matrix: column q is the self
+// block applied to the unit vector of component q (one thread per column,
+// run once per split).
 template <int V>
 __global__ void
-mk_combine (const double *x, const float *pr, int ncr, const float *pk, int nck,
-            const double *selfc, int np, double *y)
+mk_selfmat (double xa, double xc, double xm, double *S)
 {
   constexpr int C = NComp<V>::value;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= np) return;
-  float sr[C], cr[C], sk[C], ck[C];
-#pragma unroll
-  for (int q = 0; q < C; q++) sr[q] = cr[q] = sk[q] = ck[q] = 0.f;
-  for (int c = 0; c < ncr; c++)
-#pragma unroll
-    for (int q = 0; q < C; q++)
-      {
-        const float v = pr[((size_t) c * np + i) * C + q] - cr[q];
-        const float t = sr[q] + v;
-        cr[q] = (t - sr[q]) - v;
-        sr[q] = t;
-      }
-  for (int c = 0; c < nck; c++)
-#pragma unroll
-    for (int q = 0; q < C; q++)
-      {
-        const float v = pk[((size_t) c * np + i) * C + q] - ck[q];
-        const float t = sk[q] + v;
-        ck[q] = (t - sk[q]) - v;
-        sk[q] = t;
-      }
+  const int q = threadIdx.x;
+  if (q >= C) return;
   PairScalars<double> s;
-  s.xa = s.ya = selfc[3 * i];
-  s.xc = s.yc = selfc[3 * i + 1];
-  s.xm = s.ym = s.zm = selfc[3 * i + 2];
+  s.xa = s.ya = xa;
+  s.xc = s.yc = xc;
+  s.xm = s.ym = s.zm = xm;
   s.yb = s.xg = s.yg = s.yh = 0.0;
   const double e[3] = {0.0, 0.0, 0.0};
+  double u[C];
+#pragma unroll
+  for (int k = 0; k < C; k++) u[k] = (k == q) ? 1.0 : 0.0;
   GenF<V, double> g;
-  load_genf<V, double> (x + (size_t) C * i, g);
+  load_genf<V, double> (u, g);
   GenU<V, double> acc;
   acc.zero ();
   pair_apply<V, double> (e, s, g, acc);
 #pragma unroll
-  for (int q = 0; q < C; q++)
-    y[(size_t) C * i + q] = acc.v[q] + ((double) sr[q] - (double) cr[q])
-                            + 2.0 * ((double) sk[q] - (double) ck[q]);
+  for (int k = 0; k < C; k++) S[k * C + q] = acc.v[k];
+}
+
+// y = S x (FP64 self term) + sum of real partials + 2 sum of reciprocal
+// partials, one thread per (particle, component) so that the loads coalesce
+// and the FP64 work (at most five FMAs: the self block is diagonal for F and
+// T, 5 x 5 for the stresslet) spreads over the SMs; the FP32 partials are
+// summed with Kahan compensation.
+template <int V>
+__global__ void __launch_bounds__ (64)
+mk_combine (const double *x, const float *pr, int ncr, const float *pk, int nck,
+            const double *S, int np, double *y)
+{
+  constexpr int C = NComp<V>::value;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = np * C;
+  if (t >= n) return;
+  const int i = t / C, q = t - i * C;
+  float sr = 0.f, cr = 0.f, sk = 0.f, ck = 0.f;
+#pragma unroll 4
+  for (int c = 0; c < ncr; c++)
+    {
+      const float v = pr[(size_t) c * n + t] - cr;
+      const float u = sr + v;
+      cr = (u - sr) - v;
+      sr = u;
+    }
+#pragma unroll 4
+  for (int c = 0; c < nck; c++)
+    {
+      const float v = pk[(size_t) c * n + t] - ck;
+      const float u = sk + v;
+      ck = (u - sk) - v;
+      sk = u;
+    }
+  // the stresslet block couples components 6..10; F and T are diagonal
+  const int q0 = (q < 6) ? q : 6, nq = (q < 6) ? 1 : 5;
+  const double *xi = x + (size_t) C * i;
+  double self = 0.0;
+  for (int k = 0; k < nq; k++) self = fma (S[q * C + q0 + k], xi[q0 + k], self);
+  y[t] = self + ((double) sr - (double) cr) + 2.0 * ((double) sk - (double) ck);
 }
 
 // ---------------------------------------------------------------------------
@@ -561,6 +626,12 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
   if (sys->version == 2)
     {
       const double rxi2 = sys->xi2;
+      auto kkey = [] (int a, int b, int c) {
+        return ((int64_t) a << 42) ^ ((int64_t) (b + (1 << 20)) << 21) ^ (int64_t) (c + (1 << 20));
+      };
+      std::unordered_map<int64_t, int> own;
+      for (int k = 0; k < m->nk_split; k++)
+        own.emplace (kkey (m->h_k[k].m1, m->h_k[k].m2, m->h_k[k].m3), k);
       for (int m1 = 0; m1 <= sys->kmaxx; m1++)
         for (int m2 = -sys->kmaxy; m2 <= sys->kmaxy; m2++)
           for (int m3 = -sys->kmaxz; m3 <= sys->kmaxz; m3++)
@@ -580,6 +651,15 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
               r.m1 = m1; r.m2 = m2; r.m3 = m3;
               r.ex = (float) (k1 / k); r.ey = (float) (k2 / k); r.ez = (float) (k3 / k);
               r.yg = (float) (2.0 * 3.0 * (1.0 - 4.0 / 15.0 * kk) * k * kexp);
+              // the operator is linear in its coefficients, so a k vector of
+              // the split's own list takes the term into its yg; each (m1,
+              // m2, m3) then appears once, which the GEMM path relies on
+              const auto hit = own.find (kkey (m1, m2, m3));
+              if (hit != own.end ())
+                {
+                  m->h_k[(size_t) hit->second].yg += r.yg;
+                  continue;
+                }
               m->h_k.push_back (r);
               M[0] = std::max (M[0], abs (m1));
               M[1] = std::max (M[1], abs (m2));
@@ -641,7 +721,8 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   m->nchunk_r = std::max (1, std::min (64, (152 * 48 + np - 1) / np));
   const size_t off1 = (size_t) (m->M[0] + 1) * np;
   const size_t off2 = off1 + (size_t) (m->M[1] + 1) * np;
-  PhaseTables pt{(const float2 *) m->tab.p, off1, off2, m->M[0], m->M[1], m->M[2], np};
+  PhaseTables pt{(const float2 *) m->tab.p, off1, off2, m->M[0], m->M[1], m->M[2], np,
+                 (const uint4 *) m->qpos.p, (const float4 *) m->rot.p};
   {
     // reciprocal space on the tensor cores unless LIBSTOKES_GB300_KSPACE=simt
     const char *ks = getenv ("LIBSTOKES_GB300_KSPACE");
@@ -678,26 +759,92 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   if (m->tensor)
     {
       if ((e = m->sf.ensure (sizeof (float) * kgemm_sf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "structure factors");
-      if ((e = m->wop.ensure (sizeof (float2) * kgemm_w_elems (m->plan))) != cudaSuccess) return cuda_fail (e, "k operators");
-      if ((e = m->tbuf.ensure (sizeof (float2) * kgemm_t_elems (m->plan))) != cudaSuccess) return cuda_fail (e, "row phase table");
-      m->plan.T = (float2 *) m->tbuf.p;
+      if ((e = m->img_tf.ensure (sizeof (float) * kgemm_tf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image TF");
+      if ((e = m->img_tb.ensure (sizeof (float) * kgemm_tb_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image TB");
+      if ((e = m->img_zf.ensure (sizeof (float) * kgemm_zf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image ZF");
+      if ((e = m->img_wb.ensure (sizeof (float) * kgemm_wb_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image WB");
+      m->plan.TF = (float *) m->img_tf.p;
+      m->plan.TB = (float *) m->img_tb.p;
+      m->plan.ZF = (float *) m->img_zf.p;
+      m->plan.WB = (float *) m->img_wb.p;
     }
   else if ((e = m->pq.ensure (sizeof (float) * 2 * C * (size_t) (m->nkh > 0 ? m->nkh : 1))) != cudaSuccess)
     return cuda_fail (e, "pq");
   if ((e = m->part_real.ensure (sizeof (float) * (size_t) m->nchunk_r * np * C)) != cudaSuccess) return cuda_fail (e, "real partials");
   if ((e = m->part_rec.ensure (sizeof (float) * (size_t) m->nchunk_k * np * C)) != cudaSuccess) return cuda_fail (e, "k partials");
-  if ((e = m->selfbuf.ensure (sizeof (double) * 3 * np)) != cudaSuccess) return cuda_fail (e, "self");
+  // the self block as a C x C matrix, rebuilt when the split changes
+  if (m->fp != m->self_fp || !m->selfbuf.p)
+    {
+      if ((e = m->selfbuf.ensure (sizeof (double) * C * C)) != cudaSuccess) return cuda_fail (e, "self");
+      double *S = (double *) m->selfbuf.p;
+      if (c->version == 0) mk_selfmat<0><<<1, 32, 0, st>>> (m->selfc[0], m->selfc[1], m->selfc[2], S);
+      else if (c->version == 1) mk_selfmat<1><<<1, 32, 0, st>>> (m->selfc[0], m->selfc[1], m->selfc[2], S);
+      else mk_selfmat<2><<<1, 32, 0, st>>> (m->selfc[0], m->selfc[1], m->selfc[2], S);
+      if ((e = cudaStreamSynchronize (st)) != cudaSuccess) return cuda_fail (e, "mixed self matrix");
+      m->self_fp = m->fp;
+    }
+  // 1024 rotations e^{2 pi i h / 1024} as FP32 pairs hi + lo, made once
+  if (!m->rot.p)
+    {
+      std::vector<float> h (4 * 1024);
+      for (int k = 0; k < 1024; k++)
+        {
+          const double c0 = cos (2.0 * M_PI * k / 1024.0), s0 = sin (2.0 * M_PI * k / 1024.0);
+          h[4 * k] = (float) c0;
+          h[4 * k + 1] = (float) s0;
+          h[4 * k + 2] = (float) (c0 - (double) h[4 * k]);
+          h[4 * k + 3] = (float) (s0 - (double) h[4 * k + 1]);
+        }
+      if ((e = m->rot.ensure (sizeof (float) * 4 * 1024)) != cudaSuccess) return cuda_fail (e, "rotations");
+      e = cudaMemcpyAsync (m->rot.p, h.data (), sizeof (float) * 4 * 1024, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize (st);
+      if (e != cudaSuccess) return cuda_fail (e, "rotations");
+    }
+
+  m->plan.t.qpos = (const uint4 *) m->qpos.p;
+  m->plan.t.rot = (const float4 *) m->rot.p;
+  if (m->tensor)
+    {
+      // the pads of ZF and the (row, m1) slots of WB that no k vector owns
+      // stay zero; zeroed, and the TMA maps encoded, when the split or the
+      // buffers change
+      uint64_t key = m->fp * 1000003ull;
+      for (const void *p : {(const void *) m->img_tf.p, (const void *) m->img_tb.p,
+                            (const void *) m->img_zf.p, (const void *) m->img_wb.p})
+        key = (key ^ (uint64_t) (uintptr_t) p) * 1099511628211ull;
+      if (key != m->img_key)
+        {
+          e = cudaMemsetAsync (m->img_zf.p, 0, sizeof (float) * kgemm_zf_floats (m->plan), st);
+          if (e == cudaSuccess)
+            e = cudaMemsetAsync (m->img_wb.p, 0, sizeof (float) * kgemm_wb_floats (m->plan), st);
+          if (e != cudaSuccess) return cuda_fail (e, "GEMM images");
+          const int me = kgemm_maps (m->plan, &m->maps);
+          if (me) return set_error (STOKES_GPU_ECUDA, "TMA tensor maps of the GEMM images (%d)", me);
+          m->img_key = key;
+        }
+    }
 
   cudaEvent_t *E = phase_events (c, timed);
   if (E) cudaEventRecord (E[0], st);
   kmark (c, st, nullptr);
   PrepArgs pa;
   pa.pos = d_pos; pa.x = d_x; pa.np = np; pa.c = C;
-  pa.lx = sys->lx; pa.ly = sys->ly; pa.lz = sys->lz; pa.shift = sys->shear_shift;
+  {
+    const double two32 = 4294967296.0;
+    pa.sx = two32 / sys->lx; pa.sy = two32 / sys->ly; pa.sz = two32 / sys->lz;
+  }
+  pa.shift = sys->shear_shift;
+  pa.sl = sys->shear_shift / sys->lx;
   pa.shear_mode = sys->shear_mode;
-  pa.M0 = m->M[0]; pa.M1 = m->M[1]; pa.M2 = m->M[2];
+  pa.ntab = ntab;
+  pa.m0end = m->M[0] + 1;
+  pa.m1end = m->M[0] + m->M[1] + 2;
+  pa.rot = (const float4 *) m->rot.p;
   pa.qpos = (uint32_t *) m->qpos.p; pa.tab = (float2 *) m->tab.p; pa.xf = (float *) m->xf.p;
-  mk_prep<<<dim3 ((np + 15) / 16, 3), 16, 0, st>>> (pa);
+  pa.zf = m->tensor ? m->plan.ZF : nullptr;
+  pa.zplane = m->plan.pZF;
+  pa.kf = m->plan.KF;
+  mk_prep<<<dim3 ((np + PREP_P - 1) / PREP_P, (ntab + PREP_ROWS - 1) / PREP_ROWS), 128, 0, st>>> (pa);
   kmark (c, st, "mk_prep");
 
   KMixArgs ka;
@@ -712,9 +859,9 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   const int gb = (int) (((long long) np * m->nchunk_k + MX_WARPS - 1) / MX_WARPS);
   if (m->nkh > 0 && m->tensor)
     {
-      if ((e = launch_kspace_gemm (c->version, m->plan, ka.kt, m->nkh, ka.xf, (float *) m->sf.p,
-                                   (float2 *) m->wop.p, (float *) m->part_rec.p,
-                                   (int *) m->status.p, st, c)) != cudaSuccess)
+      if ((e = launch_kspace_gemm (c->version, m->plan, m->maps, ka.kt, m->nkh, (float *) m->sf.p,
+                                   (float *) m->part_rec.p, (int *) m->status.p, st, c))
+          != cudaSuccess)
         return cuda_fail (e, "reciprocal space (tensor cores)");
     }
   else if (m->nkh > 0)
@@ -758,26 +905,11 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   kmark (c, st, "mk_real");
   if (E) cudaEventRecord (E[2], st);
 
-  // self constants of the mixed split (equal spheres)
-  double *selfc = (double *) m->selfbuf.p;
-  {
-    std::vector<double> h (3 * (size_t) np);
-    for (int i = 0; i < np; i++)
-      { h[3 * i] = m->selfc[0]; h[3 * i + 1] = m->selfc[1]; h[3 * i + 2] = m->selfc[2]; }
-    // uploaded once per split change
-    if (m->fp != m->self_fp || m->self_np != np)
-      {
-        e = cudaMemcpyAsync (selfc, h.data (), sizeof (double) * 3 * np, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize (st);
-        if (e != cudaSuccess) return cuda_fail (e, "mixed self terms");
-        m->self_fp = m->fp;
-        m->self_np = np;
-      }
-  }
-  const int gc = (np + 7) / 8;      // eight particles per CTA
-  if (c->version == 0) mk_combine<0><<<gc, 8, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
-  else if (c->version == 1) mk_combine<1><<<gc, 8, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
-  else mk_combine<2><<<gc, 8, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfc, np, d_y);
+  const double *selfm = (const double *) m->selfbuf.p;
+  const int gc = (np * C + 63) / 64;
+  if (c->version == 0) mk_combine<0><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
+  else if (c->version == 1) mk_combine<1><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
+  else mk_combine<2><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
   kmark (c, st, "mk_combine");
   if (E) cudaEventRecord (E[3], st);
   if (m->tensor)
@@ -801,7 +933,8 @@ release_mixed (Ctx *c)
   if (!c->mixed) return;
   MixedState *m = c->mixed;
   for (DevBuf *b : {&m->kt, &m->qpos, &m->tab, &m->xf, &m->pq, &m->part_real, &m->part_rec,
-                    &m->selfbuf, &m->status, &m->sf, &m->wop, &m->rowm, &m->tbuf})
+                    &m->selfbuf, &m->status, &m->sf, &m->rowm, &m->rot, &m->img_tf,
+                    &m->img_tb, &m->img_zf, &m->img_wb})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
   delete m;

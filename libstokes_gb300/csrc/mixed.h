@@ -2,8 +2,10 @@
 // reciprocal-space tensor-core kernels (kspace_tc.cu).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
+#include <stdint.h>
 
 namespace lsg {
 
@@ -16,45 +18,87 @@ struct __align__ (16) MixK {
   float f0, f1, f2;
 };
 
-// per-axis phase tables e^{2 pi i m u_j}: tab[off_d + m * np + j], m = 0..M_d
+// per-axis phase tables e^{2 pi i m u_j}: tab[off_d + m * np + j], m = 0..M_d;
+// qpos: the 32-bit fixed-point fractional coordinates the tables come from
+// (x, y, z, pad per particle); rot: the 1024 rotations of phase_of
 struct PhaseTables {
   const float2 *tab;
   size_t off1, off2;
   int M0, M1, M2;
   int np;
+  const uint4 *qpos;
+  const float4 *rot;
 };
+
+// e^{2 pi i p / 2^32} to FP32 accuracy from a fixed-point phase p (turns x
+// 2^32): the nearest of 1024 tabulated rotations e^{2 pi i h / 1024} (rot[h]
+// = (hi.re, hi.im, lo.re, lo.im), each a float pair hi + lo) times a short
+// Taylor series of the remaining angle |theta| <= pi / 1024 (table-driven
+// argument reduction).  Truncation errors are below 1e-14; the result
+// carries one FP32 rounding (3e-8 measured over 2e6 random phases).
+__device__ __forceinline__ float2
+phase_of (const float4 *rot, uint32_t p)
+{
+  const uint32_t h = (p + (1u << 21)) >> 22;             // nearest table entry
+  const int32_t r = (int32_t) (p - (h << 22));           // |r| <= 2^21
+  const float th = (float) r * 1.4629180792671596e-09f;  // 2 pi / 2^32
+  const float t2 = th * th;
+  const float sn = th * (1.0f - t2 * (1.0f / 6.0f));     // sin th
+  const float dc = t2 * (0.5f - t2 * (1.0f / 24.0f));    // 1 - cos th
+  const float4 e = __ldg (rot + (h & 1023u));
+  // (e.x + e.z + i (e.y + e.w)) (1 - dc + i sn), small terms first
+  const float re = e.x + fmaf (-e.x, dc, fmaf (-e.y, sn, e.z));
+  const float im = e.y + fmaf (-e.y, dc, fmaf (e.x, sn, e.w));
+  return make_float2 (re, im);
+}
 
 // plan of the separable tensor-core reciprocal sum (kspace_tc.cu).  The k
 // vectors of the list are (m1, row) with row = one (m2, m3) combination that
-// occurs in it; R rows, n1 = M0 + 1 values of m1.
+// occurs in it; R rows, n1 = M0 + 1 values of m1.  The GEMM operands are
+// images [2 planes: TF32 hi, lo][rows][K] in FP32 (K contiguous):
+//   TF [R][KF]   T_r(j) as (Re, Im) pairs over the particles j < ldT
+//   ZF [NZ][KF]  rows (m1, re|im, q): t0[m1](j) x_q(j) in the forward sign pattern
+//   TB [np][KB]  T_r(j) as (Re, Im) pairs over the rows r < Rk
+//   WB [NZ][KB]  rows (m1, re|im, q): the k operators W in the backward pattern
 struct KGemm {
   PhaseTables t;
   const int2 *rowm;       // (m2, m3) of each row, R entries
-  int R;                  // rows
+  int R, Rk, Rp;          // rows; padded to 16 (backward K) and 32 (partials)
   int c;                  // components per particle (3, 6, 11)
   int n1;                 // M0 + 1
-  int nrt;                // forward row tiles of 64 rows
+  int nrt;                // forward row tiles of 128 rows
   int gf, ntile_f, nf;    // m1 per forward column tile, tiles, MMA N
   int jper, nsplit;       // particles per forward K slice, number of slices
   int gb, ntile_b, nb;    // m1 per backward column tile, tiles, MMA N
   int mtiles;             // 128-particle row tiles of the backward GEMM
   int rper, ksplit;       // rows per backward K slice, number of slices
-  float2 *T;              // T_r(j) = t1[m2](j) t2[m3](j), [R][ldT]
   int ldT;                // particles padded to a multiple of 16
+  int KF, KB, NZ;         // K extents (floats) of the images, rows of ZF and WB
+  float *TF, *TB, *ZF, *WB;
+  size_t pTF, pTB, pZF, pWB;   // plane strides (floats)
+};
+
+// TMA descriptors of the four images (128-byte swizzled boxes of 32 K values)
+struct KMaps {
+  CUtensorMap tf, zf, tb, wb;
 };
 
 KGemm kgemm_plan (int version, PhaseTables t, const int2 *rowm, int R);
 bool kgemm_fits (const KGemm &g);
 size_t kgemm_sf_floats (const KGemm &g);      // partial structure factors
-size_t kgemm_w_elems (const KGemm &g);        // complex operators W (float2)
-size_t kgemm_t_elems (const KGemm &g);        // row phase table T (float2)
+size_t kgemm_tf_floats (const KGemm &g);      // image sizes, both planes
+size_t kgemm_tb_floats (const KGemm &g);
+size_t kgemm_zf_floats (const KGemm &g);
+size_t kgemm_wb_floats (const KGemm &g);
 size_t kgemm_ypart_floats (const KGemm &g);   // partial y, [ksplit][ntile_b][np][c]
 int kgemm_ypart_chunks (const KGemm &g);       // ksplit * ntile_b
+int kgemm_maps (const KGemm &g, KMaps *m);     // 0 on success
 
-// forward GEMM -> per-k operators W -> backward GEMM into ypart
+// images TF, TB -> forward GEMM -> per-k operators (image WB) -> backward
+// GEMM into ypart; the image ZF is written beforehand by mk_prep
 struct Ctx;
-cudaError_t launch_kspace_gemm (int version, const KGemm &g, const MixK *kt, int nk,
-                                const float *xf, float *sf, float2 *W, float *ypart,
-                                int *status, cudaStream_t st, Ctx *prof);
+cudaError_t launch_kspace_gemm (int version, const KGemm &g, const KMaps &maps, const MixK *kt,
+                                int nk, float *sf, float *ypart, int *status, cudaStream_t st,
+                                Ctx *prof);
 
 }  // namespace lsg

@@ -39,6 +39,24 @@ smem_desc (uint32_t saddr, uint32_t lbo, uint32_t sbo)
   return d;
 }
 
+// descriptor of a K-major tile in the 128-byte swizzled layout that a TMA
+// load with CU_TENSOR_MAP_SWIZZLE_128B writes: rows of 128 bytes (32 TF32
+// values), 8-row groups 1024 bytes apart (SBO), the 16-byte chunks of row r
+// permuted by r % 8; the tile must start on a 1024-byte boundary.  The k-th
+// K step of 8 values starts 32 k bytes in (the swizzle is applied to the
+// address, so the start moves within the atom).  LBO is unused in this mode.
+__device__ __forceinline__ uint64_t
+smem_desc_sw128 (uint32_t saddr)
+{
+  uint64_t d = 0;
+  d |= (uint64_t) ((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t) 1u << 16;                 // LBO (ignored): 16 bytes
+  d |= (uint64_t) (1024u >> 4) << 32;       // SBO: 1024 bytes
+  d |= (uint64_t) 1u << 46;                 // descriptor version
+  d |= (uint64_t) 2u << 61;                 // layout: 128-byte swizzle
+  return d;
+}
+
 // instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major
 __host__ __device__ __forceinline__ uint32_t
 idesc_tf32 (uint32_t M, uint32_t N)
@@ -171,6 +189,35 @@ mbar_wait_or_abort (uint64_t *mbar, uint32_t parity, uint32_t limit, volatile in
     }
   *abort = 1;
   return false;
+}
+
+// arrive once on an mbarrier and add `bytes` to the transaction count its
+// current phase waits for (the TMA loads that follow complete them)
+__device__ __forceinline__ void
+mbar_expect_tx (uint64_t *mbar, uint32_t bytes)
+{
+  asm volatile ("{\n\t.reg .b64 st;\n\t"
+                "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                :: "r"(smem_u32 (mbar)), "r"(bytes) : "memory");
+}
+
+// 3-d tiled TMA load of one box at coordinates (c0, c1, c2) into shared
+// memory, completing `bytes of the box` on the mbarrier; tmap: the address of
+// a __grid_constant__ CUtensorMap kernel parameter
+__device__ __forceinline__ void
+tma_load_3d (void *dst, const void *tmap, int c0, int c1, int c2, uint64_t *mbar)
+{
+  asm volatile (
+    "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+    " [%0], [%1, {%2, %3, %4}], [%5];"
+    :: "r"(smem_u32 (dst)), "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32 (mbar))
+    : "memory");
+}
+
+__device__ __forceinline__ void
+tma_prefetch_desc (const void *tmap)
+{
+  asm volatile ("prefetch.tensormap [%0];" :: "l"(tmap) : "memory");
 }
 
 // generic-proxy smem writes -> visible to the tensor core (async proxy)
