@@ -24,17 +24,19 @@
 // above.  A GEMM tile is then four TMA loads (A hi, A lo, B hi, B lo, 32 K
 // values = 128 bytes per row, 128-byte swizzle) with no operand arithmetic in
 // the GEMM kernel.  The products are tcgen05 kind::tf32 MMAs (M = 128,
-// N <= 128, K = 8 per instruction) in 3xTF32: hi*hi + hi*lo + lo*hi.  The
+// N <= 256, K = 8 per instruction) in 3xTF32: hi*hi + hi*lo + lo*hi.  The
 // tensor core's FP32 accumulation truncates at the accumulator's magnitude,
-// so every 32-wide K tile starts fresh accumulators (hi*hi in one, the two
-// corrections in another) that are drained into FP32 registers (round to
-// nearest).
+// so every 32-wide K tile starts a fresh accumulator that is drained into
+// FP32 registers (round to nearest); within a tile the two small correction
+// products go in first and the hi*hi products last, so the corrections are
+// summed at their own magnitude and each later add truncates no more than
+// a hi*hi-only chain would.
 //
 // Warp roles (320 threads, one CTA per SM):
-//   warps 0-7   drain: double-buffered TMEM accumulators (2 x (main +
-//               correction) x 128 columns = 512 columns); warp w reads TMEM
-//               lanes 32 (w % 4) and columns 64 (w / 4) of each buffer
-//   warp 8      one lane issues the TMA loads of a 3-stage ring
+//   warps 0-7   drain: double-buffered TMEM accumulators (2 x 256 columns =
+//               512 columns); warp w reads TMEM lanes 32 (w % 4) and
+//               columns 128 (w / 4) of each buffer
+//   warp 8      one lane issues the TMA loads of a 2-stage ring
 //   warp 9      one lane issues the MMAs of a tile when its stage is full
 //               and its accumulator buffer has been drained
 // The roles meet only at mbarriers; every wait is bounded and watches a CTA
@@ -58,14 +60,14 @@ constexpr int NDRAIN = 8;               // drain warps 0..7
 constexpr int TMA_WARP = 8;
 constexpr int MMA_WARP = 9;
 constexpr int TM = 128;                 // MMA M
-constexpr int TN = 128;                 // largest MMA N (columns per tile)
+constexpr int TN = 256;                 // largest MMA N (columns per tile)
 constexpr int KT = 32;                  // K values per tile (128 bytes per row)
 constexpr int PT = KT / 2;              // complex entries per K tile
-constexpr int STAGES = 3;
-constexpr int CPT = TN / 2;             // accumulator columns per drain thread (64)
+constexpr int STAGES = 2;
+constexpr int CPT = TN / 2;             // accumulator columns per drain thread (128)
 constexpr uint32_t A_BYTES = TM * KT * 4;
 constexpr uint32_t B_BYTES = TN * KT * 4;
-constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;   // 64 KB: hi + lo of A and B
+constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;   // 96 KB: hi + lo of A and B
 constexpr uint32_t SMEM_DYN = STAGES * STAGE_BYTES + 1024;    // + room to align to 1 KB
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t WAIT_LIMIT = 1u << 18;   // polls of up to ~20 us each
@@ -155,7 +157,8 @@ mma_role (Sync &s, const unsigned char *smem, uint32_t tmem, uint32_t idesc, int
       const uint32_t base = umma::smem_u32 (smem) + (uint32_t) st * STAGE_BYTES;
       const uint32_t ahi = base, alo = base + A_BYTES, bhi = base + 2 * A_BYTES,
                      blo = bhi + B_BYTES;
-      const uint32_t dm = tmem + (uint32_t) (b * 2 * TN), dc = dm + TN;
+      const uint32_t d = tmem + (uint32_t) (b * TN);
+      // corrections first (summed at their own magnitude), then hi*hi
 #pragma unroll
       for (int k = 0; k < KT / 8; k++)
         {
@@ -163,10 +166,13 @@ mma_role (Sync &s, const unsigned char *smem, uint32_t tmem, uint32_t idesc, int
           const uint64_t dal = umma::smem_desc_sw128 (alo + 32 * k);
           const uint64_t dbh = umma::smem_desc_sw128 (bhi + 32 * k);
           const uint64_t dbl = umma::smem_desc_sw128 (blo + 32 * k);
-          umma::mma_tf32 (dm, dah, dbh, idesc, k ? 1u : 0u);
-          umma::mma_tf32 (dc, dah, dbl, idesc, k ? 1u : 0u);
-          umma::mma_tf32 (dc, dal, dbh, idesc, 1u);
+          umma::mma_tf32 (d, dah, dbl, idesc, k ? 1u : 0u);
+          umma::mma_tf32 (d, dal, dbh, idesc, 1u);
         }
+#pragma unroll
+      for (int k = 0; k < KT / 8; k++)
+        umma::mma_tf32 (d, umma::smem_desc_sw128 (ahi + 32 * k),
+                        umma::smem_desc_sw128 (bhi + 32 * k), idesc, 1u);
       umma::mma_commit (&s.empty[st]);
       umma::mma_commit (&s.acc_full[b]);
     }
@@ -176,7 +182,7 @@ mma_role (Sync &s, const unsigned char *smem, uint32_t tmem, uint32_t idesc, int
   umma::mbar_wait_or_abort (&s.done, 0, WAIT_LIMIT, &never);
 }
 
-// drain warps: acc += both accumulators of each tile
+// drain warps: acc += each tile's accumulator
 __device__ __forceinline__ bool
 drain_role (Sync &s, uint32_t tmem, int ntiles, float acc[CPT])
 {
@@ -189,20 +195,40 @@ drain_role (Sync &s, uint32_t tmem, int ntiles, float acc[CPT])
       const int b = t & 1;
       if (!umma::mbar_wait_or_abort (&s.acc_full[b], (t >> 1) & 1, WAIT_LIMIT, err)) return false;
       umma::fence_after_sync ();
-      const uint32_t dm = tmem + lane_base + (uint32_t) (b * 2 * TN) + col;
+      const uint32_t dm = tmem + lane_base + (uint32_t) (b * TN) + col;
 #pragma unroll
-      for (int cc = 0; cc < CPT; cc += 16)
+      for (int cc = 0; cc < CPT; cc += 32)
         {
           float m[16], c[16];
           umma::tmem_ld16 (dm + cc, m);
-          umma::tmem_ld16 (dm + TN + cc, c);
+          umma::tmem_ld16 (dm + cc + 16, c);
 #pragma unroll
-          for (int u = 0; u < 16; u++) acc[cc + u] += m[u] + c[u];
+          for (int u = 0; u < 16; u++)
+            {
+              acc[cc + u] += m[u];
+              acc[cc + 16 + u] += c[u];
+            }
         }
       umma::fence_before_sync ();
       umma::mbar_arrive (&s.acc_empty[b]);
     }
   return true;
+}
+
+// Once every tile is drained no load or MMA touches the stages any more, so
+// the drain threads park their accumulator rows there: H[row][column], row
+// stride HLD floats (odd, so a warp's 32 rows fall in distinct banks).
+constexpr int HLD = TN + 1;
+static_assert (TM * HLD * 4 <= (int) (STAGES * STAGE_BYTES), "parked tile exceeds the stages");
+
+__device__ __forceinline__ void
+park (unsigned char *smem, const float acc[CPT])
+{
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = (warp & 3) * 32 + lane, cb = (warp >> 2) * CPT;
+  float *H = reinterpret_cast<float *> (smem) + row * HLD + cb;
+#pragma unroll
+  for (int u = 0; u < CPT; u++) H[u] = acc[u];
 }
 
 // a complex value as TF32 hi and lo parts (FP32 bit patterns)
@@ -319,22 +345,23 @@ k_sfac_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
       float acc[CPT];
 #pragma unroll
       for (int u = 0; u < CPT; u++) acc[u] = 0.f;
-      if (drain_role (s, tmem, ntiles, acc) && !s.err)
+      if (drain_role (s, tmem, ntiles, acc)) park (smem, acc);
+    }
+  __syncthreads ();
+  if (!s.err)
+    {
+      // sf[split][m1][q][re|im][Rp]: rows r contiguous, so consecutive
+      // threads take consecutive rows of one column
+      const float *H = reinterpret_cast<const float *> (smem);
+      const int rows = min (TM, g.R - r0);
+      for (int e = tid; e < ncol * TM; e += NT)
         {
-          // this thread: TMEM lane = row r, 64 columns (m1, re|im, q) from
-          // (warp >> 2) * 64; sf[split][m1][q][re|im][Rp]
-          const int r = r0 + (warp & 3) * 32 + lane;
-          const int cb = (warp >> 2) * CPT;
-          if (r < g.R)
-#pragma unroll
-            for (int u = 0; u < CPT; u++)
-              {
-                const int n = cb + u;
-                if (n >= ncol) break;
-                const int m = n / (2 * C), rem = n - m * 2 * C, part = rem >= C ? 1 : 0;
-                const int q = rem - part * C;
-                sf[((((size_t) split * g.n1 + m1b + m) * C + q) * 2 + part) * g.Rp + r] = acc[u];
-              }
+          const int n = e / TM, rl = e - n * TM;
+          if (rl >= rows) continue;
+          const int m = n / (2 * C), rem = n - m * 2 * C, part = rem >= C ? 1 : 0;
+          const int q = rem - part * C;
+          sf[((((size_t) split * g.n1 + m1b + m) * C + q) * 2 + part) * g.Rp + r0 + rl] =
+            H[rl * HLD + n];
         }
     }
   __syncthreads ();
@@ -449,7 +476,6 @@ k_bp_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
   constexpr int C = NComp<V>::value;
   extern __shared__ unsigned char dsm[];
   __shared__ Sync s;
-  __shared__ float s_y[TM][C];
   unsigned char *smem = align1k (dsm);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int np = g.t.np;
@@ -463,8 +489,6 @@ k_bp_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
 
   cta_setup (s);
   const uint32_t tmem = s.tslot;
-  for (int e = tid; e < TM * C; e += NT) s_y[e / C][e % C] = 0.f;
-  __syncthreads ();
 
   if (warp == TMA_WARP)
     {
@@ -482,50 +506,32 @@ k_bp_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
       float acc[CPT];
 #pragma unroll
       for (int u = 0; u < CPT; u++) acc[u] = 0.f;
-      if (drain_role (s, tmem, ntiles, acc) && !s.err)
-        {
-          const int row = (warp & 3) * 32 + lane;
-          const int i = i0 + row;
-          if (i < np)
-            {
-              // y_i[q] += Re(conj(t0[m1])(i) H) over this thread's columns
-              float yq[C];
-#pragma unroll
-              for (int q = 0; q < C; q++) yq[q] = 0.f;
-              const int cb = (warp >> 2) * CPT;
-              int cur = -1;
-              float2 ph = make_float2 (0.f, 0.f);
-#pragma unroll
-              for (int u = 0; u < CPT; u++)
-                {
-                  const int n = cb + u;
-                  if (n >= ncol) break;
-                  const int m = n / (2 * C), rem = n - m * 2 * C, im = rem >= C, q = rem - im * C;
-                  if (m != cur)
-                    {
-                      ph = t0[(size_t) (m1b + m) * np + i];
-                      cur = m;
-                    }
-                  const float c = (im ? ph.y : ph.x) * acc[u];
-#pragma unroll
-                  for (int qq = 0; qq < C; qq++)
-                    if (qq == q) yq[qq] += c;
-                }
-#pragma unroll
-              for (int q = 0; q < C; q++) atomicAdd (&s_y[row][q], yq[q]);
-            }
-        }
+      if (drain_role (s, tmem, ntiles, acc)) park (smem, acc);
     }
   __syncthreads ();
   if (tid == 0 && s.err) atomicExch (status, 1);
+  if (!s.err)
+    {
+      // y_i[q] = sum over m1 of Re(conj(t0[m1])(i) H[i, (m1, q)]), one
+      // (particle, component) per thread
+      const float *H = reinterpret_cast<const float *> (smem);
+      const size_t chunk = (size_t) ks * gridDim.y + blockIdx.y;
+      for (int e = tid; e < TM * C; e += NT)
+        {
+          const int r = e / C, q = e - r * C, i = i0 + r;
+          if (i >= np) continue;
+          float y = 0.f;
+          for (int m = 0; m < nm1; m++)
+            {
+              const float2 ph = t0[(size_t) (m1b + m) * np + i];
+              y = fmaf (ph.x, H[r * HLD + m * 2 * C + q], y);
+              y = fmaf (ph.y, H[r * HLD + m * 2 * C + C + q], y);
+            }
+          ypart[(chunk * np + i) * C + q] = y;
+        }
+    }
   umma::fence_before_sync ();
   __syncthreads ();
-  const size_t chunk = (size_t) ks * gridDim.y + blockIdx.y;
-  for (int e = tid; e < TM * C; e += NT)
-    {
-      const int r = e / C, q = e % C;
-      if (i0 + r < np) ypart[(chunk * np + i0 + r) * C + q] = s_y[r][q];
-    }
   if (warp == 0) umma::tmem_dealloc (tmem, TMEM_COLS);
 }
 
