@@ -456,7 +456,7 @@ stokes_gpu_vjp (struct stokes *sys, const double *g, const double *f, double *dL
     return set_error (STOKES_GPU_EINVAL, "box derivatives are defined without shear");
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
-  int rc = prepare (c, sys, false);
+  int rc = prepare (c, sys, false, 1);
   if (rc) return rc;
   const int np = sys->np, C = NCOMP (sys->version), nk = c->nk;
   const size_t n = (size_t) C * np;

@@ -290,7 +290,7 @@ upload_if_changed (DevBuf &buf, uint64_t &fp, const void *host, size_t bytes,
 }
 
 int
-prepare (Ctx *c, const struct stokes *sys, bool cube)
+prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
 {
   int rc = check_sys (sys);
   if (rc) return rc;
@@ -305,6 +305,14 @@ prepare (Ctx *c, const struct stokes *sys, bool cube)
   c->rmax2 = sys->rmax2;
   c->rmin = sys->rmin;
 
+  if (tables < 0) tables = c->precision == STOKES_GPU_MIXED ? 0 : 1;
+  if (!tables)
+    {
+      // the particle table only (radii for the BD interactions)
+      build_particles (sys, c->mode, c->h_pp);
+      return upload_if_changed (c->pp, c->fp_pp, c->h_pp.data (), sizeof (double) * c->h_pp.size (),
+                                c->stream, "particle table");
+    }
   build_images (sys, cube, c->h_img);
   c->nimg = (int) c->h_img.size ();
   rc = upload_if_changed (c->img, c->fp_img, c->h_img.data (), sizeof (Img4) * c->h_img.size (),
@@ -544,7 +552,7 @@ matrix_host (struct stokes *sys, double *mat, bool cube)
   if (mat == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL mat");
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
-  int rc = prepare (c, sys, cube);
+  int rc = prepare (c, sys, cube, 1);
   if (rc) return rc;
   const int np = sys->np;
   const size_t n = (size_t) NCOMP (sys->version) * np;
@@ -575,7 +583,7 @@ atimes_matrix_host (struct stokes *sys, const double *x, double *y, bool cube)
   if (x == nullptr || y == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL x or y");
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
-  int rc = prepare (c, sys, cube);
+  int rc = prepare (c, sys, cube, 1);
   if (rc) return rc;
   const int np = sys->np;
   const size_t n = (size_t) NCOMP (sys->version) * np;
@@ -676,7 +684,7 @@ stokes_gpu_matrix_dev (struct stokes *sys, const double *d_pos, double *d_mat, v
   if (d_mat == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL mat");
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
-  int rc = prepare (c, sys, false);
+  int rc = prepare (c, sys, false, 1);
   if (rc) return rc;
   cudaStream_t st = stream ? (cudaStream_t) stream : c->stream;
   if (d_pos == nullptr)

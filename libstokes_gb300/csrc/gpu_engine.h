@@ -75,7 +75,11 @@ void build_images (const struct stokes *sys, bool cube, std::vector<Img4> &img);
 void build_ktable (const struct stokes *sys, std::vector<double> &kt);
 void build_particles (const struct stokes *sys, int mode, std::vector<double> &pp);
 int release_ctx (const struct stokes *sys);
-int prepare (Ctx *c, const struct stokes *sys, bool cube);
+// check sys and bring the context's device tables up to date.  tables: 1
+// builds the FP64 image and reciprocal tables (the FP64 product, the dense
+// builder, the adjoint), 0 skips them (the mixed product never reads them),
+// -1 chooses by the context's precision.
+int prepare (Ctx *c, const struct stokes *sys, bool cube, int tables = -1);
 int atimes_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                 cudaStream_t st, bool timed);
 int atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,

@@ -231,6 +231,34 @@ park (unsigned char *smem, const float acc[CPT])
   for (int u = 0; u < CPT; u++) H[u] = acc[u];
 }
 
+// forward drain threads: drain every tile, then column n = (m, re|im, q) of
+// row r goes to
+// Hs[((m C + q) 2 + re|im) TM + r], the order of the partial structure
+// factors sf[split][m1][q][re|im][r], so that each m1's block of rows is one
+// TMA store.  CB: the thread's first column (compile time, so the index
+// arithmetic folds away).
+template <int C, int CB>
+__device__ __forceinline__ void
+drain_park_sf (Sync &s, uint32_t tmem, int ntiles, unsigned char *smem, int ncol)
+{
+  float acc[CPT];
+#pragma unroll
+  for (int u = 0; u < CPT; u++) acc[u] = 0.f;
+  if (!drain_role (s, tmem, ntiles, acc)) return;
+  const int row = ((threadIdx.x >> 5) & 3) * 32 + (threadIdx.x & 31);
+  float *Hs = reinterpret_cast<float *> (smem) + row;
+#pragma unroll
+  for (int u = 0; u < CPT; u++)
+    {
+      constexpr int P = 2 * C;
+      const int n = CB + u;
+      const int m = n / P, rem = n - m * P, part = rem >= C ? 1 : 0, q = rem - part * C;
+      if (n < ncol) Hs[((m * C + q) * 2 + part) * TM] = acc[u];
+    }
+  // these writes are read by the TMA unit (async proxy) after the barrier
+  umma::fence_async_smem ();
+}
+
 // a complex value as TF32 hi and lo parts (FP32 bit patterns)
 __device__ __forceinline__ void
 split2 (float2 v, float2 &hi, float2 &lo)
@@ -312,7 +340,7 @@ k_tprep (KGemm g)
 template <int V>
 __global__ void __launch_bounds__ (NT, 1)
 k_sfac_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-             KGemm g, float *sf, int *status)
+             const __grid_constant__ CUtensorMap tmS, KGemm g, int *status)
 {
   constexpr int C = NComp<V>::value;
   extern __shared__ unsigned char dsm[];
@@ -342,27 +370,20 @@ k_sfac_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     }
   else
     {
-      float acc[CPT];
-#pragma unroll
-      for (int u = 0; u < CPT; u++) acc[u] = 0.f;
-      if (drain_role (s, tmem, ntiles, acc)) park (smem, acc);
+      if (warp >> 2) drain_park_sf<C, CPT> (s, tmem, ntiles, smem, ncol);
+      else drain_park_sf<C, 0> (s, tmem, ntiles, smem, ncol);
     }
   __syncthreads ();
-  if (!s.err)
+  if (!s.err && tid == 0)
     {
-      // sf[split][m1][q][re|im][Rp]: rows r contiguous, so consecutive
-      // threads take consecutive rows of one column
-      const float *H = reinterpret_cast<const float *> (smem);
-      const int rows = min (TM, g.R - r0);
-      for (int e = tid; e < ncol * TM; e += NT)
-        {
-          const int n = e / TM, rl = e - n * TM;
-          if (rl >= rows) continue;
-          const int m = n / (2 * C), rem = n - m * 2 * C, part = rem >= C ? 1 : 0;
-          const int q = rem - part * C;
-          sf[((((size_t) split * g.n1 + m1b + m) * C + q) * 2 + part) * g.Rp + r0 + rl] =
-            H[rl * HLD + n];
-        }
+      // one TMA store per m1: 2C rows (q, re|im) of 128 r each; rows past
+      // the end of sf are dropped by the TMA unit
+      const float *Hs = reinterpret_cast<const float *> (smem);
+      for (int m = 0; m < nm1; m++)
+        umma::tma_store_2d (&tmS, Hs + (size_t) m * 2 * C * TM, r0,
+                            (split * g.n1 + m1b + m) * 2 * C);
+      umma::bulk_commit ();
+      umma::bulk_wait_read ();
     }
   __syncthreads ();
   if (tid == 0 && s.err) atomicExch (status, 1);
@@ -609,30 +630,42 @@ int kgemm_ypart_chunks (const KGemm &g) { return g.ksplit * g.ntile_b; }
 size_t kgemm_ypart_floats (const KGemm &g) { return (size_t) kgemm_ypart_chunks (g) * g.t.np * g.c; }
 
 int
-kgemm_maps (const KGemm &g, KMaps *m)
+kgemm_maps (const KGemm &g, float *sf, KMaps *m)
 {
   int e = encode_planes_sw128 (&m->tf, g.TF, 2, (unsigned long long) g.R, g.KF, TM);
   if (!e) e = encode_planes_sw128 (&m->zf, g.ZF, 2, (unsigned long long) g.NZ, g.KF, g.nf);
   if (!e) e = encode_planes_sw128 (&m->tb, g.TB, 2, (unsigned long long) g.t.np, g.KB, TM);
   if (!e) e = encode_planes_sw128 (&m->wb, g.WB, 2, (unsigned long long) g.NZ, g.KB, g.nb);
+  if (!e)
+    e = encode_rows_plain (&m->sf, sf, (unsigned long long) g.nsplit * g.n1 * g.c * 2, g.Rp, TM,
+                           2 * g.c);
   return e;
 }
 
 template <int V>
 static cudaError_t
-launch_v (const KGemm &g, const KMaps &mp, const MixK *kt, int nk, float *sf, float *ypart,
+launch_v (const KGemm &g, const KMaps &mp, const MixK *kt, int nk, const float *sf, float *ypart,
           int *status, cudaStream_t st, Ctx *prof)
 {
-  cudaError_t e;
-  if ((e = cudaFuncSetAttribute (k_sfac_gemm<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int) SMEM_DYN)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute (k_bp_gemm<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int) SMEM_DYN)) != cudaSuccess)
-    return e;
+  // the shared-memory opt-in is a per-device function attribute; set once
+  // per device
+  static int attr_dev = -1;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice (&dev);
+  if (e != cudaSuccess) return e;
+  if (attr_dev != dev)
+    {
+      if ((e = cudaFuncSetAttribute (k_sfac_gemm<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int) SMEM_DYN)) != cudaSuccess)
+        return e;
+      if ((e = cudaFuncSetAttribute (k_bp_gemm<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int) SMEM_DYN)) != cudaSuccess)
+        return e;
+      attr_dev = dev;
+    }
   k_tprep<<<dim3 ((g.ldT + 31) / 32, (g.Rk + 31) / 32), 256, 0, st>>> (g);
   kmark (prof, st, "k_tprep");
-  k_sfac_gemm<V><<<dim3 (g.nrt, g.ntile_f, g.nsplit), NT, SMEM_DYN, st>>> (mp.tf, mp.zf, g, sf, status);
+  k_sfac_gemm<V><<<dim3 (g.nrt, g.ntile_f, g.nsplit), NT, SMEM_DYN, st>>> (mp.tf, mp.zf, mp.sf, g, status);
   kmark (prof, st, "k_sfac_gemm");
   k_kop<V><<<(nk + KOP_K - 1) / KOP_K, KOP_K * KOP_G, 0, st>>> (g, kt, nk, sf);
   kmark (prof, st, "k_kop");

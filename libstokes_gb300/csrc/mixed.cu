@@ -47,6 +47,10 @@ struct MixedState {
   DevBuf img_tf, img_tb, img_zf, img_wb;   // GEMM operand images (kspace_tc.cu)
   KMaps maps;
   uint64_t img_key = 0;         // buffers and plan the maps and zeroed pads belong to
+  // the real-space kernel runs on this side stream, concurrently with the
+  // reciprocal chain (low priority: it fills the SMs the chain leaves idle)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int nrow = 0;          // (m2, m3) rows of the tensor-core contraction
   int *h_status = nullptr;      // pinned copy of the kernels' status word
   bool tensor = true;           // reciprocal space on the tensor cores
@@ -103,8 +107,8 @@ fixq (double v)
 // m1 also write Z = t0[m1] x_q as TF32 hi/lo pairs in the forward GEMM's
 // sign pattern: image row (m1, re, q) = (Re Z, -Im Z), (m1, im, q) =
 // (Im Z, Re Z) at column pair j.
-// CTA (blockIdx.x, blockIdx.y): PREP_P particles x PREP_ROWS table rows; the
-// few FP64 operations per particle are repeated by each row group.
+// CTA (blockIdx.x, blockIdx.y): PREP_P particles x about PREP_ROWS table
+// rows; the few FP64 operations per particle are repeated by each row group.
 __global__ void __launch_bounds__ (128)
 mk_prep (PrepArgs a)
 {
@@ -149,10 +153,12 @@ mk_prep (PrepArgs a)
       s_q[0][t] = qu; s_q[1][t] = q1; s_q[2][t] = q2;
     }
   __syncthreads ();
-  const int r0 = blockIdx.y * PREP_ROWS, r1 = min (a.ntab, r0 + PREP_ROWS);
-  for (int e = t; e < (r1 - r0) * PREP_P; e += blockDim.x)
+  // row group y takes rows y, y + G, y + 2 G, ... (G = gridDim.y), so the
+  // flow-axis rows, which also write ZF, spread over the groups
+  const int G = gridDim.y, nr = (a.ntab - (int) blockIdx.y + G - 1) / G;
+  for (int e = t; e < nr * PREP_P; e += blockDim.x)
     {
-      const int row = r0 + e / PREP_P, jl = e % PREP_P, j = jb + jl;
+      const int row = blockIdx.y + (e / PREP_P) * G, jl = e % PREP_P, j = jb + jl;
       if (j >= a.np) continue;
       const int d = row < a.m0end ? 0 : (row < a.m1end ? 1 : 2);
       const uint32_t m = (uint32_t) (row - (d == 0 ? 0 : (d == 1 ? a.m0end : a.m1end)));
@@ -752,6 +758,15 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       if ((e = m->status.ensure (sizeof (int))) != cudaSuccess) return cuda_fail (e, "status");
       cudaMemsetAsync (m->status.p, 0, sizeof (int), st);
     }
+  if (!m->side)
+    {
+      int lo = 0, hi = 0;
+      cudaDeviceGetStreamPriorityRange (&lo, &hi);
+      if (cudaStreamCreateWithPriority (&m->side, cudaStreamNonBlocking, lo) != cudaSuccess
+          || cudaEventCreateWithFlags (&m->ev_fork, cudaEventDisableTiming) != cudaSuccess
+          || cudaEventCreateWithFlags (&m->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        return set_error (STOKES_GPU_ECUDA, "mixed product: side stream");
+    }
   if ((e = m->qpos.ensure (sizeof (uint32_t) * 4 * np)) != cudaSuccess) return cuda_fail (e, "qpos");
   if ((e = m->tab.ensure (sizeof (float2) * (size_t) ntab * np)) != cudaSuccess) return cuda_fail (e, "phase tables");
   m->plan.t.tab = (const float2 *) m->tab.p;
@@ -810,7 +825,8 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       // buffers change
       uint64_t key = m->fp * 1000003ull;
       for (const void *p : {(const void *) m->img_tf.p, (const void *) m->img_tb.p,
-                            (const void *) m->img_zf.p, (const void *) m->img_wb.p})
+                            (const void *) m->img_zf.p, (const void *) m->img_wb.p,
+                            (const void *) m->sf.p})
         key = (key ^ (uint64_t) (uintptr_t) p) * 1099511628211ull;
       if (key != m->img_key)
         {
@@ -818,7 +834,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
           if (e == cudaSuccess)
             e = cudaMemsetAsync (m->img_wb.p, 0, sizeof (float) * kgemm_wb_floats (m->plan), st);
           if (e != cudaSuccess) return cuda_fail (e, "GEMM images");
-          const int me = kgemm_maps (m->plan, &m->maps);
+          const int me = kgemm_maps (m->plan, (float *) m->sf.p, &m->maps);
           if (me) return set_error (STOKES_GPU_ECUDA, "TMA tensor maps of the GEMM images (%d)", me);
           m->img_key = key;
         }
@@ -846,6 +862,42 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   pa.kf = m->plan.KF;
   mk_prep<<<dim3 ((np + PREP_P - 1) / PREP_P, (ntab + PREP_ROWS - 1) / PREP_ROWS), 128, 0, st>>> (pa);
   kmark (c, st, "mk_prep");
+
+  RealMixArgs ra;
+  ra.qpos = (const uint32_t *) m->qpos.p; ra.xf = (const float *) m->xf.p;
+  ra.np = np; ra.nchunk = m->nchunk_r;
+  const double two32 = 4294967296.0;
+  ra.scale[0] = (float) (sys->lx / two32);
+  ra.scale[1] = (float) (sys->ly / two32);
+  ra.scale[2] = (float) (sys->lz / two32);
+  ra.shear_mode = sys->shear_mode;
+  {
+    double sq = sys->shear_shift / sys->lx * two32;
+    long long iq = llround (sq);
+    ra.shift_q = (uint32_t) (iq & 0xffffffffll);
+  }
+  ra.rc2 = (float) (m->rc * m->rc);
+  ra.rmin = (float) sys->rmin;
+  ra.xi = (float) m->xi;
+  ra.xisp = (float) (m->xi / sqrt (M_PI));
+  ra.rad = nullptr; ra.slipa = nullptr;
+  ra.partial = (float *) m->part_real.p;
+  const int gr = (int) (((long long) np * m->nchunk_r + MX_WARPS - 1) / MX_WARPS);
+  // concurrent with the reciprocal chain unless the launches are being
+  // timed one by one (then in order: reciprocal, real, combine)
+  const bool overlap = !E && !c->kprof_on && m->side;
+  auto launch_real = [&] (cudaStream_t rs) {
+    if (c->version == 0) mk_real<0, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
+    else if (c->version == 1) mk_real<1, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
+    else mk_real<2, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
+  };
+  if (overlap)
+    {
+      cudaEventRecord (m->ev_fork, st);
+      cudaStreamWaitEvent (m->side, m->ev_fork, 0);
+      launch_real (m->side);
+      cudaEventRecord (m->ev_join, m->side);
+    }
 
   KMixArgs ka;
   ka.kt = (const MixK *) m->kt.p; ka.tab = (const float2 *) m->tab.p;
@@ -878,31 +930,13 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   else
     cudaMemsetAsync (m->part_rec.p, 0, sizeof (float) * (size_t) m->nchunk_k * np * C, st);
   if (E) cudaEventRecord (E[1], st);
-
-  RealMixArgs ra;
-  ra.qpos = (const uint32_t *) m->qpos.p; ra.xf = (const float *) m->xf.p;
-  ra.np = np; ra.nchunk = m->nchunk_r;
-  const double two32 = 4294967296.0;
-  ra.scale[0] = (float) (sys->lx / two32);
-  ra.scale[1] = (float) (sys->ly / two32);
-  ra.scale[2] = (float) (sys->lz / two32);
-  ra.shear_mode = sys->shear_mode;
-  {
-    double sq = sys->shear_shift / sys->lx * two32;
-    long long iq = llround (sq);
-    ra.shift_q = (uint32_t) (iq & 0xffffffffll);
-  }
-  ra.rc2 = (float) (m->rc * m->rc);
-  ra.rmin = (float) sys->rmin;
-  ra.xi = (float) m->xi;
-  ra.xisp = (float) (m->xi / sqrt (M_PI));
-  ra.rad = nullptr; ra.slipa = nullptr;
-  ra.partial = (float *) m->part_real.p;
-  const int gr = (int) (((long long) np * m->nchunk_r + MX_WARPS - 1) / MX_WARPS);
-  if (c->version == 0) mk_real<0, MODE_MONO><<<gr, MX_WARPS * 32, 0, st>>> (ra);
-  else if (c->version == 1) mk_real<1, MODE_MONO><<<gr, MX_WARPS * 32, 0, st>>> (ra);
-  else mk_real<2, MODE_MONO><<<gr, MX_WARPS * 32, 0, st>>> (ra);
-  kmark (c, st, "mk_real");
+  if (overlap)
+    cudaStreamWaitEvent (st, m->ev_join, 0);
+  else
+    {
+      launch_real (st);
+      kmark (c, st, "mk_real");
+    }
   if (E) cudaEventRecord (E[2], st);
 
   const double *selfm = (const double *) m->selfbuf.p;
@@ -937,6 +971,9 @@ release_mixed (Ctx *c)
                     &m->img_tb, &m->img_zf, &m->img_wb})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
+  if (m->side) cudaStreamDestroy (m->side);
+  if (m->ev_fork) cudaEventDestroy (m->ev_fork);
+  if (m->ev_join) cudaEventDestroy (m->ev_join);
   delete m;
   c->mixed = nullptr;
 }

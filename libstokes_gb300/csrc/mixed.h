@@ -79,8 +79,9 @@ struct KGemm {
 };
 
 // TMA descriptors of the four images (128-byte swizzled boxes of 32 K values)
+// and of the forward partials sf (boxes of 128 rows x one m1's columns)
 struct KMaps {
-  CUtensorMap tf, zf, tb, wb;
+  CUtensorMap tf, zf, tb, wb, sf;
 };
 
 KGemm kgemm_plan (int version, PhaseTables t, const int2 *rowm, int R);
@@ -92,7 +93,7 @@ size_t kgemm_zf_floats (const KGemm &g);
 size_t kgemm_wb_floats (const KGemm &g);
 size_t kgemm_ypart_floats (const KGemm &g);   // partial y, [ksplit][ntile_b][np][c]
 int kgemm_ypart_chunks (const KGemm &g);       // ksplit * ntile_b
-int kgemm_maps (const KGemm &g, KMaps *m);     // 0 on success
+int kgemm_maps (const KGemm &g, float *sf, KMaps *m);   // 0 on success
 
 // images TF, TB -> forward GEMM -> per-k operators (image WB) -> backward
 // GEMM into ypart; the image ZF is written beforehand by mk_prep

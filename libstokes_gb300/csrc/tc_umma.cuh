@@ -214,6 +214,30 @@ tma_load_3d (void *dst, const void *tmap, int c0, int c1, int c2, uint64_t *mbar
     : "memory");
 }
 
+// 2-d tiled TMA store of one box from shared memory (128-byte aligned, the
+// box's rows back to back) to coordinates (c0, c1); parts of the box outside
+// the tensor are not written.  Completes asynchronously: commit the group and
+// wait before the shared memory is reused.
+__device__ __forceinline__ void
+tma_store_2d (const void *tmap, const void *src, int c0, int c1)
+{
+  asm volatile ("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];"
+                :: "l"(tmap), "r"(smem_u32 (src)), "r"(c0), "r"(c1) : "memory");
+}
+
+__device__ __forceinline__ void
+bulk_commit ()
+{
+  asm volatile ("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+// wait until every committed bulk store has finished reading shared memory
+__device__ __forceinline__ void
+bulk_wait_read ()
+{
+  asm volatile ("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
 __device__ __forceinline__ void
 tma_prefetch_desc (const void *tmap)
 {

@@ -64,7 +64,7 @@ stokes_gpu_count_real_terms (struct stokes *sys, long long *count)
   if (!count) return set_error (STOKES_GPU_EINVAL, "NULL count");
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
-  int rc = prepare (c, sys, false);
+  int rc = prepare (c, sys, false, 1);
   if (rc) return rc;
   cudaError_t e;
   if ((e = c->pos.ensure (sizeof (double) * 3 * sys->np)) != cudaSuccess) return cuda_fail (e, "pos");
