@@ -9,34 +9,37 @@
 //
 //   forward   S[r, (m1, q)] = sum_j T_r(j) Z_(m1,q)(j),   Z = t0[m1] x_q
 //             real rows r; columns (m1, re|im, q); K = (j, a|b) with
-//             (a, b) = (Re, Im) T_r(j):  A = TF[r][(j, a|b)];
+//             (a, b) = (Re, Im) T_r(j):  A[r][(j, a|b)];
 //             B row (m1, re, q) = (u, -v), row (m1, im, q) = (v, u) with
-//             (u, v) = Z  (ZF)
+//             (u, v) = Z  (image ZF)
 //   operator  W_k = P_k + i Q_k for every k of the half-space list (k_kop)
 //   backward  H[i, (m1, re|im, q)] = sum_r conj(T_r)(i) W[r, (m1, q)]:
-//             A' = TB[i][(r, a|b)]; B' row (m1, re, q) = (U, V), row
-//             (m1, im, q) = (V, -U) with (U, V) = W  (WB);
+//             A'[i][(r, a|b)]; B' row (m1, re, q) = (U, V), row
+//             (m1, im, q) = (V, -U) with (U, V) = W  (image WB);
 //             y_i[q] += Re(conj(t0[m1])(i) H) over m1 in the epilogue.
 //
-// Each operand is written once per product as an IMAGE: an FP32 array
+// The B operands are written once per product as IMAGES: FP32 arrays
 // [2][rows][K] (plane 0 the TF32-rounded value, plane 1 the TF32-rounded
 // remainder, x = hi + lo), K contiguous and already in the sign pattern
-// above.  A GEMM tile is then four TMA loads (A hi, A lo, B hi, B lo, 32 K
-// values = 128 bytes per row, 128-byte swizzle) with no operand arithmetic in
-// the GEMM kernel.  The products are tcgen05 kind::tf32 MMAs (M = 128,
-// N <= 256, K = 8 per instruction) in 3xTF32: hi*hi + hi*lo + lo*hi.  The
-// tensor core's FP32 accumulation truncates at the accumulator's magnitude,
-// so every 32-wide K tile starts a fresh accumulator that is drained into
-// FP32 registers (round to nearest); within a tile the two small correction
-// products go in first and the hi*hi products last, so the corrections are
-// summed at their own magnitude and each later add truncates no more than
-// a hi*hi-only chain would.
+// above, loaded per tile by TMA (32 K values = 128 bytes per row, 128-byte
+// swizzle).  The A operands -- the row phases T_r -- are not stored: the
+// worker warps build each tile straight into shared memory from the 32-bit
+// fixed-point coordinates (m2 q_y + m3 q_z mod 2^32 is the exact phase) with
+// the table-driven phase_of, in the same swizzled layout.  The products are
+// tcgen05 kind::tf32 MMAs (M = 128, N <= 256, K = 8 per instruction) in
+// 3xTF32: hi*hi + hi*lo + lo*hi.  The tensor core's FP32 accumulation
+// truncates at the accumulator's magnitude, so every 32-wide K tile starts a
+// fresh accumulator that is drained into FP32 registers (round to nearest);
+// within a tile the two small correction products go in first and the
+// hi*hi products last, so the corrections are summed at their own magnitude
+// and each later add truncates no more than a hi*hi-only chain would.
 //
 // Warp roles (320 threads, one CTA per SM):
-//   warps 0-7   drain: double-buffered TMEM accumulators (2 x 256 columns =
-//               512 columns); warp w reads TMEM lanes 32 (w % 4) and
-//               columns 128 (w / 4) of each buffer
-//   warp 8      one lane issues the TMA loads of a 2-stage ring
+//   warps 0-7   workers: build the A operand of each stage, and drain the
+//               double-buffered TMEM accumulators (2 x 256 columns = 512
+//               columns); warp w reads TMEM lanes 32 (w % 4) and columns
+//               128 (w / 4) of each buffer
+//   warp 8      one lane issues the B-operand TMA loads of a 2-stage ring
 //   warp 9      one lane issues the MMAs of a tile when its stage is full
 //               and its accumulator buffer has been drained
 // The roles meet only at mbarriers; every wait is bounded and watches a CTA
@@ -57,6 +60,7 @@ namespace {
 
 constexpr int NT = 320;                 // threads per CTA (10 warps)
 constexpr int NDRAIN = 8;               // drain warps 0..7
+constexpr int NWORK = NDRAIN * 32;      // they also build the A operand
 constexpr int TMA_WARP = 8;
 constexpr int MMA_WARP = 9;
 constexpr int TM = 128;                 // MMA M
@@ -93,7 +97,7 @@ cta_setup (Sync &s)
     {
       for (int k = 0; k < STAGES; k++)
         {
-          umma::mbar_init (&s.full[k], 1);
+          umma::mbar_init (&s.full[k], 1 + NWORK);   // TMA lane + A builders
           umma::mbar_init (&s.empty[k], 1);
         }
       for (int b = 0; b < 2; b++)
@@ -110,15 +114,14 @@ cta_setup (Sync &s)
   umma::fence_after_sync ();
 }
 
-// the TMA lane: tile t (K values k0 + 32 t ..) into stage t % STAGES; A rows
-// from arow, B rows from brow, hi and lo planes of both
+// the TMA lane: the B operand (hi and lo planes, rows from brow) of tile t
+// (K values k0 + 32 t ..) into stage t % STAGES
 __device__ __forceinline__ void
-tma_role (Sync &s, unsigned char *smem, const CUtensorMap *ta, const CUtensorMap *tb, int arow,
-          int brow, int k0, int ntiles, uint32_t b_bytes)
+tma_role (Sync &s, unsigned char *smem, const CUtensorMap *tb, int brow, int k0, int ntiles,
+          uint32_t b_bytes)
 {
   volatile int *err = &s.err;
-  const uint32_t tx = 2 * A_BYTES + 2 * b_bytes;
-  umma::tma_prefetch_desc (ta);
+  const uint32_t tx = 2 * b_bytes;
   umma::tma_prefetch_desc (tb);
   int issued = 0;
   for (int t = 0; t < ntiles; t++)
@@ -130,8 +133,6 @@ tma_role (Sync &s, unsigned char *smem, const CUtensorMap *ta, const CUtensorMap
       unsigned char *sb = smem + (size_t) st * STAGE_BYTES;
       const int kx = k0 + KT * t;
       umma::mbar_expect_tx (&s.full[st], tx);
-      umma::tma_load_3d (sb, ta, kx, arow, 0, &s.full[st]);
-      umma::tma_load_3d (sb + A_BYTES, ta, kx, arow, 1, &s.full[st]);
       umma::tma_load_3d (sb + 2 * A_BYTES, tb, kx, brow, 0, &s.full[st]);
       umma::tma_load_3d (sb + 2 * A_BYTES + B_BYTES, tb, kx, brow, 1, &s.full[st]);
       issued = t + 1;
@@ -182,12 +183,66 @@ mma_role (Sync &s, const unsigned char *smem, uint32_t tmem, uint32_t idesc, int
   umma::mbar_wait_or_abort (&s.done, 0, WAIT_LIMIT, &never);
 }
 
-// drain warps: acc += each tile's accumulator
-__device__ __forceinline__ bool
-drain_role (Sync &s, uint32_t tmem, int ntiles, float acc[CPT])
+// a complex value as TF32 hi and lo parts (FP32 bit patterns)
+__device__ __forceinline__ void
+split2 (float2 v, float2 &hi, float2 &lo)
 {
-  const int warp = threadIdx.x >> 5;
+  uint32_t hx, lx, hy, ly;
+  umma::split_tf32 (v.x, hx, lx);
+  umma::split_tf32 (v.y, hy, ly);
+  hi = make_float2 (__uint_as_float (hx), __uint_as_float (hy));
+  lo = make_float2 (__uint_as_float (lx), __uint_as_float (ly));
+}
+
+// the A hi/lo planes of one stage: chunk c (16 bytes, two complex values) of
+// row `row` in the 128-byte swizzled layout the MMA descriptors expect
+__device__ __forceinline__ void
+put_a (unsigned char *stage, int row, int c, float2 v0, float2 v1)
+{
+  float2 h0, l0, h1, l1;
+  split2 (v0, h0, l0);
+  split2 (v1, h1, l1);
+  const uint32_t o = (uint32_t) row * 128u + ((uint32_t) (c ^ (row & 7)) << 4);
+  *reinterpret_cast<float4 *> (stage + o) = make_float4 (h0.x, h0.y, h1.x, h1.y);
+  *reinterpret_cast<float4 *> (stage + A_BYTES + o) = make_float4 (l0.x, l0.y, l1.x, l1.y);
+}
+
+// worker warps 0-7: build the A operand of every stage and drain the
+// accumulators.  Thread (row = tid % 128, half = tid / 128) builds complex
+// values 8 half .. 8 half + 7 of its A row in each tile (prod (t, k): value k
+// of the row in tile t).  Tiles 0 and 1 are built up front; once tile t's
+// accumulator is full its MMAs are done, so its stage takes tile t + 2,
+// built before tile t is drained (the MMA of tile t + 1 runs meanwhile).
+template <class Prod>
+__device__ __forceinline__ bool
+worker_role (Sync &s, unsigned char *smem, uint32_t tmem, int ntiles, float acc[CPT],
+             const Prod &prod)
+{
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & 127, half = tid >> 7;
   volatile int *err = &s.err;
+  auto build = [&] (int t) {
+    unsigned char *stage = smem + (size_t) (t % STAGES) * STAGE_BYTES;
+    // the eight phases first (their loads issue back to back), then the values
+    uint32_t ph[8];
+    bool ok[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) ph[k] = prod.phase (t, 8 * half + k, ok[k]);
+    // the inputs of this stage's next tile, into L1 ahead of its build
+    if (t + STAGES < ntiles) prod.prefetch (t + STAGES, 8 * half + (threadIdx.x & 7));
+    float2 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      {
+        v[k] = phase_of (prod.rot, ph[k]);
+        if (!ok[k]) v[k] = make_float2 (0.f, 0.f);
+      }
+#pragma unroll
+    for (int c = 0; c < 4; c++) put_a (stage, row, 4 * half + c, v[2 * c], v[2 * c + 1]);
+    umma::fence_async_smem ();      // generic writes -> the MMA's async reads
+    umma::mbar_arrive (&s.full[t % STAGES]);
+  };
+  for (int t = 0; t < STAGES && t < ntiles; t++) build (t);
   const uint32_t lane_base = (uint32_t) ((warp & 3) * 32) << 16;
   const uint32_t col = (uint32_t) ((warp >> 2) * CPT);
   for (int t = 0; t < ntiles; t++)
@@ -195,6 +250,7 @@ drain_role (Sync &s, uint32_t tmem, int ntiles, float acc[CPT])
       const int b = t & 1;
       if (!umma::mbar_wait_or_abort (&s.acc_full[b], (t >> 1) & 1, WAIT_LIMIT, err)) return false;
       umma::fence_after_sync ();
+      if (t + STAGES < ntiles) build (t + STAGES);
       const uint32_t dm = tmem + lane_base + (uint32_t) (b * TN) + col;
 #pragma unroll
       for (int cc = 0; cc < CPT; cc += 32)
@@ -215,6 +271,48 @@ drain_role (Sync &s, uint32_t tmem, int ntiles, float acc[CPT])
   return true;
 }
 
+// A of the forward GEMM: row r = (m2, m3), K = particles from j0.  phase():
+// the fixed-point phase of value k of tile t (the index is clamped so the
+// load is always in bounds; ok tells whether the value is a real entry)
+struct ProdF {
+  const uint4 *qpos;
+  const float4 *rot;
+  int np, j0;
+  uint32_t m2, m3;
+  bool live;
+  __device__ __forceinline__ uint32_t phase (int t, int k, bool &ok) const
+  {
+    const int j = j0 + PT * t + k;
+    ok = live && j < np;
+    const uint4 q = __ldg (qpos + min (j, np - 1));
+    return m2 * q.y + m3 * q.z;
+  }
+  __device__ __forceinline__ void prefetch (int t, int k) const
+  {
+    umma::prefetch_l1 (qpos + min (j0 + PT * t + k, np - 1));
+  }
+};
+
+// A of the backward GEMM: row = particle (fixed-point qy, qz), K = rows from r0
+struct ProdB {
+  const int2 *rowm;
+  const float4 *rot;
+  int R, r0;
+  uint32_t qy, qz;
+  bool live;
+  __device__ __forceinline__ uint32_t phase (int t, int k, bool &ok) const
+  {
+    const int r = r0 + PT * t + k;
+    ok = live && r < R;
+    const int2 mm = __ldg (rowm + min (r, R - 1));
+    return (uint32_t) mm.x * qy + (uint32_t) mm.y * qz;
+  }
+  __device__ __forceinline__ void prefetch (int t, int k) const
+  {
+    umma::prefetch_l1 (rowm + min (r0 + PT * t + k, R - 1));
+  }
+};
+
 // Once every tile is drained no load or MMA touches the stages any more, so
 // the drain threads park their accumulator rows there: H[row][column], row
 // stride HLD floats (odd, so a warp's 32 rows fall in distinct banks).
@@ -231,20 +329,21 @@ park (unsigned char *smem, const float acc[CPT])
   for (int u = 0; u < CPT; u++) H[u] = acc[u];
 }
 
-// forward drain threads: drain every tile, then column n = (m, re|im, q) of
-// row r goes to
+// forward worker threads: build and drain every tile, then column
+// n = (m, re|im, q) of row r goes to
 // Hs[((m C + q) 2 + re|im) TM + r], the order of the partial structure
 // factors sf[split][m1][q][re|im][r], so that each m1's block of rows is one
 // TMA store.  CB: the thread's first column (compile time, so the index
 // arithmetic folds away).
 template <int C, int CB>
 __device__ __forceinline__ void
-drain_park_sf (Sync &s, uint32_t tmem, int ntiles, unsigned char *smem, int ncol)
+drain_park_sf (Sync &s, uint32_t tmem, int ntiles, unsigned char *smem, int ncol,
+               const ProdF &prod)
 {
   float acc[CPT];
 #pragma unroll
   for (int u = 0; u < CPT; u++) acc[u] = 0.f;
-  if (!drain_role (s, tmem, ntiles, acc)) return;
+  if (!worker_role (s, smem, tmem, ntiles, acc, prod)) return;
   const int row = ((threadIdx.x >> 5) & 3) * 32 + (threadIdx.x & 31);
   float *Hs = reinterpret_cast<float *> (smem) + row;
 #pragma unroll
@@ -259,88 +358,16 @@ drain_park_sf (Sync &s, uint32_t tmem, int ntiles, unsigned char *smem, int ncol
   umma::fence_async_smem ();
 }
 
-// a complex value as TF32 hi and lo parts (FP32 bit patterns)
-__device__ __forceinline__ void
-split2 (float2 v, float2 &hi, float2 &lo)
-{
-  uint32_t hx, lx, hy, ly;
-  umma::split_tf32 (v.x, hx, lx);
-  umma::split_tf32 (v.y, hy, ly);
-  hi = make_float2 (__uint_as_float (hx), __uint_as_float (hy));
-  lo = make_float2 (__uint_as_float (lx), __uint_as_float (ly));
-}
 
 }  // namespace
-
-// ---------------------------------------------------------------------------
-// images TF[r][(j, a|b)] and TB[j][(r, a|b)] of T_r(j) = e^{2 pi i (m2 u_y(j)
-// + m3 u_z(j))}, straight from the fixed-point coordinates (m2 q_y + m3 q_z
-// mod 2^32 is the exact phase in turns x 2^32).  CTA: 32 rows x 32
-// particles; the tile passes through shared memory so that both images are
-// written with coalesced 8-byte stores.  Padding (particles np..ldT of TF,
-// rows R..Rk of TB) is written as zeros.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__ (256)
-k_tprep (KGemm g)
-{
-  __shared__ float2 s_t[32][33];
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int jb = blockIdx.x * 32, rb = blockIdx.y * 32;
-  const int np = g.t.np;
-  {
-    const int j = jb + tx;
-    uint32_t qy = 0, qz = 0;
-    const bool live = j < np;
-    if (live)
-      {
-        const uint4 q = g.t.qpos[j];
-        qy = q.y;
-        qz = q.z;
-      }
-#pragma unroll
-    for (int k = 0; k < 4; k++)
-      {
-        const int rl = ty + 8 * k, r = rb + rl;
-        float2 v = make_float2 (0.f, 0.f);
-        if (live && r < g.R)
-          {
-            const int2 mm = g.rowm[r];
-            v = phase_of (g.t.rot, (uint32_t) mm.x * qy + (uint32_t) mm.y * qz);
-          }
-        s_t[rl][tx] = v;
-        if (r < g.R && j < g.ldT)
-          {
-            float2 hi, lo;
-            split2 (v, hi, lo);
-            float2 *o = reinterpret_cast<float2 *> (g.TF + (size_t) r * g.KF) + j;
-            o[0] = hi;
-            o[g.pTF / 2] = lo;
-          }
-      }
-  }
-  __syncthreads ();
-  const int r = rb + tx;
-  if (r >= g.Rk) return;
-#pragma unroll
-  for (int k = 0; k < 4; k++)
-    {
-      const int jl = ty + 8 * k, j = jb + jl;
-      if (j >= np) break;
-      float2 hi, lo;
-      split2 (s_t[tx][jl], hi, lo);
-      float2 *o = reinterpret_cast<float2 *> (g.TB + (size_t) j * g.KB) + r;
-      o[0] = hi;
-      o[g.pTB / 2] = lo;
-    }
-}
 
 // ---------------------------------------------------------------------------
 // forward: partial structure factors of one (row tile, m1 tile, particle slice)
 // ---------------------------------------------------------------------------
 template <int V>
 __global__ void __launch_bounds__ (NT, 1)
-k_sfac_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-             const __grid_constant__ CUtensorMap tmS, KGemm g, int *status)
+k_sfac_gemm (const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmS,
+             KGemm g, int *status)
 {
   constexpr int C = NComp<V>::value;
   extern __shared__ unsigned char dsm[];
@@ -360,7 +387,7 @@ k_sfac_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
   if (warp == TMA_WARP)
     {
       if (lane == 0)
-        tma_role (s, smem, &tmA, &tmB, r0, m1b * 2 * C, 2 * jb, ntiles, (uint32_t) g.nf * KT * 4);
+        tma_role (s, smem, &tmB, m1b * 2 * C, 2 * jb, ntiles, (uint32_t) g.nf * KT * 4);
       __syncwarp ();
     }
   else if (warp == MMA_WARP)
@@ -370,8 +397,19 @@ k_sfac_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     }
   else
     {
-      if (warp >> 2) drain_park_sf<C, CPT> (s, tmem, ntiles, smem, ncol);
-      else drain_park_sf<C, 0> (s, tmem, ntiles, smem, ncol);
+      // A rows: r = (m2, m3), values T_r(j) over the slice's particles
+      ProdF prod;
+      const int r = r0 + (tid & 127);
+      prod.qpos = g.t.qpos;
+      prod.rot = g.t.rot;
+      prod.np = g.t.np;
+      prod.j0 = jb;
+      prod.live = r < g.R;
+      const int2 mm = prod.live ? g.rowm[r] : make_int2 (0, 0);
+      prod.m2 = (uint32_t) mm.x;
+      prod.m3 = (uint32_t) mm.y;
+      if (warp >> 2) drain_park_sf<C, CPT> (s, tmem, ntiles, smem, ncol, prod);
+      else drain_park_sf<C, 0> (s, tmem, ntiles, smem, ncol, prod);
     }
   __syncthreads ();
   if (!s.err && tid == 0)
@@ -491,8 +529,7 @@ k_kop (KGemm g, const MixK *kt, int nk, const float *sf)
 // ---------------------------------------------------------------------------
 template <int V>
 __global__ void __launch_bounds__ (NT, 1)
-k_bp_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-           KGemm g, float *ypart, int *status)
+k_bp_gemm (const __grid_constant__ CUtensorMap tmB, KGemm g, float *ypart, int *status)
 {
   constexpr int C = NComp<V>::value;
   extern __shared__ unsigned char dsm[];
@@ -514,7 +551,7 @@ k_bp_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
   if (warp == TMA_WARP)
     {
       if (lane == 0)
-        tma_role (s, smem, &tmA, &tmB, i0, m1b * 2 * C, 2 * rb, ntiles, (uint32_t) g.nb * KT * 4);
+        tma_role (s, smem, &tmB, m1b * 2 * C, 2 * rb, ntiles, (uint32_t) g.nb * KT * 4);
       __syncwarp ();
     }
   else if (warp == MMA_WARP)
@@ -524,10 +561,21 @@ k_bp_gemm (const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     }
   else
     {
+      // A rows: particle i, values T_r(i) over the slice's rows r
+      ProdB prod;
+      const int i = i0 + (tid & 127);
+      prod.rowm = g.rowm;
+      prod.rot = g.t.rot;
+      prod.R = g.R;
+      prod.r0 = rb;
+      prod.live = i < np;
+      const uint4 q = prod.live ? g.t.qpos[i] : make_uint4 (0u, 0u, 0u, 0u);
+      prod.qy = q.y;
+      prod.qz = q.z;
       float acc[CPT];
 #pragma unroll
       for (int u = 0; u < CPT; u++) acc[u] = 0.f;
-      if (drain_role (s, tmem, ntiles, acc)) park (smem, acc);
+      if (worker_role (s, smem, tmem, ntiles, acc, prod)) park (smem, acc);
     }
   __syncthreads ();
   if (tid == 0 && s.err) atomicExch (status, 1);
@@ -604,8 +652,6 @@ kgemm_plan (int version, PhaseTables t, const int2 *rowm, int R)
   if (kss < 1) kss = 1;
   g.rper = ((R + kss - 1) / kss + PT - 1) / PT * PT;
   g.ksplit = R > 0 ? (R + g.rper - 1) / g.rper : 1;
-  g.pTF = (size_t) R * g.KF;
-  g.pTB = (size_t) t.np * g.KB;
   g.pZF = (size_t) g.NZ * g.KF;
   g.pWB = (size_t) g.NZ * g.KB;
   return g;
@@ -622,8 +668,6 @@ kgemm_sf_floats (const KGemm &g)
 {
   return (size_t) g.nsplit * g.n1 * g.c * 2 * (size_t) g.Rp;
 }
-size_t kgemm_tf_floats (const KGemm &g) { return 2 * g.pTF; }
-size_t kgemm_tb_floats (const KGemm &g) { return 2 * g.pTB; }
 size_t kgemm_zf_floats (const KGemm &g) { return 2 * g.pZF; }
 size_t kgemm_wb_floats (const KGemm &g) { return 2 * g.pWB; }
 int kgemm_ypart_chunks (const KGemm &g) { return g.ksplit * g.ntile_b; }
@@ -632,9 +676,7 @@ size_t kgemm_ypart_floats (const KGemm &g) { return (size_t) kgemm_ypart_chunks 
 int
 kgemm_maps (const KGemm &g, float *sf, KMaps *m)
 {
-  int e = encode_planes_sw128 (&m->tf, g.TF, 2, (unsigned long long) g.R, g.KF, TM);
-  if (!e) e = encode_planes_sw128 (&m->zf, g.ZF, 2, (unsigned long long) g.NZ, g.KF, g.nf);
-  if (!e) e = encode_planes_sw128 (&m->tb, g.TB, 2, (unsigned long long) g.t.np, g.KB, TM);
+  int e = encode_planes_sw128 (&m->zf, g.ZF, 2, (unsigned long long) g.NZ, g.KF, g.nf);
   if (!e) e = encode_planes_sw128 (&m->wb, g.WB, 2, (unsigned long long) g.NZ, g.KB, g.nb);
   if (!e)
     e = encode_rows_plain (&m->sf, sf, (unsigned long long) g.nsplit * g.n1 * g.c * 2, g.Rp, TM,
@@ -663,13 +705,11 @@ launch_v (const KGemm &g, const KMaps &mp, const MixK *kt, int nk, const float *
         return e;
       attr_dev = dev;
     }
-  k_tprep<<<dim3 ((g.ldT + 31) / 32, (g.Rk + 31) / 32), 256, 0, st>>> (g);
-  kmark (prof, st, "k_tprep");
-  k_sfac_gemm<V><<<dim3 (g.nrt, g.ntile_f, g.nsplit), NT, SMEM_DYN, st>>> (mp.tf, mp.zf, mp.sf, g, status);
+  k_sfac_gemm<V><<<dim3 (g.nrt, g.ntile_f, g.nsplit), NT, SMEM_DYN, st>>> (mp.zf, mp.sf, g, status);
   kmark (prof, st, "k_sfac_gemm");
   k_kop<V><<<(nk + KOP_K - 1) / KOP_K, KOP_K * KOP_G, 0, st>>> (g, kt, nk, sf);
   kmark (prof, st, "k_kop");
-  k_bp_gemm<V><<<dim3 (g.mtiles, g.ntile_b, g.ksplit), NT, SMEM_DYN, st>>> (mp.tb, mp.wb, g, ypart, status);
+  k_bp_gemm<V><<<dim3 (g.mtiles, g.ntile_b, g.ksplit), NT, SMEM_DYN, st>>> (mp.wb, g, ypart, status);
   kmark (prof, st, "k_bp_gemm");
   return cudaGetLastError ();
 }

@@ -44,7 +44,7 @@ struct MixedState {
   double selfc[3] = {0, 0, 0};
   std::vector<MixK> h_k;
   DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf, status, sf, rowm, rot;
-  DevBuf img_tf, img_tb, img_zf, img_wb;   // GEMM operand images (kspace_tc.cu)
+  DevBuf img_zf, img_wb;        // GEMM B-operand images (kspace_tc.cu)
   KMaps maps;
   uint64_t img_key = 0;         // buffers and plan the maps and zeroed pads belong to
   // the real-space kernel runs on this side stream, concurrently with the
@@ -774,12 +774,8 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   if (m->tensor)
     {
       if ((e = m->sf.ensure (sizeof (float) * kgemm_sf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "structure factors");
-      if ((e = m->img_tf.ensure (sizeof (float) * kgemm_tf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image TF");
-      if ((e = m->img_tb.ensure (sizeof (float) * kgemm_tb_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image TB");
       if ((e = m->img_zf.ensure (sizeof (float) * kgemm_zf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image ZF");
       if ((e = m->img_wb.ensure (sizeof (float) * kgemm_wb_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image WB");
-      m->plan.TF = (float *) m->img_tf.p;
-      m->plan.TB = (float *) m->img_tb.p;
       m->plan.ZF = (float *) m->img_zf.p;
       m->plan.WB = (float *) m->img_wb.p;
     }
@@ -824,8 +820,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       // stay zero; zeroed, and the TMA maps encoded, when the split or the
       // buffers change
       uint64_t key = m->fp * 1000003ull;
-      for (const void *p : {(const void *) m->img_tf.p, (const void *) m->img_tb.p,
-                            (const void *) m->img_zf.p, (const void *) m->img_wb.p,
+      for (const void *p : {(const void *) m->img_zf.p, (const void *) m->img_wb.p,
                             (const void *) m->sf.p})
         key = (key ^ (uint64_t) (uintptr_t) p) * 1099511628211ull;
       if (key != m->img_key)
@@ -950,7 +945,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     cudaMemcpyAsync (m->h_status, m->status.p, sizeof (int), cudaMemcpyDeviceToHost, st);
   e = cudaGetLastError ();
   if (e != cudaSuccess) return cuda_fail (e, "mixed kernels");
-  c->launches = m->nkh == 0 ? 3 : (m->tensor ? 7 : 5);
+  c->launches = m->nkh == 0 ? 3 : (m->tensor ? 6 : 5);
   c->timed = timed;
   return STOKES_GPU_OK;
 }
@@ -967,8 +962,8 @@ release_mixed (Ctx *c)
   if (!c->mixed) return;
   MixedState *m = c->mixed;
   for (DevBuf *b : {&m->kt, &m->qpos, &m->tab, &m->xf, &m->pq, &m->part_real, &m->part_rec,
-                    &m->selfbuf, &m->status, &m->sf, &m->rowm, &m->rot, &m->img_tf,
-                    &m->img_tb, &m->img_zf, &m->img_wb})
+                    &m->selfbuf, &m->status, &m->sf, &m->rowm, &m->rot, &m->img_zf,
+                    &m->img_wb})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
   if (m->side) cudaStreamDestroy (m->side);

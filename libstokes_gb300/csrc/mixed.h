@@ -52,14 +52,52 @@ phase_of (const float4 *rot, uint32_t p)
   return make_float2 (re, im);
 }
 
+// e^{2 pi i p / 2^32} without a table: the nearest quarter turn q (exact:
+// a swap and sign change) and sin, cos of the remaining angle |x| <= pi / 4
+// by their Taylor series to x^11 and x^12 in nested (Horner) form; x is
+// formed from the exact integer remainder with a two-part 2 pi / 2^32.  The
+// truncation errors are below 1e-11; FP32 rounding leaves about 1e-7 at most
+// (8.5e-8 measured over 3e6 random phases, 2e-8 on average).  No memory
+// access, so it suits kernels whose lanes would otherwise gather from a table.
+__device__ __forceinline__ float2
+phase_poly (uint32_t p)
+{
+  const uint32_t q = (p + (1u << 29)) >> 30;             // nearest quarter turn
+  const int32_t r = (int32_t) (p - (q << 30));           // |r| <= 2^29
+  const float ch = 1.4629180792671596e-09f;               // 2 pi / 2^32 = ch + cl
+  const float cl = -4.0709404e-17f;
+  const float rh = (float) (r & ~0xFF), rl = (float) (r & 0xFF);
+  const float x = fmaf (rh, ch, fmaf (rl, ch, rh * cl));
+  const float x2 = x * x;
+  float sn = fmaf (-x2, 1.0f / 110.0f, 1.0f);
+  sn = fmaf (-x2 * (1.0f / 72.0f), sn, 1.0f);
+  sn = fmaf (-x2 * (1.0f / 42.0f), sn, 1.0f);
+  sn = fmaf (-x2 * (1.0f / 20.0f), sn, 1.0f);
+  sn = fmaf (-x2 * (1.0f / 6.0f), sn, 1.0f);
+  sn *= x;
+  float cs = fmaf (-x2, 1.0f / 132.0f, 1.0f);
+  cs = fmaf (-x2 * (1.0f / 90.0f), cs, 1.0f);
+  cs = fmaf (-x2 * (1.0f / 56.0f), cs, 1.0f);
+  cs = fmaf (-x2 * (1.0f / 30.0f), cs, 1.0f);
+  cs = fmaf (-x2 * (1.0f / 12.0f), cs, 1.0f);
+  cs = fmaf (-x2 * 0.5f, cs, 1.0f);
+  switch (q & 3u)
+    {
+    case 0: return make_float2 (cs, sn);
+    case 1: return make_float2 (-sn, cs);
+    case 2: return make_float2 (-cs, -sn);
+    default: return make_float2 (sn, -cs);
+    }
+}
+
 // plan of the separable tensor-core reciprocal sum (kspace_tc.cu).  The k
 // vectors of the list are (m1, row) with row = one (m2, m3) combination that
-// occurs in it; R rows, n1 = M0 + 1 values of m1.  The GEMM operands are
-// images [2 planes: TF32 hi, lo][rows][K] in FP32 (K contiguous):
-//   TF [R][KF]   T_r(j) as (Re, Im) pairs over the particles j < ldT
+// occurs in it; R rows, n1 = M0 + 1 values of m1.  The B operands of the
+// GEMMs are images [2 planes: TF32 hi, lo][rows][K] in FP32 (K contiguous):
 //   ZF [NZ][KF]  rows (m1, re|im, q): t0[m1](j) x_q(j) in the forward sign pattern
-//   TB [np][KB]  T_r(j) as (Re, Im) pairs over the rows r < Rk
 //   WB [NZ][KB]  rows (m1, re|im, q): the k operators W in the backward pattern
+// The A operands (the row phases T_r(j)) are built in shared memory by the
+// GEMM kernels themselves.
 struct KGemm {
   PhaseTables t;
   const int2 *rowm;       // (m2, m3) of each row, R entries
@@ -74,29 +112,27 @@ struct KGemm {
   int rper, ksplit;       // rows per backward K slice, number of slices
   int ldT;                // particles padded to a multiple of 16
   int KF, KB, NZ;         // K extents (floats) of the images, rows of ZF and WB
-  float *TF, *TB, *ZF, *WB;
-  size_t pTF, pTB, pZF, pWB;   // plane strides (floats)
+  float *ZF, *WB;
+  size_t pZF, pWB;        // plane strides (floats)
 };
 
-// TMA descriptors of the four images (128-byte swizzled boxes of 32 K values)
+// TMA descriptors of the two images (128-byte swizzled boxes of 32 K values)
 // and of the forward partials sf (boxes of 128 rows x one m1's columns)
 struct KMaps {
-  CUtensorMap tf, zf, tb, wb, sf;
+  CUtensorMap zf, wb, sf;
 };
 
 KGemm kgemm_plan (int version, PhaseTables t, const int2 *rowm, int R);
 bool kgemm_fits (const KGemm &g);
 size_t kgemm_sf_floats (const KGemm &g);      // partial structure factors
-size_t kgemm_tf_floats (const KGemm &g);      // image sizes, both planes
-size_t kgemm_tb_floats (const KGemm &g);
-size_t kgemm_zf_floats (const KGemm &g);
+size_t kgemm_zf_floats (const KGemm &g);      // image sizes, both planes
 size_t kgemm_wb_floats (const KGemm &g);
 size_t kgemm_ypart_floats (const KGemm &g);   // partial y, [ksplit][ntile_b][np][c]
 int kgemm_ypart_chunks (const KGemm &g);       // ksplit * ntile_b
 int kgemm_maps (const KGemm &g, float *sf, KMaps *m);   // 0 on success
 
-// images TF, TB -> forward GEMM -> per-k operators (image WB) -> backward
-// GEMM into ypart; the image ZF is written beforehand by mk_prep
+// forward GEMM -> per-k operators (image WB) -> backward GEMM into ypart;
+// the image ZF is written beforehand by mk_prep
 struct Ctx;
 cudaError_t launch_kspace_gemm (int version, const KGemm &g, const KMaps &maps, const MixK *kt,
                                 int nk, float *sf, float *ypart, int *status, cudaStream_t st,

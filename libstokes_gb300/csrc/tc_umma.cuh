@@ -82,12 +82,30 @@ to_tf32 (float x)
   return r;
 }
 
-// x = hi + lo with hi, lo representable in TF32 (the 3xTF32 split)
+// TF32 rounding of an FP32 bit pattern, to nearest with ties away from zero
+// (the rounding of cvt.rna.tf32.f32): add half a TF32 unit to the magnitude
+// bits and clear the 13 bits below TF32's mantissa; a carry moves into the
+// exponent as it should.  Finite inputs.
+__device__ __forceinline__ uint32_t
+rna_tf32_bits (uint32_t u)
+{
+  return (u + 0x1000u) & 0xFFFFE000u;
+}
+
+// x = hi + lo with hi, lo representable in TF32 (the 3xTF32 split), in
+// integer and FP32 arithmetic
 __device__ __forceinline__ void
 split_tf32 (float x, uint32_t &hi, uint32_t &lo)
 {
-  hi = to_tf32 (x);
-  lo = to_tf32 (x - __uint_as_float (hi));
+  hi = rna_tf32_bits (__float_as_uint (x));
+  lo = rna_tf32_bits (__float_as_uint (x - __uint_as_float (hi)));
+}
+
+// an L1 prefetch of the line holding p (no register result)
+__device__ __forceinline__ void
+prefetch_l1 (const void *p)
+{
+  asm volatile ("prefetch.global.L1 [%0];" :: "l"(p));
 }
 
 // TMEM allocation by one full warp; the column address lands in *slot
