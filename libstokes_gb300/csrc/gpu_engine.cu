@@ -92,8 +92,18 @@ static std::unordered_map<const void *, Ctx *> g_ctx;
 static uint64_t
 fnv (const void *data, size_t n, uint64_t h = 1469598103934665603ull)
 {
+  // FNV-1a over 8-byte words (the tail byte-wise): a change detector for
+  // host tables, so word granularity is enough and 8x cheaper
   const unsigned char *b = (const unsigned char *) data;
-  for (size_t q = 0; q < n; q++) { h ^= b[q]; h *= 1099511628211ull; }
+  size_t q = 0;
+  for (; q + 8 <= n; q += 8)
+    {
+      uint64_t w;
+      memcpy (&w, b + q, 8);
+      h ^= w;
+      h *= 1099511628211ull;
+    }
+  for (; q < n; q++) { h ^= b[q]; h *= 1099511628211ull; }
   return h;
 }
 
@@ -308,7 +318,9 @@ prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
   if (tables < 0) tables = c->precision == STOKES_GPU_MIXED ? 0 : 1;
   if (!tables)
     {
-      // the particle table only (radii for the BD interactions)
+      // the particle table only (radii for the BD interactions); equal
+      // spheres without slip need none
+      if (c->mode == MODE_MONO) return STOKES_GPU_OK;
       build_particles (sys, c->mode, c->h_pp);
       return upload_if_changed (c->pp, c->fp_pp, c->h_pp.data (), sizeof (double) * c->h_pp.size (),
                                 c->stream, "particle table");

@@ -35,6 +35,12 @@ extern "C" void lsg_ewald_cutoffs (double xi, double eps, double lmin, double lm
 
 namespace lsg {
 
+static int
+cuda_ok (cudaError_t e, const char *what)
+{
+  return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, what);
+}
+
 struct MixedState {
   uint64_t fp = 0;
   double xi = 0, rc = 0, kc = 0, eta = 0, eps = 0;
@@ -51,6 +57,9 @@ struct MixedState {
   // reciprocal chain (low priority: it fills the SMs the chain leaves idle)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // the recorded launch sequence (run_mixed_sequence)
+  cudaGraphExec_t gexec = nullptr;
+  uint64_t gkey = 0, gcand = 0;
   int nrow = 0;          // (m2, m3) rows of the tensor-core contraction
   int *h_status = nullptr;      // pinned copy of the kernels' status word
   bool tensor = true;           // reciprocal space on the tensor cores
@@ -710,6 +719,82 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
   return STOKES_GPU_OK;
 }
 
+// Runs `sequence` (the launches of one mixed product on st) directly, or as
+// a CUDA graph: the first call with a new configuration launches directly,
+// the second records the sequence into a graph (stream capture), later calls
+// replay it with one launch.  The configuration key covers the split, every
+// buffer and the caller's pointers, which the recorded kernels hold.  Timed
+// or per-kernel-profiled products, products issued while the caller's
+// stream is itself being captured, and LIBSTOKES_GB300_GRAPHS=0 launch
+// directly.
+template <class Seq>
+static int
+run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_x, double *d_y,
+                    cudaStream_t st, bool timed, Seq &sequence)
+{
+  static const bool enabled = [] {
+    const char *g = getenv ("LIBSTOKES_GB300_GRAPHS");
+    return !(g && strcmp (g, "0") == 0);
+  }();
+  bool use = enabled && !timed && !c->kprof_on;
+  if (use)
+    {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing (st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+        use = false;
+    }
+  if (!use) return sequence ();
+  uint64_t key = 1469598103934665603ull;
+  auto mix = [&] (uint64_t v) { key = (key ^ v) * 1099511628211ull; };
+  mix (m->fp);
+  mix (m->img_key);
+  mix ((uint64_t) m->tensor);
+  mix ((uint64_t) m->nchunk_r);
+  mix ((uint64_t) m->nchunk_k);
+  const void *ptrs[] = {d_pos, d_x, d_y, m->kt.p, m->qpos.p, m->tab.p, m->xf.p, m->pq.p,
+                        m->part_real.p, m->part_rec.p, m->selfbuf.p, m->status.p, m->sf.p,
+                        m->rowm.p, m->rot.p, m->img_zf.p, m->img_wb.p, m->h_status};
+  for (const void *p : ptrs) mix ((uint64_t) (uintptr_t) p);
+  if (m->gexec && key == m->gkey) return cuda_ok (cudaGraphLaunch (m->gexec, st), "mixed product graph");
+  if (key != m->gcand)
+    {
+      m->gcand = key;
+      return sequence ();
+    }
+  // second call with this configuration: record it
+  if (m->gexec)
+    {
+      cudaGraphExecDestroy (m->gexec);
+      m->gexec = nullptr;
+    }
+  cudaError_t e = cudaStreamBeginCapture (st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return sequence ();
+  const int rc = sequence ();
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture (st, &g);
+  if (rc)
+    {
+      if (g) cudaGraphDestroy (g);
+      return rc;
+    }
+  if (e != cudaSuccess || !g)
+    {
+      if (g) cudaGraphDestroy (g);
+      cudaGetLastError ();
+      return sequence ();           // not recorded: launch directly
+    }
+  e = cudaGraphInstantiate (&m->gexec, g, 0);
+  cudaGraphDestroy (g);
+  if (e != cudaSuccess)
+    {
+      m->gexec = nullptr;
+      cudaGetLastError ();
+      return sequence ();
+    }
+  m->gkey = key;
+  return cuda_ok (cudaGraphLaunch (m->gexec, st), "mixed product graph");
+}
+
 int
 atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                   cudaStream_t st, bool timed)
@@ -731,7 +816,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                  (const uint4 *) m->qpos.p, (const float4 *) m->rot.p};
   {
     // reciprocal space on the tensor cores unless LIBSTOKES_GB300_KSPACE=simt
-    const char *ks = getenv ("LIBSTOKES_GB300_KSPACE");
+    const char *ks = getenv ("LIBSTOKES_GB300_KSPACE");   // read per call: tests switch it
     m->plan = kgemm_plan (c->version, pt, (const int2 *) m->rowm.p, m->nrow);
     m->tensor = !(ks && strcmp (ks, "simt") == 0) && m->nkh > 0 && kgemm_fits (m->plan);
   }
@@ -836,115 +921,122 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     }
 
   cudaEvent_t *E = phase_events (c, timed);
-  if (E) cudaEventRecord (E[0], st);
-  kmark (c, st, nullptr);
-  PrepArgs pa;
-  pa.pos = d_pos; pa.x = d_x; pa.np = np; pa.c = C;
-  {
+  // the launch sequence of one product (kernels, copies and stream events);
+  // recorded into a CUDA graph once the same configuration repeats
+  auto sequence = [&] () -> int {
+    if (E) cudaEventRecord (E[0], st);
+    kmark (c, st, nullptr);
+    PrepArgs pa;
+    pa.pos = d_pos; pa.x = d_x; pa.np = np; pa.c = C;
+    {
+      const double two32 = 4294967296.0;
+      pa.sx = two32 / sys->lx; pa.sy = two32 / sys->ly; pa.sz = two32 / sys->lz;
+    }
+    pa.shift = sys->shear_shift;
+    pa.sl = sys->shear_shift / sys->lx;
+    pa.shear_mode = sys->shear_mode;
+    pa.ntab = ntab;
+    pa.m0end = m->M[0] + 1;
+    pa.m1end = m->M[0] + m->M[1] + 2;
+    pa.rot = (const float4 *) m->rot.p;
+    pa.qpos = (uint32_t *) m->qpos.p; pa.tab = (float2 *) m->tab.p; pa.xf = (float *) m->xf.p;
+    pa.zf = m->tensor ? m->plan.ZF : nullptr;
+    pa.zplane = m->plan.pZF;
+    pa.kf = m->plan.KF;
+    mk_prep<<<dim3 ((np + PREP_P - 1) / PREP_P, (ntab + PREP_ROWS - 1) / PREP_ROWS), 128, 0, st>>> (pa);
+    kmark (c, st, "mk_prep");
+
+    RealMixArgs ra;
+    ra.qpos = (const uint32_t *) m->qpos.p; ra.xf = (const float *) m->xf.p;
+    ra.np = np; ra.nchunk = m->nchunk_r;
     const double two32 = 4294967296.0;
-    pa.sx = two32 / sys->lx; pa.sy = two32 / sys->ly; pa.sz = two32 / sys->lz;
-  }
-  pa.shift = sys->shear_shift;
-  pa.sl = sys->shear_shift / sys->lx;
-  pa.shear_mode = sys->shear_mode;
-  pa.ntab = ntab;
-  pa.m0end = m->M[0] + 1;
-  pa.m1end = m->M[0] + m->M[1] + 2;
-  pa.rot = (const float4 *) m->rot.p;
-  pa.qpos = (uint32_t *) m->qpos.p; pa.tab = (float2 *) m->tab.p; pa.xf = (float *) m->xf.p;
-  pa.zf = m->tensor ? m->plan.ZF : nullptr;
-  pa.zplane = m->plan.pZF;
-  pa.kf = m->plan.KF;
-  mk_prep<<<dim3 ((np + PREP_P - 1) / PREP_P, (ntab + PREP_ROWS - 1) / PREP_ROWS), 128, 0, st>>> (pa);
-  kmark (c, st, "mk_prep");
+    ra.scale[0] = (float) (sys->lx / two32);
+    ra.scale[1] = (float) (sys->ly / two32);
+    ra.scale[2] = (float) (sys->lz / two32);
+    ra.shear_mode = sys->shear_mode;
+    {
+      double sq = sys->shear_shift / sys->lx * two32;
+      long long iq = llround (sq);
+      ra.shift_q = (uint32_t) (iq & 0xffffffffll);
+    }
+    ra.rc2 = (float) (m->rc * m->rc);
+    ra.rmin = (float) sys->rmin;
+    ra.xi = (float) m->xi;
+    ra.xisp = (float) (m->xi / sqrt (M_PI));
+    ra.rad = nullptr; ra.slipa = nullptr;
+    ra.partial = (float *) m->part_real.p;
+    const int gr = (int) (((long long) np * m->nchunk_r + MX_WARPS - 1) / MX_WARPS);
+    // concurrent with the reciprocal chain unless the launches are being
+    // timed one by one (then in order: reciprocal, real, combine)
+    const bool overlap = !E && !c->kprof_on && m->side;
+    auto launch_real = [&] (cudaStream_t rs) {
+      if (c->version == 0) mk_real<0, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
+      else if (c->version == 1) mk_real<1, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
+      else mk_real<2, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
+    };
+    if (overlap)
+      {
+        cudaEventRecord (m->ev_fork, st);
+        cudaStreamWaitEvent (m->side, m->ev_fork, 0);
+        launch_real (m->side);
+        cudaEventRecord (m->ev_join, m->side);
+      }
 
-  RealMixArgs ra;
-  ra.qpos = (const uint32_t *) m->qpos.p; ra.xf = (const float *) m->xf.p;
-  ra.np = np; ra.nchunk = m->nchunk_r;
-  const double two32 = 4294967296.0;
-  ra.scale[0] = (float) (sys->lx / two32);
-  ra.scale[1] = (float) (sys->ly / two32);
-  ra.scale[2] = (float) (sys->lz / two32);
-  ra.shear_mode = sys->shear_mode;
-  {
-    double sq = sys->shear_shift / sys->lx * two32;
-    long long iq = llround (sq);
-    ra.shift_q = (uint32_t) (iq & 0xffffffffll);
-  }
-  ra.rc2 = (float) (m->rc * m->rc);
-  ra.rmin = (float) sys->rmin;
-  ra.xi = (float) m->xi;
-  ra.xisp = (float) (m->xi / sqrt (M_PI));
-  ra.rad = nullptr; ra.slipa = nullptr;
-  ra.partial = (float *) m->part_real.p;
-  const int gr = (int) (((long long) np * m->nchunk_r + MX_WARPS - 1) / MX_WARPS);
-  // concurrent with the reciprocal chain unless the launches are being
-  // timed one by one (then in order: reciprocal, real, combine)
-  const bool overlap = !E && !c->kprof_on && m->side;
-  auto launch_real = [&] (cudaStream_t rs) {
-    if (c->version == 0) mk_real<0, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
-    else if (c->version == 1) mk_real<1, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
-    else mk_real<2, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
+    KMixArgs ka;
+    ka.kt = (const MixK *) m->kt.p; ka.tab = (const float2 *) m->tab.p;
+    ka.xf = (const float *) m->xf.p; ka.np = np; ka.nkh = m->nkh;
+    ka.off1 = off1; ka.off2 = off2; ka.pq = (float *) m->pq.p;
+    BpMixArgs ba;
+    ba.kt = ka.kt; ba.tab = ka.tab; ba.pq = ka.pq; ba.np = np; ba.nkh = m->nkh;
+    ba.nchunk = m->nchunk_k; ba.M0 = m->M[0]; ba.M1 = m->M[1]; ba.M2 = m->M[2];
+    ba.off1 = off1; ba.off2 = off2; ba.partial = (float *) m->part_rec.p;
+    const int gk = (m->nkh + MX_WARPS - 1) / MX_WARPS;
+    const int gb = (int) (((long long) np * m->nchunk_k + MX_WARPS - 1) / MX_WARPS);
+    if (m->nkh > 0 && m->tensor)
+      {
+        if ((e = launch_kspace_gemm (c->version, m->plan, m->maps, ka.kt, m->nkh, (float *) m->sf.p,
+                                     (float *) m->part_rec.p, (int *) m->status.p, st, c))
+            != cudaSuccess)
+          return cuda_fail (e, "reciprocal space (tensor cores)");
+      }
+    else if (m->nkh > 0)
+      {
+        if (c->version == 0) mk_sfac<0><<<gk, MX_WARPS * 32, 0, st>>> (ka);
+        else if (c->version == 1) mk_sfac<1><<<gk, MX_WARPS * 32, 0, st>>> (ka);
+        else mk_sfac<2><<<gk, MX_WARPS * 32, 0, st>>> (ka);
+        kmark (c, st, "mk_sfac");
+        if (c->version == 0) mk_backproj<0><<<gb, MX_WARPS * 32, 0, st>>> (ba);
+        else if (c->version == 1) mk_backproj<1><<<gb, MX_WARPS * 32, 0, st>>> (ba);
+        else mk_backproj<2><<<gb, MX_WARPS * 32, 0, st>>> (ba);
+        kmark (c, st, "mk_backproj");
+      }
+    else
+      cudaMemsetAsync (m->part_rec.p, 0, sizeof (float) * (size_t) m->nchunk_k * np * C, st);
+    if (E) cudaEventRecord (E[1], st);
+    if (overlap)
+      cudaStreamWaitEvent (st, m->ev_join, 0);
+    else
+      {
+        launch_real (st);
+        kmark (c, st, "mk_real");
+      }
+    if (E) cudaEventRecord (E[2], st);
+
+    const double *selfm = (const double *) m->selfbuf.p;
+    const int gc = (np * C + 63) / 64;
+    if (c->version == 0) mk_combine<0><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
+    else if (c->version == 1) mk_combine<1><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
+    else mk_combine<2><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
+    kmark (c, st, "mk_combine");
+    if (E) cudaEventRecord (E[3], st);
+    if (m->tensor)
+      cudaMemcpyAsync (m->h_status, m->status.p, sizeof (int), cudaMemcpyDeviceToHost, st);
+    e = cudaGetLastError ();
+    if (e != cudaSuccess) return cuda_fail (e, "mixed kernels");
+    return STOKES_GPU_OK;
   };
-  if (overlap)
-    {
-      cudaEventRecord (m->ev_fork, st);
-      cudaStreamWaitEvent (m->side, m->ev_fork, 0);
-      launch_real (m->side);
-      cudaEventRecord (m->ev_join, m->side);
-    }
-
-  KMixArgs ka;
-  ka.kt = (const MixK *) m->kt.p; ka.tab = (const float2 *) m->tab.p;
-  ka.xf = (const float *) m->xf.p; ka.np = np; ka.nkh = m->nkh;
-  ka.off1 = off1; ka.off2 = off2; ka.pq = (float *) m->pq.p;
-  BpMixArgs ba;
-  ba.kt = ka.kt; ba.tab = ka.tab; ba.pq = ka.pq; ba.np = np; ba.nkh = m->nkh;
-  ba.nchunk = m->nchunk_k; ba.M0 = m->M[0]; ba.M1 = m->M[1]; ba.M2 = m->M[2];
-  ba.off1 = off1; ba.off2 = off2; ba.partial = (float *) m->part_rec.p;
-  const int gk = (m->nkh + MX_WARPS - 1) / MX_WARPS;
-  const int gb = (int) (((long long) np * m->nchunk_k + MX_WARPS - 1) / MX_WARPS);
-  if (m->nkh > 0 && m->tensor)
-    {
-      if ((e = launch_kspace_gemm (c->version, m->plan, m->maps, ka.kt, m->nkh, (float *) m->sf.p,
-                                   (float *) m->part_rec.p, (int *) m->status.p, st, c))
-          != cudaSuccess)
-        return cuda_fail (e, "reciprocal space (tensor cores)");
-    }
-  else if (m->nkh > 0)
-    {
-      if (c->version == 0) mk_sfac<0><<<gk, MX_WARPS * 32, 0, st>>> (ka);
-      else if (c->version == 1) mk_sfac<1><<<gk, MX_WARPS * 32, 0, st>>> (ka);
-      else mk_sfac<2><<<gk, MX_WARPS * 32, 0, st>>> (ka);
-      kmark (c, st, "mk_sfac");
-      if (c->version == 0) mk_backproj<0><<<gb, MX_WARPS * 32, 0, st>>> (ba);
-      else if (c->version == 1) mk_backproj<1><<<gb, MX_WARPS * 32, 0, st>>> (ba);
-      else mk_backproj<2><<<gb, MX_WARPS * 32, 0, st>>> (ba);
-      kmark (c, st, "mk_backproj");
-    }
-  else
-    cudaMemsetAsync (m->part_rec.p, 0, sizeof (float) * (size_t) m->nchunk_k * np * C, st);
-  if (E) cudaEventRecord (E[1], st);
-  if (overlap)
-    cudaStreamWaitEvent (st, m->ev_join, 0);
-  else
-    {
-      launch_real (st);
-      kmark (c, st, "mk_real");
-    }
-  if (E) cudaEventRecord (E[2], st);
-
-  const double *selfm = (const double *) m->selfbuf.p;
-  const int gc = (np * C + 63) / 64;
-  if (c->version == 0) mk_combine<0><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
-  else if (c->version == 1) mk_combine<1><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
-  else mk_combine<2><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
-  kmark (c, st, "mk_combine");
-  if (E) cudaEventRecord (E[3], st);
-  if (m->tensor)
-    cudaMemcpyAsync (m->h_status, m->status.p, sizeof (int), cudaMemcpyDeviceToHost, st);
-  e = cudaGetLastError ();
-  if (e != cudaSuccess) return cuda_fail (e, "mixed kernels");
+  int rs = run_mixed_sequence (c, m, d_pos, d_x, d_y, st, E != nullptr, sequence);
+  if (rs) return rs;
   c->launches = m->nkh == 0 ? 3 : (m->tensor ? 6 : 5);
   c->timed = timed;
   return STOKES_GPU_OK;
@@ -966,6 +1058,7 @@ release_mixed (Ctx *c)
                     &m->img_wb})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
+  if (m->gexec) cudaGraphExecDestroy (m->gexec);
   if (m->side) cudaStreamDestroy (m->side);
   if (m->ev_fork) cudaEventDestroy (m->ev_fork);
   if (m->ev_join) cudaEventDestroy (m->ev_join);
