@@ -684,13 +684,12 @@ kgemm_maps (const KGemm &g, float *sf, KMaps *m)
   return e;
 }
 
+// the shared-memory opt-in is a per-device function attribute; set once
+// per device
 template <int V>
 static cudaError_t
-launch_v (const KGemm &g, const KMaps &mp, const MixK *kt, int nk, const float *sf, float *ypart,
-          int *status, cudaStream_t st, Ctx *prof)
+gemm_attrs ()
 {
-  // the shared-memory opt-in is a per-device function attribute; set once
-  // per device
   static int attr_dev = -1;
   int dev = 0;
   cudaError_t e = cudaGetDevice (&dev);
@@ -705,22 +704,52 @@ launch_v (const KGemm &g, const KMaps &mp, const MixK *kt, int nk, const float *
         return e;
       attr_dev = dev;
     }
+  return cudaSuccess;
+}
+
+template <int V>
+static cudaError_t
+forward_v (const KGemm &g, const KMaps &mp, const MixK *kt, int nk, int *status, cudaStream_t st,
+           Ctx *prof)
+{
+  cudaError_t e = gemm_attrs<V> ();
+  if (e != cudaSuccess) return e;
   k_sfac_gemm<V><<<dim3 (g.nrt, g.ntile_f, g.nsplit), NT, SMEM_DYN, st>>> (mp.zf, mp.sf, g, status);
   kmark (prof, st, "k_sfac_gemm");
-  k_kop<V><<<(nk + KOP_K - 1) / KOP_K, KOP_K * KOP_G, 0, st>>> (g, kt, nk, sf);
+  k_kop<V><<<(nk + KOP_K - 1) / KOP_K, KOP_K * KOP_G, 0, st>>> (g, kt, nk, g.sf);
   kmark (prof, st, "k_kop");
-  k_bp_gemm<V><<<dim3 (g.mtiles, g.ntile_b, g.ksplit), NT, SMEM_DYN, st>>> (mp.wb, g, ypart, status);
+  return cudaGetLastError ();
+}
+
+template <int V>
+static cudaError_t
+backward_v (const KGemm &g, const KMaps &mp, float *ypart, int *status, cudaStream_t st,
+            Ctx *prof)
+{
+  cudaError_t e = gemm_attrs<V> ();
+  if (e != cudaSuccess) return e;
+  k_bp_gemm<V><<<dim3 (g.mtiles, g.ntile_b, g.ksplit), NT, SMEM_DYN, st>>> (mp.wb, g, ypart,
+                                                                            status);
   kmark (prof, st, "k_bp_gemm");
   return cudaGetLastError ();
 }
 
 cudaError_t
-launch_kspace_gemm (int version, const KGemm &g, const KMaps &maps, const MixK *kt, int nk,
-                    float *sf, float *ypart, int *status, cudaStream_t st, Ctx *prof)
+launch_kspace_forward (int version, const KGemm &g, const KMaps &maps, const MixK *kt, int nk,
+                       int *status, cudaStream_t st, Ctx *prof)
 {
-  if (version == 0) return launch_v<0> (g, maps, kt, nk, sf, ypart, status, st, prof);
-  if (version == 1) return launch_v<1> (g, maps, kt, nk, sf, ypart, status, st, prof);
-  return launch_v<2> (g, maps, kt, nk, sf, ypart, status, st, prof);
+  if (version == 0) return forward_v<0> (g, maps, kt, nk, status, st, prof);
+  if (version == 1) return forward_v<1> (g, maps, kt, nk, status, st, prof);
+  return forward_v<2> (g, maps, kt, nk, status, st, prof);
+}
+
+cudaError_t
+launch_kspace_backward (int version, const KGemm &g, const KMaps &maps, float *ypart, int *status,
+                        cudaStream_t st, Ctx *prof)
+{
+  if (version == 0) return backward_v<0> (g, maps, ypart, status, st, prof);
+  if (version == 1) return backward_v<1> (g, maps, ypart, status, st, prof);
+  return backward_v<2> (g, maps, ypart, status, st, prof);
 }
 
 }  // namespace lsg

@@ -488,44 +488,60 @@ mk_selfmat (double xa, double xc, double xm, double *S)
   for (int k = 0; k < C; k++) S[k * C + q] = acc.v[k];
 }
 
-// y = S x (FP64 self term) + sum of real partials + 2 sum of reciprocal
-// partials, one thread per (particle, component) so that the loads coalesce
-// and the FP64 work (at most five FMAs: the self block is diagonal for F and
-// T, 5 x 5 for the stresslet) spreads over the SMs; the FP32 partials are
-// summed with Kahan compensation.
-template <int V>
-__global__ void __launch_bounds__ (64)
-mk_combine (const double *x, const float *pr, int ncr, const float *pk, int nck,
-            const double *S, int np, double *y)
+// the final sum of a mixed product, y = S x + sum of the real-space partials
+// + 2 sum of the reciprocal partials (half k space)
+struct CombineArgs {
+  const double *x;      // input vector, FP64 [np c]
+  const float *pr;      // real-space partials [ncr][np c]
+  int ncr;
+  const float *pk;      // reciprocal partials [nck][np c]
+  int nck;
+  const double *S;      // self block of equal spheres, c x c
+  int np, c;
+  double *y;            // output [np c]
+};
+
+constexpr int CMB_LANES = 4;    // threads per output element
+
+// Four threads per element t = i c + q: lane l sums the chunks l, l + 4, ...
+// of both partial sets (Kahan-compensated FP32, all its loads in flight);
+// the lanes meet in FP64 through shuffles, and lane 0 adds the FP64 self
+// term (at most five FMAs: the self block is diagonal for F and T and
+// couples the five stresslet components).
+__global__ void __launch_bounds__ (256)
+mk_combine (CombineArgs a)
 {
-  constexpr int C = NComp<V>::value;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int n = np * C;
-  if (t >= n) return;
-  const int i = t / C, q = t - i * C;
+  const int n = a.np * a.c;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = g / CMB_LANES, l = g % CMB_LANES;
+  const int tt = t < n ? t : n - 1;        // the shuffles need every lane
   float sr = 0.f, cr = 0.f, sk = 0.f, ck = 0.f;
-#pragma unroll 4
-  for (int c = 0; c < ncr; c++)
+#pragma unroll 8
+  for (int k = l; k < a.ncr; k += CMB_LANES)
     {
-      const float v = pr[(size_t) c * n + t] - cr;
+      const float v = a.pr[(size_t) k * n + tt] - cr;
       const float u = sr + v;
       cr = (u - sr) - v;
       sr = u;
     }
-#pragma unroll 4
-  for (int c = 0; c < nck; c++)
+#pragma unroll 8
+  for (int k = l; k < a.nck; k += CMB_LANES)
     {
-      const float v = pk[(size_t) c * n + t] - ck;
+      const float v = a.pk[(size_t) k * n + tt] - ck;
       const float u = sk + v;
       ck = (u - sk) - v;
       sk = u;
     }
-  // the stresslet block couples components 6..10; F and T are diagonal
+  double r = ((double) sr - (double) cr) + 2.0 * ((double) sk - (double) ck);
+  r += __shfl_xor_sync (0xffffffffu, r, 1);
+  r += __shfl_xor_sync (0xffffffffu, r, 2);
+  if (l != 0 || t >= n) return;
+  const int i = t / a.c, q = t - i * a.c;
   const int q0 = (q < 6) ? q : 6, nq = (q < 6) ? 1 : 5;
-  const double *xi = x + (size_t) C * i;
+  const double *xi = a.x + (size_t) a.c * i;
   double self = 0.0;
-  for (int k = 0; k < nq; k++) self = fma (S[q * C + q0 + k], xi[q0 + k], self);
-  y[t] = self + ((double) sr - (double) cr) + 2.0 * ((double) sk - (double) ck);
+  for (int k = 0; k < nq; k++) self = fma (a.S[q * a.c + q0 + k], xi[q0 + k], self);
+  a.y[t] = self + r;
 }
 
 // ---------------------------------------------------------------------------
@@ -863,6 +879,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       if ((e = m->img_wb.ensure (sizeof (float) * kgemm_wb_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image WB");
       m->plan.ZF = (float *) m->img_zf.p;
       m->plan.WB = (float *) m->img_wb.p;
+      m->plan.sf = (float *) m->sf.p;
     }
   else if ((e = m->pq.ensure (sizeof (float) * 2 * C * (size_t) (m->nkh > 0 ? m->nkh : 1))) != cudaSuccess)
     return cuda_fail (e, "pq");
@@ -992,11 +1009,23 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     ba.off1 = off1; ba.off2 = off2; ba.partial = (float *) m->part_rec.p;
     const int gk = (m->nkh + MX_WARPS - 1) / MX_WARPS;
     const int gb = (int) (((long long) np * m->nchunk_k + MX_WARPS - 1) / MX_WARPS);
-    if (m->nkh > 0 && m->tensor)
+    CombineArgs cb;
+    cb.x = d_x;
+    cb.pr = (const float *) m->part_real.p;
+    cb.ncr = m->nchunk_r;
+    cb.pk = (const float *) m->part_rec.p;
+    cb.nck = m->nchunk_k;
+    cb.S = (const double *) m->selfbuf.p;
+    cb.np = np;
+    cb.c = C;
+    cb.y = d_y;
+    const bool fused = m->nkh > 0 && m->tensor;
+    // reciprocal space up to the k operators (tensor cores) or the SIMT sums;
+    // then the real-space partials, the back-projection and the final sum
+    if (fused)
       {
-        if ((e = launch_kspace_gemm (c->version, m->plan, m->maps, ka.kt, m->nkh, (float *) m->sf.p,
-                                     (float *) m->part_rec.p, (int *) m->status.p, st, c))
-            != cudaSuccess)
+        if ((e = launch_kspace_forward (c->version, m->plan, m->maps, ka.kt, m->nkh,
+                                        (int *) m->status.p, st, c)) != cudaSuccess)
           return cuda_fail (e, "reciprocal space (tensor cores)");
       }
     else if (m->nkh > 0)
@@ -1012,6 +1041,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       }
     else
       cudaMemsetAsync (m->part_rec.p, 0, sizeof (float) * (size_t) m->nchunk_k * np * C, st);
+    // the real-space partials must be complete before the combine
     if (E) cudaEventRecord (E[1], st);
     if (overlap)
       cudaStreamWaitEvent (st, m->ev_join, 0);
@@ -1021,12 +1051,11 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
         kmark (c, st, "mk_real");
       }
     if (E) cudaEventRecord (E[2], st);
-
-    const double *selfm = (const double *) m->selfbuf.p;
-    const int gc = (np * C + 63) / 64;
-    if (c->version == 0) mk_combine<0><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
-    else if (c->version == 1) mk_combine<1><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
-    else mk_combine<2><<<gc, 64, 0, st>>> (d_x, (const float *) m->part_real.p, m->nchunk_r, (const float *) m->part_rec.p, m->nchunk_k, selfm, np, d_y);
+    if (fused
+        && (e = launch_kspace_backward (c->version, m->plan, m->maps, (float *) m->part_rec.p,
+                                        (int *) m->status.p, st, c)) != cudaSuccess)
+      return cuda_fail (e, "reciprocal space (tensor cores)");
+    mk_combine<<<(int) (((long long) np * C * CMB_LANES + 255) / 256), 256, 0, st>>> (cb);
     kmark (c, st, "mk_combine");
     if (E) cudaEventRecord (E[3], st);
     if (m->tensor)

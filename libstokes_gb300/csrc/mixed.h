@@ -114,6 +114,7 @@ struct KGemm {
   int KF, KB, NZ;         // K extents (floats) of the images, rows of ZF and WB
   float *ZF, *WB;
   size_t pZF, pWB;        // plane strides (floats)
+  float *sf;              // forward partials [nsplit][n1][c][re|im][Rp]
 };
 
 // TMA descriptors of the two images (128-byte swizzled boxes of 32 K values)
@@ -131,11 +132,12 @@ size_t kgemm_ypart_floats (const KGemm &g);   // partial y, [ksplit][ntile_b][np
 int kgemm_ypart_chunks (const KGemm &g);       // ksplit * ntile_b
 int kgemm_maps (const KGemm &g, float *sf, KMaps *m);   // 0 on success
 
-// forward GEMM -> per-k operators (image WB) -> backward GEMM into ypart;
-// the image ZF is written beforehand by mk_prep
+// forward GEMM -> per-k operators (image WB); then the backward GEMM into
+// ypart.  The image ZF is written beforehand by mk_prep.
 struct Ctx;
-cudaError_t launch_kspace_gemm (int version, const KGemm &g, const KMaps &maps, const MixK *kt,
-                                int nk, float *sf, float *ypart, int *status, cudaStream_t st,
-                                Ctx *prof);
+cudaError_t launch_kspace_forward (int version, const KGemm &g, const KMaps &maps, const MixK *kt,
+                                   int nk, int *status, cudaStream_t st, Ctx *prof);
+cudaError_t launch_kspace_backward (int version, const KGemm &g, const KMaps &maps, float *ypart,
+                                    int *status, cudaStream_t st, Ctx *prof);
 
 }  // namespace lsg
