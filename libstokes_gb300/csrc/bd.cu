@@ -144,6 +144,9 @@ k_bd_lj (int nm, int np, int c, const double *pos, double lx, double ly, double 
   const double ai = rad ? rad[i] : 1.0;
   const float flx = (float) lx, fly = (float) ly, flz = (float) lz;
   double fx = 0.0, fy = 0.0, fz = 0.0;
+  // the reference's force (src/ev-LJ.c:185-262): the 27 cells around the
+  // primary one, the force along the primary-cell vector over the image
+  // distance
   for (int j = 0; j < np; j++)
     {
       if (j == i) continue;
@@ -183,6 +186,102 @@ k_bd_lj (int nm, int np, int c, const double *pos, double lx, double ly, double 
               fz += fr * z / r;
             }
     }
+  f[(size_t) i * c] += fx;
+  f[(size_t) i * c + 1] += fy;
+  f[(size_t) i * c + 2] += fz;
+}
+
+// EV_LJ of this library's BD engine: the nearest image (Lees-Edwards aware;
+// the overlap range is below half the box) and the force along the image
+// vector.  CTA of LJ_T targets; the sources pass through shared memory in
+// tiles of LJ_T as FP32 positions for a pre-test on the wrapped distance
+// (with a margin); the few pairs that pass it are evaluated in FP64 from
+// the global positions.
+constexpr int LJ_T = 128;
+
+__global__ void __launch_bounds__ (LJ_T)
+k_bd_lj_engine (int nm, int np, int c, const double *pos, double lx, double ly, double lz,
+                int shear_mode, double shift, const double *rad, double e_all, double r0_all,
+                const double *lje, const double *ljr0, double *f)
+{
+  __shared__ float s_p[LJ_T][4];
+  const int i = blockIdx.x * LJ_T + threadIdx.x;
+  const bool live = i < nm;
+  const int ii = live ? i : 0;
+  const double xi = pos[3 * ii], yi = pos[3 * ii + 1], zi = pos[3 * ii + 2];
+  const float fxi = (float) xi, fyi = (float) yi, fzi = (float) zi;
+  const double ai = rad ? rad[ii] : 1.0;
+  const float flx = (float) lx, fly = (float) ly, flz = (float) lz, fsh = (float) shift;
+  const float ilx = 1.0f / flx, ily = 1.0f / fly, ilz = 1.0f / flz;
+  const double dlx = 1.0 / lx, dly = 1.0 / ly, dlz = 1.0 / lz;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  for (int j0 = 0; j0 < np; j0 += LJ_T)
+    {
+      __syncthreads ();
+      const int jl = j0 + threadIdx.x;
+      if (jl < np)
+        {
+          s_p[threadIdx.x][0] = (float) pos[3 * jl];
+          s_p[threadIdx.x][1] = (float) pos[3 * jl + 1];
+          s_p[threadIdx.x][2] = (float) pos[3 * jl + 2];
+          s_p[threadIdx.x][3] = rad ? (float) rad[jl] : 1.0f;
+        }
+      __syncthreads ();
+      if (!live) continue;
+      const int nt = min (LJ_T, np - j0);
+      for (int t = 0; t < nt; t++)
+        {
+          const int j = j0 + t;
+          float sx = fxi - s_p[t][0], sy = fyi - s_p[t][1], sz = fzi - s_p[t][2];
+          if (shear_mode == 1)
+            {
+              const float k = rintf (sy * ily);
+              sy -= k * fly;
+              sx -= k * fsh;
+            }
+          else if (shear_mode == 2)
+            {
+              const float k = rintf (sz * ilz);
+              sz -= k * flz;
+              sx -= k * fsh;
+            }
+          sx -= flx * rintf (sx * ilx);
+          sy -= fly * rintf (sy * ily);
+          sz -= flz * rintf (sz * ilz);
+          const float lim = ((float) ai + s_p[t][3]) * 1.001f + 1e-3f;
+          if (sx * sx + sy * sy + sz * sz > lim * lim || j == i) continue;
+          const double aj = rad ? rad[j] : 1.0;
+          double x = xi - pos[3 * j], y = yi - pos[3 * j + 1], z = zi - pos[3 * j + 2];
+          if (shear_mode == 1)
+            {
+              const double k = rint (y * dly);
+              y -= k * ly;
+              x -= k * shift;
+            }
+          else if (shear_mode == 2)
+            {
+              const double k = rint (z * dlz);
+              z -= k * lz;
+              x -= k * shift;
+            }
+          x -= lx * rint (x * dlx);
+          y -= ly * rint (y * dly);
+          z -= lz * rint (z * dlz);
+          const double r = sqrt (x * x + y * y + z * z);
+          const double ov = ai + aj - r;
+          if (!(ov > 0.0) || !(r > 0.0)) continue;
+          const double e = lje ? sqrt (lje[i] * lje[j]) : e_all;
+          const double r0 = ljr0 ? 0.5 * (ljr0[i] + ljr0[j]) : r0_all;
+          double rl = r0 - ov;
+          if (rl < 0.0) rl = 1.0e-12;
+          const double ri = r0 / rl, ri6 = ri * ri * ri * ri * ri * ri;
+          const double fr = 12.0 * e * ri6 * ri * (ri6 - 1.0);
+          fx += fr * x / r;
+          fy += fr * y / r;
+          fz += fr * z / r;
+        }
+    }
+  if (!live) return;
   f[(size_t) i * c] += fx;
   f[(size_t) i * c + 1] += fy;
   f[(size_t) i * c + 2] += fz;
@@ -284,6 +383,7 @@ struct stokes_gpu_bd {
   lsg::DevBuf x, xmid, y, z, f, u, fext, work, lan, tmp, dots, pos_fixed;
   lsg::DevBuf xnew, lje, ljr0, ovl;    // drop-in BD_evolve_mid
   bool lj_arrays = false;              // per-particle EV_LJ coefficients in lje, ljr0
+  bool ref_lj = false;                 // drop-in: the reference's EV_LJ pair force
   double eig[2] = {0, 0};
   std::vector<double> coef;
   bool have_bounds = false;
@@ -459,7 +559,7 @@ bd_forces (stokes_gpu_bd *b, const double *d_pos, double fact)
   k_bd_force<<<gridn (b->np), 256, 0, st>>> (b->nm, b->np, b->C, fact, (const double *) b->z.p,
                                              b->fext.p ? (const double *) b->fext.p : nullptr,
                                              (double *) b->f.p);
-  if (b->p.lj_e != 0.0 || b->lj_arrays)
+  if ((b->p.lj_e != 0.0 || b->lj_arrays) && b->ref_lj)
     k_bd_lj<<<gridn (b->nm), 128, 0, st>>> (b->nm, b->np, b->C, d_pos, s->lx, s->ly, s->lz,
                                             s->shear_mode, s->shear_shift,
                                             s->a ? (const double *) b->c->pp.p : nullptr,
@@ -467,6 +567,12 @@ bd_forces (stokes_gpu_bd *b, const double *d_pos, double fact)
                                             b->lj_arrays ? (const double *) b->lje.p : nullptr,
                                             b->lj_arrays ? (const double *) b->ljr0.p : nullptr,
                                             (double *) b->f.p);
+  else if (b->p.lj_e != 0.0 || b->lj_arrays)
+    k_bd_lj_engine<<<(b->nm + LJ_T - 1) / LJ_T, LJ_T, 0, st>>> (
+      b->nm, b->np, b->C, d_pos, s->lx, s->ly, s->lz, s->shear_mode, s->shear_shift,
+      s->a ? (const double *) b->c->pp.p : nullptr, b->p.lj_e, b->p.lj_r0,
+      b->lj_arrays ? (const double *) b->lje.p : nullptr,
+      b->lj_arrays ? (const double *) b->ljr0.p : nullptr, (double *) b->f.p);
   cudaError_t e = cudaGetLastError ();
   return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "BD forces");
 }
@@ -830,6 +936,7 @@ dropin_interactions (stokes_gpu_bd *b, struct BD_params *BD, const char *fn)
 {
   cudaStream_t st = b->c->stream;
   b->lj_arrays = BD->ev_LJ != nullptr;
+  b->ref_lj = true;
   if (b->lj_arrays)
     {
       if (BD->ev_LJ->n < b->np) dropin_die (fn, "EV_LJ has fewer entries than particles");

@@ -226,6 +226,10 @@ class Oracle(_Backend):
                                            C.c_double, C.c_double, C.c_double, C.c_int, _dp,
                                            C.c_double, C.c_double, _dp, _dp, C.c_double,
                                            C.c_double, _dp, _dp]
+            lib.oracle_bd_step_ex.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                              C.c_double, C.c_double, C.c_double, C.c_double,
+                                              C.c_int, _dp, C.c_double, C.c_double, _dp, _dp,
+                                              C.c_double, C.c_double, C.c_int, _dp, _dp]
         return cls._lib
 
     def set_threads(self, n):
@@ -253,17 +257,19 @@ class Oracle(_Backend):
                                  _d(z))
         return z
 
-    def bd_step(self, x, dt, peclet, a, e0, e1, y, F=None, lj_e=0.0, lj_r0=2.0):
-        """One mid-point step from positions x with noise y; returns (x_new, z)."""
+    def bd_step(self, x, dt, peclet, a, e0, e1, y, F=None, lj_e=0.0, lj_r0=2.0, lj_image=False):
+        """One mid-point step from positions x with noise y; returns (x_new, z).
+        lj_image: EV_LJ along the nearest-image vector (this library's BD
+        engine) instead of the reference's primary-cell vector."""
         x = np.array(x, dtype=np.float64).reshape(-1).copy()
         a = np.ascontiguousarray(a, dtype=np.float64)
         y = np.ascontiguousarray(y, dtype=np.float64)
         Fp = None if F is None else np.ascontiguousarray(F, dtype=np.float64)
         z = np.zeros(self.n)
-        self._L.oracle_bd_step(self.h, self.version, self.np, *self.box, float(dt),
-                               float(peclet), len(a), _d(a), float(e0), float(e1), _d(y),
-                               None if Fp is None else _d(Fp), float(lj_e), float(lj_r0),
-                               _d(x), _d(z))
+        self._L.oracle_bd_step_ex(self.h, self.version, self.np, *self.box, float(dt),
+                                  float(peclet), len(a), _d(a), float(e0), float(e1), _d(y),
+                                  None if Fp is None else _d(Fp), float(lj_e), float(lj_r0),
+                                  1 if lj_image else 0, _d(x), _d(z))
         return x, z
 
     def count_real_terms(self):

@@ -42,16 +42,38 @@ oracle_cheb_eval (void *h, int n, int ncheb, const double *a, double e0, double 
   free (b);
 }
 
-/* EV_LJ force on each particle, added to f (stride c) */
+/* EV_LJ force on each particle, added to f (stride c).  image = 0: the
+ * reference's force (src/ev-LJ.c:185-262), along the primary-cell vector over
+ * the image distance; image = 1: the nearest image and the force along the
+ * image vector (the convention of this library's own BD engine) */
 static void
 lj_add (int np, int c, const double *pos, double lx, double ly, double lz, double e, double r0,
-        double *f)
+        int image, double *f)
 {
   for (int i = 0; i < np; i++)
     for (int j = i + 1; j < np; j++)
       {
         const double x = pos[3 * i] - pos[3 * j], y = pos[3 * i + 1] - pos[3 * j + 1],
                      z = pos[3 * i + 2] - pos[3 * j + 2];
+        if (image)
+          {
+            const double xx = x - lx * rint (x / lx), yy = y - ly * rint (y / ly),
+                         zz = z - lz * rint (z / lz);
+            const double r = sqrt (xx * xx + yy * yy + zz * zz);
+            const double ov = 2.0 - r;
+            if (!(ov > 0.0)) continue;
+            double rl = r0 - ov;
+            if (rl < 0.0) rl = 1.0e-12;
+            const double ri = r0 / rl, ri6 = pow (ri, 6.0);
+            const double fr = 12.0 * e * ri6 * ri * (ri6 - 1.0);
+            f[c * i] += fr * xx / r;
+            f[c * i + 1] += fr * yy / r;
+            f[c * i + 2] += fr * zz / r;
+            f[c * j] -= fr * xx / r;
+            f[c * j + 1] -= fr * yy / r;
+            f[c * j + 2] -= fr * zz / r;
+            continue;
+          }
         for (int kx = -1; kx <= 1; kx++)
           for (int ky = -1; ky <= 1; ky++)
             for (int kz = -1; kz <= 1; kz++)
@@ -78,10 +100,10 @@ lj_add (int np, int c, const double *pos, double lx, double ly, double lz, doubl
  * torque slots used for FT; stresslet slots absent); x: positions (in/out);
  * z_out (optional): the Chebyshev noise */
 void
-oracle_bd_step (void *h, int version, int np, double lx, double ly, double lz, double dt,
-                double peclet, int ncheb, const double *a, double e0, double e1,
-                const double *y, const double *F, double lj_e, double lj_r0, double *x,
-                double *z_out)
+oracle_bd_step_ex (void *h, int version, int np, double lx, double ly, double lz, double dt,
+                   double peclet, int ncheb, const double *a, double e0, double e1,
+                   const double *y, const double *F, double lj_e, double lj_r0, int lj_image,
+                   double *x, double *z_out)
 {
   const int c = ncomp_of (version), n = c * np;
   double *z = calloc ((size_t) n, sizeof (double));
@@ -98,7 +120,7 @@ oracle_bd_step (void *h, int version, int np, double lx, double ly, double lz, d
     {
       const double *pcur = pass == 0 ? x : xm;
       for (int k = 0; k < n; k++) f[k] = fact * z[k] + (F ? F[k] : 0.0);
-      if (lj_e != 0.0) lj_add (np, c, pcur, lx, ly, lz, lj_e, lj_r0, f);
+      if (lj_e != 0.0) lj_add (np, c, pcur, lx, ly, lz, lj_e, lj_r0, lj_image, f);
       oracle_set_pos (h, pcur);
       oracle_atimes (h, f, u);
       const double hstep = pass == 0 ? 0.5 * dt : dt;
@@ -110,4 +132,15 @@ oracle_bd_step (void *h, int version, int np, double lx, double ly, double lz, d
   free (f);
   free (u);
   free (xm);
+}
+
+/* the step with the reference's EV_LJ force */
+void
+oracle_bd_step (void *h, int version, int np, double lx, double ly, double lz, double dt,
+                double peclet, int ncheb, const double *a, double e0, double e1,
+                const double *y, const double *F, double lj_e, double lj_r0, double *x,
+                double *z_out)
+{
+  oracle_bd_step_ex (h, version, np, lx, ly, lz, dt, peclet, ncheb, a, e0, e1, y, F, lj_e, lj_r0,
+                     0, x, z_out);
 }

@@ -58,10 +58,64 @@ def test_noise_and_step_match_oracle(lib, version):
     check(lib.stokes_gpu_bd_step_noise(h, 0.0, _d(y)))
     x1 = np.zeros(3 * 40)
     check(lib.stokes_gpu_bd_get_positions(h, _d(x1)))
-    xo, _ = o.bd_step(pos, 1e-3, 1.0, a, eig[0], eig[1], y, lj_e=1.0, lj_r0=2.0)
+    xo, _ = o.bd_step(pos, 1e-3, 1.0, a, eig[0], eig[1], y, lj_e=1.0, lj_r0=2.0, lj_image=True)
     d_gpu = x1 - pos.reshape(-1)
     d_ora = xo - pos.reshape(-1)
     assert rel_l2(d_gpu, d_ora) < 1e-10
+    check(lib.stokes_gpu_bd_destroy(h))
+    s.close()
+
+
+def _boundary_pair(n, seed):
+    """RSA spheres with particles 0 and 1 moved to overlap slightly (r = 1.95)
+    across the x boundary of the box, clear of every other sphere"""
+    from libstokes_gb300.workloads import rsa_positions
+    pos, L = rsa_positions(n, 0.15, seed=seed)
+    p = pos.reshape(-1, 3).copy()
+    rest = p[2:]
+
+    def clear(q):
+        d = rest - q
+        d -= L * np.rint(d / L)
+        return np.min(np.linalg.norm(d, axis=1)) > 2.2
+
+    for y in np.linspace(1.0, L - 1.0, 25):
+        for z in np.linspace(1.0, L - 1.0, 25):
+            a, b = np.array([0.2, y, z]), np.array([L - 1.75, y, z])
+            if clear(a) and clear(b):
+                p[0], p[1] = a, b
+                return p.reshape(-1), L
+    pytest.skip("no clear spot for the boundary pair")
+
+
+def test_engine_lj_uses_the_image_vector(lib):
+    """The device engine's EV_LJ acts along the nearest-image vector: with a
+    pair overlapping across the periodic boundary the step matches the oracle
+    with that convention at 1e-10, and differs measurably from the
+    reference's primary-cell vector (about L/r times the force), which the
+    drop-in BD_evolve_mid keeps."""
+    from libstokes_gb300 import FP64, check
+    from libstokes_gb300.abi import _d, FUNC1
+    pos, L = _boundary_pair(40, 7)
+    s, h = _engine(lib, 0, pos, L, FP64)
+    # rmin = 1: the mobility of the overlapping pair at contact distance
+    s.set_misc(rmin=1.0)
+    eig = np.zeros(2)
+    check(lib.stokes_gpu_bd_estimate_bounds(h, _d(eig)))
+    y = np.random.default_rng(8).standard_normal(3 * 40)
+    a = np.zeros(20)
+    lib.chebyshev_coef(20, FUNC1(lambda t: 1.0 / np.sqrt(t)), eig[0], eig[1], _d(a))
+    check(lib.stokes_gpu_bd_set_bounds(h, _d(eig)))
+    check(lib.stokes_gpu_bd_step_noise(h, 0.0, _d(y)))
+    x1 = np.zeros(3 * 40)
+    check(lib.stokes_gpu_bd_get_positions(h, _d(x1)))
+    o = _oracle(0, pos, L)
+    o.set_misc(rmin=1.0)
+    xo, _ = o.bd_step(pos, 1e-3, 1.0, a, eig[0], eig[1], y, lj_e=1.0, lj_r0=2.0, lj_image=True)
+    xr, _ = o.bd_step(pos, 1e-3, 1.0, a, eig[0], eig[1], y, lj_e=1.0, lj_r0=2.0, lj_image=False)
+    d_gpu, d_img, d_ref = x1 - pos, xo - pos, xr - pos
+    assert rel_l2(d_gpu, d_img) < 1e-10
+    assert rel_l2(d_ref, d_img) > 1e-3
     check(lib.stokes_gpu_bd_destroy(h))
     s.close()
 
