@@ -23,10 +23,11 @@
 // remainder, x = hi + lo), K contiguous and already in the sign pattern
 // above, loaded per tile by TMA (32 K values = 128 bytes per row, 128-byte
 // swizzle).  The A operands -- the row phases T_r -- are not stored: the
-// worker warps build each tile straight into shared memory from the 32-bit
-// fixed-point coordinates (m2 q_y + m3 q_z mod 2^32 is the exact phase) with
-// the table-driven phase_of, in the same swizzled layout.  The products are
-// tcgen05 kind::tf32 MMAs (M = 128, N <= 256, K = 8 per instruction) in
+// worker warps build each tile straight into shared memory, in the same
+// swizzled layout: the forward's as products t_y[m2](j) t_z[m3](j) of the
+// per-axis phases (a particle-major table written by mk_prep), the
+// backward's by phase_of from the exact fixed-point phase m2 q_y + m3 q_z
+// mod 2^32.  The products are tcgen05 kind::tf32 MMAs (M = 128, N <= 256, K = 8 per instruction) in
 // 3xTF32: hi*hi + hi*lo + lo*hi.  The tensor core's FP32 accumulation
 // truncates at the accumulator's magnitude, so every 32-wide K tile starts a
 // fresh accumulator that is drained into FP32 registers (round to nearest);
@@ -223,20 +224,10 @@ worker_role (Sync &s, unsigned char *smem, uint32_t tmem, int ntiles, float acc[
   volatile int *err = &s.err;
   auto build = [&] (int t) {
     unsigned char *stage = smem + (size_t) (t % STAGES) * STAGE_BYTES;
-    // the eight phases first (their loads issue back to back), then the values
-    uint32_t ph[8];
-    bool ok[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) ph[k] = prod.phase (t, 8 * half + k, ok[k]);
+    float2 v[8];
+    prod.values (t, 8 * half, v);
     // the inputs of this stage's next tile, into L1 ahead of its build
     if (t + STAGES < ntiles) prod.prefetch (t + STAGES, 8 * half + (threadIdx.x & 7));
-    float2 v[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++)
-      {
-        v[k] = phase_of (prod.rot, ph[k]);
-        if (!ok[k]) v[k] = make_float2 (0.f, 0.f);
-      }
 #pragma unroll
     for (int c = 0; c < 4; c++) put_a (stage, row, 4 * half + c, v[2 * c], v[2 * c + 1]);
     umma::fence_async_smem ();      // generic writes -> the MMA's async reads
@@ -271,41 +262,64 @@ worker_role (Sync &s, unsigned char *smem, uint32_t tmem, int ntiles, float acc[
   return true;
 }
 
-// A of the forward GEMM: row r = (m2, m3), K = particles from j0.  phase():
-// the fixed-point phase of value k of tile t (the index is clamped so the
-// load is always in bounds; ok tells whether the value is a real entry)
+// A of the forward GEMM: row r = (m2, m3), K = particles from j0.  values():
+// entries k0 .. k0 + 7 of tile t, T_r(j) = t_y[m2](j) t_z[m3](j) from the
+// particle-major phase table (the 16 particles of a tile are shared by every
+// row, so these loads mostly hit L1; indices are clamped so every load is in
+// bounds, entries past the particles are zero).  The sixteen loads issue
+// back to back, then the products.
 struct ProdF {
-  const uint4 *qpos;
-  const float4 *rot;
-  int np, j0;
-  uint32_t m2, m3;
+  const float2 *tyz;
+  int wyz, np, j0;
+  int iy, iz;               // this row's entries in a particle's table row
   bool live;
-  __device__ __forceinline__ uint32_t phase (int t, int k, bool &ok) const
+  __device__ __forceinline__ void values (int t, int k0, float2 v[8]) const
   {
-    const int j = j0 + PT * t + k;
-    ok = live && j < np;
-    const uint4 q = __ldg (qpos + min (j, np - 1));
-    return m2 * q.y + m3 * q.z;
+    float2 a[8], b[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      {
+        const float2 *row = tyz + (size_t) min (j0 + PT * t + k0 + k, np - 1) * wyz;
+        a[k] = __ldg (row + iy);
+        b[k] = __ldg (row + iz);
+      }
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      {
+        const bool ok = live && j0 + PT * t + k0 + k < np;
+        v[k] = ok ? make_float2 (a[k].x * b[k].x - a[k].y * b[k].y, a[k].x * b[k].y + a[k].y * b[k].x)
+                  : make_float2 (0.f, 0.f);
+      }
   }
   __device__ __forceinline__ void prefetch (int t, int k) const
   {
-    umma::prefetch_l1 (qpos + min (j0 + PT * t + k, np - 1));
+    const float2 *row = tyz + (size_t) min (j0 + PT * t + k, np - 1) * wyz;
+    umma::prefetch_l1 (row + iy);
+    umma::prefetch_l1 (row + iz);
   }
 };
 
-// A of the backward GEMM: row = particle (fixed-point qy, qz), K = rows from r0
+// A of the backward GEMM: row = particle (fixed-point qy, qz), K = rows from
+// r0: T_r(i) from the exact fixed-point phase m2 q_y + m3 q_z mod 2^32 by the
+// table-driven phase_of (the eight rows' (m2, m3) load first, back to back)
 struct ProdB {
   const int2 *rowm;
   const float4 *rot;
   int R, r0;
   uint32_t qy, qz;
   bool live;
-  __device__ __forceinline__ uint32_t phase (int t, int k, bool &ok) const
+  __device__ __forceinline__ void values (int t, int k0, float2 v[8]) const
   {
-    const int r = r0 + PT * t + k;
-    ok = live && r < R;
-    const int2 mm = __ldg (rowm + min (r, R - 1));
-    return (uint32_t) mm.x * qy + (uint32_t) mm.y * qz;
+    int2 mm[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) mm[k] = __ldg (rowm + min (r0 + PT * t + k0 + k, R - 1));
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      {
+        const bool ok = live && r0 + PT * t + k0 + k < R;
+        const float2 p = phase_of (rot, (uint32_t) mm[k].x * qy + (uint32_t) mm[k].y * qz);
+        v[k] = ok ? p : make_float2 (0.f, 0.f);
+      }
   }
   __device__ __forceinline__ void prefetch (int t, int k) const
   {
@@ -400,14 +414,14 @@ k_sfac_gemm (const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CU
       // A rows: r = (m2, m3), values T_r(j) over the slice's particles
       ProdF prod;
       const int r = r0 + (tid & 127);
-      prod.qpos = g.t.qpos;
-      prod.rot = g.t.rot;
+      prod.tyz = g.t.tyz;
+      prod.wyz = g.t.wyz;
       prod.np = g.t.np;
       prod.j0 = jb;
       prod.live = r < g.R;
       const int2 mm = prod.live ? g.rowm[r] : make_int2 (0, 0);
-      prod.m2 = (uint32_t) mm.x;
-      prod.m3 = (uint32_t) mm.y;
+      prod.iy = g.t.M1 + mm.x;
+      prod.iz = (2 * g.t.M1 + 1) + g.t.M2 + mm.y;
       if (warp >> 2) drain_park_sf<C, CPT> (s, tmem, ntiles, smem, ncol, prod);
       else drain_park_sf<C, 0> (s, tmem, ntiles, smem, ncol, prod);
     }

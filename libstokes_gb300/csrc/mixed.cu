@@ -51,6 +51,7 @@ struct MixedState {
   std::vector<MixK> h_k;
   DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf, status, sf, rowm, rot;
   DevBuf img_zf, img_wb;        // GEMM B-operand images (kspace_tc.cu)
+  DevBuf tyz;                   // particle-major y, z phases (the GEMMs' A operands)
   KMaps maps;
   uint64_t img_key = 0;         // buffers and plan the maps and zeroed pads belong to
   // the real-space kernel runs on this side stream, concurrently with the
@@ -93,6 +94,8 @@ struct PrepArgs {
   float *zf;            // forward GEMM image ZF (tensor-core path) or NULL
   size_t zplane;        // floats per ZF plane
   int kf;               // floats per ZF row
+  float2 *tyz;          // particle-major y, z phases for both signs of m (or NULL)
+  int wyz, M1, M2;
 };
 
 constexpr int PREP_P = 32;       // particles per mk_prep CTA
@@ -173,6 +176,12 @@ mk_prep (PrepArgs a)
       const uint32_t m = (uint32_t) (row - (d == 0 ? 0 : (d == 1 ? a.m0end : a.m1end)));
       const float2 ph = phase_of (a.rot, m * s_q[d][jl]);
       a.tab[(size_t) row * a.np + j] = ph;
+      if (d != 0 && a.tyz)
+        {
+          float2 *t = a.tyz + (size_t) j * a.wyz + (d == 1 ? a.M1 : 2 * a.M1 + 1 + a.M2);
+          t[(int) m] = ph;
+          t[-(int) m] = make_float2 (ph.x, -ph.y);
+        }
       if (d == 0 && a.zf)
         for (int q = 0; q < a.c; q++)
           {
@@ -769,7 +778,7 @@ run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_
   mix ((uint64_t) m->nchunk_k);
   const void *ptrs[] = {d_pos, d_x, d_y, m->kt.p, m->qpos.p, m->tab.p, m->xf.p, m->pq.p,
                         m->part_real.p, m->part_rec.p, m->selfbuf.p, m->status.p, m->sf.p,
-                        m->rowm.p, m->rot.p, m->img_zf.p, m->img_wb.p, m->h_status};
+                        m->rowm.p, m->rot.p, m->img_zf.p, m->img_wb.p, m->h_status, m->tyz.p};
   for (const void *p : ptrs) mix ((uint64_t) (uintptr_t) p);
   if (m->gexec && key == m->gkey) return cuda_ok (cudaGraphLaunch (m->gexec, st), "mixed product graph");
   if (key != m->gcand)
@@ -880,6 +889,11 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       m->plan.ZF = (float *) m->img_zf.p;
       m->plan.WB = (float *) m->img_wb.p;
       m->plan.sf = (float *) m->sf.p;
+      const int wyz = (2 * m->M[1] + 1) + (2 * m->M[2] + 1);
+      if ((e = m->tyz.ensure (sizeof (float2) * (size_t) wyz * np)) != cudaSuccess)
+        return cuda_fail (e, "phase table (particle-major)");
+      m->plan.t.tyz = (const float2 *) m->tyz.p;
+      m->plan.t.wyz = wyz;
     }
   else if ((e = m->pq.ensure (sizeof (float) * 2 * C * (size_t) (m->nkh > 0 ? m->nkh : 1))) != cudaSuccess)
     return cuda_fail (e, "pq");
@@ -960,6 +974,10 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     pa.zf = m->tensor ? m->plan.ZF : nullptr;
     pa.zplane = m->plan.pZF;
     pa.kf = m->plan.KF;
+    pa.tyz = m->tensor ? (float2 *) m->tyz.p : nullptr;
+    pa.wyz = (2 * m->M[1] + 1) + (2 * m->M[2] + 1);
+    pa.M1 = m->M[1];
+    pa.M2 = m->M[2];
     mk_prep<<<dim3 ((np + PREP_P - 1) / PREP_P, (ntab + PREP_ROWS - 1) / PREP_ROWS), 128, 0, st>>> (pa);
     kmark (c, st, "mk_prep");
 
@@ -1084,7 +1102,7 @@ release_mixed (Ctx *c)
   MixedState *m = c->mixed;
   for (DevBuf *b : {&m->kt, &m->qpos, &m->tab, &m->xf, &m->pq, &m->part_real, &m->part_rec,
                     &m->selfbuf, &m->status, &m->sf, &m->rowm, &m->rot, &m->img_zf,
-                    &m->img_wb})
+                    &m->img_wb, &m->tyz})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
   if (m->gexec) cudaGraphExecDestroy (m->gexec);

@@ -28,6 +28,11 @@ struct PhaseTables {
   int np;
   const uint4 *qpos;
   const float4 *rot;
+  // particle-major y and z phases for both signs of m: tyz[j wyz + M1 + m2]
+  // = e^{2 pi i m2 u_y(j)}, tyz[j wyz + (2 M1 + 1) + M2 + m3] = e^{2 pi i m3
+  // u_z(j)}, wyz = (2 M1 + 1) + (2 M2 + 1)
+  const float2 *tyz;
+  int wyz;
 };
 
 // e^{2 pi i p / 2^32} to FP32 accuracy from a fixed-point phase p (turns x
