@@ -187,6 +187,46 @@ def bd_measure(lib, abi, L, torch, dev):
                                          "rmin")}}
 
 
+def matrix_measure(lib, abi, L, torch, dev, pos, Lbox):
+    """Dense FTS mobility matrix of the bench workload (N = 1000, 11000 x
+    11000 FP64 = 968 MB) at the reference split, on device memory: device
+    time (CUDA events on the builder's stream, after one warm-up build) and
+    the achieved store bandwidth, against the measured HBM copy rate.  The
+    builder evaluates the same pair-image terms as the FP64 product, 121
+    tensor entries each, so its FP64 pipe, not HBM, bounds it."""
+    w = WORKLOAD
+    s = L.System(w["version"], pos, (Lbox,) * 3, tratio=w["tratio"], eps=w["eps"])
+    n = (3, 6, 11)[w["version"]] * w["n"]
+    d_pos = torch.tensor(pos, dtype=torch.float64, device=dev).contiguous()
+    d_mat = torch.empty((n, n), dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(st.cuda_stream)
+    abi.check(lib.stokes_gpu_matrix_dev(s.sp, C.c_void_p(d_pos.data_ptr()),
+                                        C.c_void_p(d_mat.data_ptr()), sp))
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    abi.check(lib.stokes_gpu_matrix_dev(s.sp, C.c_void_p(d_pos.data_ptr()),
+                                        C.c_void_p(d_mat.data_ptr()), sp))
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    nbytes = 8.0 * n * n
+    peak = measured_peaks().get("hbm_gbs")
+    P = C.c_longlong()
+    abi.check(lib.stokes_gpu_count_real_terms(s.sp, C.byref(P)))
+    s.close()
+    del d_mat
+    torch.cuda.empty_cache()
+    gbs = nbytes / (ms * 1e-3) / 1e9
+    return {"workload": f"matrix_fts_n{w['n']}_phi{w['phi']:.2f}", "precision": "fp64",
+            "ms": ms, "bytes": nbytes, "achieved_gbs": gbs, "hbm_peak_gbs": peak,
+            "hbm_frac": gbs / peak if peak else None,
+            "pair_image_terms": P.value, "terms_per_s": P.value / (ms * 1e-3),
+            "bound": "fp64-pipe: every pair-image term of the reference split "
+                     "(xi = sqrt(pi)/L, eps 1e-12) builds an 11 x 11 block in FP64"}
+
+
 ADJ_WORKLOAD = dict(name="vjp_ft_n2048_phi0.25", version=1, n=2048, phi=0.25, seed=42)
 
 
@@ -564,6 +604,8 @@ def run_gpu(args):
         fp64_ms = e0.elapsed_time(e1) / 3
         line["fp64_path"] = {"value": 1000.0 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
                              "mixed_over_fp64": (1000.0 / ms) / (1000.0 / fp64_ms)}
+    if not args.no_matrix:
+        line["matrix"] = matrix_measure(lib, abi, L, torch, dev, pos, Lbox)
     if not args.no_bd:
         line["bd"] = bd_measure(lib, abi, L, torch, dev)
     if not args.no_adjoint:
@@ -591,6 +633,7 @@ def main():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (VJP) leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the ensemble (batch) leg")
+    ap.add_argument("--no-matrix", action="store_true", help="skip the dense-builder leg")
     ap.add_argument("--n", type=int, default=None,
                     help="override N (smaller cases for profiler captures)")
     args = ap.parse_args()

@@ -654,7 +654,12 @@ stokes_gpu_get_precision (const struct stokes *sys, int *mode)
   return STOKES_GPU_OK;
 }
 
-int stokes_gpu_release (struct stokes *sys) { return release_ctx (sys); }
+int
+stokes_gpu_release (struct stokes *sys)
+{
+  release_adjoint (sys);
+  return release_ctx (sys);
+}
 
 int
 stokes_gpu_atimes (struct stokes *sys, const double *x, double *y)

@@ -80,6 +80,9 @@ int release_ctx (const struct stokes *sys);
 // builder, the adjoint), 0 skips them (the mixed product never reads them),
 // -1 chooses by the context's precision.
 int prepare (Ctx *c, const struct stokes *sys, bool cube, int tables = -1);
+
+// drops the adjoint's private copy of sys, if any (adjoint.cu)
+void release_adjoint (const struct stokes *sys);
 int atimes_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                 cudaStream_t st, bool timed);
 int atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,

@@ -52,6 +52,8 @@ struct MixedState {
   DevBuf kt, qpos, tab, xf, pq, part_real, part_rec, selfbuf, status, sf, rowm, rot;
   DevBuf img_zf, img_wb;        // GEMM B-operand images (kspace_tc.cu)
   DevBuf tyz;                   // particle-major y, z phases (the GEMMs' A operands)
+  DevBuf img;                   // real-space lattice offsets (float4)
+  int nimg = 1;
   KMaps maps;
   uint64_t img_key = 0;         // buffers and plan the maps and zeroed pads belong to
   // the real-space kernel runs on this side stream, concurrently with the
@@ -227,6 +229,8 @@ struct RealMixArgs {
   float xi, xisp;
   const float *rad, *slipa;
   float *partial;        // [nchunk][np][c]
+  const float4 *img;     // lattice offsets added to the minimum-image difference
+  int nimg;              // 1 (the zero offset) while the cutoff is below half the box
 };
 
 // minimum-image displacement r_j - r_i from fixed-point positions
@@ -304,33 +308,46 @@ mk_real (RealMixArgs a)
   for (int jb = j0; jb < j1; jb += 32)
     {
       const int j = jb + lane;
-      bool ok = false;
-      float dx = 0.f, dy = 0.f, dz = 0.f;
+      float d0x = 0.f, d0y = 0.f, d0z = 0.f;
       if (j < j1)
         {
           const uint4 qj = reinterpret_cast<const uint4 *> (a.qpos)[j];
-          min_image (a, qi, qj, dx, dy, dz);
-          const float rr = dx * dx + dy * dy + dz * dz;
-          ok = (rr > 0.f) && (rr < a.rc2);
+          min_image (a, qi, qj, d0x, d0y, d0z);
         }
-      const unsigned b = __ballot_sync (0xffffffffu, ok);
-      if (ok)
+      // the minimum image and, when the cutoff exceeds half the box, the
+      // lattice images around it
+      for (int m = 0; m < a.nimg; m++)
         {
-          const int slot = qn + __popc (b & lt);
-          s_d[wib][slot][0] = dx;
-          s_d[wib][slot][1] = dy;
-          s_d[wib][slot][2] = dz;
-          s_j[wib][slot] = j;
-        }
-      qn += __popc (b);
-      __syncwarp ();
-      if (qn >= 32)
-        {
-          const int slot = qn - 32 + lane;
-          mix_term<V, MODE> (a, i, s_j[wib][slot], s_d[wib][slot][0], s_d[wib][slot][1],
-                             s_d[wib][slot][2], ai, acc);
-          qn -= 32;
+          const float4 T = a.img[m];
+          bool ok = false;
+          float dx = 0.f, dy = 0.f, dz = 0.f;
+          if (j < j1)
+            {
+              dx = d0x + T.x;
+              dy = d0y + T.y;
+              dz = d0z + T.z;
+              const float rr = dx * dx + dy * dy + dz * dz;
+              ok = (rr > 0.f) && (rr < a.rc2);
+            }
+          const unsigned b = __ballot_sync (0xffffffffu, ok);
+          if (ok)
+            {
+              const int slot = qn + __popc (b & lt);
+              s_d[wib][slot][0] = dx;
+              s_d[wib][slot][1] = dy;
+              s_d[wib][slot][2] = dz;
+              s_j[wib][slot] = j;
+            }
+          qn += __popc (b);
           __syncwarp ();
+          if (qn >= 32)
+            {
+              const int slot = qn - 32 + lane;
+              mix_term<V, MODE> (a, i, s_j[wib][slot], s_d[wib][slot][0], s_d[wib][slot][1],
+                                 s_d[wib][slot][2], ai, acc);
+              qn -= 32;
+              __syncwarp ();
+            }
         }
     }
   if (lane < qn)
@@ -586,27 +603,80 @@ default_eta (int np)
   return 14.0;
 }
 
+// FTS: the split may take lattice images in real space.  Measured (one
+// GB300): FTS N = 256 runs 53 us at eta 7 with images against 61 us at the
+// minimum-image eta (11.2); at N = 1000 eta 8-11 all run 86 us; at N = 4096
+// eta 11 is best either way.  F and FT keep the minimum-image split (images
+// measured slower for them).
+static double
+default_eta_images (int np)
+{
+  if (np <= 256) return 7.0;
+  if (np <= 1024) return 10.0;
+  if (np <= 4096) return 11.0;
+  return 13.0;
+}
+
 // choose xi, cutoffs and the half-space k list of the mixed split
 static int
 mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
 {
   const double eps = env_double ("LIBSTOKES_GB300_MIXED_EPS", 1e-8);
-  double eta = env_double ("LIBSTOKES_GB300_MIXED_ETA", default_eta (sys->np));
-  const uint64_t fp = mix_fingerprint (sys, eta, eps);
+  const bool images = env_double ("LIBSTOKES_GB300_MIXED_IMAGES", sys->version == 2 ? 1.0 : 0.0) != 0.0;
+  double eta = env_double ("LIBSTOKES_GB300_MIXED_ETA",
+                           images ? default_eta_images (sys->np) : default_eta (sys->np));
+  const uint64_t fp = mix_fingerprint (sys, eta + (images ? 1000.0 : 0.0), eps);
   if (fp == m->fp && m->kt.p) return STOKES_GPU_OK;
 
   const double lmin = fmin (sys->lx, fmin (sys->ly, sys->lz));
   const double lmax = fmax (sys->lx, fmax (sys->ly, sys->lz));
   const double lv = cbrt (sys->lx * sys->ly * sys->lz);
-  double xi = eta / lv, rc = 0, kc = 0;
-  for (int it = 0; it < 200; it++)
+  // xi a <= 0.5 keeps the self, real and reciprocal parts of comparable size
+  // (FP32 loses digits to their cancellation when xi a grows)
+  const double XI_CAP = 0.5;
+  double xi = std::min (eta / lv, XI_CAP), rc = 0, kc = 0;
+  if (images)
+    lsg_ewald_cutoffs (xi, eps, lmin, lmax, &rc, &kc);
+  else
     {
-      lsg_ewald_cutoffs (xi, eps, lmin, lmax, &rc, &kc);
-      if (rc <= 0.4999 * lmin) break;
-      xi *= 1.03;   // the cutoff must stay below half the box (minimum image)
+      for (int it = 0; it < 200; it++)
+        {
+          lsg_ewald_cutoffs (xi, eps, lmin, lmax, &rc, &kc);
+          if (rc <= 0.4999 * lmin) break;
+          xi *= 1.03;   // the cutoff must stay below half the box (minimum image)
+        }
+      if (rc > 0.4999 * lmin)
+        return set_error (STOKES_GPU_EINVAL, "mixed split: no real-space cutoff below L/2");
     }
-  if (rc > 0.4999 * lmin)
-    return set_error (STOKES_GPU_EINVAL, "mixed split: no real-space cutoff below L/2");
+  // lattice offsets within the cutoff of a minimum-image difference (just
+  // the zero offset while the cutoff is below half the box)
+  {
+    std::vector<float4> hi;
+    const int nx = (int) ceil (rc / sys->lx + 0.5), ny = (int) ceil (rc / sys->ly + 0.5),
+              nz = (int) ceil (rc / sys->lz + 0.5);
+    for (int a1 = -nx; a1 <= nx; a1++)
+      for (int a2 = -ny; a2 <= ny; a2++)
+        for (int a3 = -nz; a3 <= nz; a3++)
+          {
+            double tx = a1 * sys->lx, ty = a2 * sys->ly, tz = a3 * sys->lz;
+            if (sys->shear_mode == 1) tx += a2 * sys->shear_shift;
+            else if (sys->shear_mode == 2) tx += a3 * sys->shear_shift;
+            // the nearest point of the offset half-box cell must be within reach
+            const double ex = std::max (0.0, fabs (tx) - 0.5 * sys->lx
+                                               - (sys->shear_mode ? fabs (sys->shear_shift) : 0.0));
+            const double ey = std::max (0.0, fabs (ty) - 0.5 * sys->ly);
+            const double ez = std::max (0.0, fabs (tz) - 0.5 * sys->lz);
+            if (ex * ex + ey * ey + ez * ez > rc * rc) continue;
+            hi.push_back (make_float4 ((float) tx, (float) ty, (float) tz, 0.f));
+          }
+    cudaError_t e = m->img.ensure (sizeof (float4) * hi.size ());
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync (m->img.p, hi.data (), sizeof (float4) * hi.size (),
+                           cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize (c->stream);
+    if (e != cudaSuccess) return cuda_fail (e, "mixed real-space images");
+    m->nimg = (int) hi.size ();
+  }
   m->xi = xi;
   m->rc = rc;
   m->kc = kc;
@@ -778,7 +848,8 @@ run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_
   mix ((uint64_t) m->nchunk_k);
   const void *ptrs[] = {d_pos, d_x, d_y, m->kt.p, m->qpos.p, m->tab.p, m->xf.p, m->pq.p,
                         m->part_real.p, m->part_rec.p, m->selfbuf.p, m->status.p, m->sf.p,
-                        m->rowm.p, m->rot.p, m->img_zf.p, m->img_wb.p, m->h_status, m->tyz.p};
+                        m->rowm.p, m->rot.p, m->img_zf.p, m->img_wb.p, m->h_status, m->tyz.p,
+                        m->img.p};
   for (const void *p : ptrs) mix ((uint64_t) (uintptr_t) p);
   if (m->gexec && key == m->gkey) return cuda_ok (cudaGraphLaunch (m->gexec, st), "mixed product graph");
   if (key != m->gcand)
@@ -1000,6 +1071,8 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     ra.xisp = (float) (m->xi / sqrt (M_PI));
     ra.rad = nullptr; ra.slipa = nullptr;
     ra.partial = (float *) m->part_real.p;
+    ra.img = (const float4 *) m->img.p;
+    ra.nimg = m->nimg;
     const int gr = (int) (((long long) np * m->nchunk_r + MX_WARPS - 1) / MX_WARPS);
     // concurrent with the reciprocal chain unless the launches are being
     // timed one by one (then in order: reciprocal, real, combine)
@@ -1102,7 +1175,7 @@ release_mixed (Ctx *c)
   MixedState *m = c->mixed;
   for (DevBuf *b : {&m->kt, &m->qpos, &m->tab, &m->xf, &m->pq, &m->part_real, &m->part_rec,
                     &m->selfbuf, &m->status, &m->sf, &m->rowm, &m->rot, &m->img_zf,
-                    &m->img_wb, &m->tyz})
+                    &m->img_wb, &m->tyz, &m->img})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
   if (m->gexec) cudaGraphExecDestroy (m->gexec);
