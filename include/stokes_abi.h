@@ -167,9 +167,8 @@ void atimes_ewald_3all (int n, const double *x, double *y, void *user_data);
  * mat[n*n], row-major, fully overwritten; FTS in the extracted form. */
 void make_matrix_mob_ewald_3all (struct stokes *sys, double *mat);
 
-/* src/ewald.c:432-447.  Periodic systems only; the open-system branch of the
- * reference (non-ewald.c) is not part of this library and is reported as an
- * error. */
+/* src/ewald.c:432-447: the Ewald operator for periodic systems, the
+ * free-space one (atimes_nonewald_3all) otherwise. */
 void atimes_3all (int n, const double *x, double *y, void *user_data);
 /* src/ewald.c:459-472 */
 void make_matrix_mob_3all (struct stokes *sys, double *mat);
@@ -182,6 +181,18 @@ void atimes_3all_matrix (int n, const double *x, double *y, void *user_data);
  * the table versions and are served by the same kernels. */
 void atimes_ewald_3all_notbl (int n, const double *x, double *y,
                               void *user_data);
+
+/* Free-space (non-periodic) Rotne-Prager-Yamakawa operator, FP64 on the
+ * device: the self term plus every pair j != i with the scalars of
+ * src/non-ewald.c:49-210 (mono, poly, slip; rmin clamp).  atimes_3all,
+ * make_matrix_mob_3all and atimes_3all_matrix dispatch here when
+ * sys->periodic is 0; the Ewald-named entry points reject such systems.
+ * src/non-ewald.c:330-475 */
+void atimes_nonewald_3all (int n, const double *x, double *y, void *user_data);
+/* src/non-ewald.c:494-666 -- dense, row-major, FTS in the extracted form */
+void make_matrix_mob_nonewald_3all (struct stokes *sys, double *mat);
+/* src/non-ewald.c:677-706 -- dense matrix, then y = mat . x */
+void atimes_nonewald_3all_matrix (int n, const double *x, double *y, void *user_data);
 void make_matrix_mob_ewald_3all_notbl (struct stokes *sys, double *mat);
 void atimes_ewald_3all_matrix_notbl (int n, const double *x, double *y,
                                      void *user_data);

@@ -21,7 +21,7 @@ extern "C" {
 enum {
   STOKES_GPU_OK = 0,
   STOKES_GPU_EINVAL = 1,      /* bad argument (n, version, NULL pointer, ...) */
-  STOKES_GPU_ENOTPERIODIC = 2,/* open systems are not served by this library */
+  STOKES_GPU_ENOTPERIODIC = 2,/* a lattice-sum entry point called on an open system */
   STOKES_GPU_ECUDA = 3,       /* a CUDA runtime call failed */
   STOKES_GPU_ENOMEM = 4,      /* device allocation failed */
   STOKES_GPU_ETIMEOUT = 5,    /* a bounded device wait ran out */
@@ -54,8 +54,9 @@ int stokes_gpu_get_precision (const struct stokes *sys, int *mode);
 /* free the device state kept for sys (stokes_free does this too) */
 int stokes_gpu_release (struct stokes *sys);
 
-/* y = M x with host buffers; the status-returning form of
- * atimes_ewald_3all */
+/* y = M x with host buffers; the status-returning form of atimes_3all:
+ * the Ewald sum of a periodic system, the free-space sum of an open one
+ * (sys->periodic == 0, which needs neither a box nor a split) */
 int stokes_gpu_atimes (struct stokes *sys, const double *x, double *y);
 
 /* y = M x with device buffers.  d_pos: positions [np*3] on the device, or

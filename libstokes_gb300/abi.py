@@ -151,6 +151,9 @@ _SIGS = {
     "atimes_ewald_3all": (None, [C.c_int, _dp, _dp, C.c_void_p]),
     "atimes_ewald_3all_notbl": (None, [C.c_int, _dp, _dp, C.c_void_p]),
     "atimes_3all": (None, [C.c_int, _dp, _dp, C.c_void_p]),
+    "atimes_nonewald_3all": (None, [C.c_int, _dp, _dp, C.c_void_p]),
+    "make_matrix_mob_nonewald_3all": (None, [_SP, _dp]),
+    "atimes_nonewald_3all_matrix": (None, [C.c_int, _dp, _dp, C.c_void_p]),
     "make_matrix_mob_ewald_3all": (None, [_SP, _dp]),
     "make_matrix_mob_ewald_3all_notbl": (None, [_SP, _dp]),
     "make_matrix_mob_3all": (None, [_SP, _dp]),
@@ -313,7 +316,10 @@ def check(rc: int):
 class System:
     """One struct stokes built through the library's own set-up calls."""
 
-    def __init__(self, version: int, pos, box, xi=None, eps=1e-12, tratio=1.0):
+    def __init__(self, version: int, pos, box=None, xi=None, eps=1e-12, tratio=1.0,
+                 periodic=True):
+        """periodic=False builds an open system (src/stokes.c:339: the
+        default of stokes_init) with neither a box nor a split."""
         self.lib = load()
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
         self.version = int(version)
@@ -323,12 +329,15 @@ class System:
         s.version = self.version
         self.lib.stokes_set_np(self.sp, self.np, self.np)
         self.lib.stokes_set_pos(self.sp, _d(pos))
+        self._keep = []
+        if not periodic:
+            s.periodic = 0
+            return
         s.periodic = 1
         self.lib.stokes_set_l(self.sp, *[float(b) for b in box])
         if xi is None:
             xi = self.lib.xi_by_tratio(self.sp, float(tratio))
         self.lib.stokes_set_xi(self.sp, float(xi), float(eps))
-        self._keep = []
 
     def close(self):
         if getattr(self, "sp", None):
@@ -443,6 +452,39 @@ class System:
         f(self.n, _d(x), _d(y), C.cast(self.sp, C.c_void_p))
         raise_if_failed()
         return y
+
+    # the dispatchers (src/ewald.c:433-505) and the free-space operator
+    # (src/non-ewald.c:330-706)
+    def atimes_3all(self, x):
+        return self._vec(self.lib.atimes_3all, x)
+
+    def atimes_3all_matrix(self, x):
+        return self._vec(self.lib.atimes_3all_matrix, x)
+
+    def matrix_3all(self):
+        return self._mat(self.lib.make_matrix_mob_3all)
+
+    def atimes_nonewald(self, x):
+        return self._vec(self.lib.atimes_nonewald_3all, x)
+
+    def atimes_nonewald_matrix(self, x):
+        return self._vec(self.lib.atimes_nonewald_3all_matrix, x)
+
+    def matrix_nonewald(self):
+        return self._mat(self.lib.make_matrix_mob_nonewald_3all)
+
+    def _vec(self, f, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.n)
+        f(self.n, _d(x), _d(y), C.cast(self.sp, C.c_void_p))
+        raise_if_failed()
+        return y
+
+    def _mat(self, f):
+        m = np.empty((self.n, self.n))
+        f(self.sp, _d(m))
+        raise_if_failed()
+        return m
 
     def times(self):
         out = np.zeros(3)

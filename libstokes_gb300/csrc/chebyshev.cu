@@ -123,9 +123,14 @@ chebyshev_eval_ (int ncheb, const double *a, double x0, double x1, double x)
 static bool
 is_device_operator (void (*atimes) (int, const double *, double *, void *), void *user_data)
 {
-  if (atimes != atimes_ewald_3all && atimes != atimes_3all) return false;
+  // the operator the device evaluates for this system: the Ewald sum of a
+  // periodic system, the free-space sum of an open one, or the dispatcher
   const struct stokes *sys = (const struct stokes *) user_data;
-  return sys != nullptr && sys->periodic != 0;
+  if (sys == nullptr) return false;
+  if (atimes == atimes_3all) return true;
+  if (atimes == atimes_ewald_3all) return sys->periodic != 0;
+  if (atimes == atimes_nonewald_3all) return sys->periodic == 0;
+  return false;
 }
 
 // z = sum_k a_k T_k(M~) y by Clenshaw (src/chebyshev.c:163-228)

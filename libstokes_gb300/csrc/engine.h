@@ -39,6 +39,7 @@ struct RealArgs {
   const double *rad;    // radii (or 1) [np], NULL for equal spheres
   const double *slipa;  // slip-effective radii [np] (slip mode)
   double *partial;      // [nchunk][np][c]
+  int open = 0;         // non-periodic: free-space scalars (src/non-ewald.c)
 };
 
 struct RecipArgs {
@@ -62,6 +63,7 @@ struct MatArgs {
   const double *kt;
   const double2 *ph;
   double *mat;
+  int open = 0;         // non-periodic: free-space scalars (src/non-ewald.c)
 };
 
 cudaError_t launch_real_fp64 (int version, int mode, const RealArgs &a, cudaStream_t st);

@@ -197,6 +197,36 @@ template <int V, typename R> struct GenU {
   }
 };
 
+// Free-space (non-periodic) Rotne-Prager-Yamakawa mobility scalars of a pair
+// at distance r, for radii aa (target) and ab (source), in the SD form scaled
+// by the target's radius a1: the functions of src/non-ewald.c:110-152 scaled
+// as src/non-ewald.c:172-210.  Equal spheres are aa = ab = a1 = 1, which
+// reduces exactly to src/non-ewald.c:49-108; with slip, aa and ab are the
+// slip-effective radii and a1 the real one (src/non-ewald.c:443-456).
+template <int V, typename R>
+__device__ __forceinline__ void
+open_scalars (R r, R aa, R ab, R a1, PairScalars<R> &s)
+{
+  const R ri = R (1) / r, r2i = ri * ri;
+  const R s2 = aa * aa + ab * ab;
+  s.xa = (R (1.5) - R (0.5) * s2 * r2i) * ri * a1;
+  s.ya = (R (0.75) + R (0.25) * s2 * r2i) * ri * a1;
+  s.yb = s.xc = s.yc = s.xg = s.yg = s.yh = s.xm = s.ym = s.zm = R (0);
+  if (V == V_F) return;
+  const R a12 = a1 * a1, a13 = a12 * a1;
+  s.yb = R (-0.75) * r2i * a12;
+  s.xc = R (0.75) * r2i * ri * a13;
+  s.yc = R (-0.375) * r2i * ri * a13;
+  if (V == V_FT) return;
+  const R q = aa * aa / R (10) + ab * ab / R (6);
+  s.xg = (R (2.25) - R (13.5) * q * r2i) * r2i * a12;
+  s.yg = R (4.5) * q * r2i * r2i * a12;
+  s.yh = R (-1.125) * r2i * ri * a13;
+  s.xm = (R (-4.5) + R (5.4) * s2 * r2i) * r2i * ri * a13;
+  s.ym = (R (2.25) - R (3.6) * s2 * r2i) * r2i * ri * a13;
+  s.zm = R (0.9) * s2 * r2i * r2i * ri * a13;
+}
+
 // y_i += block(e, s) . x_j for one real-space (or self) term, in vector form.
 // The block is the non-self one used by the matrix-free product
 // (src/f.c:115-147, src/ft.c:179-267, src/fts.c:626-1023).

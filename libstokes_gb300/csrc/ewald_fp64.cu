@@ -37,7 +37,13 @@ real_term (const RealArgs &a, int i, int j, double dx, double dy, double dz,
   const double ri = 1.0 / r;
   const double e[3] = {dx * ri, dy * ri, dz * ri};
   PairScalars<double> s;
-  if (MODE == MODE_MONO)
+  if (a.open)
+    {
+      if (MODE == MODE_MONO) open_scalars<V, double> (r, 1.0, 1.0, 1.0, s);
+      else if (MODE == MODE_POLY) open_scalars<V, double> (r, ai, aj, ai, s);
+      else open_scalars<V, double> (r, a.slipa[i], a.slipa[j], ai, s);
+    }
+  else if (MODE == MODE_MONO)
     real_scalars_mono<V, double> (a.xi, a.xisp, r, s);
   else if (MODE == MODE_POLY)
     real_scalars_poly<V, double> (a.xi, a.xisp, r, ai, aj, ai, s);
@@ -574,7 +580,13 @@ k_matrix (MatArgs a)
     const double ri = 1.0 / r;
     const double e[3] = {dx * ri, dy * ri, dz * ri};
     PairScalars<double> s;
-    if (MODE == MODE_MONO)
+    if (a.open)
+      {
+        if (MODE == MODE_MONO) open_scalars<V, double> (r, 1.0, 1.0, 1.0, s);
+        else if (MODE == MODE_POLY) open_scalars<V, double> (r, ai, aj, ai, s);
+        else open_scalars<V, double> (r, a.slipa[i], a.slipa[j], ai, s);
+      }
+    else if (MODE == MODE_MONO)
       real_scalars_mono<V, double> (a.xi, a.xisp, r, s);
     else if (MODE == MODE_POLY)
       real_scalars_poly<V, double> (a.xi, a.xisp, r, ai, aj, ai, s);

@@ -9,12 +9,14 @@
 // own tests do (test/check-ewald.c:73-125).
 #include <cuda_runtime.h>
 
+#include <cfloat>
 #include <cmath>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <unordered_map>
 #include <vector>
@@ -157,16 +159,15 @@ release_ctx (const struct stokes *sys)
 // host-side tables
 // ---------------------------------------------------------------------------
 int
-check_sys (const struct stokes *sys)
+check_sys (const struct stokes *sys, bool open)
 {
   if (sys == nullptr) return set_error (STOKES_GPU_EINVAL, "struct stokes is NULL");
-  if (sys->periodic == 0)
-    return set_error (STOKES_GPU_ENOTPERIODIC,
-                      "open (non-periodic) systems are not served by libstokes_gb300");
   if (sys->version < 0 || sys->version > 2)
     return set_error (STOKES_GPU_EINVAL, "invalid version %d", sys->version);
   if (sys->np <= 0 || sys->pos == nullptr)
     return set_error (STOKES_GPU_EINVAL, "no particles (np = %d)", sys->np);
+  // the free-space operator needs neither a box nor a split
+  if (open) return STOKES_GPU_OK;
   if (!(sys->lx > 0.0 && sys->ly > 0.0 && sys->lz > 0.0))
     return set_error (STOKES_GPU_EINVAL, "box size not set");
   if (sys->xi <= 0.0) return set_error (STOKES_GPU_EINVAL, "Ewald xi not set");
@@ -250,7 +251,7 @@ build_ktable (const struct stokes *sys, std::vector<double> &kt)
 // per-particle arrays: radii (1 when a == NULL), slip radii, squared
 // Laplacian radii, and self scalars (src/ewald.c:540-643)
 void
-build_particles (const struct stokes *sys, int mode, std::vector<double> &pp)
+build_particles (const struct stokes *sys, int mode, std::vector<double> &pp, bool open)
 {
   const int np = sys->np;
   pp.assign ((size_t) 6 * np, 0.0);
@@ -262,7 +263,13 @@ build_particles (const struct stokes *sys, int mode, std::vector<double> &pp)
       slipa[i] = sys->slip ? sys->slip_a[i] : a;
       qa[i] = (mode == MODE_SLIP) ? slipa[i] * slipa[i] : a * a;
       double sa, sc, sm;
-      if (mode == MODE_MONO)
+      if (open)
+        {
+          // free-space self terms (src/non-ewald.c:344-358), slip factors
+          sa = 1.0; sc = 0.75; sm = 0.9;
+          if (sys->slip) { sa *= sys->slip_G32[i]; sc *= sys->slip_G30[i]; sm *= sys->slip_G52[i]; }
+        }
+      else if (mode == MODE_MONO)
         { sa = sys->self_a; sc = sys->self_c; sm = sys->self_m; }
       else
         {
@@ -302,9 +309,10 @@ upload_if_changed (DevBuf &buf, uint64_t &fp, const void *host, size_t bytes,
 int
 prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
 {
-  int rc = check_sys (sys);
+  int rc = check_sys (sys, sys && (sys->periodic == 0 || c->force_open));
   if (rc) return rc;
-  if (!cube && (sys->nr > 0) && (!sys->rlx || !sys->rly || !sys->rlz))
+  c->open = sys->periodic == 0 || c->force_open;
+  if (!c->open && !cube && (sys->nr > 0) && (!sys->rlx || !sys->rly || !sys->rlz))
     return set_error (STOKES_GPU_EINVAL, "image table missing (stokes_set_xi not called?)");
   c->sys = sys;
   c->version = sys->version;
@@ -314,28 +322,42 @@ prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
   c->xisp = sys->xi / sqrt (M_PI);
   c->rmax2 = sys->rmax2;
   c->rmin = sys->rmin;
+  if (c->open)
+    {
+      // every pair, once, in free space: one zero image, no cutoff, no k
+      c->xi = c->xisp = 0.0;
+      c->rmax2 = DBL_MAX;
+    }
 
-  if (tables < 0) tables = c->precision == STOKES_GPU_MIXED ? 0 : 1;
+  // the free-space operator has no reciprocal part: it runs in FP64 whatever
+  // the precision mode says
+  if (tables < 0) tables = c->precision == STOKES_GPU_MIXED && !c->open ? 0 : 1;
   if (!tables)
     {
       // the particle table only (radii for the BD interactions); equal
       // spheres without slip need none
       if (c->mode == MODE_MONO) return STOKES_GPU_OK;
-      build_particles (sys, c->mode, c->h_pp);
+      build_particles (sys, c->mode, c->h_pp, c->open);
       return upload_if_changed (c->pp, c->fp_pp, c->h_pp.data (), sizeof (double) * c->h_pp.size (),
                                 c->stream, "particle table");
     }
-  build_images (sys, cube, c->h_img);
+  if (c->open)
+    c->h_img.assign (1, Img4 {0.0, 0.0, 0.0, 0.0});
+  else
+    build_images (sys, cube, c->h_img);
   c->nimg = (int) c->h_img.size ();
   rc = upload_if_changed (c->img, c->fp_img, c->h_img.data (), sizeof (Img4) * c->h_img.size (),
                           c->stream, "image table");
   if (rc) return rc;
-  build_ktable (sys, c->h_kt);
+  if (c->open)
+    c->h_kt.clear ();
+  else
+    build_ktable (sys, c->h_kt);
   c->nk = (int) (c->h_kt.size () / KT_STRIDE);
   rc = upload_if_changed (c->kt, c->fp_kt, c->h_kt.data (), sizeof (double) * c->h_kt.size (),
                           c->stream, "reciprocal table");
   if (rc) return rc;
-  build_particles (sys, c->mode, c->h_pp);
+  build_particles (sys, c->mode, c->h_pp, c->open);
   rc = upload_if_changed (c->pp, c->fp_pp, c->h_pp.data (), sizeof (double) * c->h_pp.size (),
                           c->stream, "particle table");
   if (rc) return rc;
@@ -420,6 +442,7 @@ atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   a.rad = rad;
   a.slipa = slipa;
   a.partial = (double *) c->partial.p;
+  a.open = c->open ? 1 : 0;
   if ((e = launch_real_fp64 (c->version, c->mode, a, st)) != cudaSuccess)
     return cuda_fail (e, "real-space kernel");
   launches++;
@@ -476,7 +499,7 @@ int
 atimes_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y, cudaStream_t st,
             bool timed)
 {
-  if (c->precision == STOKES_GPU_MIXED)
+  if (c->precision == STOKES_GPU_MIXED && !c->open)
     return atimes_mixed_dev (c, d_pos, d_x, d_y, st, timed);
   return atimes_fp64_dev (c, d_pos, d_x, d_y, st, timed);
 }
@@ -517,7 +540,7 @@ atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
 int
 matrix_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st)
 {
-  if (c->precision == STOKES_GPU_MIXED)
+  if (c->precision == STOKES_GPU_MIXED && !c->open)
     return matrix_mixed_dev (c, d_pos, d_mat, st);
   const int np = c->np;
   cudaError_t e;
@@ -551,6 +574,7 @@ matrix_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st)
   a.kt = (const double *) c->kt.p;
   a.ph = (const double2 *) c->ph.p;
   a.mat = d_mat;
+  a.open = c->open ? 1 : 0;
   if ((e = launch_matrix_fp64 (c->version, c->mode, a, st)) != cudaSuccess)
     return cuda_fail (e, "matrix kernel");
   kmark (c, st, "k_matrix");
@@ -855,6 +879,17 @@ stokes_gpu_last_launches (const struct stokes *sys, int *count)
 
 // ---- drop-in replacements of src/ewald.c ----------------------------------
 
+// the Ewald-named entry points evaluate lattice sums: periodic systems only
+static int
+need_periodic (const struct stokes *sys, const char *fn)
+{
+  if (sys && sys->periodic == 0)
+    return set_error (STOKES_GPU_ENOTPERIODIC,
+                      "%s: the system is not periodic (the free-space operator is "
+                      "atimes_nonewald_3all)", fn);
+  return STOKES_GPU_OK;
+}
+
 static int
 check_n (const struct stokes *sys, int n)
 {
@@ -872,7 +907,7 @@ void
 atimes_ewald_3all (int n, const double *x, double *y, void *user_data)
 {
   struct stokes *sys = (struct stokes *) user_data;
-  if (check_n (sys, n) || atimes_host (sys, x, y, false))
+  if (check_n (sys, n) || need_periodic (sys, "atimes_ewald_3all") || atimes_host (sys, x, y, false))
     dropin_failed ("atimes_ewald_3all", y, n > 0 ? (size_t) n : 0);
 }
 
@@ -880,7 +915,8 @@ void
 atimes_ewald_3all_notbl (int n, const double *x, double *y, void *user_data)
 {
   struct stokes *sys = (struct stokes *) user_data;
-  if (check_n (sys, n) || atimes_host (sys, x, y, true))
+  if (check_n (sys, n) || need_periodic (sys, "atimes_ewald_3all_notbl")
+      || atimes_host (sys, x, y, true))
     dropin_failed ("atimes_ewald_3all_notbl", y, n > 0 ? (size_t) n : 0);
 }
 
@@ -895,7 +931,7 @@ atimes_3all (int n, const double *x, double *y, void *user_data)
 void
 make_matrix_mob_ewald_3all (struct stokes *sys, double *mat)
 {
-  if (matrix_host (sys, mat, false))
+  if (need_periodic (sys, "make_matrix_mob_ewald_3all") || matrix_host (sys, mat, false))
     {
       size_t n = sys && sys->version >= 0 && sys->version <= 2
         ? (size_t) NCOMP (sys->version) * (sys->np > 0 ? sys->np : 0) : 0;
@@ -906,7 +942,7 @@ make_matrix_mob_ewald_3all (struct stokes *sys, double *mat)
 void
 make_matrix_mob_ewald_3all_notbl (struct stokes *sys, double *mat)
 {
-  if (matrix_host (sys, mat, true))
+  if (need_periodic (sys, "make_matrix_mob_ewald_3all_notbl") || matrix_host (sys, mat, true))
     {
       size_t n = sys && sys->version >= 0 && sys->version <= 2
         ? (size_t) NCOMP (sys->version) * (sys->np > 0 ? sys->np : 0) : 0;
@@ -937,8 +973,49 @@ void
 atimes_ewald_3all_matrix_notbl (int n, const double *x, double *y, void *user_data)
 {
   struct stokes *sys = (struct stokes *) user_data;
-  if (check_n (sys, n) || atimes_matrix_host (sys, x, y, true))
+  if (check_n (sys, n) || need_periodic (sys, "atimes_ewald_3all_matrix_notbl")
+      || atimes_matrix_host (sys, x, y, true))
     dropin_failed ("atimes_ewald_3all_matrix_notbl", y, n > 0 ? (size_t) n : 0);
+}
+
+// the free-space (non-periodic) operator, whatever sys->periodic says
+// (src/non-ewald.c:330-706): the forced-open context around the common path
+static int
+open_call (struct stokes *sys, const std::function<int ()> &f)
+{
+  Ctx *c = sys ? get_ctx (sys, true) : nullptr;
+  if (!c) return set_error (sys ? STOKES_GPU_ECUDA : STOKES_GPU_EINVAL, "no context");
+  c->force_open = true;
+  const int rc = f ();
+  c->force_open = false;
+  return rc;
+}
+
+void
+atimes_nonewald_3all (int n, const double *x, double *y, void *user_data)
+{
+  struct stokes *sys = (struct stokes *) user_data;
+  if (check_n (sys, n) || open_call (sys, [&] { return atimes_host (sys, x, y, false); }))
+    dropin_failed ("atimes_nonewald_3all", y, n > 0 ? (size_t) n : 0);
+}
+
+void
+make_matrix_mob_nonewald_3all (struct stokes *sys, double *mat)
+{
+  if (open_call (sys, [&] { return matrix_host (sys, mat, false); }))
+    {
+      size_t n = sys && sys->version >= 0 && sys->version <= 2
+        ? (size_t) NCOMP (sys->version) * (sys->np > 0 ? sys->np : 0) : 0;
+      dropin_failed ("make_matrix_mob_nonewald_3all", mat, n * n);
+    }
+}
+
+void
+atimes_nonewald_3all_matrix (int n, const double *x, double *y, void *user_data)
+{
+  struct stokes *sys = (struct stokes *) user_data;
+  if (check_n (sys, n) || open_call (sys, [&] { return atimes_matrix_host (sys, x, y, false); }))
+    dropin_failed ("atimes_nonewald_3all_matrix", y, n > 0 ? (size_t) n : 0);
 }
 
 }  // extern "C"

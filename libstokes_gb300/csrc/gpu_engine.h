@@ -51,6 +51,9 @@ struct Ctx {
   // kernel profiling window: one event after each launch, tagged with the
   // kernel's name (nullptr marks the start of a product)
   bool kprof_on = false;
+  // non-periodic (free-space) operator: set for systems with periodic = 0 and
+  // by the *_nonewald_* entry points (force_open), src/non-ewald.c
+  bool open = false, force_open = false;
   size_t kprof_n = 0;
   std::vector<cudaEvent_t> kprof_ev;
   std::vector<const char *> kprof_name;
@@ -70,10 +73,11 @@ void dropin_failed (const char *fn, double *out, size_t nout);
 
 Ctx *get_ctx (const struct stokes *sys, bool create);
 // host tables of one system (gpu_engine.cu)
-int check_sys (const struct stokes *sys);
+int check_sys (const struct stokes *sys, bool open = false);
 void build_images (const struct stokes *sys, bool cube, std::vector<Img4> &img);
 void build_ktable (const struct stokes *sys, std::vector<double> &kt);
-void build_particles (const struct stokes *sys, int mode, std::vector<double> &pp);
+void build_particles (const struct stokes *sys, int mode, std::vector<double> &pp,
+                      bool open = false);
 int release_ctx (const struct stokes *sys);
 // check sys and bring the context's device tables up to date.  tables: 1
 // builds the FP64 image and reciprocal tables (the FP64 product, the dense

@@ -898,6 +898,9 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   if (c->mode != MODE_MONO)
     return set_error (STOKES_GPU_EINVAL,
                       "mixed precision serves equal spheres without slip; use STOKES_GPU_FP64");
+  if (c->open)
+    return set_error (STOKES_GPU_EINVAL,
+                      "mixed precision serves periodic systems; the free-space operator runs in FP64");
   if (!c->mixed) c->mixed = new MixedState ();
   MixedState *m = c->mixed;
   const struct stokes *sys = c->sys;

@@ -202,7 +202,7 @@ stokes_gpu_atimes_noalloc (struct stokes *sys, const double *d_pos, const double
   if (sys == nullptr) return set_error (STOKES_GPU_EINVAL, "struct stokes is NULL");
   if (!d_pos || !d_x || !d_y) return set_error (STOKES_GPU_EINVAL, "NULL device pointer");
   if (sys->periodic == 0)
-    return set_error (STOKES_GPU_ENOTPERIODIC, "open systems are not served by libstokes_gb300");
+    return set_error (STOKES_GPU_ENOTPERIODIC, "this entry point serves periodic systems");
   if (sys->version < 0 || sys->version > 2)
     return set_error (STOKES_GPU_EINVAL, "invalid version %d", sys->version);
   if (sys->np <= 0) return set_error (STOKES_GPU_EINVAL, "no particles");

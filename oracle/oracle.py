@@ -89,6 +89,8 @@ class _Backend:
                 "atimes": (None, [C.c_void_p, _dp, _dp]),
                 "matrix": (None, [C.c_void_p, _dp]),
                 "matvec": (None, [C.c_int, C.c_int, _dp, _dp, _dp]),
+                "atimes_nonewald": (None, [C.c_void_p, _dp, _dp]),
+                "matrix_nonewald": (None, [C.c_void_p, _dp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(lib, p + name)
@@ -186,6 +188,18 @@ class _Backend:
     def matrix(self):
         m = np.zeros((self.n, self.n))
         self._f("matrix")(self.h, _d(m))
+        return m
+
+    def atimes_nonewald(self, x):
+        """y = M x of the free-space operator (no periodic images)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.n)
+        self._f("atimes_nonewald")(self.h, _d(x), _d(y))
+        return y
+
+    def matrix_nonewald(self):
+        m = np.zeros((self.n, self.n))
+        self._f("matrix_nonewald")(self.h, _d(m))
         return m
 
     def matvec(self, mat, x):

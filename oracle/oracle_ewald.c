@@ -982,6 +982,119 @@ oracle_matrix (void *h, double *mat)
   free (kt);
 }
 
+/* free-space (non-periodic) Rotne-Prager-Yamakawa scalars at distance r for
+ * radii aa, ab in dimensional form (src/non-ewald.c:49-152; equal spheres
+ * are aa = ab = 1) */
+static void
+scalars_open (int version, double r, double aa, double ab, double *sc)
+{
+  for (int q = 0; q < NSC; q++) sc[q] = 0.0;
+  double r2 = r * r, s2 = aa * aa + ab * ab;
+  sc[XA] = (1.5 - 0.5 * s2 / r2) / r;
+  sc[YA] = (0.75 + 0.25 * s2 / r2) / r;
+  if (version == 0) return;
+  sc[YB] = -0.75 / r2;
+  sc[XC] = 0.75 / r2 / r;
+  sc[YC] = -0.375 / r2 / r;
+  if (version == 1) return;
+  double q = aa * aa / 10.0 + ab * ab / 6.0;
+  sc[XG] = (2.25 - 13.5 * q / r2) / r2;
+  sc[YG] = 4.5 * q / r2 / r2;
+  sc[YH] = -1.125 / r2 / r;
+  sc[XM] = (-4.5 + 5.4 * s2 / r2) / r2 / r;
+  sc[YM] = (2.25 - 3.6 * s2 / r2) / r2 / r;
+  sc[ZM] = 0.9 * s2 / r2 / r2 / r;
+}
+
+/* self and pair scalars of the free-space operator (src/non-ewald.c:344-471):
+ * self 1, 3/4, 9/10 (times the slip factors); pairs in the SD form scaled by
+ * the target's radius, with the slip-effective radii under slip */
+static void
+open_self (const osys *s, int i, double *sc)
+{
+  for (int q = 0; q < NSC; q++) sc[q] = 0.0;
+  double fa = 1.0, fc = 1.0, fm = 1.0;
+  if (s->slip != NULL) { fa = s->slip_G32[i]; fc = s->slip_G30[i]; fm = s->slip_G52[i]; }
+  sc[XA] = sc[YA] = 1.0 * fa;
+  sc[XC] = sc[YC] = 0.75 * fc;
+  sc[XM] = sc[YM] = sc[ZM] = 0.9 * fm;
+}
+
+static void
+open_pair (const osys *s, int i, int j, double r, double *sc)
+{
+  if (s->a == NULL && s->slip == NULL)
+    {
+      scalars_open (s->version, r, 1.0, 1.0, sc);
+      return;
+    }
+  if (s->slip == NULL)
+    scalars_open (s->version, r, s->a[i], s->a[j], sc);
+  else
+    scalars_open (s->version, r, s->slip_a[i], s->slip_a[j], sc);
+  scale_sd (s->version, rad (s, i), sc);
+}
+
+/* y = M x of the free-space operator: every pair j != i once, positions as
+ * given (no periodic images), rmin clamp (src/non-ewald.c:330-475) */
+void
+oracle_atimes_nonewald (void *h, const double *x, double *y)
+{
+  osys *s = h;
+  int c = ncomp (s->version), np = s->np;
+  memset (y, 0, sizeof (double) * (size_t) c * np);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(s->nthreads)
+  for (int i = 0; i < np; i++)
+    {
+      double sc[NSC], e[3], e0[3] = {0, 0, 0};
+      double *yi = y + c * i;
+      open_self (s, i, sc);
+      pair_vec (s->version, e0, sc, x + c * i, yi);
+      double ai = rad (s, i);
+      for (int j = 0; j < np; j++)
+        {
+          if (j == i) continue;
+          double d[3] = {s->pos[3 * j] - s->pos[3 * i], s->pos[3 * j + 1] - s->pos[3 * i + 1],
+                         s->pos[3 * j + 2] - s->pos[3 * i + 2]};
+          double r = sqrt (dot3 (d, d));
+          double rm = (ai + rad (s, j)) * s->rmin;
+          if (r < rm) r = rm;
+          e[0] = d[0] / r; e[1] = d[1] / r; e[2] = d[2] / r;
+          open_pair (s, i, j, r, sc);
+          pair_vec (s->version, e, sc, x + c * j, yi);
+        }
+    }
+}
+
+/* dense free-space matrix, extracted form (src/non-ewald.c:494-666) */
+void
+oracle_matrix_nonewald (void *h, double *mat)
+{
+  osys *s = h;
+  int c = ncomp (s->version), np = s->np, n = c * np;
+  memset (mat, 0, sizeof (double) * (size_t) n * n);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(s->nthreads)
+  for (int i = 0; i < np; i++)
+    {
+      double sc[NSC], e[3], e0[3] = {0, 0, 0};
+      open_self (s, i, sc);
+      pair_mat (s->version, 1, e0, sc, mat + (size_t) (c * i) * n + c * i, n);
+      double ai = rad (s, i);
+      for (int j = 0; j < np; j++)
+        {
+          if (j == i) continue;
+          double d[3] = {s->pos[3 * j] - s->pos[3 * i], s->pos[3 * j + 1] - s->pos[3 * i + 1],
+                         s->pos[3 * j + 2] - s->pos[3 * i + 2]};
+          double r = sqrt (dot3 (d, d));
+          double rm = (ai + rad (s, j)) * s->rmin;
+          if (r < rm) r = rm;
+          e[0] = d[0] / r; e[1] = d[1] / r; e[2] = d[2] / r;
+          open_pair (s, i, j, r, sc);
+          pair_mat (s->version, 0, e, sc, mat + (size_t) (c * i) * n + c * j, n);
+        }
+    }
+}
+
 /* extracted-form FTS product (src/matrix.c:447-478) and plain GEMV */
 void
 oracle_matvec (int version, int np, const double *mat, const double *x, double *y)

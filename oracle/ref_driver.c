@@ -14,6 +14,7 @@
 #include <string.h>
 #include "stokes.h"
 #include "ewald.h"
+#include "non-ewald.h"
 #include "matrix.h"
 #include "chebyshev.h"
 #include "libiter.h"
@@ -140,6 +141,18 @@ void ref_matrix_notbl (void *h, double *mat)
 {
   make_matrix_mob_ewald_3all_notbl (h, mat);
 }
+
+/* the free-space operator (src/non-ewald.c); periodic is cleared as the
+ * reference's own dispatcher atimes_3all would require */
+void
+ref_atimes_nonewald (void *h, const double *x, double *y)
+{
+  struct stokes *s = h;
+  int c = s->version == 0 ? 3 : (s->version == 1 ? 6 : 11);
+  atimes_nonewald_3all (c * s->np, x, y, s);
+}
+
+void ref_matrix_nonewald (void *h, double *mat) { make_matrix_mob_nonewald_3all (h, mat); }
 
 void
 ref_matvec (int version, int np, const double *mat, const double *x, double *y)

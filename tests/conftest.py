@@ -61,6 +61,44 @@ def products():
 
 
 @pytest.fixture(scope="session")
+def nonewald():
+    """Free-space cases: name -> {meta [version, rmin], pos, x, y, mat, a, slip}."""
+    z = np.load(os.path.join(GOLDEN, "nonewald.npz"))
+    cases = {}
+    for key in z.files:
+        name, field = key.split("/")
+        cases.setdefault(name, {})[field] = z[key]
+    return cases
+
+
+def make_open_oracle(case: dict):
+    from oracle.oracle import Oracle
+    o = Oracle(int(case["meta"][0]), case["pos"], (1.0, 1.0, 1.0))
+    if "a" in case:
+        o.set_radius(case["a"])
+    if "slip" in case:
+        o.set_slip(case["slip"])
+    o.set_misc(float(case["meta"][1]), 0, 0.0)
+    return o
+
+
+def make_open_system(case: dict, periodic=False):
+    """An open system as stokes_init leaves it (periodic = 0, no box, no
+    split); periodic=True gives the same particles in a box instead."""
+    from libstokes_gb300 import System
+    if periodic:
+        s = System(int(case["meta"][0]), case["pos"], (30.0, 31.0, 32.0))
+    else:
+        s = System(int(case["meta"][0]), case["pos"], periodic=False)
+    if "a" in case:
+        s.set_radius(case["a"])
+    if "slip" in case:
+        s.set_slip(case["slip"])
+    s.set_misc(float(case["meta"][1]))
+    return s
+
+
+@pytest.fixture(scope="session")
 def setup_golden():
     return np.load(os.path.join(GOLDEN, "setup.npz"))
 

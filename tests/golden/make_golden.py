@@ -192,6 +192,50 @@ def bd_fixtures() -> dict:
     return out
 
 
+def nonewald_fixtures() -> dict:
+    """The free-space operator (src/non-ewald.c): products and dense
+    matrices of the reference for every branch, the two-sphere layout of
+    test/check-minv.c:412-515 and a larger product."""
+    out = {}
+    rng = np.random.default_rng(2025)
+    N = 12
+    pos = rng.uniform(0.0, 1.0, (N, 3)) * np.array([8.0, 9.0, 10.0])
+    arad = rng.uniform(0.5, 1.5, N)
+    aslip_r = rng.uniform(0.7, 1.3, N)
+    gslip = rng.uniform(0.0, 0.5, N)
+    cases = {"mono": {}, "poly": dict(a=arad), "slip": dict(a=aslip_r, slip=gslip),
+             "slipmono": dict(slip=gslip), "rmin": dict(rmin=1.5)}
+    for v in (0, 1, 2):
+        for cname, kw in cases.items():
+            name = f"r12_v{v}_{cname}"
+            r = mk(v, pos, (8.0, 9.0, 10.0), **kw)
+            out[f"{name}/meta"] = np.array([v, kw.get("rmin", 0.0)])
+            out[f"{name}/pos"] = pos
+            if "a" in kw:
+                out[f"{name}/a"] = kw["a"]
+            if "slip" in kw:
+                out[f"{name}/slip"] = kw["slip"]
+            x = rng.standard_normal(r.n)
+            out[f"{name}/x"] = x
+            out[f"{name}/y"] = r.atimes_nonewald(x)
+            out[f"{name}/mat"] = r.matrix_nonewald()
+    # two spheres on the z axis at r = 2.5 (test/test-all.c:114,128)
+    pair = np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 2.5]])
+    r = mk(2, pair, (8.0, 9.0, 10.0))
+    out["pair_ez/meta"] = np.array([2, 0.0])
+    out["pair_ez/pos"] = pair
+    out["pair_ez/mat"] = r.matrix_nonewald()
+    # a larger FTS product (N=200 non-overlapping spheres, phi 0.2 packing)
+    pos200, _ = rsa_positions(200, 0.20, seed=11)
+    r = mk(2, pos200, (8.0, 9.0, 10.0))
+    x = rng.standard_normal(r.n)
+    out["n200_v2_mono/meta"] = np.array([2, 0.0])
+    out["n200_v2_mono/pos"] = pos200
+    out["n200_v2_mono/x"] = x
+    out["n200_v2_mono/y"] = r.atimes_nonewald(x)
+    return out
+
+
 def main(ref_root: str = "/root/reference"):
     if build_reference(ref_root) is None:
         raise SystemExit(f"reference checkout not found under {ref_root}")
@@ -357,6 +401,9 @@ def main(ref_root: str = "/root/reference"):
         ki[f"s{seed}_res53"] = np.array([lib.KIrand_genrand_res53(r) for _ in range(50)])
         ki[f"s{seed}_gauss"] = np.array([lib.KIrand_Gaussian(r) for _ in range(101)])
     np.savez_compressed(os.path.join(HERE, "kirand.npz"), **ki)
+
+    # ---- the free-space operator (the reference's non-ewald.c) -----------
+    np.savez_compressed(os.path.join(HERE, "nonewald.npz"), **nonewald_fixtures())
 
     # ---- Brownian dynamics (the reference's brownian.c) -------------------
     np.savez_compressed(os.path.join(HERE, "bd.npz"), **bd_fixtures())

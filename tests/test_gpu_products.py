@@ -119,11 +119,12 @@ def test_errors_are_reported_not_faulted(lib, products):
         lib.atimes_ewald_3all(s.n + 3, abi._d(x), abi._d(y), C.cast(s.sp, C.c_void_p))
         assert lib.stokes_gpu_last_error() == abi.STOKES_GPU_EINVAL
         assert np.isnan(y).all()
-        # open system
+        # a lattice-sum entry point on an open system
         s.s.periodic = 0
         y = np.zeros(s.n)
-        rc = lib.stokes_gpu_atimes(s.sp, abi._d(np.ones(s.n)), abi._d(y))
-        assert rc == abi.STOKES_GPU_ENOTPERIODIC
+        lib.atimes_ewald_3all(s.n, abi._d(np.ones(s.n)), abi._d(y), C.cast(s.sp, C.c_void_p))
+        assert lib.stokes_gpu_last_error() == abi.STOKES_GPU_ENOTPERIODIC
+        assert np.isnan(y).all()
         s.s.periodic = 1
         # the context still works afterwards
         y = s.atimes(case["x"])

@@ -6,7 +6,7 @@ summation order and in the algebraic arrangement of the pair tensors."""
 import numpy as np
 import pytest
 
-from conftest import make_oracle, rel_l2
+from conftest import make_open_oracle, make_oracle, rel_l2
 
 TOL = 1e-13
 
@@ -77,3 +77,44 @@ def test_oracle_shear_invariance(shear_mode):
             y = o.atimes(x)
             d = np.abs(y - y0) / np.maximum(np.abs(y0), 1.0)
             assert d.max() < tol, (v, sh, d.max())
+
+
+def test_oracle_nonewald(nonewald):
+    """The free-space restatement (oracle_atimes_nonewald,
+    oracle_matrix_nonewald) against the reference's src/non-ewald.c."""
+    for name, case in nonewald.items():
+        o = make_open_oracle(case)
+        if "x" in case:
+            err = rel_l2(o.atimes_nonewald(case["x"]), case["y"])
+            assert err < TOL, (name, err)
+        if "mat" in case:
+            m = o.matrix_nonewald()
+            scale = np.abs(case["mat"]).max()
+            assert np.abs(m - case["mat"]).max() / scale < TOL, name
+            if "x" in case:
+                assert rel_l2(o.matvec(m, case["x"]), case["y"]) < TOL, name
+
+
+def test_nonewald_two_spheres_known_answer(nonewald):
+    """Two equal spheres on the z axis at r = 2.5 (test/check-minv.c:412-515,
+    test/test-all.c:114): the blocks of the reference's matrix are the
+    Rotne-Prager-Yamakawa scalars of Durlofsky, Brady and Bossis (1987),
+    written out here independently of both implementations."""
+    r = 2.5
+    xa12, ya12 = 1.5 / r - 1.0 / r ** 3, 0.75 / r + 0.5 / r ** 3
+    yb12 = -0.75 / r ** 2
+    xc12, yc12 = 0.75 / r ** 3, -0.375 / r ** 3
+    for m in (nonewald["pair_ez"]["mat"], make_open_oracle(nonewald["pair_ez"]).matrix_nonewald()):
+        assert m.shape == (22, 22)
+        # self: a = 1, c = 3/4 (src/non-ewald.c:342-346)
+        assert np.allclose(np.diag(m)[[0, 1, 2]], 1.0, rtol=0, atol=1e-15)
+        assert np.allclose(np.diag(m)[[3, 4, 5]], 0.75, rtol=0, atol=1e-15)
+        # (U_1 | F_2): ya across e, xa along e
+        assert abs(m[0, 11] - ya12) < 1e-15 and abs(m[1, 12] - ya12) < 1e-15
+        assert abs(m[2, 13] - xa12) < 1e-15
+        # (Omega_1 | T_2): yc across e, xc along e
+        assert abs(m[3, 14] - yc12) < 1e-15 and abs(m[5, 16] - xc12) < 1e-15
+        # (U_1 | T_2): yb (T x e)
+        assert abs(m[0, 15] - yb12) < 1e-15 and abs(m[1, 14] + yb12) < 1e-15
+        # the pair sees no other coupling of U_1 to F_2
+        assert abs(m[0, 13]) < 1e-15 and abs(m[2, 11]) < 1e-15
