@@ -227,6 +227,54 @@ def matrix_measure(lib, abi, L, torch, dev, pos, Lbox):
                      "(xi = sqrt(pi)/L, eps 1e-12) builds an 11 x 11 block in FP64"}
 
 
+def open_measure(lib, abi, L, torch, dev, pos, reps: int = 20):
+    """Free-space FTS product (atimes_nonewald_3all, src/non-ewald.c:330-481)
+    of the bench's N = 1000 spheres as an open system, FP64, device buffers:
+    device time per product (CUDA events over `reps` products after three
+    warm-up products) and the pair rate, beside the CPU oracle's time for one
+    product on all host threads."""
+    from oracle.oracle import Oracle
+    w = WORKLOAD
+    s = L.System(2, pos, periodic=False)
+    n = 11 * w["n"]
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(n)
+    d_pos = torch.tensor(pos, dtype=torch.float64, device=dev).contiguous()
+    d_x = torch.tensor(x, dtype=torch.float64, device=dev)
+    d_y = torch.empty_like(d_x)
+    st = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(st.cuda_stream)
+
+    def product():
+        abi.check(lib.stokes_gpu_atimes_dev(s.sp, C.c_void_p(d_pos.data_ptr()),
+                                            C.c_void_p(d_x.data_ptr()),
+                                            C.c_void_p(d_y.data_ptr()), sp))
+    for _ in range(3):
+        product()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        product()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    s.close()
+    o = Oracle(2, pos, (1.0, 1.0, 1.0))
+    threads = os.cpu_count() or 1
+    o.set_threads(threads)
+    t0 = time.perf_counter()
+    o.atimes_nonewald(x)
+    cpu_s = time.perf_counter() - t0
+    pairs = w["n"] * (w["n"] - 1)
+    return {"workload": f"open_fts_n{w['n']}", "precision": "fp64", "ms_per_product": ms,
+            "products_per_s": 1000.0 / ms, "pairs_per_s": pairs / (ms * 1e-3),
+            "cpu_baseline": {"products_per_s": 1.0 / cpu_s, "cores": threads, "kind": "port",
+                             "sample": "one full product of the oracle (oracle_atimes_nonewald)"},
+            "bound": "fp64-pipe: N(N-1) ordered pairs, each the free-space scalars and "
+                     "the 11 x 11 pair tensor applied in FP64"}
+
+
 ADJ_WORKLOAD = dict(name="vjp_ft_n2048_phi0.25", version=1, n=2048, phi=0.25, seed=42)
 
 
@@ -606,6 +654,8 @@ def run_gpu(args):
                              "mixed_over_fp64": (1000.0 / ms) / (1000.0 / fp64_ms)}
     if not args.no_matrix:
         line["matrix"] = matrix_measure(lib, abi, L, torch, dev, pos, Lbox)
+    if not args.no_open:
+        line["open"] = open_measure(lib, abi, L, torch, dev, pos)
     if not args.no_bd:
         line["bd"] = bd_measure(lib, abi, L, torch, dev)
     if not args.no_adjoint:
@@ -634,6 +684,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (VJP) leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the ensemble (batch) leg")
     ap.add_argument("--no-matrix", action="store_true", help="skip the dense-builder leg")
+    ap.add_argument("--no-open", action="store_true",
+                    help="skip the free-space (non-periodic) operator leg")
     ap.add_argument("--n", type=int, default=None,
                     help="override N (smaller cases for profiler captures)")
     args = ap.parse_args()

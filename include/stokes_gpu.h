@@ -60,7 +60,9 @@ int stokes_gpu_release (struct stokes *sys);
 int stokes_gpu_atimes (struct stokes *sys, const double *x, double *y);
 
 /* y = M x with device buffers.  d_pos: positions [np*3] on the device, or
- * NULL to upload sys->pos.  Asynchronous on `stream`. */
+ * NULL to upload sys->pos.  Asynchronous on `stream`; NULL is the legacy
+ * default stream (the work is ordered after and before the caller's other
+ * work on it). */
 int stokes_gpu_atimes_dev (struct stokes *sys, const double *d_pos,
                            const double *d_x, double *d_y, void *stream);
 
@@ -78,7 +80,8 @@ int stokes_gpu_atimes_dev (struct stokes *sys, const double *d_pos,
 int stokes_gpu_atimes_noalloc (struct stokes *sys, const double *d_pos,
                                const double *d_x, double *d_y, void *stream);
 
-/* dense mobility matrix with host / device output */
+/* dense mobility matrix with host / device output (stream as for
+ * stokes_gpu_atimes_dev) */
 int stokes_gpu_matrix (struct stokes *sys, double *mat);
 int stokes_gpu_matrix_dev (struct stokes *sys, const double *d_pos,
                            double *d_mat, void *stream);

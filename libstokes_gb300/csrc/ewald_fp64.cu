@@ -7,6 +7,7 @@
 //              (src/ewald.c:923-1075 refactored through the structure factors)
 //  k_combine   self term + partial real-space sums + reciprocal part
 //  k_matrix    dense builder via pair moments (src/ewald.c:1092-1677)
+//  k_matrix_open  free-space dense builder (src/non-ewald.c:494-666)
 //  k_gemv      dense y = M z(x) (src/matrix.c:365-399, :447-478)
 //
 // The arithmetic is IEEE FP64 throughout; only the summation order differs
@@ -87,6 +88,18 @@ k_real (RealArgs a)
   int qn = 0;
   const unsigned lt = (1u << lane) - 1u;
 
+  // free space: every source j != i once, so the lanes stride over the
+  // sources directly (no image test, no queue); coincident positions are
+  // skipped like the self image of a lattice sum
+  if (a.open)
+    for (int j = j0 + lane; j < j1; j += 32)
+      {
+        const double dx = a.pos[3 * j] - pix, dy = a.pos[3 * j + 1] - piy;
+        const double dz = a.pos[3 * j + 2] - piz;
+        if (j != i && dx * dx + dy * dy + dz * dz != 0.0)
+          real_term<V, MODE> (a, i, j, dx, dy, dz, ai, acc);
+      }
+  else
   for (int j = j0; j < j1; j++)
     {
       const double djx = a.pos[3 * j] - pix;
@@ -679,6 +692,64 @@ k_matrix (MatArgs a)
     }
 }
 
+// Free-space dense matrix: one thread per block (i, j), consecutive j on
+// consecutive threads.  A block holds one pair term (or the self term), so
+// there is nothing to share between lanes and nothing to reduce; each thread
+// writes its block row by row (the C entries of a row are contiguous, and the
+// rows of neighbouring threads fill whole sectors in L2).
+template <int V, int MODE>
+__global__ void __launch_bounds__ (128)
+k_matrix_open (MatArgs a)
+{
+  constexpr int C = NComp<V>::value;
+  constexpr int NM = Moments<V>::N;
+  const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long) a.np * a.np) return;
+  const int i = (int) (t / a.np), j = (int) (t % a.np);
+  const bool same = (i == j);
+  double mo[NM];
+#pragma unroll
+  for (int q = 0; q < NM; q++) mo[q] = 0.0;
+  const double ai = (MODE == MODE_MONO) ? 1.0 : a.rad[i];
+  const double aj = (MODE == MODE_MONO) ? 1.0 : a.rad[j];
+  PairScalars<double> s;
+  if (same)
+    {
+      s.xa = s.ya = a.selfc[3 * i];
+      s.xc = s.yc = a.selfc[3 * i + 1];
+      s.xm = s.ym = s.zm = a.selfc[3 * i + 2];
+      s.yb = s.xg = s.yg = s.yh = 0.0;
+      const double e0[3] = {0.0, 0.0, 0.0};
+      moments_add<V> (e0, s, mo);
+    }
+  else
+    {
+      const double dx = a.pos[3 * j] - a.pos[3 * i];
+      const double dy = a.pos[3 * j + 1] - a.pos[3 * i + 1];
+      const double dz = a.pos[3 * j + 2] - a.pos[3 * i + 2];
+      const double rr = dx * dx + dy * dy + dz * dz;
+      if (rr != 0.0)
+        {
+          double r = sqrt (rr);
+          const double rm = (ai + aj) * a.rmin;
+          if (r < rm) r = rm;
+          const double ri = 1.0 / r;
+          const double e[3] = {dx * ri, dy * ri, dz * ri};
+          if (MODE == MODE_MONO) open_scalars<V, double> (r, 1.0, 1.0, 1.0, s);
+          else if (MODE == MODE_POLY) open_scalars<V, double> (r, ai, aj, ai, s);
+          else open_scalars<V, double> (r, a.slipa[i], a.slipa[j], ai, s);
+          moments_add<V> (e, s, mo);
+        }
+    }
+  const size_t n = (size_t) C * a.np;
+  double *blk = a.mat + (size_t) C * i * n + (size_t) C * j;
+#pragma unroll
+  for (int row = 0; row < C; row++)
+#pragma unroll
+    for (int col = 0; col < C; col++)
+      blk[row * n + col] = block_entry<V> (mo, row, col, same);
+}
+
 // dense y = M . z(x), one warp per row (z = extracted-form transform for FTS)
 __global__ void __launch_bounds__ (256)
 k_gemv (const double *mat, const double *z, int n, double *y)
@@ -808,6 +879,19 @@ cudaError_t
 launch_matrix_fp64 (int version, int mode, const MatArgs &a, cudaStream_t st)
 {
   const long long nw = (long long) a.np * a.np;
+  if (a.open)
+    {
+      const int grid = (int) ((nw + 127) / 128);
+#define LSG_DISPATCH(V)                                                               \
+  if (mode == MODE_MONO) k_matrix_open<V, MODE_MONO><<<grid, 128, 0, st>>> (a);      \
+  else if (mode == MODE_POLY) k_matrix_open<V, MODE_POLY><<<grid, 128, 0, st>>> (a); \
+  else k_matrix_open<V, MODE_SLIP><<<grid, 128, 0, st>>> (a);
+      if (version == 0) { LSG_DISPATCH (0) }
+      else if (version == 1) { LSG_DISPATCH (1) }
+      else { LSG_DISPATCH (2) }
+#undef LSG_DISPATCH
+      return cudaGetLastError ();
+    }
   const int grid = (int) ((nw + 3) / 4);
 #define LSG_DISPATCH(V)                                                        \
   if (mode == MODE_MONO) k_matrix<V, MODE_MONO><<<grid, 128, 0, st>>> (a);      \

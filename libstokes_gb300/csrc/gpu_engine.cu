@@ -121,6 +121,7 @@ get_ctx (const struct stokes *sys, bool create)
   if (cudaStreamCreateWithFlags (&c->stream, cudaStreamNonBlocking) != cudaSuccess)
     { delete c; return nullptr; }
   for (int q = 0; q < 4; q++) cudaEventCreate (&c->ev[q]);
+  for (int q = 0; q < 2; q++) cudaEventCreateWithFlags (&c->join[q], cudaEventDisableTiming);
   const char *env = getenv ("LIBSTOKES_GB300_PRECISION");
   c->precision = (env && strcmp (env, "mixed") == 0) ? STOKES_GPU_MIXED : STOKES_GPU_FP64;
   g_ctx[sys] = c;
@@ -134,6 +135,7 @@ free_ctx (Ctx *c)
   for (cudaEvent_t e : c->kprof_ev) cudaEventDestroy (e);
   for (DevBuf *b : c->all_buffers ()) b->release ();
   for (int q = 0; q < 4; q++) cudaEventDestroy (c->ev[q]);
+  for (int q = 0; q < 2; q++) cudaEventDestroy (c->join[q]);
   cudaStreamDestroy (c->stream);
   release_mixed (c);
   delete c;
@@ -691,6 +693,25 @@ stokes_gpu_atimes (struct stokes *sys, const double *x, double *y)
   return atimes_host (sys, x, y, false);
 }
 
+// Work for a caller's stream.  NULL names the legacy default stream (as
+// everywhere in CUDA); the work then runs on the context's own non-blocking
+// stream, ordered after the caller's earlier work and before its later work
+// by two events, which keeps graph capture and the side stream usable.
+static int
+on_caller_stream (Ctx *c, void *stream, const std::function<int (cudaStream_t)> &f)
+{
+  if (stream) return f ((cudaStream_t) stream);
+  cudaStream_t legacy = (cudaStream_t) 0;
+  cudaError_t e = cudaEventRecord (c->join[0], legacy);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent (c->stream, c->join[0], 0);
+  if (e != cudaSuccess) return cuda_fail (e, "ordering after the default stream");
+  const int rc = f (c->stream);
+  e = cudaEventRecord (c->join[1], c->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent (legacy, c->join[1], 0);
+  if (e != cudaSuccess && rc == STOKES_GPU_OK) return cuda_fail (e, "ordering before the default stream");
+  return rc;
+}
+
 int
 stokes_gpu_atimes_dev (struct stokes *sys, const double *d_pos, const double *d_x,
                        double *d_y, void *stream)
@@ -701,16 +722,17 @@ stokes_gpu_atimes_dev (struct stokes *sys, const double *d_pos, const double *d_
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
   int rc = prepare (c, sys, false);
   if (rc) return rc;
-  cudaStream_t st = stream ? (cudaStream_t) stream : c->stream;
-  if (d_pos == nullptr)
-    {
-      cudaError_t e = c->pos.ensure (sizeof (double) * 3 * sys->np);
-      if (e != cudaSuccess) return cuda_fail (e, "pos");
-      cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * sys->np,
-                       cudaMemcpyHostToDevice, st);
-      d_pos = (const double *) c->pos.p;
-    }
-  return atimes_dev (c, d_pos, d_x, d_y, st, false);
+  return on_caller_stream (c, stream, [&] (cudaStream_t st) {
+    if (d_pos == nullptr)
+      {
+        cudaError_t e = c->pos.ensure (sizeof (double) * 3 * sys->np);
+        if (e != cudaSuccess) return cuda_fail (e, "pos");
+        cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * sys->np,
+                         cudaMemcpyHostToDevice, st);
+        d_pos = (const double *) c->pos.p;
+      }
+    return atimes_dev (c, d_pos, d_x, d_y, st, false);
+  });
 }
 
 int
@@ -728,16 +750,17 @@ stokes_gpu_matrix_dev (struct stokes *sys, const double *d_pos, double *d_mat, v
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
   int rc = prepare (c, sys, false, 1);
   if (rc) return rc;
-  cudaStream_t st = stream ? (cudaStream_t) stream : c->stream;
-  if (d_pos == nullptr)
-    {
-      cudaError_t e = c->pos.ensure (sizeof (double) * 3 * sys->np);
-      if (e != cudaSuccess) return cuda_fail (e, "pos");
-      cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * sys->np,
-                       cudaMemcpyHostToDevice, st);
-      d_pos = (const double *) c->pos.p;
-    }
-  return matrix_dev (c, d_pos, d_mat, st);
+  return on_caller_stream (c, stream, [&] (cudaStream_t st) {
+    if (d_pos == nullptr)
+      {
+        cudaError_t e = c->pos.ensure (sizeof (double) * 3 * sys->np);
+        if (e != cudaSuccess) return cuda_fail (e, "pos");
+        cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * sys->np,
+                         cudaMemcpyHostToDevice, st);
+        d_pos = (const double *) c->pos.p;
+      }
+    return matrix_dev (c, d_pos, d_mat, st);
+  });
 }
 
 int

@@ -25,6 +25,7 @@ struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[4] = {};
+  cudaEvent_t join[2] = {};   // orders the context's stream inside the legacy default stream
   int precision = 0;
 
   // geometry of the last prepared system

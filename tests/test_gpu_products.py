@@ -149,3 +149,37 @@ def test_device_entry_point(lib, products):
     torch.cuda.synchronize()
     assert rel_l2(y.cpu().numpy(), case["y"]) < TOL
     s.close()
+
+
+def test_default_stream_is_ordered(lib):
+    """stream = NULL is the legacy default stream: the product is ordered
+    after the caller's earlier work on it and before its later work, so a
+    result read back on that stream without a device-wide synchronize is
+    complete."""
+    import torch
+    from libstokes_gb300 import check
+    from libstokes_gb300.workloads import rsa_positions
+    pos, L = rsa_positions(1000, 0.3, seed=2)
+    case = dict(meta=np.array([2, L, L, L, 1.0, 1e-12, 0, 0.0, 0.0]), pos=pos)
+    s = make_system(case)
+    dev = torch.device("cuda:0")
+    x = np.random.default_rng(8).standard_normal(s.n)
+    y_host = s.atimes(x)
+    with torch.cuda.stream(torch.cuda.default_stream(dev)):
+        d_pos = torch.tensor(pos, dtype=torch.float64, device=dev)
+        # the input is written by a kernel queued on the default stream
+        d_x = torch.zeros(s.n, dtype=torch.float64, device=dev)
+        d_x += torch.tensor(x, dtype=torch.float64, device=dev)
+        for _ in range(2):
+            d_y = torch.full_like(d_x, float("nan"))
+            check(lib.stokes_gpu_atimes_dev(s.sp, C.c_void_p(d_pos.data_ptr()),
+                                            C.c_void_p(d_x.data_ptr()),
+                                            C.c_void_p(d_y.data_ptr()), None))
+            y = d_y.cpu().numpy()     # a copy on the default stream
+            assert rel_l2(y, y_host) < TOL
+            d_m = torch.full((s.n, s.n), float("nan"), dtype=torch.float64, device=dev)
+            check(lib.stokes_gpu_matrix_dev(s.sp, C.c_void_p(d_pos.data_ptr()),
+                                            C.c_void_p(d_m.data_ptr()), None))
+            assert torch.isfinite(d_m).all().item()
+            del d_m
+    s.close()
