@@ -132,11 +132,12 @@ k_bd_force (int nm, int np, int c, double fact, const double *z, const double *f
 // with overlap x = ai + aj - r > 0 pushes i along the primary-cell vector
 // (pos_i - pos_j) / r with 12 e (r0/(r0-x))^7 ((r0/(r0-x))^6 - 1), as the
 // reference does.  A float minimum-image test skips the pairs that cannot
-// overlap; the candidates are redone exactly in FP64.
+// overlap; the candidates are redone exactly in FP64.  An open system
+// (periodic == 0) has the primary cell only (src/ev-LJ.c:222-233).
 __global__ void
 k_bd_lj (int nm, int np, int c, const double *pos, double lx, double ly, double lz,
          int shear_mode, double shift, const double *rad, double e_all, double r0_all,
-         const double *lje, const double *ljr0, double *f)
+         const double *lje, const double *ljr0, int open, double *f)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nm) return;
@@ -152,6 +153,22 @@ k_bd_lj (int nm, int np, int c, const double *pos, double lx, double ly, double 
       if (j == i) continue;
       const double aj = rad ? rad[j] : 1.0;
       const double x = xi - pos[3 * j], y = yi - pos[3 * j + 1], z = zi - pos[3 * j + 2];
+      if (open)
+        {
+          const double r = sqrt (x * x + y * y + z * z);
+          const double ov = ai + aj - r;
+          if (!(ov > 0.0)) continue;
+          const double e = lje ? sqrt (lje[i] * lje[j]) : e_all;
+          const double r0 = ljr0 ? 0.5 * (ljr0[i] + ljr0[j]) : r0_all;
+          double rl = r0 - ov;
+          if (rl < 0.0) rl = 1.0e-12;
+          const double ri = r0 / rl, ri6 = ri * ri * ri * ri * ri * ri;
+          const double fr = 12.0 * e * ri6 * ri * (ri6 - 1.0);
+          fx += fr * x / r;
+          fy += fr * y / r;
+          fz += fr * z / r;
+          continue;
+        }
       // float pre-test on the wrapped distance (the reference's 27 cells
       // contain the nearest image only when |x| < 1.5 L; keep the exact path
       // whenever that is not clearly the case)
@@ -196,13 +213,13 @@ k_bd_lj (int nm, int np, int c, const double *pos, double lx, double ly, double 
 // vector.  CTA of LJ_T targets; the sources pass through shared memory in
 // tiles of LJ_T as FP32 positions for a pre-test on the wrapped distance
 // (with a margin); the few pairs that pass it are evaluated in FP64 from
-// the global positions.
+// the global positions.  An open system takes the plain difference.
 constexpr int LJ_T = 128;
 
 __global__ void __launch_bounds__ (LJ_T)
 k_bd_lj_engine (int nm, int np, int c, const double *pos, double lx, double ly, double lz,
                 int shear_mode, double shift, const double *rad, double e_all, double r0_all,
-                const double *lje, const double *ljr0, double *f)
+                const double *lje, const double *ljr0, int open, double *f)
 {
   __shared__ float s_p[LJ_T][4];
   const int i = blockIdx.x * LJ_T + threadIdx.x;
@@ -233,40 +250,46 @@ k_bd_lj_engine (int nm, int np, int c, const double *pos, double lx, double ly, 
         {
           const int j = j0 + t;
           float sx = fxi - s_p[t][0], sy = fyi - s_p[t][1], sz = fzi - s_p[t][2];
-          if (shear_mode == 1)
+          if (!open)
             {
-              const float k = rintf (sy * ily);
-              sy -= k * fly;
-              sx -= k * fsh;
+              if (shear_mode == 1)
+                {
+                  const float k = rintf (sy * ily);
+                  sy -= k * fly;
+                  sx -= k * fsh;
+                }
+              else if (shear_mode == 2)
+                {
+                  const float k = rintf (sz * ilz);
+                  sz -= k * flz;
+                  sx -= k * fsh;
+                }
+              sx -= flx * rintf (sx * ilx);
+              sy -= fly * rintf (sy * ily);
+              sz -= flz * rintf (sz * ilz);
             }
-          else if (shear_mode == 2)
-            {
-              const float k = rintf (sz * ilz);
-              sz -= k * flz;
-              sx -= k * fsh;
-            }
-          sx -= flx * rintf (sx * ilx);
-          sy -= fly * rintf (sy * ily);
-          sz -= flz * rintf (sz * ilz);
           const float lim = ((float) ai + s_p[t][3]) * 1.001f + 1e-3f;
           if (sx * sx + sy * sy + sz * sz > lim * lim || j == i) continue;
           const double aj = rad ? rad[j] : 1.0;
           double x = xi - pos[3 * j], y = yi - pos[3 * j + 1], z = zi - pos[3 * j + 2];
-          if (shear_mode == 1)
+          if (!open)
             {
-              const double k = rint (y * dly);
-              y -= k * ly;
-              x -= k * shift;
+              if (shear_mode == 1)
+                {
+                  const double k = rint (y * dly);
+                  y -= k * ly;
+                  x -= k * shift;
+                }
+              else if (shear_mode == 2)
+                {
+                  const double k = rint (z * dlz);
+                  z -= k * lz;
+                  x -= k * shift;
+                }
+              x -= lx * rint (x * dlx);
+              y -= ly * rint (y * dly);
+              z -= lz * rint (z * dlz);
             }
-          else if (shear_mode == 2)
-            {
-              const double k = rint (z * dlz);
-              z -= k * lz;
-              x -= k * shift;
-            }
-          x -= lx * rint (x * dlx);
-          y -= ly * rint (y * dly);
-          z -= lz * rint (z * dlz);
           const double r = sqrt (x * x + y * y + z * z);
           const double ov = ai + aj - r;
           if (!(ov > 0.0) || !(r > 0.0)) continue;
@@ -339,11 +362,11 @@ k_bd_zcompress (int nm, int c, const double *x, double *z)
 }
 
 // number of pairs i <= j < nm closer than sqrt(rmin) (a_i + a_j) in the
-// primary cell (i != j) or in one of the 26 neighbour cells
-// (src/brownian.c:299-375)
+// primary cell (i != j) or, for a periodic system, in one of the 26
+// neighbour cells (src/brownian.c:299-375)
 __global__ void
 k_bd_overlap (int nm, const double *pos, double lx, double ly, double lz, int shear_mode,
-              double shift, const double *rad, double rmin, int *count)
+              double shift, const double *rad, double rmin, int open, int *count)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nm) return;
@@ -354,9 +377,10 @@ k_bd_overlap (int nm, const double *pos, double lx, double ly, double lz, int sh
       const double x = pos[3 * i] - pos[3 * j], y = pos[3 * i + 1] - pos[3 * j + 1],
                    z = pos[3 * i + 2] - pos[3 * j + 2];
       const double s = ai + (rad ? rad[j] : 1.0), a2 = s * s;
-      for (int kx = -1; kx <= 1; kx++)
-        for (int ky = -1; ky <= 1; ky++)
-          for (int kz = -1; kz <= 1; kz++)
+      const int K = open ? 0 : 1;
+      for (int kx = -K; kx <= K; kx++)
+        for (int ky = -K; ky <= K; ky++)
+          for (int kz = -K; kz <= K; kz++)
             {
               if (kx == 0 && ky == 0 && kz == 0 && i == j) continue;
               double xx = x + kx * lx, yy = y + ky * ly, zz = z + kz * lz;
@@ -566,13 +590,14 @@ bd_forces (stokes_gpu_bd *b, const double *d_pos, double fact)
                                             b->p.lj_e, b->p.lj_r0,
                                             b->lj_arrays ? (const double *) b->lje.p : nullptr,
                                             b->lj_arrays ? (const double *) b->ljr0.p : nullptr,
-                                            (double *) b->f.p);
+                                            s->periodic == 0, (double *) b->f.p);
   else if (b->p.lj_e != 0.0 || b->lj_arrays)
     k_bd_lj_engine<<<(b->nm + LJ_T - 1) / LJ_T, LJ_T, 0, st>>> (
       b->nm, b->np, b->C, d_pos, s->lx, s->ly, s->lz, s->shear_mode, s->shear_shift,
       s->a ? (const double *) b->c->pp.p : nullptr, b->p.lj_e, b->p.lj_r0,
       b->lj_arrays ? (const double *) b->lje.p : nullptr,
-      b->lj_arrays ? (const double *) b->ljr0.p : nullptr, (double *) b->f.p);
+      b->lj_arrays ? (const double *) b->ljr0.p : nullptr, s->periodic == 0,
+      (double *) b->f.p);
   cudaError_t e = cudaGetLastError ();
   return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "BD forces");
 }
@@ -1005,7 +1030,7 @@ dropin_overlap (stokes_gpu_bd *b, const double *d_pos, double rmin, const char *
   k_bd_overlap<<<gridn (b->nm), 128, 0, st>>> (b->nm, d_pos, s->lx, s->ly, s->lz, s->shear_mode,
                                                s->shear_shift,
                                                s->a ? (const double *) b->c->pp.p : nullptr, rmin,
-                                               (int *) b->ovl.p);
+                                               s->periodic == 0, (int *) b->ovl.p);
   int cnt = 0;
   e = cudaMemcpyAsync (&cnt, b->ovl.p, sizeof (int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize (st);

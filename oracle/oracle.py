@@ -228,6 +228,7 @@ class Oracle(_Backend):
                                           _dp, C.POINTER(C.c_double)])
             lib.oracle_atimes_part.argtypes = [C.c_void_p, _dp, _dp, C.c_int]
             lib.oracle_atimes_rows.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int]
+            lib.oracle_set_open.argtypes = [C.c_void_p, C.c_int]
             lib.oracle_count_real_terms.restype = C.c_longlong
             lib.oracle_count_real_terms.argtypes = [C.c_void_p]
             lib.oracle_count_k.restype = C.c_int
@@ -271,10 +272,17 @@ class Oracle(_Backend):
                                  _d(z))
         return z
 
+    def set_open(self, open_=True):
+        """Make atimes / cheb_eval / bd_step use the free-space operator (an
+        open system, periodic = 0)."""
+        self._open = bool(open_)
+        self._L.oracle_set_open(self.h, 1 if open_ else 0)
+
     def bd_step(self, x, dt, peclet, a, e0, e1, y, F=None, lj_e=0.0, lj_r0=2.0, lj_image=False):
         """One mid-point step from positions x with noise y; returns (x_new, z).
         lj_image: EV_LJ along the nearest-image vector (this library's BD
-        engine) instead of the reference's primary-cell vector."""
+        engine) instead of the reference's primary-cell vector.  An open
+        system (set_open) takes the plain pair vector."""
         x = np.array(x, dtype=np.float64).reshape(-1).copy()
         a = np.ascontiguousarray(a, dtype=np.float64)
         y = np.ascontiguousarray(y, dtype=np.float64)
@@ -283,7 +291,8 @@ class Oracle(_Backend):
         self._L.oracle_bd_step_ex(self.h, self.version, self.np, *self.box, float(dt),
                                   float(peclet), len(a), _d(a), float(e0), float(e1), _d(y),
                                   None if Fp is None else _d(Fp), float(lj_e), float(lj_r0),
-                                  1 if lj_image else 0, _d(x), _d(z))
+                                  2 if getattr(self, "_open", False) else (1 if lj_image else 0),
+                                  _d(x), _d(z))
         return x, z
 
     def count_real_terms(self):

@@ -45,7 +45,8 @@ oracle_cheb_eval (void *h, int n, int ncheb, const double *a, double e0, double 
 /* EV_LJ force on each particle, added to f (stride c).  image = 0: the
  * reference's force (src/ev-LJ.c:185-262), along the primary-cell vector over
  * the image distance; image = 1: the nearest image and the force along the
- * image vector (the convention of this library's own BD engine) */
+ * image vector (the convention of this library's own BD engine); image = 2:
+ * an open system, the pair vector itself (src/ev-LJ.c:222-233) */
 static void
 lj_add (int np, int c, const double *pos, double lx, double ly, double lz, double e, double r0,
         int image, double *f)
@@ -57,8 +58,10 @@ lj_add (int np, int c, const double *pos, double lx, double ly, double lz, doubl
                      z = pos[3 * i + 2] - pos[3 * j + 2];
         if (image)
           {
-            const double xx = x - lx * rint (x / lx), yy = y - ly * rint (y / ly),
-                         zz = z - lz * rint (z / lz);
+            const int wrap = image == 1;
+            const double xx = wrap ? x - lx * rint (x / lx) : x;
+            const double yy = wrap ? y - ly * rint (y / ly) : y;
+            const double zz = wrap ? z - lz * rint (z / lz) : z;
             const double r = sqrt (xx * xx + yy * yy + zz * zz);
             const double ov = 2.0 - r;
             if (!(ov > 0.0)) continue;

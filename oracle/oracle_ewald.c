@@ -67,6 +67,7 @@ typedef struct {
   double *rlx, *rly, *rlz;
   int *rmx, *rmy, *rmz;
   int nthreads;
+  int open;          /* oracle_atimes evaluates the free-space operator */
 } osys;
 
 static int
@@ -906,11 +907,20 @@ oracle_atimes_rows (void *h, const double *x, double *y, int i0, int i1)
   atimes_rows (s, x, y, 3, i0 < 0 ? 0 : i0, i1 > s->np ? s->np : i1);
 }
 
+void oracle_atimes_nonewald (void *h, const double *x, double *y);
+
+/* the operator of the system: the Ewald sum, or the free-space sum once
+ * oracle_set_open (h, 1) was called (src/ewald.c:433-447 on periodic) */
 void
 oracle_atimes (void *h, const double *x, double *y)
 {
-  oracle_atimes_part (h, x, y, 3);
+  if (((osys *) h)->open)
+    oracle_atimes_nonewald (h, x, y);
+  else
+    oracle_atimes_part (h, x, y, 3);
 }
+
+void oracle_set_open (void *h, int open) { ((osys *) h)->open = open; }
 
 /* dense mobility matrix, extracted form (restates src/ewald.c:1092-1677) */
 void

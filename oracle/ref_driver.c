@@ -154,6 +154,10 @@ ref_atimes_nonewald (void *h, const double *x, double *y)
 
 void ref_matrix_nonewald (void *h, double *mat) { make_matrix_mob_nonewald_3all (h, mat); }
 
+/* sys->periodic: 0 makes the dispatchers (atimes_3all, make_matrix_mob_3all)
+ * and the BD routines take the free-space branch */
+void ref_set_periodic (void *h, int p) { ((struct stokes *) h)->periodic = p; }
+
 void
 ref_matvec (int version, int np, const double *mat, const double *x, double *y)
 {

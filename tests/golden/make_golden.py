@@ -115,9 +115,15 @@ BD_CASES = [
     ("ft_q", 1, 20, 0.15, 6, 44, 2.0, 1e-3, 2, 24, (0.5, 2.0), 0.0, 1e-12, (0, 0.0), True, True),
     ("f_shear", 0, 24, 0.20, 7, 45, 1.0, 1e-3, 2, 20, None, 0.0, 1e-12, (1, 2.0), False, False),
 ]
+# open systems (periodic = 0, src/brownian.c:336 and src/ev-LJ.c:234): the
+# free-space operator, no images in EV_LJ or in the overlap check
+BD_OPEN_CASES = [
+    ("open_f_lj", 0, 27, 0.20, 3, 46, 1.0, 1e-3, 3, 20, (1.0, 2.0), 0.0, 1e-12, (0, 0.0), True, False),
+    ("open_ft_halving", 1, 20, 0.25, 9, 47, 1.0, 2e-2, 3, 24, (1.0, 2.0), 0.9, 1e-4, (0, 0.0), True, False),
+]
 
 
-def bd_fixtures() -> dict:
+def bd_fixtures(cases=None, periodic=True) -> dict:
     """BD_calc_FB / BD_evolve_mid of the reference on small periodic systems.
     ARPACK is absent, so the bounds are the extreme eigenvalues of the
     reference's dense mobility matrix widened by (0.8, 1.05); BD->eps = 10
@@ -134,6 +140,8 @@ def bd_fixtures() -> dict:
     lib.ref_xi_by_tratio.argtypes = [C.c_void_p, C.c_double]
     lib.ref_set_split.argtypes = [C.c_void_p, C.c_double, C.c_double]
     lib.ref_matrix.argtypes = [C.c_void_p, dp]
+    lib.ref_matrix_nonewald.argtypes = [C.c_void_p, dp]
+    lib.ref_set_periodic.argtypes = [C.c_void_p, C.c_int]
     lib.refbd_set_shear.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.refbd_calc_fb.argtypes = [C.c_void_p, C.c_ulong, C.c_double, C.c_int, C.c_double,
                                   C.c_double, C.c_double, dp]
@@ -142,7 +150,7 @@ def bd_fixtures() -> dict:
                               C.c_double, C.c_double, C.c_double, dp, dp, dp, dp, dp, dp]
     out = {}
     for (name, ver, n, phi, pseed, rseed, pe, dt, steps, nminv, lj, bdrmin, dtlim, shear,
-         with_ft, with_q) in BD_CASES:
+         with_ft, with_q) in (BD_CASES if cases is None else cases):
         pos, L = rsa_positions(n, phi, seed=pseed)
         c = (3, 6, 11)[ver]
         h = lib.ref_new(ver, n, d(pos), L, L, L)
@@ -150,7 +158,11 @@ def bd_fixtures() -> dict:
         if shear[0]:
             lib.refbd_set_shear(h, shear[0], shear[1])
         M = np.zeros((c * n, c * n))
-        lib.ref_matrix(h, d(M))
+        if periodic:
+            lib.ref_matrix(h, d(M))
+        else:
+            lib.ref_set_periodic(h, 0)
+            lib.ref_matrix_nonewald(h, d(M))
         ev = np.linalg.eigvalsh(0.5 * (M + M.T))
         eig = np.array([0.8 * ev[0], 1.05 * ev[-1]])
         rng = np.random.default_rng(pseed + 1000)
@@ -177,7 +189,7 @@ def bd_fixtures() -> dict:
         lib.ref_free(h)
         rec = dict(version=ver, pos=pos.ravel(), box=L, eig=eig, z_fb=z, fb_seed=rseed + 100,
                    seed=rseed, peclet=pe, dt=dt, n_minv=nminv, bd_rmin=bdrmin, dt_lim=dtlim,
-                   shear=np.array(shear, float), traj=traj, dts=dts,
+                   shear=np.array(shear, float), traj=traj, dts=dts, periodic=int(periodic),
                    lj=np.array(lj if lj is not None else (0.0, 0.0)))
         if F is not None:
             rec["F"] = F
@@ -406,7 +418,8 @@ def main(ref_root: str = "/root/reference"):
     np.savez_compressed(os.path.join(HERE, "nonewald.npz"), **nonewald_fixtures())
 
     # ---- Brownian dynamics (the reference's brownian.c) -------------------
-    np.savez_compressed(os.path.join(HERE, "bd.npz"), **bd_fixtures())
+    np.savez_compressed(os.path.join(HERE, "bd.npz"),
+                        **bd_fixtures(), **bd_fixtures(BD_OPEN_CASES, periodic=False))
 
     # ---- struct layouts of the Brownian-dynamics interface ---------------
     json.dump(bd_layouts(ref_root), open(os.path.join(HERE, "bd_layouts.json"), "w"), indent=1)

@@ -120,6 +120,45 @@ def test_engine_lj_uses_the_image_vector(lib):
     s.close()
 
 
+def test_engine_on_an_open_system(lib):
+    """The device engine on an open system (periodic = 0): the free-space
+    operator in the noise and both products, EV_LJ on the plain pair vector.
+    One step with a given noise vector against the oracle at 1e-10."""
+    from libstokes_gb300 import FP64, check
+    from libstokes_gb300.abi import _d, FUNC1
+    from libstokes_gb300.workloads import rsa_positions
+    pos, L = rsa_positions(40, 0.3, seed=12)
+    p = pos.reshape(-1, 3).copy()
+    p[1] = p[0] + np.array([1.9, 0.0, 0.0])    # one overlapping pair for EV_LJ
+    keep = np.linalg.norm(p[2:] - p[1], axis=1) > 2.5
+    p = np.vstack([p[:2], p[2:][keep]])
+    n = len(p)
+    s, h = _engine(lib, 1, p, L, FP64)
+    s.s.periodic = 0
+    s.set_misc(rmin=1.0)
+    check(lib.stokes_gpu_bd_destroy(h))
+    from libstokes_gb300.abi import BDParams
+    prm = BDParams(peclet=1.0, dt=1e-3, n_cheb=20, n_lanczos=20, cheb_eps=1e-2, check_every=1,
+                   lj_e=1.0, lj_r0=2.0, seed=5, precision=FP64)
+    h = C.c_void_p()
+    check(lib.stokes_gpu_bd_create(s.sp, C.byref(prm), C.byref(h)))
+    eig = np.zeros(2)
+    check(lib.stokes_gpu_bd_estimate_bounds(h, _d(eig)))
+    y = np.random.default_rng(9).standard_normal(6 * n)
+    a = np.zeros(20)
+    lib.chebyshev_coef(20, FUNC1(lambda t: 1.0 / np.sqrt(t)), eig[0], eig[1], _d(a))
+    check(lib.stokes_gpu_bd_step_noise(h, 0.0, _d(y)))
+    x1 = np.zeros(3 * n)
+    check(lib.stokes_gpu_bd_get_positions(h, _d(x1)))
+    o = _oracle(1, p, L)
+    o.set_misc(rmin=1.0)
+    o.set_open(True)
+    xo, _ = o.bd_step(p, 1e-3, 1.0, a, eig[0], eig[1], y, lj_e=1.0, lj_r0=2.0)
+    assert rel_l2(x1 - p.reshape(-1), xo - p.reshape(-1)) < 1e-10
+    check(lib.stokes_gpu_bd_destroy(h))
+    s.close()
+
+
 def test_lanczos_bounds_bracket_the_spectrum(lib):
     from libstokes_gb300 import FP64, check
     from libstokes_gb300.abi import _d

@@ -1,7 +1,9 @@
 """libstokes' own BD entry points (BD_calc_FB, BD_evolve_mid) on the GPU
 against the reference's brownian.c on identical inputs (tests/golden/bd.npz):
 F with EV_LJ, F with overlap-driven dt halving (1st- and 2nd-stage redo),
-FT with constant force/torque and quaternions, F under simple shear.  The
+FT with constant force/torque and quaternions, F under simple shear, and
+open systems (periodic = 0: the free-space operator, EV_LJ and the
+overlap check without images; F with EV_LJ, FT with dt halving).  The
 noise comes from the same KIrand stream, the bounds and coefficients are
 preset as in the fixtures.  FP64 path: positions to 1e-9; mixed path: the
 displacement to 1e-5 relative."""
@@ -14,7 +16,7 @@ import pytest
 from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
-CASES = ["f_lj", "f_halving", "ft_q", "f_shear"]
+CASES = ["f_lj", "f_halving", "ft_q", "f_shear", "open_f_lj", "open_ft_halving"]
 
 
 def bd_case(name):
@@ -37,6 +39,8 @@ class Run:
         self.n = len(r["pos"]) // 3
         L = float(r["box"])
         self.s = System(ver, r["pos"], (L, L, L))
+        if "periodic" in r and int(r["periodic"]) == 0:
+            self.s.s.periodic = 0
         if r["shear"][0]:
             lib.stokes_set_shear(self.s.sp, int(r["shear"][0]), float(r["shear"][1]))
         self.s.set_precision(precision)
