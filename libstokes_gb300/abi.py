@@ -32,6 +32,16 @@ STOKES_GPU_EACCURACY = 6
 STOKES_GPU_ETOOBIG = 7
 FP64 = 0
 MIXED = 1
+SOLVE_RES = 0
+SOLVE_MOB_FTS = 1
+
+
+class IterStruct(C.Structure):
+    """struct iter (include/stokes_iter.h)."""
+    _fields_ = [("solver", C.c_char_p), ("max", C.c_int), ("restart", C.c_int),
+                ("eps", C.c_double), ("n", C.c_int), ("guess", _dp), ("flag_guess", C.c_int),
+                ("debug", C.c_int), ("out", C.c_void_p), ("niter", C.c_int),
+                ("res", C.c_double)]
 
 
 class StokesStruct(C.Structure):
@@ -177,6 +187,16 @@ _SIGS = {
     "stokes_gpu_get_precision": (C.c_int, [_SP, _ip]),
     "stokes_gpu_release": (C.c_int, [_SP]),
     "stokes_gpu_atimes": (C.c_int, [_SP, _dp, _dp]),
+    # iterative solves (include/stokes_iter.h)
+    "iter_init": (C.c_void_p, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int, _dp, C.c_int,
+                               C.c_int, C.c_void_p]),
+    "iter_free": (None, [C.c_void_p]),
+    "stokes_set_iter": (None, [_SP, C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int,
+                               C.c_void_p]),
+    "solve_iter": (None, [C.c_int, _dp, _dp, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "solve_mob_3fts_0": (None, [_SP, C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "stokes_gpu_solve": (C.c_int, [_SP, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_double,
+                                   C.POINTER(C.c_int), _dp]),
     "stokes_gpu_atimes_dev": (C.c_int, [_SP, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "stokes_gpu_atimes_noalloc": (C.c_int, [_SP, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p]),

@@ -10,8 +10,8 @@
  * reference bit for bit.
  *
  * Not rebuilt here: the lubrication tables (poly_table, twobody_f_list,
- * slip_table) and the iterative-solver settings (stokes_set_iter); the
- * mobility kernels do not read them.
+ * slip_table); the mobility kernels do not read them.  The iterative-solver
+ * settings (stokes_set_iter) go to this library's iter_init (krylov.cu).
  */
 #include <math.h>
 #include <stdio.h>
@@ -19,6 +19,7 @@
 #include <string.h>
 
 #include "stokes_gpu.h"
+#include "stokes_iter.h"
 
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
@@ -78,9 +79,28 @@ stokes_free (struct stokes *sys)
   stokes_unset_radius (sys);
   stokes_unset_slip (sys);
   free_tables (sys);
-  /* sys->it belongs to the iterative-solver library; libstokes frees it with
-   * iter_free(), which this library does not provide */
+  /* the iterative-solver settings (src/stokes.c:440) */
+  if (sys->it != NULL) iter_free (sys->it);
   free (sys);
+}
+
+/* iterative-solver settings (src/stokes.c:790-812): the guess is kept
+ * between solves (flag_guess 1, zero at first) */
+void
+stokes_set_iter (struct stokes *sys, const char *solver, int max, int restart, double eps,
+                 int debug, FILE *out)
+{
+  int n;
+  if (sys->version == 0) n = sys->np * 3;
+  else if (sys->version == 1) n = sys->np * 6;
+  else if (sys->version == 2) n = sys->np * 11;
+  else
+    {
+      fprintf (stderr, "libstokes stokes_set_iter : invalid version %d\n", sys->version);
+      exit (1);
+    }
+  if (sys->it != NULL) iter_free (sys->it);
+  sys->it = iter_init (solver, max, restart, eps, n, NULL, 1, debug, out);
 }
 
 void
