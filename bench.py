@@ -249,16 +249,22 @@ def open_measure(lib, abi, L, torch, dev, pos, reps: int = 20):
         abi.check(lib.stokes_gpu_atimes_dev(s.sp, C.c_void_p(d_pos.data_ptr()),
                                             C.c_void_p(d_x.data_ptr()),
                                             C.c_void_p(d_y.data_ptr()), sp))
-    for _ in range(3):
-        product()
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
-    for _ in range(reps):
-        product()
-    e1.record(st)
-    torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1) / reps
+    def timed():
+        for _ in range(3):
+            product()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            product()
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps
+    ms = timed()
+    y64 = d_y.cpu().numpy()
+    s.set_precision(abi.MIXED)
+    ms_mixed = timed()
+    err_mixed = float(np.linalg.norm(d_y.cpu().numpy() - y64) / np.linalg.norm(y64))
     s.close()
     o = Oracle(2, pos, (1.0, 1.0, 1.0))
     threads = os.cpu_count() or 1
@@ -269,6 +275,8 @@ def open_measure(lib, abi, L, torch, dev, pos, reps: int = 20):
     pairs = w["n"] * (w["n"] - 1)
     return {"workload": f"open_fts_n{w['n']}", "precision": "fp64", "ms_per_product": ms,
             "products_per_s": 1000.0 / ms, "pairs_per_s": pairs / (ms * 1e-3),
+            "mixed": {"ms_per_product": ms_mixed, "products_per_s": 1000.0 / ms_mixed,
+                      "pairs_per_s": pairs / (ms_mixed * 1e-3), "rel_err_vs_fp64": err_mixed},
             "cpu_baseline": {"products_per_s": 1.0 / cpu_s, "cores": threads, "kind": "port",
                              "sample": "one full product of the oracle (oracle_atimes_nonewald)"},
             "bound": "fp64-pipe: N(N-1) ordered pairs, each the free-space scalars and "

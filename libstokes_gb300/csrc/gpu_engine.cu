@@ -331,8 +331,8 @@ prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
       c->rmax2 = DBL_MAX;
     }
 
-  // the free-space operator has no reciprocal part: it runs in FP64 whatever
-  // the precision mode says
+  // the free-space products (FP64 and mixed) read the particle table and the
+  // FP64 set-up of the open system
   if (tables < 0) tables = c->precision == STOKES_GPU_MIXED && !c->open ? 0 : 1;
   if (!tables)
     {
@@ -501,8 +501,9 @@ int
 atimes_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y, cudaStream_t st,
             bool timed)
 {
-  if (c->precision == STOKES_GPU_MIXED && !c->open)
-    return atimes_mixed_dev (c, d_pos, d_x, d_y, st, timed);
+  if (c->precision == STOKES_GPU_MIXED)
+    return c->open ? atimes_open_f32_dev (c, d_pos, d_x, d_y, st, timed)
+                   : atimes_mixed_dev (c, d_pos, d_x, d_y, st, timed);
   return atimes_fp64_dev (c, d_pos, d_x, d_y, st, timed);
 }
 

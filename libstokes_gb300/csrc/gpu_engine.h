@@ -61,9 +61,11 @@ struct Ctx {
 
   MixedState *mixed = nullptr;
 
-  std::array<DevBuf *, 12> all_buffers ()
+  DevBuf openf;   // scratch of the mixed-precision free-space product
+
+  std::array<DevBuf *, 13> all_buffers ()
   {
-    return {&pos, &x, &y, &img, &kt, &pp, &ph, &sf, &yrec, &partial, &mat, &zbuf};
+    return {&pos, &x, &y, &img, &kt, &pp, &ph, &sf, &yrec, &partial, &mat, &zbuf, &openf};
   }
 };
 
@@ -101,6 +103,9 @@ void kmark (Ctx *c, cudaStream_t st, const char *name);
 int atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                       cudaStream_t st, bool timed);
 int matrix_mixed_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st);
+// free-space product of an open system in mixed precision (open_f32.cu)
+int atimes_open_f32_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
+                         cudaStream_t st, bool timed);
 void release_mixed (Ctx *c);
 
 }  // namespace lsg
