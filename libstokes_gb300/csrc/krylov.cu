@@ -37,10 +37,13 @@ namespace {
 constexpr int KT = 256;          // threads of the vector kernels
 constexpr int MDOT_CHUNK = 8192; // elements per block of a partial dot product
 
+// the block's sum in thread 0 (callable repeatedly: the first barrier keeps
+// a new call from overwriting partials an earlier call is still reading)
 __device__ __forceinline__ double
 block_sum (double v)
 {
   __shared__ double sh[KT / 32];
+  __syncthreads ();
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync (0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
   __syncthreads ();
@@ -124,17 +127,299 @@ k_fts_mob_out (int np, const double *x, const double *z, double *y)
   y[k] = ((k % 11) < 6 ? x[k] : 0.0) - z[k];
 }
 
+
+// One Arnoldi step after the product w = A v_j, in one cooperative launch
+// (all blocks resident): both Gram-Schmidt passes, the normalisation of
+// v_{j+1}, and -- in block 0 -- the Givens rotation of the new Hessenberg
+// column with the residual estimate res[j] = |g_{j+1}| / |b|.  Block b owns
+// one contiguous slice of the elements in every pass, so the updates of w
+// need no grid barrier; the partial dot products do (three per step), and
+// each pass has its own partial buffer so that no block overwrites partials
+// another block is still reading.  Within a block, warp q forms the slice's
+// dot products with v_q, v_{q+8}, ... (its loads stream along the slice),
+// and the update runs one element per thread over all k.  The barrier is a counter and a
+// generation word with a bounded wait: a block that gives up sets *status
+// and returns.
+struct ArnArgs {
+  double *V;          // (m + 1) x n basis, v_k at V + k n
+  double *w;          // the product A v_j (overwritten)
+  double *xin;        // fixed input of the next product: receives v_{j+1}
+  int n, j, m;
+  double *part;       // [3][G][m + 2] partial sums
+  double *H;          // Hessenberg columns, H[col (m + 1) + row]; rotated
+                      // once their Givens step ran
+  double *cs, *sn, *g;
+  int gcol;           // column the extra block rotates (-1: none)
+  double *res;        // [m] residual estimates
+  double bnrm;
+  unsigned *bar;      // arrival count, generation
+  int *status;        // nonzero: a barrier wait ran out
+};
+
+constexpr long long BAR_SPINS = 1ll << 22;   // about 0.1 - 1 s of polling
+
+__device__ bool
+grid_barrier (unsigned *bar, int *status)
+{
+  __shared__ int s_ok;
+  __syncthreads ();
+  if (threadIdx.x == 0)
+    {
+      volatile unsigned *gen = bar + 1;
+      const unsigned g0 = *gen;
+      __threadfence ();
+      int ok = 1;
+      if (atomicAdd (bar, 1u) == gridDim.x - 1)
+        {
+          bar[0] = 0;
+          __threadfence ();
+          atomicAdd (bar + 1, 1u);
+        }
+      else
+        {
+          long long spins = 0;
+          while (*gen == g0)
+            {
+              if (++spins > BAR_SPINS || *(volatile int *) status)
+                {
+                  atomicExch (status, 1);
+                  ok = 0;
+                  break;
+                }
+              __nanosleep (32);
+            }
+        }
+      __threadfence ();
+      s_ok = ok;
+    }
+  __syncthreads ();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ double
+warp_total (double v)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync (0xffffffffu, v, o);
+  return v;
+}
+
+// Givens step of Hessenberg column c by one block: the earlier rotations
+// and the column come to shared memory in parallel, one thread runs the
+// chain there (through global memory it would pay an L2 round trip per
+// step); sc: 3 (m + 2) doubles of shared memory
+__device__ void
+givens_column (const ArnArgs &a, int c, double *sc)
+{
+  const int ld = a.m + 2;
+  double *col = sc, *cs = sc + ld, *sn = sc + 2 * ld;
+  double *gcol = a.H + (size_t) c * (a.m + 1);
+  for (int i = threadIdx.x; i <= c + 1; i += blockDim.x) col[i] = gcol[i];
+  for (int i = threadIdx.x; i < c; i += blockDim.x)
+    {
+      cs[i] = a.cs[i];
+      sn[i] = a.sn[i];
+    }
+  __syncthreads ();
+  if (threadIdx.x == 0)
+    {
+      for (int i = 0; i < c; i++)
+        {
+          const double t0 = cs[i] * col[i] + sn[i] * col[i + 1];
+          col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
+          col[i] = t0;
+        }
+      const double r = hypot (col[c], col[c + 1]);
+      const double ir = r > 0.0 ? 1.0 / r : 0.0;
+      const double cc = r > 0.0 ? col[c] * ir : 1.0, ss = col[c + 1] * ir;
+      col[c] = r;
+      col[c + 1] = 0.0;
+      a.cs[c] = cc;
+      a.sn[c] = ss;
+      const double gc = a.g[c];
+      a.g[c + 1] = -ss * gc;
+      a.g[c] = cc * gc;
+      a.res[c] = fabs (ss * gc) / a.bnrm;
+    }
+  __syncthreads ();
+  for (int i = threadIdx.x; i <= c + 1; i += blockDim.x) gcol[i] = col[i];
+}
+
+// the Givens step of column c alone (before the residual history is read)
+__global__ void __launch_bounds__ (KT)
+k_givens (ArnArgs a, int c)
+{
+  extern __shared__ double s_g3[];
+  givens_column (a, c, s_g3);
+}
+
+__global__ void __launch_bounds__ (KT)
+k_arnoldi (ArnArgs a)
+{
+  extern __shared__ double s_h[];   // [m + 2] each: h, this pass, cs, sn
+  __shared__ double s_red[KT / 64][64];
+  __shared__ double s_w1;
+  double *h = s_h, *hp = s_h + (a.m + 2);
+  // blocks 0 .. G-1 own slices; block G (the last) rotates column gcol of
+  // the previous step meanwhile, off the path of the next product
+  const int G = gridDim.x - 1, b = blockIdx.x, J = a.j + 1, ld = a.m + 2;
+  const int tid = threadIdx.x, lane = tid & 31, wq = tid >> 5;
+  if (b == G)
+    {
+      if (a.gcol >= 0) givens_column (a, a.gcol, s_h);
+      if (!grid_barrier (a.bar, a.status)) return;
+      grid_barrier (a.bar, a.status);
+      return;
+    }
+  // this block's slice [i0, i1), whole warps of elements
+  const int per = ((a.n + G - 1) / G + 31) / 32 * 32;
+  const int i0 = min (a.n, b * per), i1 = min (a.n, i0 + per);
+  double *w = a.w;
+  for (int k = tid; k < J; k += KT) h[k] = 0.0;
+  for (int pass = 0; pass < 2; pass++)
+    {
+      double *part = a.part + (size_t) pass * G * ld;
+      // slice dot products: warp wq takes k = kb + 8 r, r < 4, four
+      // independent sums in flight
+      for (int kb = wq; kb < J; kb += 32)
+        {
+          double d[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll 2
+          for (int i = i0 + lane; i < i1; i += 32)
+            {
+              const double wi = w[i];
+#pragma unroll
+              for (int r = 0; r < 4; r++)
+                {
+                  const int k = kb + 8 * r;
+                  if (k < J) d[r] += a.V[(size_t) k * a.n + i] * wi;
+                }
+            }
+#pragma unroll
+          for (int r = 0; r < 4; r++) d[r] = warp_total (d[r]);
+          if (lane == 0)
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+              if (kb + 8 * r < J) part[(size_t) b * ld + kb + 8 * r] = d[r];
+        }
+      if (pass == 1)
+        {
+          // |w1|^2 of the slice: |w2|^2 = |w1|^2 - |h2|^2 saves a barrier
+          double t = 0.0;
+          for (int i = i0 + tid; i < i1; i += KT) t += w[i] * w[i];
+          t = block_sum (t);
+          if (tid == 0) part[(size_t) b * ld + a.m + 1] = t;
+        }
+      if (!grid_barrier (a.bar, a.status)) return;
+      // totals over the blocks: eight threads per entry, then three shuffles
+      // (other blocks' partials through L2 with __ldcg, not a stale L1 line)
+      const int ne = J + pass;
+      for (int kb = 0; kb < ne; kb += KT / 8)
+        {
+          const int k = kb + (tid >> 3), sub = tid & 7;
+          const int kk = k < J ? k : a.m + 1;
+          // eight loads in flight per thread: the loop is bound by L2
+          // latency (across the two dies), not by the adds
+          const double *pk = a.part + (size_t) pass * G * ld + kk;
+          double t = 0.0;
+          if (k < ne)
+#pragma unroll 8
+            for (int q = sub; q < G; q += 8) t += __ldcg (pk + (size_t) q * ld);
+          t += __shfl_xor_sync (0xffffffffu, t, 1);
+          t += __shfl_xor_sync (0xffffffffu, t, 2);
+          t += __shfl_xor_sync (0xffffffffu, t, 4);
+          if (sub == 0 && k < ne)
+            {
+              if (k < J)
+                {
+                  hp[k] = t;
+                  h[k] += t;
+                }
+              else
+                s_w1 = t;
+            }
+        }
+      __syncthreads ();
+      // w -= V hp: four threads per element, each over every fourth k
+      for (int base = i0; base < i1; base += 64)
+        {
+          const int i = base + (tid & 63), kg = tid >> 6;
+          double s0 = 0.0, s1 = 0.0;
+          if (i < i1)
+            for (int k = kg; k < J; k += 8)
+              {
+                s0 += a.V[(size_t) k * a.n + i] * hp[k];
+                if (k + 4 < J) s1 += a.V[(size_t) (k + 4) * a.n + i] * hp[k + 4];
+              }
+          s_red[kg][tid & 63] = s0 + s1;
+          __syncthreads ();
+          if (kg == 0 && i < i1)
+            w[i] -= (s_red[0][tid] + s_red[1][tid]) + (s_red[2][tid] + s_red[3][tid]);
+          __syncthreads ();
+        }
+    }
+  // |w|^2 = |w1|^2 - |h2|^2 and v_{j+1} = w / |w|
+  __shared__ double s_nrm, s_inv;
+  if (wq == 0)
+    {
+      double t = 0.0;
+      for (int k = lane; k < J; k += 32) t += hp[k] * hp[k];
+      t = warp_total (t);
+      if (lane == 0)
+        {
+          const double n2 = s_w1 - t;
+          s_nrm = n2 > 0.0 ? sqrt (n2) : 0.0;
+          s_inv = s_nrm > 0.0 ? 1.0 / s_nrm : 0.0;
+        }
+    }
+  __syncthreads ();
+  const double nrm = s_nrm, inv = s_inv;
+  double *vn = a.V + (size_t) (a.j + 1) * a.n;
+  for (int i = i0 + tid; i < i1; i += KT)
+    {
+      const double v = w[i] * inv;
+      vn[i] = v;
+      a.xin[i] = v;
+    }
+  if (b != 0) return;
+  // column j of the Hessenberg matrix, unrotated: h and |w|
+  double *col = a.H + (size_t) a.j * (a.m + 1);
+  for (int i = tid; i <= a.j; i += KT) col[i] = h[i];
+  if (tid == 0) col[a.j + 1] = nrm;
+}
+
+// y = R^{-1} g over the first jj columns (R: the rotated Hessenberg matrix),
+// one warp: back substitution with the lanes over the known y_k
+__global__ void
+k_lsq (const double *H, const double *g, int m, int jj, double *y)
+{
+  const int lane = threadIdx.x & 31;
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  for (int i = jj - 1; i >= 0; i--)
+    {
+      double s = 0.0;
+      for (int k = i + 1 + lane; k < jj; k += 32) s += H[(size_t) k * (m + 1) + i] * y[k];
+      s = warp_total (s);
+      if (lane == 0)
+        {
+          const double d = H[(size_t) i * (m + 1) + i];
+          y[i] = d != 0.0 ? (g[i] - s) / d : 0.0;
+        }
+      __syncwarp ();
+    }
+}
+
 inline int grid_of (long long n) { return (int) ((n + KT - 1) / KT); }
 
 // device workspace of the solver (one per host thread)
 struct Krylov {
-  DevBuf V, w, t, part, h, h2, s2, cv, b, x;
-  double *pin = nullptr;     // pinned host staging: h column or scalars
+  DevBuf V, w, t, part, h, h2, s2, cv, b, x, arn, xin;
+  double *pin = nullptr;     // pinned host staging: residual history, scalars
   size_t pin_cap = 0;
   cudaStream_t own = nullptr;  // stream for foreign operators
+  int coop_blocks = 0;         // co-resident blocks of k_arnoldi on this device
   ~Krylov ()
   {
-    for (DevBuf *d : {&V, &w, &t, &part, &h, &h2, &s2, &cv, &b, &x}) d->release ();
+    for (DevBuf *d : {&V, &w, &t, &part, &h, &h2, &s2, &cv, &b, &x, &arn, &xin}) d->release ();
     if (pin) cudaFreeHost (pin);
     if (own) cudaStreamDestroy (own);
   }
@@ -152,6 +437,10 @@ struct Krylov {
 thread_local Krylov t_kry;
 
 using Apply = std::function<int (const double *d_in, double *d_out)>;
+
+// iterations between two reads of the residual history: the products of an
+// Arnoldi step are queued without a host round-trip in between
+constexpr int CHECK_EVERY = 4;
 
 struct Gmres {
   Krylov &K;
@@ -187,24 +476,47 @@ gmres_dev (int n, const double *d_b, double *d_x, const Apply &A, int m, int max
   Krylov &K = t_kry;
   if (m > n) m = n;
   if (m < 1) m = 1;
-  Gmres G {K, n, m, st, (n + MDOT_CHUNK - 1) / MDOT_CHUNK};
+  Gmres Gm {K, n, m, st, (n + MDOT_CHUNK - 1) / MDOT_CHUNK};
   cudaError_t e;
+  if (K.coop_blocks == 0)
+    {
+      int dev = 0, sms = 0, per = 0;
+      cudaGetDevice (&dev);
+      cudaDeviceGetAttribute (&sms, cudaDevAttrMultiProcessorCount, dev);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor (&per, k_arnoldi, KT,
+                                                         4 * sizeof (double) * 258);
+      if (e != cudaSuccess) return cuda_fail (e, "GMRES occupancy");
+      K.coop_blocks = sms * (per > 0 ? per : 1);
+    }
+  if (m > 256) m = 256;   // the shared h arrays of k_arnoldi
+  // slices of about 64 elements: the FP64 work of a step spread over many SMs
+  int G = (n + 63) / 64;
+  if (G > K.coop_blocks - 1) G = K.coop_blocks - 1;
+  if (G > 2 * 152) G = 2 * 152;
+  if (G < 1) G = 1;
+  const size_t ld = (size_t) m + 2;
+  // arn: H (m + 1) m | cs m | sn m | g m + 1 | res m | part 3 G ld | bar, status
+  const size_t o_cs = (size_t) (m + 1) * m, o_sn = o_cs + m, o_g = o_sn + m, o_res = o_g + m + 1;
+  const size_t o_part = o_res + m, o_bar = o_part + 3 * (size_t) G * ld;
   if ((e = K.V.ensure (sizeof (double) * (size_t) (m + 1) * n)) != cudaSuccess
       || (e = K.w.ensure (sizeof (double) * n)) != cudaSuccess
-      || (e = K.part.ensure (sizeof (double) * (size_t) (m + 1) * G.nch)) != cudaSuccess
-      || (e = K.h.ensure (sizeof (double) * (m + 2))) != cudaSuccess
-      || (e = K.h2.ensure (sizeof (double) * (m + 2))) != cudaSuccess
+      || (e = K.xin.ensure (sizeof (double) * n)) != cudaSuccess
+      || (e = K.part.ensure (sizeof (double) * (size_t) (m + 1) * Gm.nch)) != cudaSuccess
       || (e = K.s2.ensure (sizeof (double) * 2)) != cudaSuccess
       || (e = K.cv.ensure (sizeof (double) * (m + 1))) != cudaSuccess
-      || (e = K.pinned ((size_t) m + 2)) != cudaSuccess)
+      || (e = K.arn.ensure (sizeof (double) * (o_bar + 2))) != cudaSuccess
+      || (e = K.pinned ((size_t) m + 4)) != cudaSuccess)
     return cuda_fail (e, "GMRES workspace");
-  double *V = (double *) K.V.p, *w = (double *) K.w.p, *h = (double *) K.h.p;
-  double *h2 = (double *) K.h2.p;
+  double *V = (double *) K.V.p, *w = (double *) K.w.p;
+  double *arn = (double *) K.arn.p;
+  unsigned *bar = (unsigned *) (arn + o_bar);
+  int *status = (int *) (bar + 2);
+  cudaMemsetAsync (bar, 0, 2 * sizeof (double), st);
   const int gn = grid_of (n);
 
   int rc;
   double bn2;
-  if ((rc = G.norm2_host (d_b, &bn2))) return rc;
+  if ((rc = Gm.norm2_host (d_b, &bn2))) return rc;
   const double bnrm = sqrt (bn2);
   *iters = 0;
   if (!(bnrm > 0.0))
@@ -215,7 +527,23 @@ gmres_dev (int n, const double *d_b, double *d_x, const Apply &A, int m, int max
       return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "GMRES");
     }
 
-  std::vector<double> H ((size_t) (m + 1) * m), cs (m), sn (m), g (m + 1), y (m);
+  ArnArgs aa;
+  aa.V = V;
+  aa.w = w;
+  aa.xin = (double *) K.xin.p;
+  aa.n = n;
+  aa.m = m;
+  aa.part = arn + o_part;
+  aa.H = arn;
+  aa.cs = arn + o_cs;
+  aa.sn = arn + o_sn;
+  aa.g = arn + o_g;
+  aa.res = arn + o_res;
+  aa.bnrm = bnrm;
+  aa.bar = bar;
+  aa.status = status;
+  const size_t smem = 4 * sizeof (double) * ld;
+
   int total = 0;
   double rel = HUGE_VAL;
   for (;;)
@@ -224,73 +552,68 @@ gmres_dev (int n, const double *d_b, double *d_x, const Apply &A, int m, int max
       if ((rc = A (d_x, w))) return rc;
       k_vaxpby<<<gn, KT, 0, st>>> (n, 1.0, d_b, -1.0, w, V);
       double beta2;
-      if ((rc = G.norm2_host (V, &beta2))) return rc;
-      const double beta = sqrt (beta2);
-      rel = beta / bnrm;
+      if ((rc = Gm.norm2_host (V, &beta2))) return rc;
+      rel = sqrt (beta2) / bnrm;
       if (dbg) fprintf (dbg, "gmres: %d applications, residual %.6e\n", total, rel);
       if (rel <= eps || total >= maxit) break;
-      k_vaxpby<<<gn, KT, 0, st>>> (n, 1.0 / beta, V, 0.0, V, V);
-      std::fill (g.begin (), g.end (), 0.0);
-      g[0] = beta;
-      int j = 0;
-      bool done = false;
-      for (; j < m && total < maxit; j++)
+      // v_0 = r / |r|, g = (|r|, 0, ...)
+      cudaMemsetAsync (aa.g, 0, sizeof (double) * (m + 1), st);
+      k_vnormalize<<<gn, KT, 0, st>>> (V, (const double *) K.s2.p, aa.g, V, n);
+      int jj = 0, checked = 0;
+      aa.gcol = -1;            // column whose Givens step is still due
+      bool conv = false;
+      for (int j = 0; j < m && total < maxit; j++)
         {
-          double *vj = V + (size_t) j * n, *vn = V + (size_t) (j + 1) * n;
-          if ((rc = A (vj, w))) return rc;
+          // the product reads a fixed buffer: with the same pointers every
+          // step, the mixed path replays its recorded graph (k_arnoldi
+          // leaves v_{j+1} there; v_0 is copied)
+          if (j == 0)
+            cudaMemcpyAsync (K.xin.p, V, sizeof (double) * n, cudaMemcpyDeviceToDevice, st);
+          if ((rc = A ((const double *) K.xin.p, w))) return rc;
           total++;
-          // CGS2: h = V^T w, w -= V h, twice
-          G.mdot (V, j + 1, w, h, 0);
-          k_vcombine<<<gn, KT, 0, st>>> (w, V, (size_t) n, h, j + 1, n, -1.0);
-          G.mdot (V, j + 1, w, h2, 0);
-          k_vcombine<<<gn, KT, 0, st>>> (w, V, (size_t) n, h2, j + 1, n, -1.0);
-          k_vaxpby<<<1, KT, 0, st>>> (j + 1, 1.0, h, 1.0, h2, h);
-          G.mdot (w, 1, w, (double *) K.s2.p, 0);
-          k_vnormalize<<<gn, KT, 0, st>>> (w, (const double *) K.s2.p, h + j + 1, vn, n);
-          cudaMemcpyAsync (K.pin, h, sizeof (double) * (j + 2), cudaMemcpyDeviceToHost, st);
+          aa.j = j;
+          void *args[] = {&aa};
+          // G slice blocks and one block for the Givens step of column j - 1
+          e = cudaLaunchCooperativeKernel ((const void *) k_arnoldi, G + 1, KT, args, smem, st);
+          if (e != cudaSuccess) return cuda_fail (e, "Arnoldi step");
+          aa.gcol = j;
+          const bool last = j == m - 1 || total >= maxit;
+          if ((j + 1 - checked) < CHECK_EVERY && !last) continue;
+          // the Givens step of column j itself, then the residual history
+          k_givens<<<1, KT, smem, st>>> (aa, j);
+          aa.gcol = -1;
+          // residual history of the steps since the last read, and the
+          // barrier status
+          const int cnt = j + 1 - checked;
+          cudaMemcpyAsync (K.pin, aa.res + checked, sizeof (double) * cnt,
+                           cudaMemcpyDeviceToHost, st);
+          cudaMemcpyAsync (K.pin + cnt, status, sizeof (int), cudaMemcpyDeviceToHost, st);
           if ((e = cudaStreamSynchronize (st)) != cudaSuccess) return cuda_fail (e, "GMRES step");
-          // Givens rotations of column j of the Hessenberg matrix
-          double *col = &H[(size_t) j * (m + 1)];
-          for (int i = 0; i <= j + 1; i++) col[i] = K.pin[i];
-          for (int i = 0; i < j; i++)
+          int stat = 0;
+          memcpy (&stat, K.pin + cnt, sizeof (int));
+          if (stat)
+            return set_error (STOKES_GPU_ETIMEOUT, "GMRES: a grid barrier wait ran out");
+          for (int q = 0; q < cnt; q++)
             {
-              const double t0 = cs[i] * col[i] + sn[i] * col[i + 1];
-              col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
-              col[i] = t0;
+              if (dbg)
+                fprintf (dbg, "gmres: step %d, residual estimate %.6e\n", checked + q, K.pin[q]);
+              if (K.pin[q] <= eps)
+                {
+                  jj = checked + q + 1;
+                  conv = true;
+                  break;
+                }
             }
-          const double r = hypot (col[j], col[j + 1]);
-          cs[j] = r > 0.0 ? col[j] / r : 1.0;
-          sn[j] = r > 0.0 ? col[j + 1] / r : 0.0;
-          col[j] = r;
-          col[j + 1] = 0.0;
-          g[j + 1] = -sn[j] * g[j];
-          g[j] = cs[j] * g[j];
-          rel = fabs (g[j + 1]) / bnrm;
-          if (dbg) fprintf (dbg, "gmres: %d applications, residual estimate %.6e\n", total, rel);
-          if (rel <= eps || K.pin[j + 1] == 0.0)
-            {
-              j++;
-              done = true;
-              break;
-            }
+          if (conv) break;
+          checked = j + 1;
+          jj = j + 1;
         }
-      // y = R^{-1} g, x += V y
-      for (int i = j - 1; i >= 0; i--)
+      // x += V y, y = R^{-1} g over the steps taken (or up to convergence)
+      if (jj > 0)
         {
-          double s = g[i];
-          for (int k = i + 1; k < j; k++) s -= H[(size_t) k * (m + 1) + i] * y[k];
-          const double d = H[(size_t) i * (m + 1) + i];
-          y[i] = d != 0.0 ? s / d : 0.0;
+          k_lsq<<<1, 32, 0, st>>> (arn, aa.g, m, jj, (double *) K.cv.p);
+          k_vcombine<<<gn, KT, 0, st>>> (d_x, V, (size_t) n, (const double *) K.cv.p, jj, n, 1.0);
         }
-      if (j > 0)
-        {
-          for (int i = 0; i < j; i++) K.pin[i] = y[i];
-          cudaMemcpyAsync (K.cv.p, K.pin, sizeof (double) * j, cudaMemcpyHostToDevice, st);
-          k_vcombine<<<gn, KT, 0, st>>> (d_x, V, (size_t) n, (const double *) K.cv.p, j, n, 1.0);
-          // the pinned buffer is reused below: finish the copy first
-          if ((e = cudaStreamSynchronize (st)) != cudaSuccess) return cuda_fail (e, "GMRES update");
-        }
-      (void) done;   // the true residual at the top of the loop decides
     }
   *iters = total;
   *res = rel;
