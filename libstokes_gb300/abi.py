@@ -36,6 +36,17 @@ SOLVE_RES = 0
 SOLVE_MOB_FTS = 1
 
 
+class TrajFrame(C.Structure):
+    """struct stokes_traj_frame (include/stokes_traj.h)."""
+    _fields_ = [("time", C.c_double), ("shear_shift", C.c_double)] + [
+        (k, _dp) for k in ("x", "u", "o", "e", "f", "t", "s", "q", "xf")] + [
+        ("rng", C.c_void_p)]
+
+
+TRAJ_X, TRAJ_U, TRAJ_O, TRAJ_E, TRAJ_F, TRAJ_T, TRAJ_S, TRAJ_Q, TRAJ_XF, TRAJ_RNG = (
+    1, 2, 4, 8, 16, 32, 64, 128, 256, 512)
+
+
 class IterStruct(C.Structure):
     """struct iter (include/stokes_iter.h)."""
     _fields_ = [("solver", C.c_char_p), ("max", C.c_int), ("restart", C.c_int),
@@ -187,6 +198,15 @@ _SIGS = {
     "stokes_gpu_get_precision": (C.c_int, [_SP, _ip]),
     "stokes_gpu_release": (C.c_int, [_SP]),
     "stokes_gpu_atimes": (C.c_int, [_SP, _dp, _dp]),
+    # trajectory files (include/stokes_traj.h)
+    "stokes_traj_create": (C.c_void_p, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    "stokes_traj_open": (C.c_void_p, [C.c_char_p]),
+    "stokes_traj_close": (None, [C.c_void_p]),
+    "stokes_traj_append": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "stokes_traj_read": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "stokes_traj_nframes": (C.c_int, [C.c_void_p]),
+    "stokes_traj_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), C.POINTER(C.c_int), _dp, _dp, _dp]),
     # iterative solves (include/stokes_iter.h)
     "iter_init": (C.c_void_p, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int, _dp, C.c_int,
                                C.c_int, C.c_void_p]),

@@ -27,7 +27,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-Wall", "--expt-relaxed-constexpr",
                      "-I", INCLUDE, "-I", CSRC]
-CC_FLAGS = ["-O2", "-fPIC", "-std=c11", "-Wall", "-I", INCLUDE, "-I", CSRC]
+# -ffp-contract=off: the host set-up gives the same bits on x86 and Arm
+CC_FLAGS = ["-O2", "-fPIC", "-std=c11", "-Wall", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 
 def _nvcc() -> str:

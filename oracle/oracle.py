@@ -39,7 +39,9 @@ def build_oracle(force: bool = False) -> str:
         obj = ORACLE_SO + "." + os.path.basename(src) + ".o"
         cc = "g++" if src.endswith(".cpp") else "gcc"
         std = ["-std=c++17"] if src.endswith(".cpp") else []
-        subprocess.check_call([cc, "-O2", "-fPIC", "-fopenmp"] + std + ["-c", src, "-o", obj])
+        # no contraction of a * b + c into FMA: the same bits on x86 and Arm
+        subprocess.check_call([cc, "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off"] + std
+                              + ["-c", src, "-o", obj])
         objs.append(obj)
     subprocess.check_call(["g++", "-shared", "-fopenmp", "-o", ORACLE_SO] + objs + ["-lm"])
     for obj in objs:

@@ -124,3 +124,43 @@ def test_get_fact_and_n(lib):
     assert lib.BD_get_n(run.s.sp) == 6 * run.n
     assert abs(lib.BD_params_get_fact(run.bd, 1e-3) - np.sqrt(2.0 / (2.0 * 1e-3))) < 1e-15
     run.close()
+
+
+def test_resume_from_checkpoint(lib, tmp_path):
+    """A run stopped after two steps and resumed from its checkpoint file
+    (positions, time and the generator state, include/stokes_traj.h)
+    continues exactly as the uninterrupted run."""
+    from libstokes_gb300 import FP64
+    from libstokes_gb300.abi import TrajFrame, _d
+    r = bd_case("f_lj")
+    run = Run(lib, r, int(r["seed"]), FP64)
+    x = r["pos"].copy()
+    t = 0.0
+    path = str(tmp_path / "bd.traj").encode()
+    tr = lib.stokes_traj_create(path, run.n, 0, 1 | 512, run.s.sp)
+    for _ in range(2):
+        t += lib.BD_evolve_mid(t, run.bd, _dp(x), None, float(r["dt"]))
+    fr = TrajFrame()
+    fr.time = t
+    fr.x = _d(x)
+    fr.rng = C.cast(run.bd.contents.rng, C.c_void_p)
+    assert lib.stokes_traj_append(tr, C.byref(fr)) == 0
+    lib.stokes_traj_close(tr)
+    for _ in range(2):
+        t += lib.BD_evolve_mid(t, run.bd, _dp(x), None, float(r["dt"]))
+    run.close()
+
+    run2 = Run(lib, r, 12345, FP64)        # another seed: the file sets the state
+    tr = lib.stokes_traj_open(path)
+    x2 = np.zeros(3 * run2.n)
+    rd = TrajFrame()
+    rd.x = _d(x2)
+    rd.rng = C.cast(run2.bd.contents.rng, C.c_void_p)
+    assert lib.stokes_traj_read(tr, 0, C.byref(rd)) == 0
+    lib.stokes_traj_close(tr)
+    t2 = rd.time
+    for _ in range(2):
+        t2 += lib.BD_evolve_mid(t2, run2.bd, _dp(x2), None, float(r["dt"]))
+    assert t2 == t
+    np.testing.assert_array_equal(x2, x)
+    run2.close()
