@@ -490,8 +490,16 @@ collect_times (Ctx *c)
   // events: start, end of the reciprocal part before the real space, end of
   // the real space, end; the reciprocal time is the rest of the product
   float t_real = 0.f, t_all = 0.f;
-  cudaEventElapsedTime (&t_real, c->ev[1], c->ev[2]);
-  cudaEventElapsedTime (&t_all, c->ev[0], c->ev[3]);
+  if (cudaEventElapsedTime (&t_all, c->ev[0], c->ev[3]) != cudaSuccess)
+    {
+      cudaGetLastError ();   // leave no error for the next launch check
+      return;
+    }
+  if (cudaEventElapsedTime (&t_real, c->ev[1], c->ev[2]) != cudaSuccess)
+    {
+      cudaGetLastError ();
+      t_real = (float) c->times[1];
+    }
   c->times[0] = t_all;
   c->times[1] = t_real;
   c->times[2] = t_all - t_real;
@@ -510,6 +518,20 @@ atimes_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y, cudaStr
 // host buffers in and out; positions from sys->pos
 void clear_error () { t_err = STOKES_GPU_OK; t_msg[0] = 0; }
 
+// the device address of a pinned (page-locked, mapped) host buffer, or
+// nullptr for any other memory
+static void *
+mapped_host (const void *p)
+{
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes (&at, p) != cudaSuccess)
+    {
+      cudaGetLastError ();
+      return nullptr;
+    }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int
 atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
 {
@@ -522,14 +544,30 @@ atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
   const int np = sys->np, n = NCOMP (sys->version) * np;
   cudaError_t e;
   if ((e = c->pos.ensure (sizeof (double) * 3 * np)) != cudaSuccess) return cuda_fail (e, "pos");
-  if ((e = c->x.ensure (sizeof (double) * n)) != cudaSuccess) return cuda_fail (e, "x");
-  if ((e = c->y.ensure (sizeof (double) * n)) != cudaSuccess) return cuda_fail (e, "y");
+  // pinned host buffers (cudaHostAlloc, cudaHostRegister) are used in place
+  // through their device mapping -- over the CPU-GPU link -- without a
+  // staging copy and its latency: y always (each element is written once),
+  // x on the mixed paths, which read it twice (the FP64 kernels read x once
+  // per reciprocal vector or pair and take a device copy); other host
+  // memory goes through device copies
+  const double *d_x = c->precision == STOKES_GPU_MIXED ? (const double *) mapped_host (x) : nullptr;
+  double *d_y = (double *) mapped_host (y);
+  if (!d_x)
+    {
+      if ((e = c->x.ensure (sizeof (double) * n)) != cudaSuccess) return cuda_fail (e, "x");
+      cudaMemcpyAsync (c->x.p, x, sizeof (double) * n, cudaMemcpyHostToDevice, c->stream);
+      d_x = (const double *) c->x.p;
+    }
+  if (!d_y)
+    {
+      if ((e = c->y.ensure (sizeof (double) * n)) != cudaSuccess) return cuda_fail (e, "y");
+    }
   cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * np, cudaMemcpyHostToDevice, c->stream);
-  cudaMemcpyAsync (c->x.p, x, sizeof (double) * n, cudaMemcpyHostToDevice, c->stream);
-  rc = atimes_dev (c, (const double *) c->pos.p, (const double *) c->x.p, (double *) c->y.p,
-                   c->stream, true);
+  rc = atimes_dev (c, (const double *) c->pos.p, d_x, d_y ? d_y : (double *) c->y.p, c->stream,
+                   true);
   if (rc) return rc;
-  e = cudaMemcpyAsync (y, c->y.p, sizeof (double) * n, cudaMemcpyDeviceToHost, c->stream);
+  e = d_y ? cudaSuccess
+          : cudaMemcpyAsync (y, c->y.p, sizeof (double) * n, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize (c->stream);
   if (e != cudaSuccess) return cuda_fail (e, "atimes");
   collect_times (c);

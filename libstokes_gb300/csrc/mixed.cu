@@ -818,20 +818,22 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
 // a CUDA graph: the first call with a new configuration launches directly,
 // the second records the sequence into a graph (stream capture), later calls
 // replay it with one launch.  The configuration key covers the split, every
-// buffer and the caller's pointers, which the recorded kernels hold.  Timed
-// or per-kernel-profiled products, products issued while the caller's
-// stream is itself being captured, and LIBSTOKES_GB300_GRAPHS=0 launch
-// directly.
+// buffer, the caller's pointers and the phase events, which the recorded
+// nodes hold.  Products inside a profiling window, products issued while
+// the caller's stream is itself being captured, and
+// LIBSTOKES_GB300_GRAPHS=0 launch directly.
 template <class Seq>
 static int
 run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_x, double *d_y,
-                    cudaStream_t st, bool timed, Seq &sequence)
+                    cudaStream_t st, cudaEvent_t *E, Seq &sequence)
 {
   static const bool enabled = [] {
     const char *g = getenv ("LIBSTOKES_GB300_GRAPHS");
     return !(g && strcmp (g, "0") == 0);
   }();
-  bool use = enabled && !timed && !c->kprof_on;
+  // the context's own phase events record from inside the graph (event
+  // record nodes); a profiling window's ring of events changes per product
+  bool use = enabled && !c->kprof_on && (E == nullptr || E == c->ev);
   if (use)
     {
       cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -851,7 +853,17 @@ run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_
                         m->rowm.p, m->rot.p, m->img_zf.p, m->img_wb.p, m->h_status, m->tyz.p,
                         m->img.p};
   for (const void *p : ptrs) mix ((uint64_t) (uintptr_t) p);
-  if (m->gexec && key == m->gkey) return cuda_ok (cudaGraphLaunch (m->gexec, st), "mixed product graph");
+  mix ((uint64_t) (uintptr_t) E);
+  // a captured cudaEventRecord is only a dependency, not a record: around a
+  // replay the start and end events are recorded on the stream itself, and
+  // the real / reciprocal split keeps the last direct launch's events
+  auto replay = [&] () -> int {
+    if (E) cudaEventRecord (E[0], st);
+    const cudaError_t le = cudaGraphLaunch (m->gexec, st);
+    if (E) cudaEventRecord (E[3], st);
+    return cuda_ok (le, "mixed product graph");
+  };
+  if (m->gexec && key == m->gkey) return replay ();
   if (key != m->gcand)
     {
       m->gcand = key;
@@ -888,7 +900,7 @@ run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_
       return sequence ();
     }
   m->gkey = key;
-  return cuda_ok (cudaGraphLaunch (m->gexec, st), "mixed product graph");
+  return replay ();
 }
 
 int
@@ -1158,7 +1170,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     if (e != cudaSuccess) return cuda_fail (e, "mixed kernels");
     return STOKES_GPU_OK;
   };
-  int rs = run_mixed_sequence (c, m, d_pos, d_x, d_y, st, E != nullptr, sequence);
+  int rs = run_mixed_sequence (c, m, d_pos, d_x, d_y, st, E, sequence);
   if (rs) return rs;
   c->launches = m->nkh == 0 ? 3 : (m->tensor ? 6 : 5);
   c->timed = timed;
