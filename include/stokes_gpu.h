@@ -54,6 +54,11 @@ int stokes_gpu_get_precision (const struct stokes *sys, int *mode);
 /* free the device state kept for sys (stokes_free does this too) */
 int stokes_gpu_release (struct stokes *sys);
 
+/* called by stokes_set_xi: notes the split and tables it built, so that
+ * the FP64 products may run at a cheaper split while the struct still holds
+ * exactly those tables (tables set by hand are used as they are) */
+void stokes_gpu_note_split (const struct stokes *sys);
+
 /* y = M x with host buffers; the status-returning form of atimes_3all:
  * the Ewald sum of a periodic system, the free-space sum of an open one
  * (sys->periodic == 0, which needs neither a box nor a split) */

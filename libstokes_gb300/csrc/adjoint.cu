@@ -536,7 +536,12 @@ stokes_gpu_vjp (struct stokes *sys, const double *g, const double *f, double *dL
   }
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  // the adjoint's own split (or, with eta 0, the system's): not the tuned
+  // split of the FP64 products
+  const bool tune = c->tune;
+  c->tune = false;
   int rc = prepare (c, sys, false, 1);
+  c->tune = tune;
   if (rc) return rc;
   const int np = sys->np, C = NCOMP (sys->version), nk = c->nk;
   const size_t n = (size_t) C * np;

@@ -138,6 +138,7 @@ free_ctx (Ctx *c)
   for (int q = 0; q < 2; q++) cudaEventDestroy (c->join[q]);
   cudaStreamDestroy (c->stream);
   release_mixed (c);
+  if (c->tuned) stokes_free (c->tuned);
   delete c;
 }
 
@@ -308,6 +309,133 @@ upload_if_changed (DevBuf &buf, uint64_t &fp, const void *host, size_t bytes,
   return STOKES_GPU_OK;
 }
 
+// ---- the tuned FP64 split ---------------------------------------------------
+// The reference's split xi = sqrt(pi) / L puts nearly all of the work in
+// real space (hundreds of lattice images at N = 1000).  For equal spheres the
+// FP64 products run at xi = eta / V^(1/3) instead (eta 6 up to 1024
+// particles, 8 up to 4096, 10 above; LIBSTOKES_GB300_FP64_ETA sets it, 0
+// keeps the reference's split), set up by the reference's own rules on a
+// private copy of the system.  The sum is split-invariant to rounding
+// (measured 5e-15 to 8e-15 against the reference's split) -- except under
+// the rmin clamp, which changes only the real-space part, so systems with
+// rmin > 0 keep the reference's split.  libstokes' FTS result depends on its
+// xi through the sign of its reciprocal G term (src/ewald.c:1060-1066):
+// y(xi) = y_inv + 2 G(xi), G the reciprocal G part as libstokes evaluates
+// it.  The tuned table therefore carries the invariant sign (-G on the tuned
+// k set) and adds 2 G(xi_ref) on the reference's k set, which reproduces
+// y(xi_ref).
+static double
+tuned_eta (int np)
+{
+  static const double env = [] {
+    const char *s = getenv ("LIBSTOKES_GB300_FP64_ETA");
+    return s ? atof (s) : -1.0;
+  }();
+  if (env >= 0.0) return env;
+  return np <= 1024 ? 6.0 : (np <= 4096 ? 8.0 : 10.0);
+}
+
+// the split and tables stokes_set_xi built for each system
+struct SplitNote {
+  double v[8];
+  const void *rl[3];
+};
+static std::unordered_map<const void *, SplitNote> g_split;   // guarded by g_mu
+
+static SplitNote
+split_note (const struct stokes *sys)
+{
+  SplitNote n;
+  const double v[8] = {sys->xi, sys->ewald_eps, sys->rmax2, sys->kmax, (double) sys->nr,
+                       (double) sys->kmaxx, (double) sys->kmaxy, (double) sys->kmaxz};
+  memcpy (n.v, v, sizeof v);
+  n.rl[0] = sys->rlx;
+  n.rl[1] = sys->rly;
+  n.rl[2] = sys->rlz;
+  return n;
+}
+
+static bool
+split_is_as_set (const struct stokes *sys)
+{
+  const SplitNote now = split_note (sys);
+  std::lock_guard<std::mutex> lk (g_mu);
+  auto it = g_split.find (sys);
+  return it != g_split.end () && memcmp (&it->second, &now, sizeof now) == 0;
+}
+
+static bool
+tuned_applies (const Ctx *c, const struct stokes *sys, bool cube)
+{
+  const double eta = tuned_eta (sys->np);
+  return c->tune && eta > 0.0 && !cube && !c->open && sys->periodic && split_is_as_set (sys)
+         && sys->a == nullptr && sys->slip == nullptr && sys->shear_mode == 0
+         && sys->rmin == 0.0 && sys->np > 0 && eta > sys->xi * cbrt (sys->lx * sys->ly * sys->lz);
+}
+
+// the private copy at the tuned split (rebuilt when the box, size, version
+// or accuracy change)
+static const struct stokes *
+tuned_system (Ctx *c, const struct stokes *sys)
+{
+  const double eps = sys->ewald_eps > 0.0 ? sys->ewald_eps : 1e-12;
+  const double eta = tuned_eta (sys->np);
+  const double key[7] = {sys->lx, sys->ly, sys->lz, (double) sys->np, (double) sys->version,
+                         eta, eps};
+  if (c->tuned && memcmp (c->tuned_key, key, sizeof key) == 0) return c->tuned;
+  if (c->tuned) stokes_free (c->tuned);
+  struct stokes *sv = stokes_init ();
+  if (!sv) return nullptr;
+  sv->version = sys->version;
+  sv->periodic = 1;
+  stokes_set_np (sv, sys->np, sys->nm);
+  stokes_set_l (sv, sys->lx, sys->ly, sys->lz);
+  stokes_set_xi (sv, eta / cbrt (sys->lx * sys->ly * sys->lz), eps);
+  c->tuned = sv;
+  memcpy (c->tuned_key, key, sizeof key);
+  return sv;
+}
+
+// FTS: -G on the tuned k set, +2 G(xi_ref) on the reference's k set (merged
+// into a tuned entry with the same k, appended otherwise)
+static void
+g_correction (const struct stokes *sys, std::vector<double> &kt)
+{
+  const double k0x = 2.0 * M_PI / sys->lx, k0y = 2.0 * M_PI / sys->ly, k0z = 2.0 * M_PI / sys->lz;
+  auto key = [] (long long a, long long b, long long c) {
+    return (a + 4096) * 8192 * 8192 + (b + 4096) * 8192 + (c + 4096);
+  };
+  std::unordered_map<long long, size_t> at;
+  const size_t nk = kt.size () / KT_STRIDE;
+  for (size_t q = 0; q < nk; q++)
+    {
+      double *row = &kt[q * KT_STRIDE];
+      row[KT_YG] = -row[KT_YG];
+      at.emplace (key (llrint (row[KT_KX] / k0x), llrint (row[KT_KY] / k0y),
+                       llrint (row[KT_KZ] / k0z)), q);
+    }
+  std::vector<double> ref;
+  build_ktable (sys, ref);
+  const size_t nr = ref.size () / KT_STRIDE;
+  for (size_t q = 0; q < nr; q++)
+    {
+      const double *row = &ref[q * KT_STRIDE];
+      const double g2 = 2.0 * row[KT_YG];
+      const auto hit = at.find (key (llrint (row[KT_KX] / k0x), llrint (row[KT_KY] / k0y),
+                                     llrint (row[KT_KZ] / k0z)));
+      if (hit != at.end ())
+        {
+          kt[hit->second * KT_STRIDE + KT_YG] += g2;
+          continue;
+        }
+      double add[KT_STRIDE];
+      memcpy (add, row, sizeof add);
+      add[KT_YA] = add[KT_YB] = add[KT_YC] = add[KT_YH] = add[KT_YM] = 0.0;
+      add[KT_YG] = g2;
+      kt.insert (kt.end (), add, add + KT_STRIDE);
+    }
+}
+
 int
 prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
 {
@@ -343,10 +471,20 @@ prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
       return upload_if_changed (c->pp, c->fp_pp, c->h_pp.data (), sizeof (double) * c->h_pp.size (),
                                 c->stream, "particle table");
     }
+  // the system whose split the FP64 tables follow
+  const struct stokes *ts = sys;
+  if (tuned_applies (c, sys, cube))
+    {
+      ts = tuned_system (c, sys);
+      if (!ts) return set_error (STOKES_GPU_ENOMEM, "tuned split");
+      c->xi = ts->xi;
+      c->xisp = ts->xi / sqrt (M_PI);
+      c->rmax2 = ts->rmax2;
+    }
   if (c->open)
     c->h_img.assign (1, Img4 {0.0, 0.0, 0.0, 0.0});
   else
-    build_images (sys, cube, c->h_img);
+    build_images (ts, cube, c->h_img);
   c->nimg = (int) c->h_img.size ();
   rc = upload_if_changed (c->img, c->fp_img, c->h_img.data (), sizeof (Img4) * c->h_img.size (),
                           c->stream, "image table");
@@ -354,12 +492,16 @@ prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
   if (c->open)
     c->h_kt.clear ();
   else
-    build_ktable (sys, c->h_kt);
+    {
+      build_ktable (ts, c->h_kt);
+      if (ts != sys && sys->version == 2) g_correction (sys, c->h_kt);
+    }
   c->nk = (int) (c->h_kt.size () / KT_STRIDE);
   rc = upload_if_changed (c->kt, c->fp_kt, c->h_kt.data (), sizeof (double) * c->h_kt.size (),
                           c->stream, "reciprocal table");
   if (rc) return rc;
-  build_particles (sys, c->mode, c->h_pp, c->open);
+  // self terms at the split of the tables (radii: the system's own)
+  build_particles (ts, c->mode, c->h_pp, c->open);
   rc = upload_if_changed (c->pp, c->fp_pp, c->h_pp.data (), sizeof (double) * c->h_pp.size (),
                           c->stream, "particle table");
   if (rc) return rc;
@@ -723,7 +865,20 @@ int
 stokes_gpu_release (struct stokes *sys)
 {
   release_adjoint (sys);
+  {
+    std::lock_guard<std::mutex> lk (g_mu);
+    g_split.erase (sys);
+  }
   return release_ctx (sys);
+}
+
+void
+stokes_gpu_note_split (const struct stokes *sys)
+{
+  if (!sys) return;
+  const SplitNote n = split_note (sys);
+  std::lock_guard<std::mutex> lk (g_mu);
+  g_split[sys] = n;
 }
 
 int

@@ -55,6 +55,12 @@ struct Ctx {
   // non-periodic (free-space) operator: set for systems with periodic = 0 and
   // by the *_nonewald_* entry points (force_open), src/non-ewald.c
   bool open = false, force_open = false;
+  // FP64 products of an equal-sphere periodic system run at a cheaper
+  // Ewald split than the reference's (prepare): a private copy of the
+  // system set up at that split, its key, and whether prepare may use it
+  struct stokes *tuned = nullptr;
+  double tuned_key[7] = {0, 0, 0, 0, 0, 0, 0};
+  bool tune = true;
   size_t kprof_n = 0;
   std::vector<cudaEvent_t> kprof_ev;
   std::vector<const char *> kprof_name;

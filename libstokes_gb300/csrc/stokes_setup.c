@@ -364,6 +364,7 @@ stokes_set_xi (struct stokes *sys, double xi, double ewald_eps)
   sys->nr = nr;
   fill_k_table (sys);
   sys->flag_table = 1;
+  stokes_gpu_note_split (sys);
 }
 
 double
