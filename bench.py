@@ -214,7 +214,7 @@ def matrix_measure(lib, abi, L, torch, dev, pos, Lbox):
     nbytes = 8.0 * n * n
     peak = measured_peaks().get("hbm_gbs")
     P = C.c_longlong()
-    abi.check(lib.stokes_gpu_count_real_terms(s.sp, C.byref(P)))
+    abi.check(lib.stokes_gpu_count_real_terms_dense(s.sp, C.byref(P)))
     s.close()
     del d_mat
     torch.cuda.empty_cache()

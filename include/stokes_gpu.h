@@ -167,8 +167,11 @@ int stokes_gpu_kprof_end (struct stokes *sys, int max_kernels, char *names, doub
 int stokes_gpu_last_launches (const struct stokes *sys, int *count);
 
 /* number of real-space (i, j, image) terms with 0 < r^2 <= rmax2 -- the
- * unit count of the real-space roofline */
+ * unit count of the real-space roofline -- at the split of the FP64
+ * product (the tuned split where it applies) and at that of the dense
+ * builder (the reference's split) */
 int stokes_gpu_count_real_terms (struct stokes *sys, long long *count);
+int stokes_gpu_count_real_terms_dense (struct stokes *sys, long long *count);
 
 /* split chosen by the mixed path for sys (after its first mixed product):
  * xi, rc, kc, eta = xi V^(1/3), eps, half-space k count, max |m| per axis */

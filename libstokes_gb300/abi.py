@@ -198,6 +198,7 @@ _SIGS = {
     "stokes_gpu_get_precision": (C.c_int, [_SP, _ip]),
     "stokes_gpu_release": (C.c_int, [_SP]),
     "stokes_gpu_note_split": (None, [_SP]),
+    "stokes_gpu_count_real_terms_dense": (C.c_int, [_SP, C.POINTER(C.c_longlong)]),
     "stokes_gpu_atimes": (C.c_int, [_SP, _dp, _dp]),
     # trajectory files (include/stokes_traj.h)
     "stokes_traj_create": (C.c_void_p, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),

@@ -462,6 +462,10 @@ prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
   // the free-space products (FP64 and mixed) read the particle table and the
   // FP64 set-up of the open system
   if (tables < 0) tables = c->precision == STOKES_GPU_MIXED && !c->open ? 0 : 1;
+  // the dense builder pays for every k vector once per pair: it keeps the
+  // reference's split, which is light in reciprocal space
+  const bool dense = tables == 2;
+  if (dense) tables = 1;
   if (!tables)
     {
       // the particle table only (radii for the BD interactions); equal
@@ -473,7 +477,7 @@ prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
     }
   // the system whose split the FP64 tables follow
   const struct stokes *ts = sys;
-  if (tuned_applies (c, sys, cube))
+  if (!dense && tuned_applies (c, sys, cube))
     {
       ts = tuned_system (c, sys);
       if (!ts) return set_error (STOKES_GPU_ENOMEM, "tuned split");
@@ -772,7 +776,7 @@ matrix_host (struct stokes *sys, double *mat, bool cube)
   if (mat == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL mat");
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
-  int rc = prepare (c, sys, cube, 1);
+  int rc = prepare (c, sys, cube, 2);
   if (rc) return rc;
   const int np = sys->np;
   const size_t n = (size_t) NCOMP (sys->version) * np;
@@ -803,7 +807,7 @@ atimes_matrix_host (struct stokes *sys, const double *x, double *y, bool cube)
   if (x == nullptr || y == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL x or y");
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
-  int rc = prepare (c, sys, cube, 1);
+  int rc = prepare (c, sys, cube, 2);
   if (rc) return rc;
   const int np = sys->np;
   const size_t n = (size_t) NCOMP (sys->version) * np;
@@ -942,7 +946,7 @@ stokes_gpu_matrix_dev (struct stokes *sys, const double *d_pos, double *d_mat, v
   if (d_mat == nullptr) return set_error (STOKES_GPU_EINVAL, "NULL mat");
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
-  int rc = prepare (c, sys, false, 1);
+  int rc = prepare (c, sys, false, 2);
   if (rc) return rc;
   return on_caller_stream (c, stream, [&] (cudaStream_t st) {
     if (d_pos == nullptr)

@@ -89,8 +89,9 @@ void build_particles (const struct stokes *sys, int mode, std::vector<double> &p
                       bool open = false);
 int release_ctx (const struct stokes *sys);
 // check sys and bring the context's device tables up to date.  tables: 1
-// builds the FP64 image and reciprocal tables (the FP64 product, the dense
-// builder, the adjoint), 0 skips them (the mixed product never reads them),
+// builds the FP64 image and reciprocal tables of the FP64 product (the
+// tuned split where it applies), 2 those of the dense builder (the
+// reference's split), 0 skips them (the mixed product never reads them),
 // -1 chooses by the context's precision.
 int prepare (Ctx *c, const struct stokes *sys, bool cube, int tables = -1);
 

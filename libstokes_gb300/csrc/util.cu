@@ -58,13 +58,13 @@ using namespace lsg;
 
 extern "C" {
 
-int
-stokes_gpu_count_real_terms (struct stokes *sys, long long *count)
+static int
+count_terms (struct stokes *sys, int tables, long long *count)
 {
   if (!count) return set_error (STOKES_GPU_EINVAL, "NULL count");
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
-  int rc = prepare (c, sys, false, 1);
+  int rc = prepare (c, sys, false, tables);
   if (rc) return rc;
   cudaError_t e;
   if ((e = c->pos.ensure (sizeof (double) * 3 * sys->np)) != cudaSuccess) return cuda_fail (e, "pos");
@@ -84,6 +84,20 @@ stokes_gpu_count_real_terms (struct stokes *sys, long long *count)
   if (e != cudaSuccess) return cuda_fail (e, "count");
   *count = (long long) h;
   return STOKES_GPU_OK;
+}
+
+// terms of the FP64 product's split (the tuned one where it applies)
+int
+stokes_gpu_count_real_terms (struct stokes *sys, long long *count)
+{
+  return count_terms (sys, 1, count);
+}
+
+// terms of the dense builder's split (the reference's)
+int
+stokes_gpu_count_real_terms_dense (struct stokes *sys, long long *count)
+{
+  return count_terms (sys, 2, count);
 }
 
 // GFLOP/s (2 flops per FMA) of an FMA-chain kernel filling the GPU
