@@ -215,14 +215,32 @@ def matrix_measure(lib, abi, L, torch, dev, pos, Lbox):
     peak = measured_peaks().get("hbm_gbs")
     P = C.c_longlong()
     abi.check(lib.stokes_gpu_count_real_terms_dense(s.sp, C.byref(P)))
+    # the split-precision builder (FP32 terms, FP64 entries) on the same
+    # system, and its largest entry error against the FP64 matrix
+    s.set_precision(abi.MIXED)
+    d_m32 = torch.empty_like(d_mat)
+    abi.check(lib.stokes_gpu_matrix_dev(s.sp, C.c_void_p(d_pos.data_ptr()),
+                                        C.c_void_p(d_m32.data_ptr()), sp))
+    torch.cuda.synchronize(dev)
+    e0.record(st)
+    abi.check(lib.stokes_gpu_matrix_dev(s.sp, C.c_void_p(d_pos.data_ptr()),
+                                        C.c_void_p(d_m32.data_ptr()), sp))
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms32 = e0.elapsed_time(e1)
+    err32 = float((d_m32 - d_mat).abs().max() / d_mat.abs().max())
     s.close()
-    del d_mat
+    del d_mat, d_m32
     torch.cuda.empty_cache()
     gbs = nbytes / (ms * 1e-3) / 1e9
     return {"workload": f"matrix_fts_n{w['n']}_phi{w['phi']:.2f}", "precision": "fp64",
             "ms": ms, "bytes": nbytes, "achieved_gbs": gbs, "hbm_peak_gbs": peak,
             "hbm_frac": gbs / peak if peak else None,
             "pair_image_terms": P.value, "terms_per_s": P.value / (ms * 1e-3),
+            "mixed": {"ms": ms32, "achieved_gbs": nbytes / (ms32 * 1e-3) / 1e9,
+                      "hbm_frac": (nbytes / (ms32 * 1e-3) / 1e9) / peak if peak else None,
+                      "max_err_over_max_entry": err32,
+                      "precision": "FP32 terms, FP64 entries (k_matrix_f32)"},
             "bound": "fp64-pipe: every pair-image term of the reference split "
                      "(xi = sqrt(pi)/L, eps 1e-12) builds an 11 x 11 block in FP64"}
 

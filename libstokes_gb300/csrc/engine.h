@@ -64,6 +64,11 @@ struct MatArgs {
   const double2 *ph;
   double *mat;
   int open = 0;         // non-periodic: free-space scalars (src/non-ewald.c)
+  int f32 = 0;          // equal spheres: FP32 terms (k_matrix_f32), with
+  const float4 *imgf = nullptr;   // the images as hi + lo floats,
+  const float4 *imgl = nullptr;
+  const float *ktf = nullptr;     // [nk][KTF_STRIDE]: e, ya, yb, yc, yg, yh, ym
+  const float2 *phf = nullptr;    // [nk][np] phases
 };
 
 cudaError_t launch_real_fp64 (int version, int mode, const RealArgs &a, cudaStream_t st);
@@ -74,6 +79,9 @@ cudaError_t launch_combine_fp64 (int version, const double *x, const double *par
                                  int nchunk, const double *yrec, const double *selfc,
                                  int np, double *y, cudaStream_t st);
 cudaError_t launch_matrix_fp64 (int version, int mode, const MatArgs &a, cudaStream_t st);
+constexpr int KTF_STRIDE = 12;   // floats per reciprocal vector of the FP32 builder
+cudaError_t launch_phase_f32 (const double *pos, const double *kt, int nk, int np, float2 *phf,
+                              cudaStream_t st);
 cudaError_t launch_gemv_fp64 (int version, const double *mat, const double *x,
                               double *zbuf, int np, double *y, cudaStream_t st);
 

@@ -404,29 +404,29 @@ __device__ __forceinline__ int sym4 (int a, int b, int c, int d)
     }
 }
 
-template <int V>
+template <int V, typename R = double>
 __device__ __forceinline__ void
-moments_add (const double e[3], const PairScalars<double> &s, double *mo)
+moments_add (const R e[3], const PairScalars<R> &s, R *mo)
 {
-  const double e2[6] = {e[0] * e[0], e[0] * e[1], e[0] * e[2], e[1] * e[1], e[1] * e[2], e[2] * e[2]};
-  const double a2 = s.xa - s.ya;
+  const R e2[6] = {e[0] * e[0], e[0] * e[1], e[0] * e[2], e[1] * e[1], e[1] * e[2], e[2] * e[2]};
+  const R a2 = s.xa - s.ya;
   mo[MO_A0] += s.ya;
 #pragma unroll
   for (int q = 0; q < 6; q++) mo[MO_A2 + q] += a2 * e2[q];
   if (V == V_F) return;
-  const double c2 = s.xc - s.yc;
+  const R c2 = s.xc - s.yc;
 #pragma unroll
   for (int q = 0; q < 3; q++) mo[MO_B1 + q] += s.yb * e[q];
   mo[MO_C0] += s.yc;
 #pragma unroll
   for (int q = 0; q < 6; q++) mo[MO_C2 + q] += c2 * e2[q];
   if (V == V_FT) return;
-  const double g1 = -s.xg / 3.0, g2 = s.yg, g3 = s.xg - 2.0 * s.yg;
-  const double m1 = 1.5 * s.xm - 2.0 * s.ym + 0.5 * s.zm;
-  const double m2 = -0.5 * s.xm + 0.5 * s.zm;
-  const double m3 = s.xm / 6.0 - 0.5 * s.zm;
-  const double m4 = 0.5 * s.ym - 0.5 * s.zm;
-  const double m5 = 0.5 * s.zm;
+  const R g1 = -s.xg / R (3.0), g2 = s.yg, g3 = s.xg - R (2.0) * s.yg;
+  const R m1 = R (1.5) * s.xm - R (2.0) * s.ym + R (0.5) * s.zm;
+  const R m2 = -R (0.5) * s.xm + R (0.5) * s.zm;
+  const R m3 = s.xm / R (6.0) - R (0.5) * s.zm;
+  const R m4 = R (0.5) * s.ym - R (0.5) * s.zm;
+  const R m5 = R (0.5) * s.zm;
 #pragma unroll
   for (int q = 0; q < 3; q++)
     {
@@ -434,7 +434,7 @@ moments_add (const double e[3], const PairScalars<double> &s, double *mo)
       mo[MO_G2 + q] += g2 * e[q];
     }
   // e3: xxx xxy xxz xyy xyz xzz yyy yyz yzz zzz
-  const double e3[10] = {e2[0] * e[0], e2[0] * e[1], e2[0] * e[2], e2[1] * e[1], e2[1] * e[2],
+  const R e3[10] = {e2[0] * e[0], e2[0] * e[1], e2[0] * e[2], e2[1] * e[1], e2[1] * e[2],
                          e2[2] * e[2], e2[3] * e[1], e2[3] * e[2], e2[4] * e[2], e2[5] * e[2]};
 #pragma unroll
   for (int q = 0; q < 10; q++) mo[MO_G3 + q] += g3 * e3[q];
@@ -446,7 +446,7 @@ moments_add (const double e[3], const PairScalars<double> &s, double *mo)
       mo[MO_M4B + q] += m4 * e2[q];
     }
   // e4: xxxx xxxy xxxz xxyy xxyz xxzz xyyy xyyz xyzz xzzz yyyy yyyz yyzz yzzz zzzz
-  const double e4[15] = {e2[0] * e2[0], e2[0] * e2[1], e2[0] * e2[2], e2[0] * e2[3], e2[0] * e2[4],
+  const R e4[15] = {e2[0] * e2[0], e2[0] * e2[1], e2[0] * e2[2], e2[0] * e2[3], e2[0] * e2[4],
                          e2[0] * e2[5], e2[1] * e2[3], e2[1] * e2[4], e2[1] * e2[5], e2[2] * e2[5],
                          e2[3] * e2[3], e2[3] * e2[4], e2[3] * e2[5], e2[4] * e2[5], e2[5] * e2[5]};
 #pragma unroll
@@ -455,11 +455,12 @@ moments_add (const double e[3], const PairScalars<double> &s, double *mo)
   mo[MO_M5] += m5;
 }
 
-__device__ __forceinline__ double
+template <typename R = double>
+__device__ __forceinline__ R
 levi (int a, int b, int c)
 {
-  if (a == b || b == c || a == c) return 0.0;
-  return ((a == 0 && b == 1) || (a == 1 && b == 2) || (a == 2 && b == 0)) ? 1.0 : -1.0;
+  if (a == b || b == c || a == c) return R (0);
+  return ((a == 0 && b == 1) || (a == 1 && b == 2) || (a == 2 && b == 0)) ? R (1) : R (-1);
 }
 
 // stresslet slots (xx, xy, xz, yz, yy) -> tensor indices
@@ -471,52 +472,56 @@ slot_ab (int q, int &a, int &b)
   b = B[q];
 }
 
-__device__ __forceinline__ double kd (int a, int b) { return a == b ? 1.0 : 0.0; }
+template <typename R = double>
+__device__ __forceinline__ R kd (int a, int b) { return a == b ? R (1) : R (0); }
 
 // G_(ab)c from moments
-__device__ __forceinline__ double
-g_tensor (const double *mo, int a, int b, int c)
+template <typename R>
+__device__ __forceinline__ R
+g_tensor (const R *mo, int a, int b, int c)
 {
-  return mo[MO_G1 + c] * kd (a, b) + mo[MO_G2 + a] * kd (b, c) + mo[MO_G2 + b] * kd (a, c)
+  return mo[MO_G1 + c] * kd<R> (a, b) + mo[MO_G2 + a] * kd<R> (b, c) + mo[MO_G2 + b] * kd<R> (a, c)
     + mo[MO_G3 + sym3 (a, b, c)];
 }
 // H_(ab)c = sum_n eps_bcn H2[an] + eps_acn H2[bn]
-__device__ __forceinline__ double
-h_tensor (const double *mo, int a, int b, int c)
+template <typename R>
+__device__ __forceinline__ R
+h_tensor (const R *mo, int a, int b, int c)
 {
-  double v = 0.0;
+  R v = R (0);
   for (int n = 0; n < 3; n++)
-    v += levi (b, c, n) * mo[MO_H2 + sym2 (a, n)] + levi (a, c, n) * mo[MO_H2 + sym2 (b, n)];
+    v += levi<R> (b, c, n) * mo[MO_H2 + sym2 (a, n)] + levi<R> (a, c, n) * mo[MO_H2 + sym2 (b, n)];
   return v;
 }
 // M_(ab)(cd)
-__device__ __forceinline__ double
-m_tensor (const double *mo, int a, int b, int c, int d)
+template <typename R>
+__device__ __forceinline__ R
+m_tensor (const R *mo, int a, int b, int c, int d)
 {
   return mo[MO_M4 + sym4 (a, b, c, d)]
-    + mo[MO_M2 + sym2 (c, d)] * kd (a, b) + mo[MO_M2 + sym2 (a, b)] * kd (c, d)
-    + mo[MO_M3] * kd (a, b) * kd (c, d)
-    + mo[MO_M4B + sym2 (a, d)] * kd (b, c) + mo[MO_M4B + sym2 (a, c)] * kd (b, d)
-    + mo[MO_M4B + sym2 (b, d)] * kd (a, c) + mo[MO_M4B + sym2 (b, c)] * kd (a, d)
-    + mo[MO_M5] * (kd (a, c) * kd (b, d) + kd (b, c) * kd (a, d));
+    + mo[MO_M2 + sym2 (c, d)] * kd<R> (a, b) + mo[MO_M2 + sym2 (a, b)] * kd<R> (c, d)
+    + mo[MO_M3] * kd<R> (a, b) * kd<R> (c, d)
+    + mo[MO_M4B + sym2 (a, d)] * kd<R> (b, c) + mo[MO_M4B + sym2 (a, c)] * kd<R> (b, d)
+    + mo[MO_M4B + sym2 (b, d)] * kd<R> (a, c) + mo[MO_M4B + sym2 (b, c)] * kd<R> (a, d)
+    + mo[MO_M5] * (kd<R> (a, c) * kd<R> (b, d) + kd<R> (b, c) * kd<R> (a, d));
 }
 
 // one block entry (extracted form) from the moments; same = (i == j)
-template <int V>
-__device__ __forceinline__ double
-block_entry (const double *mo, int row, int col, bool same)
+template <int V, typename R = double>
+__device__ __forceinline__ R
+block_entry (const R *mo, int row, int col, bool same)
 {
-  const double sgn = same ? -1.0 : 1.0;   // src/ft.c:61-75, src/fts.c:72-104
+  const R sgn = same ? R (-1) : R (1);   // src/ft.c:61-75, src/fts.c:72-104
   if (row < 3)
     {
       const int a = row;
       if (col < 3)
-        return mo[MO_A0] * kd (a, col) + mo[MO_A2 + sym2 (a, col)];
+        return mo[MO_A0] * kd<R> (a, col) + mo[MO_A2 + sym2 (a, col)];
       if (col < 6)
         {
           const int b = col - 3;
-          double v = 0.0;
-          for (int n = 0; n < 3; n++) v += levi (a, b, n) * mo[MO_B1 + n];
+          R v = R (0);
+          for (int n = 0; n < 3; n++) v += levi<R> (a, b, n) * mo[MO_B1 + n];
           return sgn * v;
         }
       int p, q;
@@ -528,12 +533,12 @@ block_entry (const double *mo, int row, int col, bool same)
       const int a = row - 3;
       if (col < 3)
         {
-          double v = 0.0;
-          for (int n = 0; n < 3; n++) v += levi (a, col, n) * mo[MO_B1 + n];
+          R v = R (0);
+          for (int n = 0; n < 3; n++) v += levi<R> (a, col, n) * mo[MO_B1 + n];
           return v;
         }
       if (col < 6)
-        return mo[MO_C0] * kd (a, col - 3) + mo[MO_C2 + sym2 (a, col - 3)];
+        return mo[MO_C0] * kd<R> (a, col - 3) + mo[MO_C2 + sym2 (a, col - 3)];
       int p, q;
       slot_ab (col - 6, p, q);
       return h_tensor (mo, p, q, a);
@@ -750,6 +755,157 @@ k_matrix_open (MatArgs a)
       blk[row * n + col] = block_entry<V> (mo, row, col, same);
 }
 
+// Split-precision dense builder for equal spheres: the structure of
+// k_matrix (one warp per pair, compacted image candidates, lanes over the
+// reciprocal vectors) with the terms in FP32 and no FP64 work per term (the
+// FP64 pipe of this GPU is 1/64 of FP32).  Separations r_j - r_i + image
+// are formed from hi + lo float pairs of both (the difference of the hi
+// parts is exact where it cancels, so a separation carries one FP32
+// rounding); the cutoff test runs on them (a candidate it misjudges lies at
+// the cutoff, where its term is below the split's accuracy).  Reciprocal
+// phases and coefficients come from float copies of the FP64 tables.
+// Moments accumulate in FP32 per lane (about ten terms each at the
+// reference's split), the lanes meet in FP32, and the block entries are
+// stored as FP64.  About 1e-7 of the largest entry against the FP64 builder.
+// phf[k * np + j] = (cos, sin)(k.r_j) in FP32, from FP64 arguments
+__global__ void
+k_phase_f32 (const double *pos, const double *kt, int nk, int np, float2 *phf)
+{
+  const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long) nk * np) return;
+  const int k = (int) (t / np), j = (int) (t % np);
+  const double *K = kt + KT_STRIDE * k;
+  const double th = K[KT_KX] * pos[3 * j] + K[KT_KY] * pos[3 * j + 1] + K[KT_KZ] * pos[3 * j + 2];
+  double sn, cs;
+  sincos (th, &sn, &cs);
+  phf[t] = make_float2 ((float) cs, (float) sn);
+}
+
+cudaError_t
+launch_phase_f32 (const double *pos, const double *kt, int nk, int np, float2 *phf,
+                  cudaStream_t st)
+{
+  const long long t = (long long) nk * np;
+  k_phase_f32<<<(int) ((t + 255) / 256), 256, 0, st>>> (pos, kt, nk, np, phf);
+  return cudaGetLastError ();
+}
+
+template <int V>
+__global__ void __launch_bounds__ (128)
+k_matrix_f32 (MatArgs a)
+{
+  constexpr int C = NComp<V>::value;
+  constexpr int NM = Moments<V>::N;
+  __shared__ float s_qd[4][RS_QCAP][3];
+  __shared__ float s_mo[4][NM];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long w = (long long) blockIdx.x * 4 + wib;
+  if (w >= (long long) a.np * a.np) return;
+  const int i = (int) (w / a.np), j = (int) (w % a.np);
+  const bool same = (i == j);
+  float mo[NM];
+#pragma unroll
+  for (int q = 0; q < NM; q++) mo[q] = 0.0f;
+  if (same && lane == 0)
+    {
+      PairScalars<float> s;
+      s.xa = s.ya = (float) a.selfc[3 * i];
+      s.xc = s.yc = (float) a.selfc[3 * i + 1];
+      s.xm = s.ym = s.zm = (float) a.selfc[3 * i + 2];
+      s.yb = s.xg = s.yg = s.yh = 0.0f;
+      const float e0[3] = {0.0f, 0.0f, 0.0f};
+      moments_add<V, float> (e0, s, mo);
+    }
+  const double djx = a.pos[3 * j] - a.pos[3 * i];
+  const double djy = a.pos[3 * j + 1] - a.pos[3 * i + 1];
+  const double djz = a.pos[3 * j + 2] - a.pos[3 * i + 2];
+  const float fjx = (float) djx, fjy = (float) djy, fjz = (float) djz;
+  const float ljx = (float) (djx - (double) fjx), ljy = (float) (djy - (double) fjy),
+              ljz = (float) (djz - (double) fjz);
+  const float rmax2f = (float) a.rmax2;
+  const float xi = (float) a.xi, xisp = (float) a.xisp, rmin2 = (float) (2.0 * a.rmin);
+  const unsigned lt = (1u << lane) - 1u;
+  int qn = 0;
+  auto real_one = [&] (float dx, float dy, float dz) {
+    float r = sqrtf (dx * dx + dy * dy + dz * dz);
+    if (r < rmin2) r = rmin2;
+    const float ri = 1.0f / r;
+    const float e[3] = {dx * ri, dy * ri, dz * ri};
+    PairScalars<float> s;
+    real_scalars_mono<V, float> (xi, xisp, r, s);
+    moments_add<V, float> (e, s, mo);
+  };
+  for (int m0 = 0; m0 < a.nimg; m0 += 32)
+    {
+      const int m = m0 + lane;
+      bool ok = false;
+      float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+      if (m < a.nimg)
+        {
+          const float4 Lh = a.imgf[m], Ll = a.imgl[m];
+          dx = (fjx + Lh.x) + (ljx + Ll.x);
+          dy = (fjy + Lh.y) + (ljy + Ll.y);
+          dz = (fjz + Lh.z) + (ljz + Ll.z);
+          const float rr = dx * dx + dy * dy + dz * dz;
+          // the zero separation (the pair's own image 0, or a distinct pair
+          // at identical positions) is skipped, as in k_matrix
+          ok = (rr != 0.0f) && (rr <= rmax2f);
+        }
+      const unsigned b2 = __ballot_sync (0xffffffffu, ok);
+      if (ok)
+        {
+          const int slot = qn + __popc (b2 & lt);
+          s_qd[wib][slot][0] = (float) dx;
+          s_qd[wib][slot][1] = (float) dy;
+          s_qd[wib][slot][2] = (float) dz;
+        }
+      qn += __popc (b2);
+      __syncwarp ();
+      if (qn >= 32)
+        {
+          const int slot = qn - 32 + lane;
+          real_one (s_qd[wib][slot][0], s_qd[wib][slot][1], s_qd[wib][slot][2]);
+          qn -= 32;
+          __syncwarp ();
+        }
+    }
+  if (lane < qn) real_one (s_qd[wib][lane][0], s_qd[wib][lane][1], s_qd[wib][lane][2]);
+
+  // reciprocal vectors: cos(k.(r_j - r_i)) from the float phase table
+  for (int k = lane; k < a.nk; k += 32)
+    {
+      const float *K = a.ktf + KTF_STRIDE * k;
+      const float2 pi_ = a.phf[(size_t) k * a.np + i];
+      const float2 pj = a.phf[(size_t) k * a.np + j];
+      const float cf = pj.x * pi_.x + pj.y * pi_.y;
+      const float sf = pj.x * pi_.y - pj.y * pi_.x;
+      const float e[3] = {K[0], K[1], K[2]};
+      PairScalars<float> s;
+      s.xa = 0.0f; s.ya = cf * K[3];
+      s.yb = sf * K[4];
+      s.xc = 0.0f; s.yc = cf * K[5];
+      s.xg = 0.0f; s.yg = sf * K[6];
+      s.yh = cf * K[7];
+      s.xm = 0.0f; s.ym = cf * K[8]; s.zm = 0.0f;
+      moments_add<V, float> (e, s, mo);
+    }
+
+#pragma unroll
+  for (int q = 0; q < NM; q++)
+    {
+      const float v = warp_sum (mo[q]);
+      if (lane == 0) s_mo[wib][q] = v;
+    }
+  __syncwarp ();
+  const size_t n = (size_t) C * a.np;
+  double *blk = a.mat + (size_t) C * i * n + (size_t) C * j;
+  for (int t = lane; t < C * C; t += 32)
+    {
+      const int row = t / C, col = t % C;
+      blk[row * n + col] = (double) block_entry<V, float> (s_mo[wib], row, col, same);
+    }
+}
+
 // dense y = M . z(x), one warp per row (z = extracted-form transform for FTS)
 __global__ void __launch_bounds__ (256)
 k_gemv (const double *mat, const double *z, int n, double *y)
@@ -893,6 +1049,13 @@ launch_matrix_fp64 (int version, int mode, const MatArgs &a, cudaStream_t st)
       return cudaGetLastError ();
     }
   const int grid = (int) ((nw + 3) / 4);
+  if (a.f32 && mode == MODE_MONO)
+    {
+      if (version == 0) k_matrix_f32<0><<<grid, 128, 0, st>>> (a);
+      else if (version == 1) k_matrix_f32<1><<<grid, 128, 0, st>>> (a);
+      else k_matrix_f32<2><<<grid, 128, 0, st>>> (a);
+      return cudaGetLastError ();
+    }
 #define LSG_DISPATCH(V)                                                        \
   if (mode == MODE_MONO) k_matrix<V, MODE_MONO><<<grid, 128, 0, st>>> (a);      \
   else if (mode == MODE_POLY) k_matrix<V, MODE_POLY><<<grid, 128, 0, st>>> (a); \

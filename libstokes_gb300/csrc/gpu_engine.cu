@@ -727,19 +727,21 @@ atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
 int
 matrix_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st)
 {
-  if (c->precision == STOKES_GPU_MIXED && !c->open)
-    return matrix_mixed_dev (c, d_pos, d_mat, st);
   const int np = c->np;
   cudaError_t e;
   if ((e = c->ph.ensure (sizeof (double2) * (size_t) (c->nk > 0 ? c->nk : 1) * np)) != cudaSuccess)
     return cuda_fail (e, "phase table");
   int launches = 0;
+  // mixed precision: FP32 terms for equal spheres (unequal radii and slip,
+  // and open systems, keep the FP64 builder)
+  const bool f32 = c->precision == STOKES_GPU_MIXED && !c->open && c->mode == MODE_MONO;
   kmark (c, st, nullptr);
   if (c->nk > 0)
     {
-      if ((e = launch_phase_fp64 (d_pos, (const double *) c->kt.p, c->nk, np,
-                                  (double2 *) c->ph.p, st)) != cudaSuccess)
-        return cuda_fail (e, "phase kernel");
+      e = f32 ? launch_phase_f32 (d_pos, (const double *) c->kt.p, c->nk, np, (float2 *) c->ph.p, st)
+              : launch_phase_fp64 (d_pos, (const double *) c->kt.p, c->nk, np, (double2 *) c->ph.p,
+                                   st);
+      if (e != cudaSuccess) return cuda_fail (e, "phase kernel");
       launches++;
       kmark (c, st, "k_phase");
     }
@@ -762,9 +764,44 @@ matrix_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st)
   a.ph = (const double2 *) c->ph.p;
   a.mat = d_mat;
   a.open = c->open ? 1 : 0;
+  a.f32 = f32 ? 1 : 0;
+  if (f32)
+    {
+      // float copies: images as hi + lo pairs, then the k table (e, ya..ym)
+      const size_t ni = (size_t) c->nimg, nk = (size_t) c->nk;
+      std::vector<float> f (8 * ni + KTF_STRIDE * nk + 4, 0.0f);
+      for (size_t q = 0; q < ni; q++)
+        {
+          const double v[3] = {c->h_img[q].x, c->h_img[q].y, c->h_img[q].z};
+          for (int d = 0; d < 3; d++)
+            {
+              const float hi = (float) v[d];
+              f[4 * q + d] = hi;
+              f[4 * (ni + q) + d] = (float) (v[d] - (double) hi);
+            }
+        }
+      float *kf = f.data () + 8 * ni;
+      for (size_t k = 0; k < nk; k++)
+        {
+          const double *K = c->h_kt.data () + KT_STRIDE * k;
+          const int src[9] = {KT_EX, KT_EY, KT_EZ, KT_YA, KT_YB, KT_YC, KT_YG, KT_YH, KT_YM};
+          for (int q = 0; q < 9; q++) kf[KTF_STRIDE * k + q] = (float) K[src[q]];
+        }
+      if ((e = c->imgf.ensure (sizeof (float) * f.size ())) != cudaSuccess)
+        return cuda_fail (e, "FP32 tables");
+      // pageable source: the copy is staged before the call returns, so the
+      // vector may go out of scope
+      if ((e = cudaMemcpyAsync (c->imgf.p, f.data (), sizeof (float) * f.size (),
+                                cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail (e, "FP32 tables");
+      a.imgf = (const float4 *) c->imgf.p;
+      a.imgl = a.imgf + ni;
+      a.ktf = (const float *) c->imgf.p + 8 * ni;
+      a.phf = (const float2 *) c->ph.p;
+    }
   if ((e = launch_matrix_fp64 (c->version, c->mode, a, st)) != cudaSuccess)
     return cuda_fail (e, "matrix kernel");
-  kmark (c, st, "k_matrix");
+  kmark (c, st, a.f32 ? "k_matrix_f32" : "k_matrix");
   c->launches = launches + 1;
   return STOKES_GPU_OK;
 }

@@ -68,10 +68,11 @@ struct Ctx {
   MixedState *mixed = nullptr;
 
   DevBuf openf;   // scratch of the mixed-precision free-space product
+  DevBuf imgf;    // the images in FP32 (split-precision dense builder)
 
-  std::array<DevBuf *, 13> all_buffers ()
+  std::array<DevBuf *, 14> all_buffers ()
   {
-    return {&pos, &x, &y, &img, &kt, &pp, &ph, &sf, &yrec, &partial, &mat, &zbuf, &openf};
+    return {&pos, &x, &y, &img, &kt, &pp, &ph, &sf, &yrec, &partial, &mat, &zbuf, &openf, &imgf};
   }
 };
 
@@ -109,7 +110,6 @@ void kmark (Ctx *c, cudaStream_t st, const char *name);
 // mixed-precision path (mixed.cu)
 int atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                       cudaStream_t st, bool timed);
-int matrix_mixed_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st);
 // free-space product of an open system in mixed precision (open_f32.cu)
 int atimes_open_f32_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                          cudaStream_t st, bool timed);

@@ -1177,12 +1177,6 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   return STOKES_GPU_OK;
 }
 
-int
-matrix_mixed_dev (Ctx *, const double *, double *, cudaStream_t)
-{
-  return set_error (STOKES_GPU_EINVAL, "the dense builder runs in FP64 only");
-}
-
 void
 release_mixed (Ctx *c)
 {

@@ -119,3 +119,35 @@ def test_mixed_rejects_unsupported(lib):
     with pytest.raises(GPUError):
         s.atimes(np.ones(60))
     s.close()
+
+
+@pytest.mark.parametrize("version,n,phi", [(0, 200, 0.2), (1, 150, 0.25), (2, 120, 0.3)])
+def test_mixed_dense_builder(lib, version, n, phi):
+    """The split-precision dense builder (k_matrix_f32: FP32 terms, FP64
+    entries) against the FP64 builder on the same system: largest entry
+    error <= 1e-6 of the largest entry; the matrix route of the product
+    (atimes_3all_matrix) against the FP64 product at the mixed bar."""
+    a, b, x = _pair(version, n, phi)
+    m64 = a.matrix()
+    m32 = b.matrix()
+    err = np.abs(m32 - m64).max() / np.abs(m64).max()
+    assert err < 1e-6, err
+    assert err > 0.0              # the FP32 builder, not the FP64 one
+    y = b.atimes_matrix(x)
+    assert rel_l2(y, a.atimes(x)) < TOL
+    a.close()
+    b.close()
+
+
+def test_mixed_dense_builder_golden(lib, products):
+    """Against the reference's own matrices (tests/golden), equal spheres."""
+    from conftest import make_system
+    from libstokes_gb300 import MIXED
+    for name in ("sc8_v0", "sc8_v1", "sc8_v2", "r12_v2_mono", "r12_v1_shear1"):
+        case = products[name]
+        s = make_system(case)
+        s.set_precision(MIXED)
+        m = s.matrix()
+        ref = case["mat"]
+        assert np.abs(m - ref).max() / np.abs(ref).max() < 1e-6, name
+        s.close()
