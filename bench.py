@@ -337,6 +337,54 @@ def solve_measure(lib, abi, L, torch, dev, pos, Lbox, product_ms):
             "timing": "wall clock around stokes_gpu_solve (host buffers in and out)"}
 
 
+def scale_measure(lib, abi, L, torch, dev, sizes=(4096, 16384), reps=10):
+    """The mixed FTS product at larger N (phi 0.30, the same placement
+    rule): products/s on device buffers (CUDA events on a side stream), the
+    per-kernel times of a separate profiled pass, and the roofline of the
+    dominant main-stream kernel, to show how the kernels behave as the
+    tensor-core GEMMs grow past the bench workload's small tiles."""
+    from libstokes_gb300.workloads import rsa_positions
+    out = []
+    for n in sizes:
+        pos, Lb = rsa_positions(n, WORKLOAD["phi"], seed=WORKLOAD["pos_seed"])
+        s = L.System(2, pos, (Lb,) * 3, tratio=WORKLOAD["tratio"], eps=WORKLOAD["eps"])
+        s.set_precision(abi.MIXED)
+        d_pos = torch.tensor(pos, dtype=torch.float64, device=dev).contiguous()
+        d_x = torch.randn(11 * n, dtype=torch.float64, device=dev)
+        d_y = torch.empty_like(d_x)
+        st = torch.cuda.Stream(dev)
+        sp = C.c_void_p(st.cuda_stream)
+
+        def product():
+            abi.check(lib.stokes_gpu_atimes_dev(s.sp, C.c_void_p(d_pos.data_ptr()),
+                                                C.c_void_p(d_x.data_ptr()),
+                                                C.c_void_p(d_y.data_ptr()), sp))
+        with torch.cuda.stream(st):
+            for _ in range(3):
+                product()
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                product()
+            e1.record(st)
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1) / reps
+            abi.check(lib.stokes_gpu_kprof_begin(s.sp, 16 * 3))
+            for _ in range(3):
+                product()
+            torch.cuda.synchronize(dev)
+        kprof = abi.kernel_profile(lib, s.sp)
+        kernels_ms = {k: v[0] / max(v[1], 1) for k, v in kprof.items()}
+        roof = roofline(lib, abi, s, 2, n, 11, kernels_ms, "mixed")
+        s.close()
+        out.append({"n": n, "ms_per_product": ms, "products_per_s": 1000.0 / ms,
+                    "kernels_ms": kernels_ms,
+                    "roofline": {k: roof.get(k) for k in ("kernel", "achieved", "peak", "frac",
+                                                          "kernel_ms", "unit")}})
+    return out
+
+
 ADJ_WORKLOAD = dict(name="vjp_ft_n2048_phi0.25", version=1, n=2048, phi=0.25, seed=42)
 
 
@@ -729,6 +777,8 @@ def run_gpu(args):
         line["open"] = open_measure(lib, abi, L, torch, dev, pos)
     if not args.no_solve and not fp64:
         line["solve"] = solve_measure(lib, abi, L, torch, dev, pos, Lbox, ms)
+    if not args.no_scale and not fp64:
+        line["scale"] = scale_measure(lib, abi, L, torch, dev)
     if not args.no_bd:
         line["bd"] = bd_measure(lib, abi, L, torch, dev)
     if not args.no_adjoint:
@@ -758,6 +808,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the ensemble (batch) leg")
     ap.add_argument("--no-matrix", action="store_true", help="skip the dense-builder leg")
     ap.add_argument("--no-solve", action="store_true", help="skip the iterative-solve leg")
+    ap.add_argument("--no-scale", action="store_true",
+                    help="skip the larger-N legs of the mixed product")
     ap.add_argument("--no-open", action="store_true",
                     help="skip the free-space (non-periodic) operator leg")
     ap.add_argument("--n", type=int, default=None,
