@@ -605,6 +605,24 @@ def roofline(lib, abi, sysm, version, n, c, kernels_ms, precision) -> dict:
     return out
 
 
+def max_over_ranks(v: float, world: int, dev=None) -> float:
+    """The largest value over the ranks of the initialised process group (the
+    slowest replica sets the step time); the value itself for one rank."""
+    if world <= 1:
+        return float(v)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(ms_max: float, world: int) -> float:
+    """Whole-job products/s: every replica does one product per step, the
+    step lasting as long as the slowest replica's."""
+    return world * 1000.0 / ms_max
+
+
 def run_gpu(args):
     import torch
     import libstokes_gb300 as L
@@ -688,13 +706,8 @@ def run_gpu(args):
     cnt = C.c_int()
     abi.check(lib.stokes_gpu_profile_end(sysm.sp, prof.ctypes.data_as(C.POINTER(C.c_double)),
                                          C.byref(cnt)))
-    ms = sum(step_ms) / len(step_ms)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 1000.0 / ms
+    ms = max_over_ranks(sum(step_ms) / len(step_ms), world, dev)
+    value = aggregate_rate(ms, world)
     launches = C.c_int()
     abi.check(lib.stokes_gpu_last_launches(sysm.sp, C.byref(launches)))
 
@@ -712,12 +725,7 @@ def run_gpu(args):
     for _ in range(args.steps):
         lib.atimes_ewald_3all(nvec, px, py, C.cast(sysm.sp, C.c_void_p))
     torch.cuda.synchronize(dev)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world, dev)
     abi.raise_if_failed()
 
     if rank != 0:
