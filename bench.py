@@ -423,6 +423,60 @@ def adjoint_measure(lib, abi, L):
             "timing": "wall clock around one call each, host buffers"}
 
 
+def fit_measure(lib, abi, L, steps=200):
+    """Positions fitted to a target velocity field (FT, N = 2048, phi 0.25):
+    loss |M(r) f - u*|^2 with u* = M(r*) f at r* = r + 0.05 N(0,1), the
+    gradient from the VJP at g = 2 (M f - u*), a step along -gradient with
+    backtracking (halve until the loss falls, then double the next trial).
+    Every step runs one VJP and one or more FP64 forward products through
+    the host API."""
+    from libstokes_gb300.workloads import rsa_positions
+    w = ADJ_WORKLOAD
+    pos, Lb = rsa_positions(w["n"], w["phi"], seed=w["seed"])
+    c = (3, 6, 11)[w["version"]]
+    rng = np.random.default_rng(10)
+    f = rng.standard_normal(c * w["n"])
+    t = L.System(w["version"], pos + 0.05 * rng.standard_normal(pos.shape), (Lb,) * 3)
+    u_star = t.atimes(f)
+    t.close()
+    s = L.System(w["version"], pos, (Lb,) * 3)
+    dp = abi._dp
+    dr = np.zeros(3 * w["n"])
+    db = np.zeros(3)
+
+    def loss_at(x):
+        lib.stokes_set_pos(s.sp, x.ctypes.data_as(dp))
+        r = s.atimes(f) - u_star
+        return float(r @ r), r
+
+    x = pos.reshape(-1).copy()
+    lv, r = loss_at(x)
+    l0 = lv
+    step, products = 1e-3, 1
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g = 2.0 * r
+        abi.check(lib.stokes_gpu_vjp(s.sp, g.ctypes.data_as(dp), f.ctypes.data_as(dp),
+                                     dr.ctypes.data_as(dp), db.ctypes.data_as(dp), None))
+        for _ in range(30):
+            xn = x - step * dr
+            ln, rn = loss_at(xn)
+            products += 1
+            if ln < lv:
+                break
+            step *= 0.5
+        if not ln < lv:
+            break
+        x, lv, r = xn, ln, rn
+        step *= 2.0
+    wall = time.perf_counter() - t0
+    s.close()
+    return {"workload": "fit_ft_n2048_phi0.25_200steps", "steps": steps, "wall_s": wall,
+            "s_per_step": wall / steps, "forward_products": products, "loss_initial": l0,
+            "loss_final": lv, "loss_ratio": lv / l0, "precision": "fp64 forward and VJP",
+            "timing": "wall clock, host buffers"}
+
+
 BATCH_WORKLOAD = dict(name="ensemble_512_n16-512_phi0.05-0.35_F_FT", nsys=512, nmin=16,
                       nmax=512, phimin=0.05, phimax=0.35, seed=2024, bd_steps=10, n_cheb=30)
 
@@ -791,6 +845,7 @@ def run_gpu(args):
         line["bd"] = bd_measure(lib, abi, L, torch, dev)
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measure(lib, abi, L)
+        line["adjoint"]["fit"] = fit_measure(lib, abi, L)
     if not args.no_batch:
         line["batch"] = batch_measure(lib, abi, L)
     if not args.no_cpu_baseline:
