@@ -622,7 +622,7 @@ static int
 mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
 {
   const double eps = env_double ("LIBSTOKES_GB300_MIXED_EPS", 1e-8);
-  const bool images = env_double ("LIBSTOKES_GB300_MIXED_IMAGES", sys->version == 2 ? 1.0 : 0.0) != 0.0;
+  bool images = env_double ("LIBSTOKES_GB300_MIXED_IMAGES", sys->version == 2 ? 1.0 : 0.0) != 0.0;
   double eta = env_double ("LIBSTOKES_GB300_MIXED_ETA",
                            images ? default_eta_images (sys->np) : default_eta (sys->np));
   const uint64_t fp = mix_fingerprint (sys, eta + (images ? 1000.0 : 0.0), eps);
@@ -635,9 +635,7 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
   // (FP32 loses digits to their cancellation when xi a grows)
   const double XI_CAP = 0.5;
   double xi = std::min (eta / lv, XI_CAP), rc = 0, kc = 0;
-  if (images)
-    lsg_ewald_cutoffs (xi, eps, lmin, lmax, &rc, &kc);
-  else
+  if (!images)
     {
       for (int it = 0; it < 200; it++)
         {
@@ -645,9 +643,16 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
           if (rc <= 0.4999 * lmin) break;
           xi *= 1.03;   // the cutoff must stay below half the box (minimum image)
         }
-      if (rc > 0.4999 * lmin)
-        return set_error (STOKES_GPU_EINVAL, "mixed split: no real-space cutoff below L/2");
+      // a small box would need xi above the cap for a minimum-image cutoff:
+      // take lattice images in real space instead (measured: F and FT at
+      // L = 6 reached 1e-5 against FP64 at the forced xi, 1e-7 with images)
+      if (rc > 0.4999 * lmin || xi > XI_CAP)
+        {
+          images = true;
+          xi = std::min (eta / lv, XI_CAP);
+        }
     }
+  if (images) lsg_ewald_cutoffs (xi, eps, lmin, lmax, &rc, &kc);
   // lattice offsets within the cutoff of a minimum-image difference (just
   // the zero offset while the cutoff is below half the box)
   {

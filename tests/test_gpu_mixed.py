@@ -151,3 +151,37 @@ def test_mixed_dense_builder_golden(lib, products):
         ref = case["mat"]
         assert np.abs(m - ref).max() / np.abs(ref).max() < 1e-6, name
         s.close()
+
+
+@pytest.mark.parametrize("version", [0, 1, 2])
+@pytest.mark.parametrize("n", [1, 2, 3, 17])
+def test_tiny_systems(lib, version, n):
+    """One, two, three and seventeen spheres (tensor-core tiles almost all
+    padding): FP64 against the oracle at 1e-12, mixed against FP64 at the
+    mixed bar, and the split-precision dense builder against the FP64 one."""
+    from conftest import make_oracle
+    from libstokes_gb300 import FP64, MIXED, System
+    rng = np.random.default_rng(40 + n + 10 * version)
+    L = 6.0 if n < 10 else 9.0
+    pos = np.zeros((n, 3))
+    for i in range(n):                      # rejection: centres 2 apart
+        while True:
+            p = rng.uniform(0, L, 3)
+            d = pos[:i] - p
+            d -= L * np.rint(d / L)
+            if i == 0 or np.min(np.linalg.norm(d, axis=1)) > 2.05:
+                pos[i] = p
+                break
+    case = dict(meta=np.array([version, L, L, L, 1.0, 1e-12, 0, 0.0, 0.0]), pos=pos)
+    x = rng.standard_normal((3, 6, 11)[version] * n)
+    a = System(version, pos, (L, L, L))
+    a.set_precision(FP64)
+    y64 = a.atimes(x)
+    assert rel_l2(y64, make_oracle(case).atimes(x)) < 1e-12
+    b = System(version, pos, (L, L, L))
+    b.set_precision(MIXED)
+    assert rel_l2(b.atimes(x), y64) < TOL
+    m64, m32 = a.matrix(), b.matrix()
+    assert np.abs(m32 - m64).max() / np.abs(m64).max() < 1e-6
+    a.close()
+    b.close()
