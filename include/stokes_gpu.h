@@ -75,7 +75,7 @@ int stokes_gpu_atimes_dev (struct stokes *sys, const double *d_pos,
  * libstokes.  For callers that may not allocate on the device while they
  * run (a fixed memory budget owned by another framework, steps that must
  * never enter the driver's allocator): all scratch lives in one fixed
- * 5.05 MiB device array per GPU, reserved when the library is loaded.
+ * 5.06 MiB device array per GPU, reserved when the library is loaded.
  * Limits: np <= 512, at most 2048 real-space images and 512 reciprocal
  * vectors; larger systems get STOKES_GPU_ETOOBIG.  d_pos [np*3], d_x, d_y
  * [np*{3,6,11}] are device buffers of the caller; stream may be NULL (the

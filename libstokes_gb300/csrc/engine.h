@@ -20,7 +20,11 @@ enum {
   KT_EX, KT_EY, KT_EZ,          // k / |k|
   KT_K, KT_KK, KT_KEXP,         // |k|, |k|^2, pi/V (1 + k4z (1 + 2 k4z)) / k^2 exp(-k4z)
   KT_YA, KT_YB, KT_YC, KT_YG, KT_YH, KT_YM,  // equal-sphere weights
-  KT_STRIDE = 16
+  // unequal radii: factors of the G coefficient and of all the others on
+  // the weights the kernels derive from KT_KEXP (1 and 1 but in the tuned
+  // split's G correction)
+  KT_GF, KT_AF,
+  KT_STRIDE = 18
 };
 
 // structure-factor row per k: C | S | Cq | Sq, each up to 11 values

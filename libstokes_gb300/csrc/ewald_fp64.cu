@@ -285,15 +285,17 @@ k_backproj (const double2 *ph, const double *kt, const double *sf, int nk, int n
           const double kk = K[KT_KK], kn = K[KT_K], kexp = K[KT_KEXP];
           const double aa2 = aa * aa, aa3 = aa2 * aa;
           // weights without the source radius, and their q_j coefficients
-          const double ya0 = aa * 6.0 * (1.0 - kk * qai / 6.0) * kexp;
-          const double ya1 = -aa * kk * kexp;
-          const double yb = aa2 * 3.0 * kn * kexp;
-          const double yc = aa3 * 1.5 * kk * kexp;
-          const double yg0 = aa2 * 3.0 * (1.0 - kk * qai / 10.0) * kn * kexp;
-          const double yg1 = -aa2 * 0.5 * kk * kn * kexp;
-          const double yh = aa3 * 1.5 * kk * kexp;
-          const double ym0 = aa3 * 3.0 * (1.0 - kk * qai / 10.0) * kk * kexp;
-          const double ym1 = -aa3 * 0.3 * kk * kk * kexp;
+          // KT_GF, KT_AF: 1 but in the tuned split's G correction
+          const double gx = kexp * K[KT_GF], ax = kexp * K[KT_AF];
+          const double ya0 = aa * 6.0 * (1.0 - kk * qai / 6.0) * ax;
+          const double ya1 = -aa * kk * ax;
+          const double yb = aa2 * 3.0 * kn * ax;
+          const double yc = aa3 * 1.5 * kk * ax;
+          const double yg0 = aa2 * 3.0 * (1.0 - kk * qai / 10.0) * kn * gx;
+          const double yg1 = -aa2 * 0.5 * kk * kn * gx;
+          const double yh = aa3 * 1.5 * kk * ax;
+          const double ym0 = aa3 * 3.0 * (1.0 - kk * qai / 10.0) * kk * ax;
+          const double ym1 = -aa3 * 0.3 * kk * kk * ax;
           // v1 = c_i C + s_i S, v2 = s_i C - c_i S; same with the weighted Cq, Sq
           double t1[C], t2[C], u1[C], u2[C];
 #pragma unroll

@@ -241,6 +241,7 @@ build_ktable (const struct stokes *sys, std::vector<double> &kt)
           row[KT_KX] = k1; row[KT_KY] = k2; row[KT_KZ] = k3;
           row[KT_EX] = k1 / k; row[KT_EY] = k2 / k; row[KT_EZ] = k3 / k;
           row[KT_K] = k; row[KT_KK] = kk; row[KT_KEXP] = kexp;
+          row[KT_GF] = row[KT_AF] = 1.0;
           row[KT_YA] = 6.0 * (1.0 - kk / 3.0) * kexp;
           row[KT_YB] = 3.0 * k * kexp;
           row[KT_YC] = 1.5 * kk * kexp;
@@ -254,8 +255,12 @@ build_ktable (const struct stokes *sys, std::vector<double> &kt)
 // per-particle arrays: radii (1 when a == NULL), slip radii, squared
 // Laplacian radii, and self scalars (src/ewald.c:540-643)
 void
-build_particles (const struct stokes *sys, int mode, std::vector<double> &pp, bool open)
+build_particles (const struct stokes *sys, int mode, std::vector<double> &pp, bool open,
+                 const struct stokes *split)
 {
+  // the self terms follow the split of `split` (the tuned one), the radii
+  // and slip factors are the system's own
+  const struct stokes *sp = split ? split : sys;
   const int np = sys->np;
   pp.assign ((size_t) 6 * np, 0.0);
   double *rad = pp.data (), *slipa = rad + np, *qa = slipa + np, *selfc = qa + np;
@@ -273,15 +278,15 @@ build_particles (const struct stokes *sys, int mode, std::vector<double> &pp, bo
           if (sys->slip) { sa *= sys->slip_G32[i]; sc *= sys->slip_G30[i]; sm *= sys->slip_G52[i]; }
         }
       else if (mode == MODE_MONO)
-        { sa = sys->self_a; sc = sys->self_c; sm = sys->self_m; }
+        { sa = sp->self_a; sc = sp->self_c; sm = sp->self_m; }
       else
         {
           const double a2 = a * a, a3 = a2 * a;
           double fa = 1.0, fc = 1.0, fm = 1.0;
           if (sys->slip) { fa = sys->slip_G32[i]; fc = sys->slip_G30[i]; fm = sys->slip_G52[i]; }
-          sa = 1.0 * fa - a * sys->xiaspi * (6.0 - 40.0 / 3.0 * sys->xia2 * a2);
-          sc = 0.75 * fc - a3 * sys->xiaspi * sys->xia2 * 10.0;
-          sm = 0.9 * fm - a3 * sys->xiaspi * sys->xia2 * (12.0 - 30.24 * sys->xia2 * a2);
+          sa = 1.0 * fa - a * sp->xiaspi * (6.0 - 40.0 / 3.0 * sp->xia2 * a2);
+          sc = 0.75 * fc - a3 * sp->xiaspi * sp->xia2 * 10.0;
+          sm = 0.9 * fm - a3 * sp->xiaspi * sp->xia2 * (12.0 - 30.24 * sp->xia2 * a2);
         }
       selfc[3 * i] = sa;
       selfc[3 * i + 1] = sc;
@@ -311,8 +316,9 @@ upload_if_changed (DevBuf &buf, uint64_t &fp, const void *host, size_t bytes,
 
 // ---- the tuned FP64 split ---------------------------------------------------
 // The reference's split xi = sqrt(pi) / L puts nearly all of the work in
-// real space (hundreds of lattice images at N = 1000).  For equal spheres the
-// FP64 products run at xi = eta / V^(1/3) instead (eta 6 up to 1024
+// real space (hundreds of lattice images at N = 1000).  The FP64 products
+// of equal and unequal spheres (not slip: libstokes' slip sum depends on xi
+// beyond the G term, 1e-2 between splits) run at xi = eta / V^(1/3) instead (eta 6 up to 1024
 // particles, 8 up to 4096, 10 above; LIBSTOKES_GB300_FP64_ETA sets it, 0
 // keeps the reference's split), set up by the reference's own rules on a
 // private copy of the system.  The sum is split-invariant to rounding
@@ -323,7 +329,9 @@ upload_if_changed (DevBuf &buf, uint64_t &fp, const void *host, size_t bytes,
 // y(xi) = y_inv + 2 G(xi), G the reciprocal G part as libstokes evaluates
 // it.  The tuned table therefore carries the invariant sign (-G on the tuned
 // k set) and adds 2 G(xi_ref) on the reference's k set, which reproduces
-// y(xi_ref).
+// y(xi_ref).  For unequal radii the kernels derive the weights from KT_KEXP;
+// G is linear in it, so the table's factors KT_GF (G) and KT_AF (the rest)
+// express the same correction.
 static double
 tuned_eta (int np)
 {
@@ -369,7 +377,7 @@ tuned_applies (const Ctx *c, const struct stokes *sys, bool cube)
 {
   const double eta = tuned_eta (sys->np);
   return c->tune && eta > 0.0 && !cube && !c->open && sys->periodic && split_is_as_set (sys)
-         && sys->a == nullptr && sys->slip == nullptr && sys->shear_mode == 0
+         && sys->slip == nullptr && sys->shear_mode == 0
          && sys->rmin == 0.0 && sys->np > 0 && eta > sys->xi * cbrt (sys->lx * sys->ly * sys->lz);
 }
 
@@ -411,6 +419,7 @@ g_correction (const struct stokes *sys, std::vector<double> &kt)
     {
       double *row = &kt[q * KT_STRIDE];
       row[KT_YG] = -row[KT_YG];
+      row[KT_GF] = -1.0;        // the same for the weights derived from KT_KEXP
       at.emplace (key (llrint (row[KT_KX] / k0x), llrint (row[KT_KY] / k0y),
                        llrint (row[KT_KZ] / k0z)), q);
     }
@@ -425,13 +434,19 @@ g_correction (const struct stokes *sys, std::vector<double> &kt)
                                      llrint (row[KT_KZ] / k0z)));
       if (hit != at.end ())
         {
-          kt[hit->second * KT_STRIDE + KT_YG] += g2;
+          // G is linear in kexp: -G(kexp_t) + 2 G(kexp_ref) = G(kexp_t) (-1 +
+          // 2 kexp_ref / kexp_t) for the derived weights
+          double *t = &kt[hit->second * KT_STRIDE];
+          t[KT_YG] += g2;
+          t[KT_GF] = -1.0 + 2.0 * row[KT_KEXP] / t[KT_KEXP];
           continue;
         }
       double add[KT_STRIDE];
       memcpy (add, row, sizeof add);
       add[KT_YA] = add[KT_YB] = add[KT_YC] = add[KT_YH] = add[KT_YM] = 0.0;
       add[KT_YG] = g2;
+      add[KT_GF] = 2.0;
+      add[KT_AF] = 0.0;
       kt.insert (kt.end (), add, add + KT_STRIDE);
     }
 }
@@ -505,7 +520,7 @@ prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
                           c->stream, "reciprocal table");
   if (rc) return rc;
   // self terms at the split of the tables (radii: the system's own)
-  build_particles (ts, c->mode, c->h_pp, c->open);
+  build_particles (sys, c->mode, c->h_pp, c->open, ts);
   rc = upload_if_changed (c->pp, c->fp_pp, c->h_pp.data (), sizeof (double) * c->h_pp.size (),
                           c->stream, "particle table");
   if (rc) return rc;

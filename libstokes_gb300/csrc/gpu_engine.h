@@ -87,7 +87,7 @@ int check_sys (const struct stokes *sys, bool open = false);
 void build_images (const struct stokes *sys, bool cube, std::vector<Img4> &img);
 void build_ktable (const struct stokes *sys, std::vector<double> &kt);
 void build_particles (const struct stokes *sys, int mode, std::vector<double> &pp,
-                      bool open = false);
+                      bool open = false, const struct stokes *split = nullptr);
 int release_ctx (const struct stokes *sys);
 // check sys and bring the context's device tables up to date.  tables: 1
 // builds the FP64 image and reciprocal tables of the FP64 product (the

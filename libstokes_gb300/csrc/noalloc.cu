@@ -13,7 +13,7 @@
 // Limits (checked, STOKES_GPU_ETOOBIG beyond them): at most 512 particles,
 // 2048 real-space images and 512 reciprocal vectors -- systems of up to a
 // few hundred spheres, such as the members of an ensemble.  The array takes
-// 5,296,128 bytes (5.05 MiB) on every GPU that loads the library and stays
+// 5,304,320 bytes (5.06 MiB) on every GPU that loads the library and stays
 // there until the process exits.
 //
 // The first call on each device looks up the array's device address
@@ -149,6 +149,7 @@ na_ktable (const struct stokes *sys, int *nk_out)
           r[KT_KX] = k1; r[KT_KY] = k2; r[KT_KZ] = k3;
           r[KT_EX] = k1 / k; r[KT_EY] = k2 / k; r[KT_EZ] = k3 / k;
           r[KT_K] = k; r[KT_KK] = kk; r[KT_KEXP] = kexp;
+          r[KT_GF] = r[KT_AF] = 1.0;
           r[KT_YA] = 6.0 * (1.0 - kk / 3.0) * kexp;
           r[KT_YB] = 3.0 * k * kexp;
           r[KT_YC] = 1.5 * kk * kexp;
