@@ -318,12 +318,15 @@ def solve_measure(lib, abi, L, torch, dev, pos, Lbox, product_ms):
     x = np.zeros(n)
     abi.check(lib.stokes_gpu_solve(s.sp, 0, abi._d(b), abi._d(x), 30, 1000, 1e-5, C.byref(it),
                                    C.byref(res)))      # warm-up: graphs, workspace
-    x[:] = 0.0
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    abi.check(lib.stokes_gpu_solve(s.sp, 0, abi._d(b), abi._d(x), 30, 1000, 1e-5, C.byref(it),
-                                   C.byref(res)))
-    wall = time.perf_counter() - t0
+    walls = []
+    for _ in range(3):
+        x[:] = 0.0
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        abi.check(lib.stokes_gpu_solve(s.sp, 0, abi._d(b), abi._d(x), 30, 1000, 1e-5,
+                                       C.byref(it), C.byref(res)))
+        walls.append(time.perf_counter() - t0)
+    wall = float(np.median(walls))
     s.close()
     iters = it.value
     # every restart cycle adds one residual product to the iterations
@@ -334,7 +337,9 @@ def solve_measure(lib, abi, L, torch, dev, pos, Lbox, product_ms):
             "ms_per_iteration": 1000.0 * wall / max(iters, 1),
             "product_ms": product_ms, "products": products,
             "product_share": products * product_ms / (1000.0 * wall),
-            "timing": "wall clock around stokes_gpu_solve (host buffers in and out)"}
+            "ms_runs": [1000.0 * t for t in walls],
+            "timing": "wall clock around stokes_gpu_solve (host buffers in and out), "
+                      "median of 3 solves"}
 
 
 def scale_measure(lib, abi, L, torch, dev, sizes=(4096, 16384), reps=10):
