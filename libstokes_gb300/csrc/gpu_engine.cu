@@ -136,6 +136,7 @@ free_ctx (Ctx *c)
   for (DevBuf *b : c->all_buffers ()) b->release ();
   for (int q = 0; q < 4; q++) cudaEventDestroy (c->ev[q]);
   for (int q = 0; q < 2; q++) cudaEventDestroy (c->join[q]);
+  if (c->hpos) cudaFreeHost (c->hpos);
   cudaStreamDestroy (c->stream);
   release_mixed (c);
   if (c->tuned) stokes_free (c->tuned);
@@ -693,6 +694,36 @@ mapped_host (const void *p)
   return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
+// the positions as the mixed kernels read them from a host call: sys->pos in
+// place when it is pinned, else a copy in the context's pinned mirror. The
+// mixed kernels read each coordinate once (mk_prep, k_open_prep convert
+// them), so a read over the CPU-GPU link replaces the staging copy of
+// pageable memory. Called only between synchronised host calls, so no
+// kernel is reading the mirror while it is rewritten.
+static const double *
+mapped_positions (Ctx *c, const struct stokes *sys)
+{
+  const size_t bytes = sizeof (double) * 3 * sys->np;
+  if (const double *p = (const double *) mapped_host (sys->pos)) return p;
+  if (c->hpos_bytes < bytes)
+    {
+      if (c->hpos) cudaFreeHost (c->hpos);
+      c->hpos = nullptr;
+      c->hpos_bytes = 0;
+      if (cudaHostAlloc ((void **) &c->hpos, bytes, cudaHostAllocMapped) != cudaSuccess)
+        {
+          cudaGetLastError ();
+          c->hpos = nullptr;
+          return nullptr;
+        }
+      c->hpos_dev = (const double *) mapped_host (c->hpos);
+      if (!c->hpos_dev) return nullptr;
+      c->hpos_bytes = bytes;
+    }
+  memcpy (c->hpos, sys->pos, bytes);
+  return c->hpos_dev;
+}
+
 int
 atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
 {
@@ -723,9 +754,14 @@ atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
     {
       if ((e = c->y.ensure (sizeof (double) * n)) != cudaSuccess) return cuda_fail (e, "y");
     }
-  cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * np, cudaMemcpyHostToDevice, c->stream);
-  rc = atimes_dev (c, (const double *) c->pos.p, d_x, d_y ? d_y : (double *) c->y.p, c->stream,
-                   true);
+  const double *d_pos = c->precision == STOKES_GPU_MIXED ? mapped_positions (c, sys) : nullptr;
+  if (!d_pos)
+    {
+      cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * np, cudaMemcpyHostToDevice,
+                       c->stream);
+      d_pos = (const double *) c->pos.p;
+    }
+  rc = atimes_dev (c, d_pos, d_x, d_y ? d_y : (double *) c->y.p, c->stream, true);
   if (rc) return rc;
   e = d_y ? cudaSuccess
           : cudaMemcpyAsync (y, c->y.p, sizeof (double) * n, cudaMemcpyDeviceToHost, c->stream);

@@ -70,6 +70,12 @@ struct Ctx {
   DevBuf openf;   // scratch of the mixed-precision free-space product
   DevBuf imgf;    // the images in FP32 (split-precision dense builder)
 
+  // pinned, mapped mirror of sys->pos for the host entry points of the
+  // mixed paths, whose kernels read the positions once
+  double *hpos = nullptr;
+  const double *hpos_dev = nullptr;   // its device address
+  size_t hpos_bytes = 0;
+
   std::array<DevBuf *, 14> all_buffers ()
   {
     return {&pos, &x, &y, &img, &kt, &pp, &ph, &sf, &yrec, &partial, &mat, &zbuf, &openf, &imgf};

@@ -213,3 +213,35 @@ def test_pinned_host_buffers(lib, mixed):
         y_pageable = s.atimes(x)
         np.testing.assert_array_equal(hy.numpy(), y_pageable)
     s.close()
+
+
+@pytest.mark.parametrize("periodic", [True, False])
+def test_mixed_host_positions_follow_moves(lib, periodic):
+    """The mixed host call reads the positions through a pinned mirror of
+    sys->pos: moving the particles between calls gives the device entry
+    point's result on the new positions, bit for bit (the same kernels on
+    the same values), for the Ewald and the free-space sum."""
+    import torch
+    from conftest import make_open_system
+    from libstokes_gb300 import MIXED, check
+    from libstokes_gb300.workloads import rsa_positions
+    pos, L = rsa_positions(200, 0.2, seed=9)
+    case = dict(meta=np.array([1, L, L, L, 1.0, 1e-12, 0, 0.0, 0.0]), pos=pos)
+    s = make_system(case) if periodic else make_open_system(dict(meta=np.array([1, 0.0]), pos=pos))
+    s.set_precision(MIXED)
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(5)
+    for step in range(3):
+        p = pos + 0.05 * step * rng.standard_normal(pos.shape)
+        s.set_pos(p)
+        x = rng.standard_normal(s.n)
+        y_host = s.atimes_3all(x)
+        dx = torch.tensor(x, device=dev)
+        dy = torch.empty_like(dx)
+        dp = torch.tensor(p.ravel(), device=dev)
+        check(lib.stokes_gpu_atimes_dev(s.sp, C.c_void_p(dp.data_ptr()), C.c_void_p(dx.data_ptr()),
+                                        C.c_void_p(dy.data_ptr()),
+                                        C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(y_host, dy.cpu().numpy())
+    s.close()
