@@ -215,12 +215,13 @@ def test_pinned_host_buffers(lib, mixed):
     s.close()
 
 
-@pytest.mark.parametrize("periodic", [True, False])
-def test_mixed_host_positions_follow_moves(lib, periodic):
+@pytest.mark.parametrize("periodic,pinned", [(True, False), (False, False), (True, True)])
+def test_mixed_host_positions_follow_moves(lib, periodic, pinned):
     """The mixed host call reads the positions through a pinned mirror of
-    sys->pos: moving the particles between calls gives the device entry
-    point's result on the new positions, bit for bit (the same kernels on
-    the same values), for the Ewald and the free-space sum."""
+    sys->pos, or in place when sys->pos is itself pinned: moving the
+    particles between calls gives the device entry point's result on the
+    new positions, bit for bit (the same kernels on the same values), for
+    the Ewald and the free-space sum."""
     import torch
     from conftest import make_open_system
     from libstokes_gb300 import MIXED, check
@@ -231,6 +232,10 @@ def test_mixed_host_positions_follow_moves(lib, periodic):
     s.set_precision(MIXED)
     dev = torch.device("cuda:0")
     rng = np.random.default_rng(5)
+    rt = torch.cuda.cudart()
+    addr = C.cast(s.sp.contents.pos, C.c_void_p).value
+    if pinned:
+        assert int(rt.cudaHostRegister(addr, 8 * pos.size, 0)) == 0
     for step in range(3):
         p = pos + 0.05 * step * rng.standard_normal(pos.shape)
         s.set_pos(p)
@@ -244,4 +249,6 @@ def test_mixed_host_positions_follow_moves(lib, periodic):
                                         C.c_void_p(torch.cuda.current_stream().cuda_stream)))
         torch.cuda.synchronize()
         np.testing.assert_array_equal(y_host, dy.cpu().numpy())
+    if pinned:
+        assert int(rt.cudaHostUnregister(addr)) == 0
     s.close()
