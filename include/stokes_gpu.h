@@ -75,12 +75,16 @@ int stokes_gpu_atimes_dev (struct stokes *sys, const double *d_pos,
  * libstokes.  For callers that may not allocate on the device while they
  * run (a fixed memory budget owned by another framework, steps that must
  * never enter the driver's allocator): all scratch lives in one fixed
- * 5.06 MiB device array per GPU, reserved when the library is loaded.
- * Limits: np <= 512, at most 2048 real-space images and 512 reciprocal
- * vectors; larger systems get STOKES_GPU_ETOOBIG.  d_pos [np*3], d_x, d_y
- * [np*{3,6,11}] are device buffers of the caller; stream may be NULL (the
- * default stream).  The first call on a device looks up the array's
- * address; make it before any stream capture.  All calls share the array:
+ * 5.06 MiB device array per GPU, reserved when this library's device module
+ * is loaded on that GPU.  With lazy module loading (CUDA's default) that
+ * happens during the first call on the device, so make one warm-up call per
+ * device before the allocation-free region (or set
+ * CUDA_MODULE_LOADING=EAGER).  Limits: np <= 512, at most 2048 real-space
+ * images and 512 reciprocal vectors; larger systems get STOKES_GPU_ETOOBIG.
+ * d_pos [np*3], d_x, d_y [np*{3,6,11}] are device buffers of the caller;
+ * stream may be NULL (the default stream).  No call can be captured into a
+ * CUDA graph: each waits for its small table uploads, and a call on a
+ * capturing stream returns STOKES_GPU_EINVAL.  All calls share the array:
  * calls that overlap on one GPU race on it. */
 int stokes_gpu_atimes_noalloc (struct stokes *sys, const double *d_pos,
                                const double *d_x, double *d_y, void *stream);
@@ -173,6 +177,11 @@ int stokes_gpu_last_launches (const struct stokes *sys, int *count);
 int stokes_gpu_count_real_terms (struct stokes *sys, long long *count);
 int stokes_gpu_count_real_terms_dense (struct stokes *sys, long long *count);
 
+/* number of real-space (i, j, image) terms the mixed product evaluates
+ * (0 < r^2 < rc^2 at the mixed split, after its first mixed product): the
+ * unit count of the mixed real-space roofline.  No counterpart in libstokes. */
+int stokes_gpu_count_mixed_real_terms (struct stokes *sys, long long *count);
+
 /* split chosen by the mixed path for sys (after its first mixed product):
  * xi, rc, kc, eta = xi V^(1/3), eps, half-space k count, max |m| per axis */
 int stokes_gpu_mixed_split (struct stokes *sys, double *info9);
@@ -192,6 +201,16 @@ int stokes_gpu_selftest_tma (double *max_rel_err);
 /* measured FMA throughput of the current GPU in GFLOP/s (2 flops per FMA),
  * fp64 = 1 for FP64, 0 for FP32 */
 int stokes_gpu_peak_fma (int fp64, double *gflops);
+
+/* Failure injection for tests of the bounded device waits (no counterpart
+ * in libstokes; process-wide, 0 and 0 restore normal operation).
+ * gemm_polls > 0: the MMA lane of every tensor-core k-space GEMM first waits
+ * that many polls (about 20 us each) on an mbarrier that nothing arrives at;
+ * the wait runs out, the CTA's roles stop, the kernel raises its status word
+ * and the mixed product reports STOKES_GPU_ETIMEOUT.  barrier_spins > 0: the
+ * GMRES grid barrier gives up after that many polls, and the solve reports
+ * STOKES_GPU_ETIMEOUT. */
+int stokes_gpu_test_stall_waits (int gemm_polls, long long barrier_spins);
 
 #ifdef __cplusplus
 }

@@ -233,7 +233,9 @@ _SIGS = {
     "stokes_gpu_kprof_end": (C.c_int, [_SP, C.c_int, C.c_char_p, _dp, _ip, _ip]),
     "stokes_gpu_profile_end": (C.c_int, [_SP, _dp, _ip]),
     "stokes_gpu_count_real_terms": (C.c_int, [_SP, C.POINTER(C.c_longlong)]),
+    "stokes_gpu_count_mixed_real_terms": (C.c_int, [_SP, C.POINTER(C.c_longlong)]),
     "stokes_gpu_peak_fma": (C.c_int, [C.c_int, _dp]),
+    "stokes_gpu_test_stall_waits": (C.c_int, [C.c_int, C.c_longlong]),
     "stokes_gpu_mixed_split": (C.c_int, [_SP, _dp]),
     "stokes_gpu_selftest_tensor": (C.c_int, [_dp]),
     "stokes_gpu_selftest_tma": (C.c_int, [_dp]),

@@ -690,6 +690,7 @@ stokes_gpu_bd_create (struct stokes *sys, const struct stokes_gpu_bd_params *p,
     return set_error (STOKES_GPU_EINVAL, "bad BD parameters");
   if (sys->nm != sys->np)
     return set_error (STOKES_GPU_EINVAL, "the BD engine serves systems without fixed particles");
+  if (int rc = check_positions (sys->pos, sys->np)) return rc;
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
   int rc = prepare (c, sys, false);
@@ -741,6 +742,7 @@ stokes_gpu_bd_set_positions (stokes_gpu_bd *b, const double *x)
 {
   clear_error ();
   if (!b || !x) return set_error (STOKES_GPU_EINVAL, "NULL argument");
+  if (int rc = check_positions (x, b->nm)) return rc;
   memcpy (b->sys->pos, x, sizeof (double) * 3 * b->nm);
   cudaError_t e = cudaMemcpyAsync (b->x.p, b->sys->pos, sizeof (double) * 3 * b->np,
                                    cudaMemcpyHostToDevice, b->c->stream);

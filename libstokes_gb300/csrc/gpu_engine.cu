@@ -178,6 +178,16 @@ check_sys (const struct stokes *sys, bool open)
   return STOKES_GPU_OK;
 }
 
+int
+check_positions (const double *pos, int np)
+{
+  for (int k = 0; k < 3 * np; k++)
+    if (!std::isfinite (pos[k]))
+      return set_error (STOKES_GPU_EINVAL, "non-finite position of particle %d (%c = %g)", k / 3,
+                        "xyz"[k % 3], pos[k]);
+  return STOKES_GPU_OK;
+}
+
 // real-space image list.  Table form: images of sys->rl* with the shear
 // shift of src/ewald.c:678-686 folded in.  Cube form ("_notbl"): the cube
 // |m| <= rmax{x,y,z} with the running shear shift of src/ewald.c:1843-1861
@@ -733,6 +743,7 @@ atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
   int rc = prepare (c, sys, cube);
   if (rc) return rc;
+  if ((rc = check_positions (sys->pos, sys->np))) return rc;
   const int np = sys->np, n = NCOMP (sys->version) * np;
   cudaError_t e;
   if ((e = c->pos.ensure (sizeof (double) * 3 * np)) != cudaSuccess) return cuda_fail (e, "pos");
@@ -767,6 +778,9 @@ atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
           : cudaMemcpyAsync (y, c->y.p, sizeof (double) * n, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize (c->stream);
   if (e != cudaSuccess) return cuda_fail (e, "atimes");
+  // a bounded wait of this product's tensor-core kernels that ran out
+  if (c->precision == STOKES_GPU_MIXED && !c->open && (rc = mixed_check_status (c)) != 0)
+    return rc;
   collect_times (c);
   sys->cpu1 = c->times[0];
   sys->cpu2 = c->times[1];
@@ -866,6 +880,7 @@ matrix_host (struct stokes *sys, double *mat, bool cube)
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
   int rc = prepare (c, sys, cube, 2);
   if (rc) return rc;
+  if ((rc = check_positions (sys->pos, sys->np))) return rc;
   const int np = sys->np;
   const size_t n = (size_t) NCOMP (sys->version) * np;
   cudaError_t e;

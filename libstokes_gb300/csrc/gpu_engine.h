@@ -90,6 +90,9 @@ void dropin_failed (const char *fn, double *out, size_t nout);
 Ctx *get_ctx (const struct stokes *sys, bool create);
 // host tables of one system (gpu_engine.cu)
 int check_sys (const struct stokes *sys, bool open = false);
+// STOKES_GPU_EINVAL when a coordinate of the host positions pos[3 np] is NaN
+// or infinite (the kernels would turn it into a wrong result, not an error)
+int check_positions (const double *pos, int np);
 void build_images (const struct stokes *sys, bool cube, std::vector<Img4> &img);
 void build_ktable (const struct stokes *sys, std::vector<double> &kt);
 void build_particles (const struct stokes *sys, int mode, std::vector<double> &pp,
@@ -120,5 +123,16 @@ int atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_
 int atimes_open_f32_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                          cudaStream_t st, bool timed);
 void release_mixed (Ctx *c);
+// after the stream of a mixed product was synchronised: STOKES_GPU_ETIMEOUT
+// (and the status word cleared) when a bounded wait of its tensor-core
+// kernels ran out, else STOKES_GPU_OK
+int mixed_check_status (Ctx *c);
+
+// failure-injection settings of stokes_gpu_test_stall_waits (util.cu): polls
+// of an extra wait of the k-space GEMMs' MMA lane on an mbarrier that nothing
+// arrives at (0: no such wait), and the spin limit of the GMRES grid barrier
+// (0: the default)
+extern int g_test_gemm_stall;
+extern long long g_test_bar_spins;
 
 }  // namespace lsg

@@ -154,12 +154,13 @@ struct ArnArgs {
   double bnrm;
   unsigned *bar;      // arrival count, generation
   int *status;        // nonzero: a barrier wait ran out
+  long long spins;    // polls of a barrier wait before it gives up
 };
 
 constexpr long long BAR_SPINS = 1ll << 22;   // about 0.1 - 1 s of polling
 
 __device__ bool
-grid_barrier (unsigned *bar, int *status)
+grid_barrier (unsigned *bar, int *status, long long max_spins)
 {
   __shared__ int s_ok;
   __syncthreads ();
@@ -180,7 +181,7 @@ grid_barrier (unsigned *bar, int *status)
           long long spins = 0;
           while (*gen == g0)
             {
-              if (++spins > BAR_SPINS || *(volatile int *) status)
+              if (++spins > max_spins || *(volatile int *) status)
                 {
                   atomicExch (status, 1);
                   ok = 0;
@@ -266,8 +267,8 @@ k_arnoldi (ArnArgs a)
   if (b == G)
     {
       if (a.gcol >= 0) givens_column (a, a.gcol, s_h);
-      if (!grid_barrier (a.bar, a.status)) return;
-      grid_barrier (a.bar, a.status);
+      if (!grid_barrier (a.bar, a.status, a.spins)) return;
+      grid_barrier (a.bar, a.status, a.spins);
       return;
     }
   // this block's slice [i0, i1), whole warps of elements
@@ -309,7 +310,7 @@ k_arnoldi (ArnArgs a)
           t = block_sum (t);
           if (tid == 0) part[(size_t) b * ld + a.m + 1] = t;
         }
-      if (!grid_barrier (a.bar, a.status)) return;
+      if (!grid_barrier (a.bar, a.status, a.spins)) return;
       // totals over the blocks: eight threads per entry, then three shuffles
       // (other blocks' partials through L2 with __ldcg, not a stale L1 line)
       const int ne = J + pass;
@@ -542,6 +543,7 @@ gmres_dev (int n, const double *d_b, double *d_x, const Apply &A, int m, int max
   aa.bnrm = bnrm;
   aa.bar = bar;
   aa.status = status;
+  aa.spins = g_test_bar_spins > 0 ? g_test_bar_spins : BAR_SPINS;
   const size_t smem = 4 * sizeof (double) * ld;
 
   int total = 0;

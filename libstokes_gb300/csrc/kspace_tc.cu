@@ -79,6 +79,7 @@ constexpr uint32_t WAIT_LIMIT = 1u << 18;   // polls of up to ~20 us each
 
 struct Sync {
   uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], done;
+  uint64_t never;       // nothing arrives here: the wait of the failure-injection test
   uint32_t tslot;
   int err;
 };
@@ -107,6 +108,7 @@ cta_setup (Sync &s)
           umma::mbar_init (&s.acc_empty[b], NDRAIN * 32);
         }
       umma::mbar_init (&s.done, 1);
+      umma::mbar_init (&s.never, 1);
       s.err = 0;
       umma::fence_mbar_init ();
     }
@@ -146,9 +148,13 @@ tma_role (Sync &s, unsigned char *smem, const CUtensorMap *tb, int brow, int k0,
 
 // the MMA lane: tile t in stage t % STAGES, accumulator buffer t & 1
 __device__ __forceinline__ void
-mma_role (Sync &s, const unsigned char *smem, uint32_t tmem, uint32_t idesc, int ntiles)
+mma_role (Sync &s, const unsigned char *smem, uint32_t tmem, uint32_t idesc, int ntiles,
+          int stall)
 {
   volatile int *err = &s.err;
+  // failure injection (tests): a wait that cannot complete runs out, raises
+  // the CTA error flag and ends every role before any MMA is issued
+  if (stall > 0 && !umma::mbar_wait_or_abort (&s.never, 0, (uint32_t) stall, err)) ntiles = 0;
   for (int t = 0; t < ntiles; t++)
     {
       const int st = t % STAGES, b = t & 1;
@@ -406,7 +412,7 @@ k_sfac_gemm (const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CU
     }
   else if (warp == MMA_WARP)
     {
-      if (lane == 0) mma_role (s, smem, tmem, umma::idesc_tf32 (TM, g.nf), ntiles);
+      if (lane == 0) mma_role (s, smem, tmem, umma::idesc_tf32 (TM, g.nf), ntiles, g.stall);
       __syncwarp ();
     }
   else
@@ -570,7 +576,7 @@ k_bp_gemm (const __grid_constant__ CUtensorMap tmB, KGemm g, float *ypart, int *
     }
   else if (warp == MMA_WARP)
     {
-      if (lane == 0) mma_role (s, smem, tmem, umma::idesc_tf32 (TM, g.nb), ntiles);
+      if (lane == 0) mma_role (s, smem, tmem, umma::idesc_tf32 (TM, g.nb), ntiles, g.stall);
       __syncwarp ();
     }
   else

@@ -841,7 +841,7 @@ run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_
   }();
   // the context's own phase events record from inside the graph (event
   // record nodes); a profiling window's ring of events changes per product
-  bool use = enabled && !c->kprof_on && (E == nullptr || E == c->ev);
+  bool use = enabled && !c->kprof_on && (E == nullptr || E == c->ev) && m->plan.stall == 0;
   if (use)
     {
       cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -937,6 +937,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     // reciprocal space on the tensor cores unless LIBSTOKES_GB300_KSPACE=simt
     const char *ks = getenv ("LIBSTOKES_GB300_KSPACE");   // read per call: tests switch it
     m->plan = kgemm_plan (c->version, pt, (const int2 *) m->rowm.p, m->nrow);
+    m->plan.stall = g_test_gemm_stall;
     m->tensor = !(ks && strcmp (ks, "simt") == 0) && m->nkh > 0 && kgemm_fits (m->plan);
   }
   if (m->tensor)
@@ -1185,6 +1186,17 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   return STOKES_GPU_OK;
 }
 
+int
+mixed_check_status (Ctx *c)
+{
+  MixedState *m = c->mixed;
+  if (!m || !m->h_status || !*m->h_status) return STOKES_GPU_OK;
+  *m->h_status = 0;
+  cudaMemsetAsync (m->status.p, 0, sizeof (int), c->stream);
+  cudaStreamSynchronize (c->stream);
+  return set_error (STOKES_GPU_ETIMEOUT, "a tensor-core wait of the mixed product ran out");
+}
+
 void
 release_mixed (Ctx *c)
 {
@@ -1203,6 +1215,68 @@ release_mixed (Ctx *c)
   c->mixed = nullptr;
 }
 
+// (i, j, image) terms with 0 < r^2 < rc^2 under the test mk_real applies
+// (fixed-point minimum image plus the split's lattice offsets, FP32
+// distances): the unit count of the mixed real-space roofline
+__global__ void
+mk_count_real (RealMixArgs a, unsigned long long *count)
+{
+  const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long cnt = 0;
+  if (t < (long long) a.np * a.np)
+    {
+      const int i = (int) (t / a.np), j = (int) (t % a.np);
+      const uint4 qi = reinterpret_cast<const uint4 *> (a.qpos)[i];
+      const uint4 qj = reinterpret_cast<const uint4 *> (a.qpos)[j];
+      float d0x, d0y, d0z;
+      min_image (a, qi, qj, d0x, d0y, d0z);
+      for (int m = 0; m < a.nimg; m++)
+        {
+          const float4 T = a.img[m];
+          const float dx = d0x + T.x, dy = d0y + T.y, dz = d0z + T.z;
+          const float rr = dx * dx + dy * dy + dz * dz;
+          cnt += (rr > 0.f && rr < a.rc2) ? 1ull : 0ull;
+        }
+    }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync (0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd (count, cnt);
+}
+
+int
+mixed_count_real (Ctx *c, long long *out)
+{
+  if (!c->mixed || !c->mixed->qpos.p)
+    return set_error (STOKES_GPU_EINVAL, "no mixed product run yet");
+  MixedState *m = c->mixed;
+  const struct stokes *sys = c->sys;
+  RealMixArgs ra;
+  memset (&ra, 0, sizeof ra);
+  ra.qpos = (const uint32_t *) m->qpos.p;
+  ra.np = c->np;
+  const double two32 = 4294967296.0;
+  ra.scale[0] = (float) (sys->lx / two32);
+  ra.scale[1] = (float) (sys->ly / two32);
+  ra.scale[2] = (float) (sys->lz / two32);
+  ra.shear_mode = sys->shear_mode;
+  ra.shift_q = (uint32_t) (llround (sys->shear_shift / sys->lx * two32) & 0xffffffffll);
+  ra.rc2 = (float) (m->rc * m->rc);
+  ra.img = (const float4 *) m->img.p;
+  ra.nimg = m->nimg;
+  DevBuf cnt;
+  cudaError_t e = cnt.ensure (sizeof (unsigned long long));
+  if (e != cudaSuccess) return cuda_fail (e, "count");
+  cudaMemsetAsync (cnt.p, 0, sizeof (unsigned long long), c->stream);
+  const long long nt = (long long) c->np * c->np;
+  mk_count_real<<<(int) ((nt + 255) / 256), 256, 0, c->stream>>> (ra, (unsigned long long *) cnt.p);
+  unsigned long long h = 0;
+  e = cudaMemcpyAsync (&h, cnt.p, sizeof h, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize (c->stream);
+  cnt.release ();
+  if (e != cudaSuccess) return cuda_fail (e, "count");
+  *out = (long long) h;
+  return STOKES_GPU_OK;
+}
+
 int
 mixed_split_info (Ctx *c, double *out)
 {
@@ -1214,6 +1288,16 @@ mixed_split_info (Ctx *c, double *out)
 }
 
 }  // namespace lsg
+
+extern "C" int
+stokes_gpu_count_mixed_real_terms (struct stokes *sys, long long *count)
+{
+  using namespace lsg;
+  if (!sys || !count) return set_error (STOKES_GPU_EINVAL, "NULL argument");
+  Ctx *c = get_ctx (sys, false);
+  if (!c) return set_error (STOKES_GPU_EINVAL, "no product run for this system yet");
+  return mixed_count_real (c, count);
+}
 
 extern "C" int
 stokes_gpu_mixed_split (struct stokes *sys, double *info9)

@@ -120,6 +120,8 @@ struct KGemm {
   float *ZF, *WB;
   size_t pZF, pWB;        // plane strides (floats)
   float *sf;              // forward partials [nsplit][n1][c][re|im][Rp]
+  int stall;              // > 0 (tests only): the MMA lane first waits that many
+                          // polls on an mbarrier that nothing arrives at
 };
 
 // TMA descriptors of the two images (128-byte swizzled boxes of 32 K values)

@@ -17,10 +17,20 @@
 // there until the process exits.
 //
 // The first call on each device looks up the array's device address
-// (cudaGetSymbolAddress) with that device current; make that first call
-// before any stream capture.  Every call waits for its small table uploads
-// to finish before it returns; the kernels themselves run asynchronously on
-// the caller's stream.
+// (cudaGetSymbolAddress) with that device current.  With lazy module loading
+// (CUDA's default) that lookup is also what loads this library's device
+// module on the device, and loading a module reserves its static arrays
+// through the driver: make one warm-up call on each device before the
+// region in which nothing may allocate, or run with
+// CUDA_MODULE_LOADING=EAGER, which loads the module (and reserves the array)
+// when the CUDA context is created.
+//
+// No call of this entry point can be recorded into a CUDA graph: every call
+// copies its small tables from host memory and waits for those copies
+// (cudaStreamSynchronize) before it returns, and a synchronize is illegal on
+// a capturing stream.  A call on a stream that is being captured is refused
+// with STOKES_GPU_EINVAL before it touches the stream.  The kernels
+// themselves run asynchronously on the caller's stream.
 //
 // Every call uses the same array and leaves its last contents in it.  Calls
 // that overlap on the same GPU -- on different streams, or from different
@@ -207,11 +217,25 @@ stokes_gpu_atimes_noalloc (struct stokes *sys, const double *d_pos, const double
   if (sys->version < 0 || sys->version > 2)
     return set_error (STOKES_GPU_EINVAL, "invalid version %d", sys->version);
   if (sys->np <= 0) return set_error (STOKES_GPU_EINVAL, "no particles");
+  if (!(sys->lx > 0.0 && sys->ly > 0.0 && sys->lz > 0.0))
+    return set_error (STOKES_GPU_EINVAL, "box size not set");
+  if (!(sys->xi > 0.0)) return set_error (STOKES_GPU_EINVAL, "Ewald xi not set");
   if (sys->np > NA_MAX_NP)
     return set_error (STOKES_GPU_ETOOBIG, "%d particles; this entry point takes at most %d",
                       sys->np, NA_MAX_NP);
   if (sys->nr > 0 && (!sys->rlx || !sys->rly || !sys->rlz))
     return set_error (STOKES_GPU_EINVAL, "image table missing (stokes_set_xi not called?)");
+  cudaStream_t st = (cudaStream_t) stream;
+  {
+    // the table uploads end in a synchronize, which a capture cannot record
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const cudaError_t ce = cudaStreamIsCapturing (st, &cs);
+    if (ce != cudaSuccess) return cuda_fail (ce, "cudaStreamIsCapturing");
+    if (cs != cudaStreamCaptureStatusNone)
+      return set_error (STOKES_GPU_EINVAL,
+                        "stokes_gpu_atimes_noalloc cannot be captured into a CUDA graph "
+                        "(it waits for its table uploads)");
+  }
   const int np = sys->np;
   const int mode = sys->slip ? MODE_SLIP : (sys->a ? MODE_POLY : MODE_MONO);
   void *base = nullptr;
@@ -232,7 +256,6 @@ stokes_gpu_atimes_noalloc (struct stokes *sys, const double *d_pos, const double
   double *yrec = (double *) (b + NA_YREC);
   double *sf = (double *) (b + NA_SF);
   double2 *ph = (double2 *) (b + NA_PH);
-  cudaStream_t st = (cudaStream_t) stream;
 
   // derived tables into the scratch; the copies complete before the host
   // staging is released

@@ -6,7 +6,7 @@
  * produced are the reference's: same self constants (src/stokes.c:714-716),
  * same cutoff search with safety factor 1.15 and shrink factor 0.99
  * (src/stokes.c:655-700, 726-758), same image-table rule
- * (src/stokes.c:193-233) -- tests/test_setup.py checks them against the
+ * (src/stokes.c:193-233) -- tests/test_abi.py checks them against the
  * reference bit for bit.
  *
  * Not rebuilt here: the lubrication tables (poly_table, twobody_f_list,

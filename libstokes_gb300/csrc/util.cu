@@ -52,6 +52,9 @@ k_fma_chain (R seed, int iters, R *sink)
   if (s == R (-12345.0)) sink[0] = s;  // keeps the chain alive
 }
 
+int g_test_gemm_stall = 0;
+long long g_test_bar_spins = 0;
+
 }  // namespace lsg
 
 using namespace lsg;
@@ -98,6 +101,17 @@ int
 stokes_gpu_count_real_terms_dense (struct stokes *sys, long long *count)
 {
   return count_terms (sys, 2, count);
+}
+
+// failure injection for the tests of the bounded device waits
+int
+stokes_gpu_test_stall_waits (int gemm_polls, long long barrier_spins)
+{
+  if (gemm_polls < 0 || barrier_spins < 0)
+    return set_error (STOKES_GPU_EINVAL, "negative wait limit");
+  g_test_gemm_stall = gemm_polls;
+  g_test_bar_spins = barrier_spins;
+  return STOKES_GPU_OK;
 }
 
 // GFLOP/s (2 flops per FMA) of an FMA-chain kernel filling the GPU

@@ -49,9 +49,11 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
-def build_reference(ref_root: str = "/root/reference") -> str | None:
-    """Compile the reference's own sources into oracle/_ref (needs the checkout)."""
-    if not os.path.isdir(os.path.join(ref_root, "src")):
+def build_reference(ref_root: str | None = None) -> str | None:
+    """Compile the reference's own sources into oracle/_ref.  ref_root: the
+    libstokes checkout (default: $LIBSTOKES_REF); None when there is none."""
+    ref_root = ref_root or os.environ.get("LIBSTOKES_REF")
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "src")):
         return None
     repo = os.path.dirname(HERE)
     subprocess.check_call(["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"),

@@ -248,7 +248,11 @@ def nonewald_fixtures() -> dict:
     return out
 
 
-def main(ref_root: str = "/root/reference"):
+def main(ref_root: str | None = None):
+    """ref_root: the libstokes checkout (argument or $LIBSTOKES_REF)."""
+    ref_root = ref_root or os.environ.get("LIBSTOKES_REF")
+    if not ref_root:
+        raise SystemExit("usage: make_golden.py <libstokes checkout> (or set LIBSTOKES_REF)")
     if build_reference(ref_root) is None:
         raise SystemExit(f"reference checkout not found under {ref_root}")
     json.dump(layout(ref_root), open(os.path.join(HERE, "struct_stokes_layout.json"), "w"),
