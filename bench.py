@@ -168,9 +168,10 @@ BD_WORKLOAD = dict(name="bd_f_n4096_phi0.20", version=0, n=4096, phi=0.20, seed=
                    steps=1000, steps_fp64=40, steps_dropin=4)
 
 
-def _bd_engine_run(lib, abi, L, pos, Lb, precision, steps):
+def _bd_engine_run(lib, abi, L, pos, Lb, precision, steps, budget_s=None):
     """Wall time of `steps` mid-point steps of the device engine (after one
-    warm-up step, which also runs the Lanczos bounds)."""
+    warm-up step, which also runs the Lanczos bounds); with a budget, steps
+    run one at a time and stop once the budget is spent (at least one)."""
     import torch
     w = BD_WORKLOAD
     s = L.System(w["version"], pos, (Lb,) * 3)
@@ -188,7 +189,14 @@ def _bd_engine_run(lib, abi, L, pos, Lb, precision, steps):
     abi.check(lib.stokes_gpu_bd_stats(h, st0.ctypes.data_as(abi._dp)))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    abi.check(lib.stokes_gpu_bd_run(h, w["warm"] * w["dt"], steps))
+    if budget_s is None:
+        abi.check(lib.stokes_gpu_bd_run(h, w["warm"] * w["dt"], steps))
+    else:
+        done = 0
+        while done < steps and (done == 0 or time.perf_counter() - t0 < budget_s):
+            abi.check(lib.stokes_gpu_bd_run(h, (w["warm"] + done) * w["dt"], 1))
+            done += 1
+        steps = done
     dt_wall = time.perf_counter() - t0
     st = np.zeros(4)
     abi.check(lib.stokes_gpu_bd_stats(h, st.ctypes.data_as(abi._dp)))
@@ -200,7 +208,7 @@ def _bd_engine_run(lib, abi, L, pos, Lb, precision, steps):
             "bound_estimates": st[1]}
 
 
-def _bd_dropin_run(lib, abi, L, pos, Lb, precision, steps):
+def _bd_dropin_run(lib, abi, L, pos, Lb, precision, steps, budget_s=20.0):
     """Wall time per step of libstokes' own BD_evolve_mid (src/brownian.c:
     2352-2560) through this library: EV_LJ as the reference applies it
     (src/ev-LJ.c:186-265, force along the primary-cell vector), Chebyshev
@@ -228,8 +236,11 @@ def _bd_dropin_run(lib, abi, L, pos, Lb, precision, steps):
     t = 0.0
     t += lib.BD_evolve_mid(t, bd, x.ctypes.data_as(dp), None, w["dt"])   # bounds + warm-up
     t0 = time.perf_counter()
-    for _ in range(steps):
+    done = 0
+    while done < steps and (done == 0 or time.perf_counter() - t0 < budget_s):
         t += lib.BD_evolve_mid(t, bd, x.ctypes.data_as(dp), None, w["dt"])
+        done += 1
+    steps = done
     dt_wall = time.perf_counter() - t0
     abi.raise_if_failed()
     lib.BD_params_free(bd)
@@ -254,7 +265,7 @@ def bd_measure(lib, abi, L, torch, dev):
     w = BD_WORKLOAD
     pos, Lb = rsa_positions(w["n"], w["phi"], seed=w["seed"])
     mixed = _bd_engine_run(lib, abi, L, pos, Lb, abi.MIXED, w["steps"])
-    fp64 = _bd_engine_run(lib, abi, L, pos, Lb, abi.FP64, w["steps_fp64"])
+    fp64 = _bd_engine_run(lib, abi, L, pos, Lb, abi.FP64, w["steps_fp64"], budget_s=20.0)
     d_mixed = _bd_dropin_run(lib, abi, L, pos, Lb, abi.MIXED, w["steps_dropin"])
     d_fp64 = _bd_dropin_run(lib, abi, L, pos, Lb, abi.FP64, w["steps_dropin"])
     return {"workload": w["name"], "steps_per_s": mixed["steps_per_s"],

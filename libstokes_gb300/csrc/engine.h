@@ -44,6 +44,10 @@ struct RealArgs {
   const double *slipa;  // slip-effective radii [np] (slip mode)
   double *partial;      // [nchunk][np][c]
   int open = 0;         // non-periodic: free-space scalars (src/non-ewald.c)
+  // rmin clamp at a split other than the struct's own: the clamped pairs
+  // take the clamp's change at the struct's split xi_ref (clampfix = 1)
+  int clampfix = 0;
+  double xi_ref = 0.0, xisp_ref = 0.0;
 };
 
 struct RecipArgs {

@@ -24,6 +24,28 @@ constexpr int RS_WARPS = 4;            // warps per CTA
 constexpr int RS_QCAP = 64;            // per-warp queue of accepted terms
 constexpr int RS_IMG_SMEM = 2048;      // images staged in shared memory
 
+// The rmin clamp (src/ewald.c:693-699: r raised to (a_i + a_j) rmin, and
+// e = d / r with the raised r) changes only the real-space term of a pair.
+// Unclamped, the sum does not depend on the split, so at a split xi other
+// than the struct's own xi_ref (clampfix) a clamped pair contributes
+//   T(d/rm; s_ref(rm)) + T(d/r; s_xi(r) - s_ref(r)),
+// the clamped term of the struct's split plus the change of the unclamped
+// term between the splits; the latter is smooth in r and comes from
+// split_diff without cancellation, however close the pair.  Equal spheres.
+template <int V>
+__device__ __noinline__ void
+clamp_term (const RealArgs &a, double dx, double dy, double dz, double r, double rm,
+            const GenF<V, double> &g, GenU<V, double> &acc)
+{
+  PairScalars<double> sc, ds;
+  real_scalars_mono<V, double> (a.xi_ref, a.xisp_ref, rm, sc);
+  split_diff<V, double> (a.xi_ref, a.xi, r, ds);
+  const double ec[3] = {dx / rm, dy / rm, dz / rm};
+  const double e0[3] = {dx / r, dy / r, dz / r};
+  pair_apply<V, double> (ec, sc, g, acc);
+  pair_apply<V, double> (e0, ds, g, acc);
+}
+
 template <int V, int MODE>
 __device__ __forceinline__ void
 real_term (const RealArgs &a, int i, int j, double dx, double dy, double dz,
@@ -34,7 +56,17 @@ real_term (const RealArgs &a, int i, int j, double dx, double dy, double dz,
   double aj = 1.0;
   if (MODE != MODE_MONO) aj = a.rad[j];
   const double rm = (ai + aj) * a.rmin;
-  if (r < rm) r = rm;
+  if (r < rm)
+    {
+      if (MODE == MODE_MONO && a.clampfix && !a.open)
+        {
+          GenF<V, double> g;
+          load_genf<V, double> (a.x + NComp<V>::value * j, g);
+          clamp_term<V> (a, dx, dy, dz, r, rm, g, acc);
+          return;
+        }
+      r = rm;
+    }
   const double ri = 1.0 / r;
   const double e[3] = {dx * ri, dy * ri, dz * ri};
   PairScalars<double> s;

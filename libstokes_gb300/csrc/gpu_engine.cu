@@ -334,8 +334,11 @@ upload_if_changed (DevBuf &buf, uint64_t &fp, const void *host, size_t bytes,
 // keeps the reference's split), set up by the reference's own rules on a
 // private copy of the system.  The sum is split-invariant to rounding
 // (measured 5e-15 to 8e-15 against the reference's split) -- except under
-// the rmin clamp, which changes only the real-space part, so systems with
-// rmin > 0 keep the reference's split.  libstokes' FTS result depends on its
+// the rmin clamp, which changes only the real-space part of the clamped
+// (overlapping) pairs: the real-space kernel adds that change at the
+// reference's split to each clamped pair (clamp_term, ewald_fp64.cu), which
+// needs the clamp radius below half the box (only the minimum image of a pair
+// can be clamped).  libstokes' FTS result depends on its
 // xi through the sign of its reciprocal G term (src/ewald.c:1060-1066):
 // y(xi) = y_inv + 2 G(xi), G the reciprocal G part as libstokes evaluates
 // it.  The tuned table therefore carries the invariant sign (-G on the tuned
@@ -387,9 +390,17 @@ static bool
 tuned_applies (const Ctx *c, const struct stokes *sys, bool cube)
 {
   const double eta = tuned_eta (sys->np);
+  // the clamp (rmin > 0) of equal spheres, when only the minimum image of a
+  // pair can be clamped
+  bool clamp_ok = sys->rmin == 0.0;
+  if (!clamp_ok && sys->rmin > 0.0 && sys->a == nullptr)
+    {
+      const double lmin = std::min (sys->lx, std::min (sys->ly, sys->lz));
+      clamp_ok = 2.0 * sys->rmin < 0.5 * lmin;
+    }
   return c->tune && eta > 0.0 && !cube && !c->open && sys->periodic && split_is_as_set (sys)
          && sys->slip == nullptr && sys->shear_mode == 0
-         && sys->rmin == 0.0 && sys->np > 0 && eta > sys->xi * cbrt (sys->lx * sys->ly * sys->lz);
+         && clamp_ok && sys->np > 0 && eta > sys->xi * cbrt (sys->lx * sys->ly * sys->lz);
 }
 
 // the private copy at the tuned split (rebuilt when the box, size, version
@@ -475,6 +486,7 @@ prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
   c->np = sys->np;
   c->mode = sys->slip ? MODE_SLIP : (sys->a ? MODE_POLY : MODE_MONO);
   c->xi = sys->xi;
+  c->xi_ref = sys->xi;
   c->xisp = sys->xi / sqrt (M_PI);
   c->rmax2 = sys->rmax2;
   c->rmin = sys->rmin;
@@ -617,6 +629,9 @@ atimes_fp64_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   a.slipa = slipa;
   a.partial = (double *) c->partial.p;
   a.open = c->open ? 1 : 0;
+  a.clampfix = (!c->open && c->rmin > 0.0 && c->xi != c->xi_ref) ? 1 : 0;
+  a.xi_ref = c->xi_ref;
+  a.xisp_ref = c->xi_ref / sqrt (M_PI);
   if ((e = launch_real_fp64 (c->version, c->mode, a, st)) != cudaSuccess)
     return cuda_fail (e, "real-space kernel");
   launches++;

@@ -32,6 +32,7 @@ struct Ctx {
   const struct stokes *sys = nullptr;
   int version = 0, np = 0, mode = 0;
   double xi = 0, xisp = 0, rmax2 = 0, rmin = 0;
+  double xi_ref = 0;      // the struct's own split (differs from xi at the tuned split)
   int nimg = 0, nk = 0;
   uint64_t fp_img = 0, fp_kt = 0, fp_pp = 0;
   std::vector<Img4> h_img;

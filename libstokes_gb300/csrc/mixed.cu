@@ -70,6 +70,9 @@ struct MixedState {
   uint64_t self_fp = 0;
   int self_np = 0;
   int nchunk_r = 1, nchunk_k = 1;
+  int real_g = 1;               // warps per target of mk_real
+  int nc[3] = {0, 0, 0};        // cell list of mk_real (nc[0] == 0: no cells)
+  DevBuf sq, cstart;
 };
 
 constexpr int MX_WARPS = 8;      // warps per CTA in the mixed kernels
@@ -92,7 +95,7 @@ struct PrepArgs {
   const float4 *rot;    // e^{2 pi i h / 1024}, h = 0..1023: (hi.re, hi.im, lo.re, lo.im)
   uint32_t *qpos;       // [np][4] fixed-point x, y, z (+ pad)
   float2 *tab;          // [ntab][np]
-  float *xf;            // [np*c]
+  float *xf;            // [np][cpad(c)]
   float *zf;            // forward GEMM image ZF (tensor-core path) or NULL
   size_t zplane;        // floats per ZF plane
   int kf;               // floats per ZF row
@@ -133,11 +136,13 @@ mk_prep (PrepArgs a)
   {
     const size_t e0 = (size_t) jb * a.c;
     const int nx = PREP_P * a.c;
+    const int cp = (a.c + 3) & ~3;
     for (int e = t; e < nx; e += blockDim.x)
       {
         const float v = (e0 + e < (size_t) a.np * a.c) ? (float) a.x[e0 + e] : 0.f;
         s_x[e] = v;
-        if (blockIdx.y == 0 && e0 + e < (size_t) a.np * a.c) a.xf[e0 + e] = v;
+        if (blockIdx.y == 0 && e0 + e < (size_t) a.np * a.c)
+          a.xf[(size_t) (jb + e / a.c) * cp + e % a.c] = v;
       }
   }
   if (t < PREP_P)
@@ -218,19 +223,35 @@ tab_get (const float2 *t, int m, size_t stride, size_t j)
   return m < 0 ? make_float2 (v.x, -v.y) : v;
 }
 
+// components of x per particle in the padded FP32 copy xf (float4 loads)
+__host__ __device__ constexpr int
+cpad (int c)
+{
+  return (c + 3) & ~3;
+}
+
 struct RealMixArgs {
-  const uint32_t *qpos;
-  const float *xf;
-  int np, nchunk;
+  const uint32_t *qpos;  // [np][4] fixed-point positions
+  const float *xf;       // [np][cpad(c)] FP32 x
+  int np;
+  int G;                 // warps per target (their sums meet in shared memory)
   float scale[3];        // L_d / 2^32
   int shear_mode;
   uint32_t shift_q;      // shift / lx * 2^32 (two's complement)
   float rc2, rmin;
   float xi, xisp;
   const float *rad, *slipa;
-  float *partial;        // [nchunk][np][c]
+  float *out;            // [2][np][c]: the compensated sum of each target as hi + lo
   const float4 *img;     // lattice offsets added to the minimum-image difference
   int nimg;              // 1 (the zero offset) while the cutoff is below half the box
+  // cell list (NULL cstart: every particle is a candidate source)
+  const uint4 *sq;       // particles in cell order: (q_x, q_y, q_z, particle index)
+  const int *cstart;     // [ncell + 1] first slot of each cell in sq
+  int nc[3];             // cells per axis (cell side >= rc / 2)
+  // rmin clamp: the clamped pairs take the clamp's change at the struct's
+  // own split xi_ref (clampfix = 1), see mix_term
+  int clampfix;
+  float xi_ref, xisp_ref;
 };
 
 // minimum-image displacement r_j - r_i from fixed-point positions
@@ -258,107 +279,351 @@ min_image (const RealMixArgs &a, uint4 qi, uint4 qj, float &dx, float &dy, float
   dz = (float) (int32_t) uz * a.scale[2];
 }
 
-template <int V, int MODE>
-__device__ __forceinline__ void
-mix_term (const RealMixArgs &a, int i, int j, float dx, float dy, float dz, float ai,
-          GenU<V, float> &acc)
+// The rmin clamp of libstokes (src/ewald.c:693-699: r raised to (a_i + a_j)
+// rmin, e = d / r with the raised r) changes the real-space term of a
+// clamped pair only; unclamped, the sum does not depend on the split.  At
+// the mixed split a clamped pair therefore contributes
+//   T(d/rm; s_ref(rm)) + T(d/r; s_xi(r) - s_ref(r))
+// (the clamped term of the struct's split, plus the change of the unclamped
+// term between the splits, which split_diff gives without cancellation).
+template <int V>
+__device__ __noinline__ void
+clamp_term (const RealMixArgs &a, float4 d, float r, float rm, const GenF<V, float> &g,
+            GenU<V, float> &t)
 {
-  const float rr = dx * dx + dy * dy + dz * dz;
-  float r = sqrtf (rr);
-  float aj = 1.0f;
-  if (MODE != MODE_MONO) aj = a.rad[j];
-  const float rm = (ai + aj) * a.rmin;
-  if (r < rm) r = rm;
-  const float ri = 1.0f / r;
-  const float e[3] = {dx * ri, dy * ri, dz * ri};
-  PairScalars<float> s;
-  if (MODE == MODE_MONO)
-    real_scalars_mono<V, float> (a.xi, a.xisp, r, s);
-  else if (MODE == MODE_POLY)
-    real_scalars_poly<V, float> (a.xi, a.xisp, r, ai, aj, ai, s);
-  else
-    real_scalars_poly<V, float> (a.xi, a.xisp, r, a.slipa[i], a.slipa[j], ai, s);
-  GenF<V, float> g;
-  load_genf<V, float> (a.xf + (size_t) NComp<V>::value * j, g);
-  pair_apply<V, float> (e, s, g, acc);
+  PairScalars<float> sc, ds;
+  real_scalars_mono<V, float> (a.xi_ref, a.xisp_ref, rm, sc);
+  split_diff<V, float> (a.xi_ref, a.xi, r, ds);
+  const float ec[3] = {d.x / rm, d.y / rm, d.z / rm};
+  const float e0[3] = {d.x / r, d.y / r, d.z / r};
+  t.zero ();
+  pair_apply<V, float> (ec, sc, g, t);
+  pair_apply<V, float> (e0, ds, g, t);
 }
 
-// one warp per (target i, source chunk); lanes test 32 sources at a time and
-// compact the ones inside the cutoff
-template <int V, int MODE>
-__global__ void __launch_bounds__ (MX_WARPS * 32)
+// one pair term (source j at displacement d from the target) into t
+template <int V>
+__device__ __forceinline__ void
+mix_term (const RealMixArgs &a, float4 d, GenU<V, float> &t)
+{
+  const int j = __float_as_int (d.w);
+  const float rr = d.x * d.x + d.y * d.y + d.z * d.z;
+  float r = sqrtf (rr);
+  const float rm = 2.0f * a.rmin;          // (a_i + a_j) rmin for unit spheres
+  const bool fix = r < rm && a.clampfix;
+  if (r < rm && !a.clampfix) r = rm;
+  constexpr int C = NComp<V>::value, CP = cpad (C);
+  // x_j as float4 loads of the padded copy
+  float xj[CP];
+  const float4 *src = reinterpret_cast<const float4 *> (a.xf + (size_t) CP * j);
+#pragma unroll
+  for (int k = 0; k < CP / 4; k++)
+    {
+      const float4 v = __ldg (src + k);
+      xj[4 * k] = v.x; xj[4 * k + 1] = v.y; xj[4 * k + 2] = v.z; xj[4 * k + 3] = v.w;
+    }
+  GenF<V, float> g;
+  load_genf<V, float> (xj, g);
+  if (fix)
+    {
+      clamp_term<V> (a, d, r, rm, g, t);
+      return;
+    }
+  const float ri = 1.0f / r;
+  const float e[3] = {d.x * ri, d.y * ri, d.z * ri};
+  PairScalars<float> s;
+  real_scalars_mono<V, float> (a.xi, a.xisp, r, s);
+  t.zero ();
+  pair_apply<V, float> (e, s, g, t);
+}
+
+// Kahan (compensated) addition of a term t into the running sum (s, c):
+// s + c carries the exact sum of the terms up to one FP32 rounding of c
+template <int V>
+__device__ __forceinline__ void
+kahan_add (GenU<V, float> &s, GenU<V, float> &c, const GenU<V, float> &t)
+{
+#pragma unroll
+  for (int q = 0; q < NComp<V>::value; q++)
+    {
+      const float y = t.v[q] + c.v[q];
+      const float u = s.v[q] + y;
+      c.v[q] = y - (u - s.v[q]);
+      s.v[q] = u;
+    }
+}
+
+// error-free sum of two values: a + b = s + e exactly
+__device__ __forceinline__ void
+two_sum (float a, float b, float &s, float &e)
+{
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+constexpr int RG_WARPS = 8;      // warps per CTA of mk_real
+constexpr int RG_QCAP = 192;     // queue entries per warp (the reduction reuses them)
+
+// The real-space sum of the mixed split: G warps per target particle.  Each
+// warp takes a share of the candidate sources (a slice of all particles, or
+// rows of neighbouring cells of the cell list), tests 32 at a time against
+// the cutoff (the minimum image and, for cutoffs beyond half the box, the
+// split's lattice offsets) and queues the accepted pairs (displacement and
+// source index, one float4 each) in shared memory; every 32 queued pairs the
+// lanes evaluate one term each, so the FP32 pipe only sees accepted terms.
+// Each lane keeps a Kahan-compensated sum per component; the 32 lanes meet
+// in shared memory (two lanes per component, each adding 16 compensated
+// lane sums with TwoSum), then the G warps of the target; the result is
+// written as the FP32 pair hi + lo, which the combine adds in FP64.
+template <int V>
+__global__ void __launch_bounds__ (RG_WARPS * 32)
 mk_real (RealMixArgs a)
 {
   constexpr int C = NComp<V>::value;
-  __shared__ float s_d[MX_WARPS][MX_QCAP][3];
-  __shared__ int s_j[MX_WARPS][MX_QCAP];
+  __shared__ float4 s_q[RG_WARPS][RG_QCAP];
+  __shared__ float s_red[RG_WARPS][2][C];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const long long w = (long long) blockIdx.x * MX_WARPS + wib;
-  if (w >= (long long) a.np * a.nchunk) return;
-  const int i = (int) (w % a.np);
-  const int chunk = (int) (w / a.np);
-  const int j0 = (int) ((long long) a.np * chunk / a.nchunk);
-  const int j1 = (int) ((long long) a.np * (chunk + 1) / a.nchunk);
-  const uint4 qi = reinterpret_cast<const uint4 *> (a.qpos)[i];
-  const float ai = (MODE == MODE_MONO) ? 1.0f : a.rad[i];
-  GenU<V, float> acc;
-  acc.zero ();
-  int qn = 0;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int jb = j0; jb < j1; jb += 32)
+  const int tpc = RG_WARPS / a.G;                       // targets per CTA
+  const int tl = wib / a.G, part = wib - tl * a.G;
+  const int slot = blockIdx.x * tpc + tl;
+  const bool live = slot < a.np;
+  const bool cells = a.cstart != nullptr;
+  uint4 qi = make_uint4 (0u, 0u, 0u, 0u);
+  int i = 0;
+  if (live)
     {
-      const int j = jb + lane;
-      float d0x = 0.f, d0y = 0.f, d0z = 0.f;
-      if (j < j1)
+      if (cells)
         {
-          const uint4 qj = reinterpret_cast<const uint4 *> (a.qpos)[j];
-          min_image (a, qi, qj, d0x, d0y, d0z);
+          qi = a.sq[slot];
+          i = (int) qi.w;
         }
-      // the minimum image and, when the cutoff exceeds half the box, the
-      // lattice images around it
-      for (int m = 0; m < a.nimg; m++)
+      else
         {
-          const float4 T = a.img[m];
-          bool ok = false;
-          float dx = 0.f, dy = 0.f, dz = 0.f;
-          if (j < j1)
-            {
-              dx = d0x + T.x;
-              dy = d0y + T.y;
-              dz = d0z + T.z;
-              const float rr = dx * dx + dy * dy + dz * dz;
-              ok = (rr > 0.f) && (rr < a.rc2);
-            }
-          const unsigned b = __ballot_sync (0xffffffffu, ok);
-          if (ok)
-            {
-              const int slot = qn + __popc (b & lt);
-              s_d[wib][slot][0] = dx;
-              s_d[wib][slot][1] = dy;
-              s_d[wib][slot][2] = dz;
-              s_j[wib][slot] = j;
-            }
-          qn += __popc (b);
-          __syncwarp ();
-          if (qn >= 32)
-            {
-              const int slot = qn - 32 + lane;
-              mix_term<V, MODE> (a, i, s_j[wib][slot], s_d[wib][slot][0], s_d[wib][slot][1],
-                                 s_d[wib][slot][2], ai, acc);
-              qn -= 32;
-              __syncwarp ();
-            }
+          qi = reinterpret_cast<const uint4 *> (a.qpos)[slot];
+          i = slot;
         }
     }
-  if (lane < qn)
-    mix_term<V, MODE> (a, i, s_j[wib][lane], s_d[wib][lane][0], s_d[wib][lane][1],
-                       s_d[wib][lane][2], ai, acc);
-  float *out = a.partial + ((size_t) chunk * a.np + i) * C;
-#pragma unroll
-  for (int q = 0; q < C; q++)
+  GenU<V, float> sum, cmp, t;
+  sum.zero ();
+  cmp.zero ();
+  float4 *q = s_q[wib];
+  int qn = 0;
+  const unsigned lt = (1u << lane) - 1u;
+
+  // test the candidate sources s0 .. s1 - 1 (slots of the source array)
+  auto scan = [&] (int s0, int s1) {
+    for (int sb = s0; sb < s1; sb += 32)
+      {
+        const int sj = sb + lane;
+        float d0x = 0.f, d0y = 0.f, d0z = 0.f;
+        int j = 0;
+        if (sj < s1)
+          {
+            const uint4 qj = cells ? a.sq[sj] : reinterpret_cast<const uint4 *> (a.qpos)[sj];
+            j = cells ? (int) qj.w : sj;
+            min_image (a, qi, qj, d0x, d0y, d0z);
+          }
+        for (int m = 0; m < a.nimg; m++)
+          {
+            const float4 T = a.img[m];
+            float dx = 0.f, dy = 0.f, dz = 0.f;
+            bool ok = false;
+            if (sj < s1)
+              {
+                dx = d0x + T.x;
+                dy = d0y + T.y;
+                dz = d0z + T.z;
+                const float rr = dx * dx + dy * dy + dz * dz;
+                ok = (rr > 0.f) && (rr < a.rc2);
+              }
+            const unsigned b = __ballot_sync (0xffffffffu, ok);
+            if (ok) q[qn + __popc (b & lt)] = make_float4 (dx, dy, dz, __int_as_float (j));
+            qn += __popc (b);
+            __syncwarp ();
+            if (qn >= 32)
+              {
+                mix_term<V> (a, q[qn - 32 + lane], t);
+                kahan_add<V> (sum, cmp, t);
+                qn -= 32;
+                __syncwarp ();
+              }
+          }
+      }
+  };
+
+  if (live)
     {
-      const float v = warp_sum (acc.v[q]);
-      if (lane == 0) out[q] = v;
+      if (!cells)
+        scan ((int) ((long long) a.np * part / a.G), (int) ((long long) a.np * (part + 1) / a.G));
+      else
+        {
+          // rows (dx, dy) of the 5 x 5 x 5 neighbouring cells (cell side >=
+          // rc / 2); the 5 cells of a row along z are one or two contiguous
+          // runs of slots; the rows are dealt round-robin to the G warps
+          const int cx = (int) (((unsigned long long) qi.x * (unsigned) a.nc[0]) >> 32);
+          const int cy = (int) (((unsigned long long) qi.y * (unsigned) a.nc[1]) >> 32);
+          const int cz = (int) (((unsigned long long) qi.z * (unsigned) a.nc[2]) >> 32);
+          const int nz = a.nc[2];
+          for (int row = part; row < 25; row += a.G)
+            {
+              const int ox = row / 5 - 2, oy = row % 5 - 2;
+              const int x = (cx + ox + a.nc[0]) % a.nc[0], y = (cy + oy + a.nc[1]) % a.nc[1];
+              const int base = (x * a.nc[1] + y) * nz;
+              const int z0 = cz - 2, z1 = cz + 2;          // inclusive, may wrap
+              if (z0 >= 0 && z1 < nz)
+                scan (a.cstart[base + z0], a.cstart[base + z1 + 1]);
+              else if (z0 < 0)
+                {
+                  scan (a.cstart[base], a.cstart[base + z1 + 1]);
+                  scan (a.cstart[base + z0 + nz], a.cstart[base + nz]);
+                }
+              else
+                {
+                  scan (a.cstart[base + z0], a.cstart[base + nz]);
+                  scan (a.cstart[base], a.cstart[base + z1 - nz + 1]);
+                }
+            }
+        }
+      if (lane < qn)
+        {
+          mix_term<V> (a, q[lane], t);
+          kahan_add<V> (sum, cmp, t);
+        }
+    }
+  // the 32 lane sums of this warp: (s, c) rows of 2C + 1 floats in the
+  // (now empty) queue; lane q + 11 h adds lanes 16 h .. 16 h + 15 of
+  // component q
+  __syncwarp ();
+  constexpr int RW = 2 * C + 1;
+  static_assert (32 * RW * 4 <= RG_QCAP * 16, "reduction rows exceed the queue");
+  float *w = reinterpret_cast<float *> (q);
+#pragma unroll
+  for (int k = 0; k < C; k++)
+    {
+      w[lane * RW + k] = sum.v[k];
+      w[lane * RW + C + k] = cmp.v[k];
+    }
+  __syncwarp ();
+  float S = 0.f, E = 0.f;
+  const int comp = lane % C, half = lane / C;
+  if (lane < 2 * C)
+    for (int l = 16 * half; l < 16 * half + 16; l++)
+      {
+        float s2, e2;
+        two_sum (S, w[l * RW + comp], s2, e2);
+        S = s2;
+        E += e2 + w[l * RW + C + comp];
+      }
+  {
+    const float So = __shfl_down_sync (0xffffffffu, S, C);
+    const float Eo = __shfl_down_sync (0xffffffffu, E, C);
+    if (lane < C)
+      {
+        float s2, e2;
+        two_sum (S, So, s2, e2);
+        s_red[wib][0][lane] = s2;
+        s_red[wib][1][lane] = E + Eo + e2;
+      }
+  }
+  __syncthreads ();
+  // the G warps of the target: part 0 adds them and writes hi, lo
+  if (live && part == 0 && lane < C)
+    {
+      float S0 = s_red[wib][0][lane], E0 = s_red[wib][1][lane];
+      for (int p = 1; p < a.G; p++)
+        {
+          float s2, e2;
+          two_sum (S0, s_red[wib + p][0][lane], s2, e2);
+          S0 = s2;
+          E0 += e2 + s_red[wib + p][1][lane];
+        }
+      const float hi = S0 + E0;
+      const float lo = E0 - (hi - S0);
+      a.out[(size_t) i * C + lane] = hi;
+      a.out[((size_t) a.np + i) * C + lane] = lo;
+    }
+}
+
+// The cell list of mk_real: particles sorted by cell, stably (in particle
+// order within a cell, so the sums are reproducible).  One CTA of 1024
+// threads; warp w owns particles [w N / 32, (w + 1) N / 32): it counts them
+// per cell (its own row of counts); thread c turns column c (cell c) into
+// the warps' offsets within the cell, a block scan of the cell totals gives
+// the cell starts, and each warp places its particles in order, 32 at a
+// time, lanes of one cell ranked by __match_any_sync.
+constexpr int CELL_THREADS = 1024;
+constexpr int CELL_MAX = 1000;           // cells (<= CELL_THREADS: one per thread)
+
+__global__ void __launch_bounds__ (CELL_THREADS)
+mk_cells (const uint4 *qpos, int np, int nc0, int nc1, int nc2, int *cstart, uint4 *sq)
+{
+  extern __shared__ int s_cnt[];          // [32][ncell]: counts, then slots
+  __shared__ int s_part[32];
+  const int ncell = nc0 * nc1 * nc2;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int k = threadIdx.x; k < 32 * ncell; k += blockDim.x) s_cnt[k] = 0;
+  __syncthreads ();
+  const int p0 = (int) ((long long) np * w / 32), p1 = (int) ((long long) np * (w + 1) / 32);
+  auto cell_of = [&] (uint4 q) {
+    const int x = (int) (((unsigned long long) q.x * (unsigned) nc0) >> 32);
+    const int y = (int) (((unsigned long long) q.y * (unsigned) nc1) >> 32);
+    const int z = (int) (((unsigned long long) q.z * (unsigned) nc2) >> 32);
+    return (x * nc1 + y) * nc2 + z;
+  };
+  for (int p = p0 + lane; p < p1; p += 32) atomicAdd (&s_cnt[w * ncell + cell_of (qpos[p])], 1);
+  __syncthreads ();
+  const int c = threadIdx.x;
+  int tot = 0;
+  if (c < ncell)
+    for (int ww = 0; ww < 32; ww++)
+      {
+        const int v = s_cnt[ww * ncell + c];
+        s_cnt[ww * ncell + c] = tot;
+        tot += v;
+      }
+  // block-wide exclusive scan of the cell totals
+  int v = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+    {
+      const int n = __shfl_up_sync (0xffffffffu, v, o);
+      if (lane >= o) v += n;
+    }
+  if (lane == 31) s_part[w] = v;
+  __syncthreads ();
+  if (w == 0)
+    {
+      int pv = s_part[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1)
+        {
+          const int n = __shfl_up_sync (0xffffffffu, pv, o);
+          if (lane >= o) pv += n;
+        }
+      s_part[lane] = pv;
+    }
+  __syncthreads ();
+  const int start = v - tot + (w > 0 ? s_part[w - 1] : 0);
+  if (c < ncell)
+    {
+      for (int ww = 0; ww < 32; ww++) s_cnt[ww * ncell + c] += start;
+      cstart[c] = start;
+      if (c == ncell - 1) cstart[ncell] = start + tot;
+    }
+  __syncthreads ();
+  for (int pb = p0; pb < p1; pb += 32)
+    {
+      const int p = pb + lane;
+      const bool ok = p < p1;
+      const uint4 qv = ok ? qpos[p] : make_uint4 (0u, 0u, 0u, 0u);
+      const int cc = ok ? cell_of (qv) : -1;
+      const unsigned peers = __match_any_sync (0xffffffffu, cc);
+      const int rank = __popc (peers & ((1u << lane) - 1u));
+      if (ok) sq[s_cnt[w * ncell + cc] + rank] = make_uint4 (qv.x, qv.y, qv.z, (unsigned) p);
+      __syncwarp ();
+      if (ok && rank == 0) s_cnt[w * ncell + cc] += __popc (peers);
+      __syncwarp ();
     }
 }
 
@@ -390,7 +655,7 @@ mk_sfac (KMixArgs a)
     {
       const float2 ph = cmul (cmul (tab_get (t0, K.m1, a.np, j), tab_get (t1, K.m2, a.np, j)),
                               tab_get (t2, K.m3, a.np, j));
-      const float *xj = a.xf + (size_t) C * j;
+      const float *xj = a.xf + (size_t) cpad (C) * j;
 #pragma unroll
       for (int q = 0; q < C; q++)
         {
@@ -855,11 +1120,13 @@ run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_
   mix (m->img_key);
   mix ((uint64_t) m->tensor);
   mix ((uint64_t) m->nchunk_r);
+  mix ((uint64_t) m->real_g);
+  mix ((uint64_t) m->nc[0] * 1000003ull + (uint64_t) m->nc[1] * 1009ull + (uint64_t) m->nc[2]);
   mix ((uint64_t) m->nchunk_k);
   const void *ptrs[] = {d_pos, d_x, d_y, m->kt.p, m->qpos.p, m->tab.p, m->xf.p, m->pq.p,
                         m->part_real.p, m->part_rec.p, m->selfbuf.p, m->status.p, m->sf.p,
                         m->rowm.p, m->rot.p, m->img_zf.p, m->img_wb.p, m->h_status, m->tyz.p,
-                        m->img.p};
+                        m->img.p, m->sq.p, m->cstart.p};
   for (const void *p : ptrs) mix ((uint64_t) (uintptr_t) p);
   mix ((uint64_t) (uintptr_t) E);
   // a captured cudaEventRecord is only a dependency, not a record: around a
@@ -928,7 +1195,32 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   if (rc) return rc;
   const int np = c->np, C = NCOMP (c->version);
   const int ntab = (m->M[0] + 1) + (m->M[1] + 1) + (m->M[2] + 1);
-  m->nchunk_r = std::max (1, std::min (64, (152 * 48 + np - 1) / np));
+  // the real-space sum: G warps per target, the smallest power of two that
+  // gives about 16 warps per SM; its hi + lo output is two combine chunks
+  m->nchunk_r = 2;
+  {
+    int g = 1;
+    while (g < 8 && (long long) np * g < 152 * 16) g *= 2;
+    const int ge = (int) env_double ("LIBSTOKES_GB300_REAL_G", 0.0);
+    if (ge == 1 || ge == 2 || ge == 4 || ge == 8) g = ge;
+    m->real_g = g;
+  }
+  // cell list when the box holds at least 6 cells of side >= rc / 2 per axis
+  // (5 x 5 x 5 neighbouring cells then prune the candidates) on an
+  // unsheared lattice with the minimum image alone
+  {
+    int nc[3];
+    const double L[3] = {sys->lx, sys->ly, sys->lz};
+    bool ok = sys->shear_mode == 0 && m->nimg == 1
+              && env_double ("LIBSTOKES_GB300_CELLS", 1.0) != 0.0;
+    for (int d = 0; d < 3; d++)
+      {
+        nc[d] = std::min (10, (int) floor (2.0 * L[d] / m->rc));
+        ok = ok && nc[d] >= 6;
+      }
+    if (ok && nc[0] * nc[1] * nc[2] > CELL_MAX) ok = false;
+    for (int d = 0; d < 3; d++) m->nc[d] = ok ? nc[d] : 0;
+  }
   const size_t off1 = (size_t) (m->M[0] + 1) * np;
   const size_t off2 = off1 + (size_t) (m->M[1] + 1) * np;
   PhaseTables pt{(const float2 *) m->tab.p, off1, off2, m->M[0], m->M[1], m->M[2], np,
@@ -975,7 +1267,16 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   if ((e = m->qpos.ensure (sizeof (uint32_t) * 4 * np)) != cudaSuccess) return cuda_fail (e, "qpos");
   if ((e = m->tab.ensure (sizeof (float2) * (size_t) ntab * np)) != cudaSuccess) return cuda_fail (e, "phase tables");
   m->plan.t.tab = (const float2 *) m->tab.p;
-  if ((e = m->xf.ensure (sizeof (float) * (size_t) C * np)) != cudaSuccess) return cuda_fail (e, "xf");
+  if ((e = m->xf.ensure (sizeof (float) * (size_t) cpad (C) * np)) != cudaSuccess) return cuda_fail (e, "xf");
+  if (m->nc[0])
+    {
+      const int ncell = m->nc[0] * m->nc[1] * m->nc[2];
+      if ((e = m->sq.ensure (sizeof (uint4) * np)) != cudaSuccess) return cuda_fail (e, "cell order");
+      if ((e = m->cstart.ensure (sizeof (int) * (ncell + 1))) != cudaSuccess) return cuda_fail (e, "cell starts");
+      if ((e = cudaFuncSetAttribute (mk_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int) sizeof (int) * 32 * CELL_MAX)) != cudaSuccess)
+        return cuda_fail (e, "cell kernel attribute");
+    }
   if (m->tensor)
     {
       if ((e = m->sf.ensure (sizeof (float) * kgemm_sf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "structure factors");
@@ -1077,8 +1378,9 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     kmark (c, st, "mk_prep");
 
     RealMixArgs ra;
+    memset (&ra, 0, sizeof ra);
     ra.qpos = (const uint32_t *) m->qpos.p; ra.xf = (const float *) m->xf.p;
-    ra.np = np; ra.nchunk = m->nchunk_r;
+    ra.np = np; ra.G = m->real_g;
     const double two32 = 4294967296.0;
     ra.scale[0] = (float) (sys->lx / two32);
     ra.scale[1] = (float) (sys->ly / two32);
@@ -1094,17 +1396,35 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     ra.xi = (float) m->xi;
     ra.xisp = (float) (m->xi / sqrt (M_PI));
     ra.rad = nullptr; ra.slipa = nullptr;
-    ra.partial = (float *) m->part_real.p;
+    ra.clampfix = sys->rmin > 0.0 ? 1 : 0;
+    ra.xi_ref = (float) sys->xi;
+    ra.xisp_ref = (float) (sys->xi / sqrt (M_PI));
+    ra.out = (float *) m->part_real.p;
     ra.img = (const float4 *) m->img.p;
     ra.nimg = m->nimg;
-    const int gr = (int) (((long long) np * m->nchunk_r + MX_WARPS - 1) / MX_WARPS);
+    if (m->nc[0])
+      {
+        ra.sq = (const uint4 *) m->sq.p;
+        ra.cstart = (const int *) m->cstart.p;
+        for (int d = 0; d < 3; d++) ra.nc[d] = m->nc[d];
+      }
+    const int tpc = RG_WARPS / m->real_g;
+    const int gr = (np + tpc - 1) / tpc;
     // concurrent with the reciprocal chain unless the launches are being
     // timed one by one (then in order: reciprocal, real, combine)
     const bool overlap = !E && !c->kprof_on && m->side;
     auto launch_real = [&] (cudaStream_t rs) {
-      if (c->version == 0) mk_real<0, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
-      else if (c->version == 1) mk_real<1, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
-      else mk_real<2, MODE_MONO><<<gr, MX_WARPS * 32, 0, rs>>> (ra);
+      if (m->nc[0])
+        {
+          const int ncell = m->nc[0] * m->nc[1] * m->nc[2];
+          mk_cells<<<1, CELL_THREADS, sizeof (int) * 32 * ncell, rs>>> (
+            (const uint4 *) m->qpos.p, np, m->nc[0], m->nc[1], m->nc[2], (int *) m->cstart.p,
+            (uint4 *) m->sq.p);
+          kmark (c, rs, "mk_cells");
+        }
+      if (c->version == 0) mk_real<0><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
+      else if (c->version == 1) mk_real<1><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
+      else mk_real<2><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
     };
     if (overlap)
       {
@@ -1181,7 +1501,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   };
   int rs = run_mixed_sequence (c, m, d_pos, d_x, d_y, st, E, sequence);
   if (rs) return rs;
-  c->launches = m->nkh == 0 ? 3 : (m->tensor ? 6 : 5);
+  c->launches = (m->nkh == 0 ? 3 : (m->tensor ? 6 : 5)) + (m->nc[0] ? 1 : 0);
   c->timed = timed;
   return STOKES_GPU_OK;
 }
@@ -1204,7 +1524,7 @@ release_mixed (Ctx *c)
   MixedState *m = c->mixed;
   for (DevBuf *b : {&m->kt, &m->qpos, &m->tab, &m->xf, &m->pq, &m->part_real, &m->part_rec,
                     &m->selfbuf, &m->status, &m->sf, &m->rowm, &m->rot, &m->img_zf,
-                    &m->img_wb, &m->tyz, &m->img})
+                    &m->img_wb, &m->tyz, &m->img, &m->sq, &m->cstart})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
   if (m->gexec) cudaGraphExecDestroy (m->gexec);
