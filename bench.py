@@ -400,45 +400,49 @@ def open_measure(lib, abi, L, torch, dev, pos, reps: int = 20):
                      "the 11 x 11 pair tensor applied in FP64"}
 
 
-def solve_measure(lib, abi, L, torch, dev, pos, Lbox, product_ms):
+def solve_measure(lib, abi, L, torch, dev, pos, Lbox, product_ms, eps=1e-10):
     """FTS resistance solve M x = b (solve_iter with atimes_3all, the call of
-    src/ewald-3fts.c:71) on the bench's N = 1000 spheres, mixed precision,
-    GMRES(30) to eps 1e-5 from a zero start (the mixed product carries
-    about 3e-7, so 1e-6 sits at its noise floor): wall time of the whole solve
-    (host-driven: one small copy per iteration), iterations, and the share
-    of the time the products take (iterations x the timed product)."""
+    src/ewald-3fts.c:71) on the bench's N = 1000 spheres to eps 1e-10 from a
+    zero start: mixed precision (GMRES(30) on the mixed product inside FP64
+    iterative refinement; every residual test uses the FP64 product) against
+    the plain FP64 GMRES(30) solve; wall time of the whole solve (host
+    buffers in and out), operator applications, and the relative difference
+    of the two solutions."""
     w = WORKLOAD
     s = L.System(w["version"], pos, (Lbox,) * 3, tratio=w["tratio"], eps=w["eps"])
-    s.set_precision(abi.MIXED)
     n = s.n
     b = np.random.default_rng(11).standard_normal(n)
     it = C.c_int()
     res = C.c_double()
-    x = np.zeros(n)
-    abi.check(lib.stokes_gpu_solve(s.sp, 0, abi._d(b), abi._d(x), 30, 1000, 1e-5, C.byref(it),
-                                   C.byref(res)))      # warm-up: graphs, workspace
-    walls = []
-    for _ in range(3):
-        x[:] = 0.0
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        abi.check(lib.stokes_gpu_solve(s.sp, 0, abi._d(b), abi._d(x), 30, 1000, 1e-5,
-                                       C.byref(it), C.byref(res)))
-        walls.append(time.perf_counter() - t0)
-    wall = float(np.median(walls))
+    out = {"workload": f"solve_res_fts_n{w['n']}_phi{w['phi']:.2f}", "eps": eps}
+    sols = {}
+    for name, prec, reps in (("mixed_refined", abi.MIXED, 3), ("fp64", abi.FP64, 1)):
+        s.set_precision(prec)
+        x = np.zeros(n)
+        abi.check(lib.stokes_gpu_solve(s.sp, 0, abi._d(b), abi._d(x), 30, 5000, 1e-4,
+                                       C.byref(it), C.byref(res)))  # warm-up: graphs, workspace
+        walls = []
+        for _ in range(reps):
+            x[:] = 0.0
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            abi.check(lib.stokes_gpu_solve(s.sp, 0, abi._d(b), abi._d(x), 30, 5000, eps,
+                                           C.byref(it), C.byref(res)))
+            walls.append(time.perf_counter() - t0)
+        sols[name] = x.copy()
+        out[name] = {"ms": 1000.0 * float(np.median(walls)), "applications": it.value,
+                     "relative_residual_fp64": res.value,
+                     "ms_runs": [1000.0 * t for t in walls]}
     s.close()
-    iters = it.value
-    # every restart cycle adds one residual product to the iterations
-    products = iters + max(1, (iters + 29) // 30) + 1
-    return {"workload": f"solve_res_fts_n{w['n']}_phi{w['phi']:.2f}", "precision": "mixed",
-            "solver": "GMRES(30), CGS2 in one cooperative kernel per step, eps 1e-5", "iterations": iters,
-            "relative_residual": res.value, "ms": 1000.0 * wall,
-            "ms_per_iteration": 1000.0 * wall / max(iters, 1),
-            "product_ms": product_ms, "products": products,
-            "product_share": products * product_ms / (1000.0 * wall),
-            "ms_runs": [1000.0 * t for t in walls],
-            "timing": "wall clock around stokes_gpu_solve (host buffers in and out), "
-                      "median of 3 solves"}
+    out["mixed_refined"]["solver"] = ("GMRES(30) on the mixed product inside FP64 iterative "
+                                      "refinement (residuals from the FP64 product)")
+    out["fp64"]["solver"] = "GMRES(30) on the FP64 product"
+    out["speedup_mixed_refined_over_fp64"] = out["fp64"]["ms"] / out["mixed_refined"]["ms"]
+    out["rel_diff_solutions"] = float(np.linalg.norm(sols["mixed_refined"] - sols["fp64"])
+                                      / np.linalg.norm(sols["fp64"]))
+    out["product_ms_mixed"] = product_ms
+    out["timing"] = "wall clock around stokes_gpu_solve (host buffers), median of 3 (mixed), 1 (fp64)"
+    return out
 
 
 def scale_measure(lib, abi, L, torch, dev, sizes=(4096, 16384), reps=10):

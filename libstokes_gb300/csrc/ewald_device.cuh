@@ -43,18 +43,59 @@ template <typename R> __device__ __forceinline__ R dev_sqrt (R x);
 template <> __device__ __forceinline__ double dev_sqrt<double> (double x) { return sqrt (x); }
 template <> __device__ __forceinline__ float dev_sqrt<float> (float x) { return sqrtf (x); }
 
+// erfc(x) and exp(-x^2) for x >= 0, x2 = x^2 (the two transcendentals of
+// every real-space term)
+template <typename R>
+__device__ __forceinline__ void
+erfc_exp (R x, R x2, R &ec, R &e)
+{
+  ec = dev_erfc<R> (x);
+  e = dev_exp<R> (-x2);
+}
+
+// FP32: one exponential for both.  erfc(x) = exp(-x^2) R(x) with the smooth
+// R(x) = exp(x^2) erfc(x) approximated as t Q(u), t = 1 / (1 + x / 2) (the
+// variable of the rational erfc approximation in Press et al., Numerical
+// Recipes, "erfcc"), u = (t - 0.2222) / 0.3889 mapping x in [0, 7] to
+// [-1, 1], Q of degree 9 with coefficients fitted here (weighted least
+// squares on the relative error, 3500 points against a 40-digit evaluation):
+// approximation error 7e-9, 3e-7 worst case with the FP32 arithmetic, about
+// the error of the library erfcf.  Beyond x = 7 erfc < 5e-23 and the terms
+// it enters are negligible.  exp: the hardware exponential (__expf), whose
+// relative error grows as |x2| 6e-8; where that matters (x2 >> 1) the term
+// itself is negligible.
+template <>
+__device__ __forceinline__ void
+erfc_exp<float> (float x, float x2, float &ec, float &e)
+{
+  e = __expf (-x2);
+  const float t = __frcp_rn (fmaf (0.5f, x, 1.0f));
+  const float u = fmaf (2.5714285714285714f, t, -1.5714285714285716f);
+  float q = 4.768114822208366e-06f;
+  q = fmaf (q, u, -2.873052176671487e-05f);
+  q = fmaf (q, u, -1.653469624654579e-05f);
+  q = fmaf (q, u, 0.0003848538656271584f);
+  q = fmaf (q, u, -0.00027154337201642197f);
+  q = fmaf (q, u, -0.004794785092242448f);
+  q = fmaf (q, u, 0.0034944894230291255f);
+  q = fmaf (q, u, 0.08977352324023499f);
+  q = fmaf (q, u, 0.31723869625882506f);
+  q = fmaf (q, u, 0.594215256210305f);
+  ec = e * (t * q);
+}
+
 // Monodisperse real-space scalars (unit radius) at distance r for splitting
 // parameter xi: the closed forms of src/ewald.c:49-186, arranged in Horner
-// form in u2 = (xi r)^2.  xisp = xi / sqrt(pi).
+// form in u2 = (xi r)^2.  xisp = xi / sqrt(pi).  ri = 1 / r.
 template <int V, typename R>
 __device__ __forceinline__ void
-real_scalars_mono (R xi, R xisp, R r, PairScalars<R> &s)
+real_scalars_mono_ri (R xi, R xisp, R r, R ri, PairScalars<R> &s)
 {
   const R u2 = (xi * r) * (xi * r);
-  const R ri = R (1) / r;
   const R ri2 = ri * ri;
-  const R ec = dev_erfc<R> (xi * r);
-  const R ex = xisp * dev_exp<R> (-u2);
+  R ec, eg;
+  erfc_exp<R> (xi * r, u2, ec, eg);
+  const R ex = xisp * eg;
 
   const R a1 = (R (0.75) + R (0.5) * ri2) * ri * ec
     + ((R (1) + u2 * (R (14) + R (4) * u2 * (u2 - R (5)))) * ri2 - R (4.5) + R (3) * u2) * ex;
@@ -97,6 +138,13 @@ real_scalars_mono (R xi, R xisp, R r, PairScalars<R> &s)
     + (R (-1.5) * u2 * (R (8) - R (4) * u2)
        - R (1.2) * (R (-3) + u2 * (R (-2) + u2 * (R (-26) + u2 * (R (26) - R (4) * u2)))) * ri2)
       * ri2 * ex;
+}
+
+template <int V, typename R>
+__device__ __forceinline__ void
+real_scalars_mono (R xi, R xisp, R r, PairScalars<R> &s)
+{
+  real_scalars_mono_ri<V, R> (xi, xisp, r, R (1) / r, s);
 }
 
 // Difference of the monodisperse real-space scalars between two splits,
@@ -162,8 +210,9 @@ real_scalars_poly (R xi, R xisp, R r, R aa, R ab, R asd, PairScalars<R> &s)
   const R u2 = (xi * r) * (xi * r);
   const R ri = R (1) / r;
   const R ri2 = ri * ri, ri3 = ri2 * ri, ri4 = ri2 * ri2, ri5 = ri3 * ri2;
-  const R ec = dev_erfc<R> (xi * r);
-  const R ex = xisp * dev_exp<R> (-u2);
+  R ec, eg;
+  erfc_exp<R> (xi * r, u2, ec, eg);
+  const R ex = xisp * eg;
   const R sa2 = aa * aa + ab * ab;
 
   const R k0 = R (2) * (R (-3) + R (2) * u2) * ex + ec * ri;
@@ -174,8 +223,8 @@ real_scalars_poly (R xi, R xisp, R r, R aa, R ab, R asd, PairScalars<R> &s)
   const R h2 = R (-4) * ri2 * (R (3) + u2 * (R (2) + u2 * (R (-16) + R (4) * u2))) * ex
     - R (6) * ri3 * ec;
 
-  s.ya = R (0.75) * (k0 + k2 * sa2 / R (6));
-  s.xa = R (0.75) * (h0 + h2 * sa2 / R (6)) + s.ya;
+  s.ya = R (0.75) * (k0 + k2 * sa2 * R (1.0 / 6.0));
+  s.xa = R (0.75) * (h0 + h2 * sa2 * R (1.0 / 6.0)) + s.ya;
   s.yb = s.xc = s.yc = s.xg = s.yg = s.yh = s.xm = s.ym = s.zm = R (0);
   s.xa *= asd;
   s.ya *= asd;
@@ -198,16 +247,16 @@ real_scalars_poly (R xi, R xisp, R r, R aa, R ab, R asd, PairScalars<R> &s)
     + R (24) * ri5 * ec;
   const R h2d = R (4) * ri3 * (R (9) + u2 * (R (6) + u2 * (R (36) + u2 * (R (-48) + R (8) * u2)))) * ex
     + R (18) * ri4 * ec;
-  const R wg = aa * aa / R (10) + ab * ab / R (6);
+  const R wg = aa * aa * R (0.1) + ab * ab * R (1.0 / 6.0);
   s.xg = R (-3) * (R (-0.75) * ri * h0 - R (0.75) * ri * h2 * wg) * asd2;
   s.yg = (R (-0.375) * (k0d + h0 * ri) - R (0.375) * (k2d + h2 * ri) * wg) * asd2;
   s.yh = R (-0.1875) * (k0dd + (-k0d - h0d + R (2) * h0 * ri) * ri) * asd3;
-  const R m5 = R (-0.375) * (k0d + h0 * ri) * ri - R (0.375) * (k2d + h2 * ri) * ri * sa2 / R (10);
+  const R m5 = R (-0.375) * (k0d + h0 * ri) * ri - R (0.375) * (k2d + h2 * ri) * ri * sa2 * R (0.1);
   const R zm = R (2) * m5;
-  const R m3 = R (-0.75) * h0 * ri2 - R (0.75) * h2 * ri2 * sa2 / R (10);
+  const R m3 = R (-0.75) * h0 * ri2 - R (0.75) * h2 * ri2 * sa2 * R (0.1);
   const R xm = R (6) * m3 + R (3) * zm;
   const R m4 = R (-0.1875) * (k0dd + (-k0d + R (3) * h0d - R (6) * h0 * ri) * ri)
-    - R (0.1875) * (k2dd + (-k2d + R (3) * h2d - R (6) * h2 * ri) * ri) * sa2 / R (10);
+    - R (0.1875) * (k2dd + (-k2d + R (3) * h2d - R (6) * h2 * ri) * ri) * sa2 * R (0.1);
   const R ym = R (2) * m4 + zm;
   s.zm = zm * asd3;
   s.xm = xm * asd3;
@@ -269,7 +318,7 @@ open_scalars (R r, R aa, R ab, R a1, PairScalars<R> &s)
   s.xc = R (0.75) * r2i * ri * a13;
   s.yc = R (-0.375) * r2i * ri * a13;
   if (V == V_FT) return;
-  const R q = aa * aa / R (10) + ab * ab / R (6);
+  const R q = aa * aa * R (0.1) + ab * ab * R (1.0 / 6.0);
   s.xg = (R (2.25) - R (13.5) * q * r2i) * r2i * a12;
   s.yg = R (4.5) * q * r2i * r2i * a12;
   s.yh = R (-1.125) * r2i * ri * a13;
@@ -315,10 +364,10 @@ pair_apply (const R e[3], const PairScalars<R> &s, const GenF<V, R> &g, GenU<V, 
   const R Se2 = Sxz * e[0] + Syz * e[1];
   const R eSe = e[0] * Se0 + e[1] * Se1 + e[2] * Se2;
   const R trS = Sxx + Syy;
-  const R g1 = -s.xg / R (3), g2 = s.yg, g3 = s.xg - R (2) * s.yg;
+  const R g1 = -s.xg * R (1.0 / 3.0), g2 = s.yg, g3 = s.xg - R (2) * s.yg;
   const R m1 = R (1.5) * s.xm - R (2) * s.ym + R (0.5) * s.zm;
   const R m2 = R (-0.5) * s.xm + R (0.5) * s.zm;
-  const R m3 = s.xm / R (6) - R (0.5) * s.zm;
+  const R m3 = s.xm * R (1.0 / 6.0) - R (0.5) * s.zm;
   const R m4x2 = s.ym - s.zm;          // 2 m4
   const R m5x2 = s.zm;                 // 2 m5
 

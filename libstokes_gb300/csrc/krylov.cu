@@ -414,13 +414,15 @@ inline int grid_of (long long n) { return (int) ((n + KT - 1) / KT); }
 // device workspace of the solver (one per host thread)
 struct Krylov {
   DevBuf V, w, t, part, h, h2, s2, cv, b, x, arn, xin;
+  DevBuf rr, dd, t2;           // refinement: FP64 residual, correction, product
   double *pin = nullptr;     // pinned host staging: residual history, scalars
   size_t pin_cap = 0;
   cudaStream_t own = nullptr;  // stream for foreign operators
   int coop_blocks = 0;         // co-resident blocks of k_arnoldi on this device
   ~Krylov ()
   {
-    for (DevBuf *d : {&V, &w, &t, &part, &h, &h2, &s2, &cv, &b, &x, &arn, &xin}) d->release ();
+    for (DevBuf *d : {&V, &w, &t, &part, &h, &h2, &s2, &cv, &b, &x, &arn, &xin, &rr, &dd, &t2})
+      d->release ();
     if (pin) cudaFreeHost (pin);
     if (own) cudaStreamDestroy (own);
   }
@@ -659,8 +661,79 @@ settings_of (const struct iter *it)
   return s;
 }
 
+// Mixed-precision solve with FP64 iterative refinement: the residual
+// r = b - A64 x always comes from the FP64 product, and each correction d
+// solves A_mixed d = r by GMRES on the mixed product to a relative accuracy
+// eps |b| / |r| (not below 1e-5: the mixed product carries about 3e-7, so
+// GMRES stalls near 1e-6); x += d in FP64.  A correction reduces the error by
+// about cond(A) times the mixed product's error, so eps = 1e-10 takes two to
+// four FP64 products.  Convergence: |b - A64 x| <= eps |b|.  *iters counts
+// every operator application (mixed and FP64).
+int
+refine_dev (int n, const double *d_b, double *d_x, const Apply &A, const Apply &A64, int m,
+            int maxit, double eps, cudaStream_t st, int *iters, double *res, FILE *dbg)
+{
+  Krylov &K = t_kry;
+  cudaError_t e;
+  if ((e = K.rr.ensure (sizeof (double) * n)) != cudaSuccess
+      || (e = K.dd.ensure (sizeof (double) * n)) != cudaSuccess
+      || (e = K.t2.ensure (sizeof (double) * n)) != cudaSuccess
+      || (e = K.part.ensure (sizeof (double) * (size_t) ((n + MDOT_CHUNK - 1) / MDOT_CHUNK)))
+           != cudaSuccess
+      || (e = K.s2.ensure (sizeof (double) * 2)) != cudaSuccess
+      || (e = K.pinned (4)) != cudaSuccess)
+    return cuda_fail (e, "refinement workspace");
+  double *r = (double *) K.rr.p, *d = (double *) K.dd.p, *t = (double *) K.t2.p;
+  Gmres Gm {K, n, 1, st, (n + MDOT_CHUNK - 1) / MDOT_CHUNK};
+  const int gn = grid_of (n);
+  int rc;
+  double bn2;
+  if ((rc = Gm.norm2_host (d_b, &bn2))) return rc;
+  const double bnrm = sqrt (bn2);
+  if (!(bnrm > 0.0))
+    {
+      cudaMemsetAsync (d_x, 0, sizeof (double) * n, st);
+      *iters = 0;
+      *res = 0.0;
+      e = cudaStreamSynchronize (st);
+      return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "refinement");
+    }
+  int total = 0;
+  double rel = HUGE_VAL;
+  for (int outer = 0; outer < 16; outer++)
+    {
+      // r = b - A64 x
+      if ((rc = A64 (d_x, t))) return rc;
+      total++;
+      k_vaxpby<<<gn, KT, 0, st>>> (n, 1.0, d_b, -1.0, t, r);
+      double r2;
+      if ((rc = Gm.norm2_host (r, &r2))) return rc;
+      const double rel_new = sqrt (r2) / bnrm;
+      if (dbg) fprintf (dbg, "refinement: %d applications, FP64 residual %.6e\n", total, rel_new);
+      // stop when converged, out of applications, or no longer improving
+      if (rel_new <= eps || total >= maxit || !(rel_new < 0.5 * rel))
+        {
+          rel = std::min (rel, rel_new);
+          break;
+        }
+      rel = rel_new;
+      const double ein = std::max (eps / rel, 1e-5);
+      cudaMemsetAsync (d, 0, sizeof (double) * n, st);
+      int it = 0;
+      double ir = 0.0;
+      if ((rc = gmres_dev (n, r, d, A, m, maxit - total, ein, st, &it, &ir, dbg))) return rc;
+      total += it + 1;       // its iterations and its start residual
+      k_vaxpby<<<gn, KT, 0, st>>> (n, 1.0, d_x, 1.0, d, d_x);
+    }
+  *iters = total;
+  *res = rel;
+  e = cudaGetLastError ();
+  return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "refinement kernels");
+}
+
 // solve with the system's own operator: op 0 A = M, op 1 the FTS mobility
-// operator.  x: start vector in, solution out (host)
+// operator.  x: start vector in, solution out (host).  Mixed precision:
+// GMRES on the mixed product inside FP64 iterative refinement (refine_dev).
 int
 solve_own (struct stokes *sys, int op, bool force_open, const double *b, double *x,
            const Settings &S, int *iters, double *res)
@@ -668,7 +741,9 @@ solve_own (struct stokes *sys, int op, bool force_open, const double *b, double 
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
   c->force_open = force_open;
-  int rc = prepare (c, sys, false);
+  const bool refine = c->precision == STOKES_GPU_MIXED;
+  // the FP64 tables as well when the FP64 product computes the residuals
+  int rc = prepare (c, sys, false, refine ? 1 : -1);
   if (rc)
     {
       c->force_open = false;
@@ -704,8 +779,34 @@ solve_own (struct stokes *sys, int op, bool force_open, const double *b, double 
     A = [&] (const double *in, double *out) -> int {
       return atimes_dev (c, d_pos, in, out, st, false);
     };
-  rc = gmres_dev (n, (const double *) K.b.p, (double *) K.x.p, A, S.m, S.max, S.eps, st, iters,
-                  res, S.dbg);
+  if (refine)
+    {
+      double *tmp64 = nullptr;
+      if ((e = K.h2.ensure (sizeof (double) * n)) != cudaSuccess)
+        {
+          c->force_open = false;
+          return cuda_fail (e, "solve buffers");
+        }
+      tmp64 = (double *) K.h2.p;
+      Apply A64;
+      if (op == STOKES_GPU_SOLVE_MOB_FTS)
+        A64 = [&] (const double *in, double *out) -> int {
+          k_fts_mask<<<grid_of (n), KT, 0, st>>> (np, in, tmp64);
+          int r = atimes_fp64_dev (c, d_pos, tmp64, out, st, false);
+          if (r) return r;
+          k_fts_mob_out<<<grid_of (n), KT, 0, st>>> (np, in, out, out);
+          return STOKES_GPU_OK;
+        };
+      else
+        A64 = [&] (const double *in, double *out) -> int {
+          return atimes_fp64_dev (c, d_pos, in, out, st, false);
+        };
+      rc = refine_dev (n, (const double *) K.b.p, (double *) K.x.p, A, A64, S.m, S.max, S.eps,
+                       st, iters, res, S.dbg);
+    }
+  else
+    rc = gmres_dev (n, (const double *) K.b.p, (double *) K.x.p, A, S.m, S.max, S.eps, st,
+                    iters, res, S.dbg);
   if (!rc)
     {
       e = cudaMemcpyAsync (x, K.x.p, sizeof (double) * n, cudaMemcpyDeviceToHost, st);

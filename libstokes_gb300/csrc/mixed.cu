@@ -248,10 +248,12 @@ struct RealMixArgs {
   const uint4 *sq;       // particles in cell order: (q_x, q_y, q_z, particle index)
   const int *cstart;     // [ncell + 1] first slot of each cell in sq
   int nc[3];             // cells per axis (cell side >= rc / 2)
-  // rmin clamp: the clamped pairs take the clamp's change at the struct's
-  // own split xi_ref (clampfix = 1), see mix_term
+  // rmin clamp (rm2 = (2 rmin)^2): with clampfix the clamped pairs are left
+  // to mk_clamp, which evaluates them at the struct's own split xi_ref
   int clampfix;
+  float rm2;
   float xi_ref, xisp_ref;
+  float *out_clamp;      // [np][c]: mk_clamp's sums (a third combine chunk)
 };
 
 // minimum-image displacement r_j - r_i from fixed-point positions
@@ -279,39 +281,25 @@ min_image (const RealMixArgs &a, uint4 qi, uint4 qj, float &dx, float &dy, float
   dz = (float) (int32_t) uz * a.scale[2];
 }
 
-// The rmin clamp of libstokes (src/ewald.c:693-699: r raised to (a_i + a_j)
-// rmin, e = d / r with the raised r) changes the real-space term of a
-// clamped pair only; unclamped, the sum does not depend on the split.  At
-// the mixed split a clamped pair therefore contributes
-//   T(d/rm; s_ref(rm)) + T(d/r; s_xi(r) - s_ref(r))
-// (the clamped term of the struct's split, plus the change of the unclamped
-// term between the splits, which split_diff gives without cancellation).
-template <int V>
-__device__ __noinline__ void
-clamp_term (const RealMixArgs &a, float4 d, float r, float rm, const GenF<V, float> &g,
-            GenU<V, float> &t)
-{
-  PairScalars<float> sc, ds;
-  real_scalars_mono<V, float> (a.xi_ref, a.xisp_ref, rm, sc);
-  split_diff<V, float> (a.xi_ref, a.xi, r, ds);
-  const float ec[3] = {d.x / rm, d.y / rm, d.z / rm};
-  const float e0[3] = {d.x / r, d.y / r, d.z / r};
-  t.zero ();
-  pair_apply<V, float> (ec, sc, g, t);
-  pair_apply<V, float> (e0, ds, g, t);
-}
-
-// one pair term (source j at displacement d from the target) into t
+// one pair term (source j at displacement d from the target) into t; pairs
+// under the rmin clamp arrive here only when the clamp is applied in place
+// (clampfix = 0); otherwise mk_clamp takes them
 template <int V>
 __device__ __forceinline__ void
 mix_term (const RealMixArgs &a, float4 d, GenU<V, float> &t)
 {
   const int j = __float_as_int (d.w);
   const float rr = d.x * d.x + d.y * d.y + d.z * d.z;
-  float r = sqrtf (rr);
+  // 1 / r from the reciprocal square root with one Newton step (1 ulp)
+  float ri = rsqrtf (rr);
+  ri = ri * fmaf (-0.5f * rr, ri * ri, 1.5f);
+  float r = rr * ri;
   const float rm = 2.0f * a.rmin;          // (a_i + a_j) rmin for unit spheres
-  const bool fix = r < rm && a.clampfix;
-  if (r < rm && !a.clampfix) r = rm;
+  if (r < rm)
+    {
+      r = rm;
+      ri = 1.0f / rm;
+    }
   constexpr int C = NComp<V>::value, CP = cpad (C);
   // x_j as float4 loads of the padded copy
   float xj[CP];
@@ -324,15 +312,9 @@ mix_term (const RealMixArgs &a, float4 d, GenU<V, float> &t)
     }
   GenF<V, float> g;
   load_genf<V, float> (xj, g);
-  if (fix)
-    {
-      clamp_term<V> (a, d, r, rm, g, t);
-      return;
-    }
-  const float ri = 1.0f / r;
   const float e[3] = {d.x * ri, d.y * ri, d.z * ri};
   PairScalars<float> s;
-  real_scalars_mono<V, float> (a.xi, a.xisp, r, s);
+  real_scalars_mono_ri<V, float> (a.xi, a.xisp, r, ri, s);
   t.zero ();
   pair_apply<V, float> (e, s, g, t);
 }
@@ -377,7 +359,7 @@ constexpr int RG_QCAP = 192;     // queue entries per warp (the reduction reuses
 // lane sums with TwoSum), then the G warps of the target; the result is
 // written as the FP32 pair hi + lo, which the combine adds in FP64.
 template <int V>
-__global__ void __launch_bounds__ (RG_WARPS * 32)
+__global__ void __launch_bounds__ (RG_WARPS * 32, 3)
 mk_real (RealMixArgs a)
 {
   constexpr int C = NComp<V>::value;
@@ -435,7 +417,7 @@ mk_real (RealMixArgs a)
                 dy = d0y + T.y;
                 dz = d0z + T.z;
                 const float rr = dx * dx + dy * dy + dz * dz;
-                ok = (rr > 0.f) && (rr < a.rc2);
+                ok = (rr > 0.f) && (rr < a.rc2) && !(a.clampfix && rr < a.rm2);
               }
             const unsigned b = __ballot_sync (0xffffffffu, ok);
             if (ok) q[qn + __popc (b & lt)] = make_float4 (dx, dy, dz, __int_as_float (j));
@@ -542,6 +524,67 @@ mk_real (RealMixArgs a)
       const float lo = E0 - (hi - S0);
       a.out[(size_t) i * C + lane] = hi;
       a.out[((size_t) a.np + i) * C + lane] = lo;
+    }
+}
+
+// The rmin clamp of libstokes (src/ewald.c:693-699: r raised to (a_i + a_j)
+// rmin = rm, e = d / r with the raised r) changes the real-space term of a
+// clamped pair only; unclamped, the sum does not depend on the split.  At
+// the mixed split a clamped pair therefore contributes
+//   T(d/rm; s_ref(rm)) + T(d/r; s_xi(r) - s_ref(r)):
+// the clamped term of the struct's split xi_ref, plus the change of the
+// unclamped term between the splits, which split_diff gives without
+// cancellation however close the pair.  mk_real skips these pairs; one warp
+// per target here tests the candidates (minimum image and the split's
+// lattice offsets) and sums the few clamped terms.
+template <int V>
+__global__ void __launch_bounds__ (256)
+mk_clamp (RealMixArgs a)
+{
+  constexpr int C = NComp<V>::value, CP = cpad (C);
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (i >= a.np) return;
+  const uint4 qi = reinterpret_cast<const uint4 *> (a.qpos)[i];
+  float acc[C];
+#pragma unroll
+  for (int q = 0; q < C; q++) acc[q] = 0.f;
+  const float rm = sqrtf (a.rm2);
+  for (int j = lane; j < a.np; j += 32)
+    {
+      const uint4 qj = reinterpret_cast<const uint4 *> (a.qpos)[j];
+      float d0x, d0y, d0z;
+      min_image (a, qi, qj, d0x, d0y, d0z);
+      for (int m = 0; m < a.nimg; m++)
+        {
+          const float4 T = a.img[m];
+          const float dx = d0x + T.x, dy = d0y + T.y, dz = d0z + T.z;
+          const float rr = dx * dx + dy * dy + dz * dz;
+          if (!(rr > 0.f && rr < a.rm2)) continue;
+          const float r = sqrtf (rr);
+          float xj[CP];
+#pragma unroll
+          for (int k = 0; k < C; k++) xj[k] = a.xf[(size_t) CP * j + k];
+          GenF<V, float> g;
+          load_genf<V, float> (xj, g);
+          PairScalars<float> sc, ds;
+          real_scalars_mono<V, float> (a.xi_ref, a.xisp_ref, rm, sc);
+          split_diff<V, float> (a.xi_ref, a.xi, r, ds);
+          const float ec[3] = {dx / rm, dy / rm, dz / rm};
+          const float e0[3] = {dx / r, dy / r, dz / r};
+          GenU<V, float> t;
+          t.zero ();
+          pair_apply<V, float> (ec, sc, g, t);
+          pair_apply<V, float> (e0, ds, g, t);
+#pragma unroll
+          for (int q = 0; q < C; q++) acc[q] += t.v[q];
+        }
+    }
+#pragma unroll
+  for (int q = 0; q < C; q++)
+    {
+      const float v = warp_sum (acc[q]);
+      if (lane == 0) a.out_clamp[(size_t) i * C + q] = v;
     }
 }
 
@@ -1195,12 +1238,15 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   if (rc) return rc;
   const int np = c->np, C = NCOMP (c->version);
   const int ntab = (m->M[0] + 1) + (m->M[1] + 1) + (m->M[2] + 1);
-  // the real-space sum: G warps per target, the smallest power of two that
-  // gives about 16 warps per SM; its hi + lo output is two combine chunks
-  m->nchunk_r = 2;
+  // the real-space sum: G warps per target; its hi + lo output is two
+  // combine chunks.  Fine work units balance best over the SMs (a wave
+  // model with dynamic CTA scheduling, 3 CTAs of 8 warps per SM: at N = 1000
+  // and 4096 the finest split needs the fewest rounds of 32-term batches),
+  // while every warp pays one reduction: 8 warps per target up to 2048
+  // particles, 4 above
+  m->nchunk_r = sys->rmin > 0.0 ? 3 : 2;       // + the clamp kernel's sums
   {
-    int g = 1;
-    while (g < 8 && (long long) np * g < 152 * 16) g *= 2;
+    int g = np <= 2048 ? 8 : 4;
     const int ge = (int) env_double ("LIBSTOKES_GB300_REAL_G", 0.0);
     if (ge == 1 || ge == 2 || ge == 4 || ge == 8) g = ge;
     m->real_g = g;
@@ -1397,6 +1443,8 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     ra.xisp = (float) (m->xi / sqrt (M_PI));
     ra.rad = nullptr; ra.slipa = nullptr;
     ra.clampfix = sys->rmin > 0.0 ? 1 : 0;
+    ra.rm2 = (float) (4.0 * sys->rmin * sys->rmin);
+    ra.out_clamp = (float *) m->part_real.p + (size_t) 2 * np * C;
     ra.xi_ref = (float) sys->xi;
     ra.xisp_ref = (float) (sys->xi / sqrt (M_PI));
     ra.out = (float *) m->part_real.p;
@@ -1425,6 +1473,13 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       if (c->version == 0) mk_real<0><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
       else if (c->version == 1) mk_real<1><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
       else mk_real<2><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
+      if (ra.clampfix)
+        {
+          const int gc = (np + 7) / 8;
+          if (c->version == 0) mk_clamp<0><<<gc, 256, 0, rs>>> (ra);
+          else if (c->version == 1) mk_clamp<1><<<gc, 256, 0, rs>>> (ra);
+          else mk_clamp<2><<<gc, 256, 0, rs>>> (ra);
+        }
     };
     if (overlap)
       {
@@ -1501,7 +1556,8 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   };
   int rs = run_mixed_sequence (c, m, d_pos, d_x, d_y, st, E, sequence);
   if (rs) return rs;
-  c->launches = (m->nkh == 0 ? 3 : (m->tensor ? 6 : 5)) + (m->nc[0] ? 1 : 0);
+  c->launches = (m->nkh == 0 ? 3 : (m->tensor ? 6 : 5)) + (m->nc[0] ? 1 : 0)
+                + (sys->rmin > 0.0 ? 1 : 0);
   c->timed = timed;
   return STOKES_GPU_OK;
 }
