@@ -549,7 +549,8 @@ k_kop (KGemm g, const MixK *kt, int nk, const float *sf)
 // ---------------------------------------------------------------------------
 template <int V>
 __global__ void __launch_bounds__ (NT, 1)
-k_bp_gemm (const __grid_constant__ CUtensorMap tmB, KGemm g, float *ypart, int *status)
+k_bp_gemm (const __grid_constant__ CUtensorMap tmB, KGemm g, float *ypart, BpFinal fin,
+           int *status)
 {
   constexpr int C = NComp<V>::value;
   extern __shared__ unsigned char dsm[];
@@ -622,6 +623,52 @@ k_bp_gemm (const __grid_constant__ CUtensorMap tmB, KGemm g, float *ypart, int *
   umma::fence_before_sync ();
   __syncthreads ();
   if (warp == 0) umma::tmem_dealloc (tmem, TMEM_COLS);
+
+  // the last CTA of this particle tile adds up every partial of its
+  // particles (BpFinal); the others are done
+  __shared__ int s_last;
+  __threadfence ();                   // this CTA's partials, before its arrival
+  __syncthreads ();
+  if (tid == 0)
+    {
+      const unsigned total = gridDim.y * gridDim.z;
+      s_last = atomicAdd (fin.cnt + blockIdx.x, 1u) == total - 1u;
+    }
+  __syncthreads ();
+  if (!s_last) return;
+  __threadfence ();
+  const int nck = gridDim.y * gridDim.z;
+  const size_t n = (size_t) np * C;
+  for (int e = tid; e < TM * C; e += NT)
+    {
+      const int r = e / C, q = e - r * C, i = i0 + r;
+      if (i >= np) continue;
+      const size_t t = (size_t) i * C + q;
+      float sr = 0.f, cr = 0.f, sk = 0.f, ck = 0.f;
+      for (int k = 0; k < fin.ncr; k++)
+        {
+          const float v = __ldcg (fin.pr + (size_t) k * n + t) - cr;
+          const float u = sr + v;
+          cr = (u - sr) - v;
+          sr = u;
+        }
+      for (int k = 0; k < nck; k++)
+        {
+          const float v = __ldcg (ypart + (size_t) k * n + t) - ck;
+          const float u = sk + v;
+          ck = (u - sk) - v;
+          sk = u;
+        }
+      const double rs = ((double) sr - (double) cr) + 2.0 * ((double) sk - (double) ck);
+      // the self block is diagonal for F and T and couples the five
+      // stresslet components
+      const int q0 = (q < 6) ? q : 6, nq = (q < 6) ? 1 : 5;
+      const double *xi = fin.x + (size_t) C * i;
+      double self = 0.0;
+      for (int k = 0; k < nq; k++) self = fma (fin.S[q * C + q0 + k], xi[q0 + k], self);
+      fin.y[t] = self + rs;
+    }
+  if (tid == 0) fin.cnt[blockIdx.x] = 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -743,13 +790,13 @@ forward_v (const KGemm &g, const KMaps &mp, const MixK *kt, int nk, int *status,
 
 template <int V>
 static cudaError_t
-backward_v (const KGemm &g, const KMaps &mp, float *ypart, int *status, cudaStream_t st,
-            Ctx *prof)
+backward_v (const KGemm &g, const KMaps &mp, float *ypart, const BpFinal &fin, int *status,
+            cudaStream_t st, Ctx *prof)
 {
   cudaError_t e = gemm_attrs<V> ();
   if (e != cudaSuccess) return e;
   k_bp_gemm<V><<<dim3 (g.mtiles, g.ntile_b, g.ksplit), NT, SMEM_DYN, st>>> (mp.wb, g, ypart,
-                                                                            status);
+                                                                            fin, status);
   kmark (prof, st, "k_bp_gemm");
   return cudaGetLastError ();
 }
@@ -764,12 +811,12 @@ launch_kspace_forward (int version, const KGemm &g, const KMaps &maps, const Mix
 }
 
 cudaError_t
-launch_kspace_backward (int version, const KGemm &g, const KMaps &maps, float *ypart, int *status,
-                        cudaStream_t st, Ctx *prof)
+launch_kspace_backward (int version, const KGemm &g, const KMaps &maps, float *ypart,
+                        const BpFinal &fin, int *status, cudaStream_t st, Ctx *prof)
 {
-  if (version == 0) return backward_v<0> (g, maps, ypart, status, st, prof);
-  if (version == 1) return backward_v<1> (g, maps, ypart, status, st, prof);
-  return backward_v<2> (g, maps, ypart, status, st, prof);
+  if (version == 0) return backward_v<0> (g, maps, ypart, fin, status, st, prof);
+  if (version == 1) return backward_v<1> (g, maps, ypart, fin, status, st, prof);
+  return backward_v<2> (g, maps, ypart, fin, status, st, prof);
 }
 
 }  // namespace lsg

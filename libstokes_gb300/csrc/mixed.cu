@@ -73,6 +73,8 @@ struct MixedState {
   int real_g = 1;               // warps per target of mk_real
   int nc[3] = {0, 0, 0};        // cell list of mk_real (nc[0] == 0: no cells)
   DevBuf sq, cstart;
+  DevBuf bpcnt;                 // arrival counters of the backward GEMM's final sum
+  int bpcnt_n = 0;
 };
 
 constexpr int MX_WARPS = 8;      // warps per CTA in the mixed kernels
@@ -281,9 +283,9 @@ min_image (const RealMixArgs &a, uint4 qi, uint4 qj, float &dx, float &dy, float
   dz = (float) (int32_t) uz * a.scale[2];
 }
 
-// one pair term (source j at displacement d from the target) into t; pairs
-// under the rmin clamp arrive here only when the clamp is applied in place
-// (clampfix = 0); otherwise mk_clamp takes them
+// one pair term (source j at displacement d from the target) added to t;
+// pairs under the rmin clamp arrive here only when the clamp is applied in
+// place (clampfix = 0); otherwise mk_clamp takes them
 template <int V>
 __device__ __forceinline__ void
 mix_term (const RealMixArgs &a, float4 d, GenU<V, float> &t)
@@ -315,24 +317,7 @@ mix_term (const RealMixArgs &a, float4 d, GenU<V, float> &t)
   const float e[3] = {d.x * ri, d.y * ri, d.z * ri};
   PairScalars<float> s;
   real_scalars_mono_ri<V, float> (a.xi, a.xisp, r, ri, s);
-  t.zero ();
   pair_apply<V, float> (e, s, g, t);
-}
-
-// Kahan (compensated) addition of a term t into the running sum (s, c):
-// s + c carries the exact sum of the terms up to one FP32 rounding of c
-template <int V>
-__device__ __forceinline__ void
-kahan_add (GenU<V, float> &s, GenU<V, float> &c, const GenU<V, float> &t)
-{
-#pragma unroll
-  for (int q = 0; q < NComp<V>::value; q++)
-    {
-      const float y = t.v[q] + c.v[q];
-      const float u = s.v[q] + y;
-      c.v[q] = y - (u - s.v[q]);
-      s.v[q] = u;
-    }
 }
 
 // error-free sum of two values: a + b = s + e exactly
@@ -346,6 +331,9 @@ two_sum (float a, float b, float &s, float &e)
 
 constexpr int RG_WARPS = 8;      // warps per CTA of mk_real
 constexpr int RG_QCAP = 192;     // queue entries per warp (the reduction reuses them)
+constexpr int RG_MAXIMG = 4;     // lattice offsets tested per candidate in one pass
+// a pass adds at most 32 RG_MAXIMG entries to at most 31 left over
+static_assert (31 + 32 * RG_MAXIMG <= RG_QCAP, "mk_real queue too small");
 
 // The real-space sum of the mixed split: G warps per target particle.  Each
 // warp takes a share of the candidate sources (a slice of all particles, or
@@ -354,9 +342,12 @@ constexpr int RG_QCAP = 192;     // queue entries per warp (the reduction reuses
 // split's lattice offsets) and queues the accepted pairs (displacement and
 // source index, one float4 each) in shared memory; every 32 queued pairs the
 // lanes evaluate one term each, so the FP32 pipe only sees accepted terms.
-// Each lane keeps a Kahan-compensated sum per component; the 32 lanes meet
-// in shared memory (two lanes per component, each adding 16 compensated
-// lane sums with TwoSum), then the G warps of the target; the result is
+// With lattice offsets (cutoff beyond half the box) each lane tests all
+// offsets of its source into a bit mask and one warp prefix sum places the
+// accepted ones.  Each lane sums its terms per component (a few tens at
+// most); the per-particle sum over lanes and warps is compensated: the 32
+// lane sums meet in shared memory with TwoSum (two lanes per component,
+// 16 lane sums each), then the G warps of the target, and the result is
 // written as the FP32 pair hi + lo, which the combine adds in FP64.
 template <int V>
 __global__ void __launch_bounds__ (RG_WARPS * 32, 3)
@@ -386,9 +377,8 @@ mk_real (RealMixArgs a)
           i = slot;
         }
     }
-  GenU<V, float> sum, cmp, t;
+  GenU<V, float> sum;
   sum.zero ();
-  cmp.zero ();
   float4 *q = s_q[wib];
   int qn = 0;
   const unsigned lt = (1u << lane) - 1u;
@@ -406,30 +396,62 @@ mk_real (RealMixArgs a)
             j = cells ? (int) qj.w : sj;
             min_image (a, qi, qj, d0x, d0y, d0z);
           }
-        for (int m = 0; m < a.nimg; m++)
+        if (a.nimg == 1)
           {
-            const float4 T = a.img[m];
-            float dx = 0.f, dy = 0.f, dz = 0.f;
-            bool ok = false;
-            if (sj < s1)
-              {
-                dx = d0x + T.x;
-                dy = d0y + T.y;
-                dz = d0z + T.z;
-                const float rr = dx * dx + dy * dy + dz * dz;
-                ok = (rr > 0.f) && (rr < a.rc2) && !(a.clampfix && rr < a.rm2);
-              }
+            // minimum image only: one ballot places the accepted pairs
+            const float rr = d0x * d0x + d0y * d0y + d0z * d0z;
+            const bool ok = sj < s1 && rr > 0.f && rr < a.rc2 && !(a.clampfix && rr < a.rm2);
             const unsigned b = __ballot_sync (0xffffffffu, ok);
-            if (ok) q[qn + __popc (b & lt)] = make_float4 (dx, dy, dz, __int_as_float (j));
+            if (ok) q[qn + __popc (b & lt)] = make_float4 (d0x, d0y, d0z, __int_as_float (j));
             qn += __popc (b);
+          }
+        else
+          for (int m0 = 0; m0 < a.nimg; m0 += RG_MAXIMG)
+            {
+              // this lane's accepted offsets m0 .. m0 + 3 as a bit mask, then
+              // a warp prefix sum of the counts places them
+              unsigned mask = 0u;
+              if (sj < s1)
+#pragma unroll
+                for (int k = 0; k < RG_MAXIMG; k++)
+                  {
+                    if (m0 + k >= a.nimg) break;
+                    const float4 T = a.img[m0 + k];
+                    const float dx = d0x + T.x, dy = d0y + T.y, dz = d0z + T.z;
+                    const float rr = dx * dx + dy * dy + dz * dz;
+                    if (rr > 0.f && rr < a.rc2 && !(a.clampfix && rr < a.rm2)) mask |= 1u << k;
+                  }
+              const int cnt = __popc (mask);
+              int pre = cnt;
+#pragma unroll
+              for (int o = 1; o < 32; o <<= 1)
+                {
+                  const int v = __shfl_up_sync (0xffffffffu, pre, o);
+                  if (lane >= o) pre += v;
+                }
+              int slot = qn + pre - cnt;
+              while (mask)
+                {
+                  const int k = __ffs (mask) - 1;
+                  mask &= mask - 1u;
+                  const float4 T = a.img[m0 + k];
+                  q[slot++] = make_float4 (d0x + T.x, d0y + T.y, d0z + T.z, __int_as_float (j));
+                }
+              qn += __shfl_sync (0xffffffffu, pre, 31);
+              __syncwarp ();
+              while (qn >= 32)
+                {
+                  mix_term<V> (a, q[qn - 32 + lane], sum);
+                  qn -= 32;
+                  __syncwarp ();
+                }
+            }
+        __syncwarp ();
+        if (qn >= 32)
+          {
+            mix_term<V> (a, q[qn - 32 + lane], sum);
+            qn -= 32;
             __syncwarp ();
-            if (qn >= 32)
-              {
-                mix_term<V> (a, q[qn - 32 + lane], t);
-                kahan_add<V> (sum, cmp, t);
-                qn -= 32;
-                __syncwarp ();
-              }
           }
       }
   };
@@ -467,11 +489,7 @@ mk_real (RealMixArgs a)
                 }
             }
         }
-      if (lane < qn)
-        {
-          mix_term<V> (a, q[lane], t);
-          kahan_add<V> (sum, cmp, t);
-        }
+      if (lane < qn) mix_term<V> (a, q[lane], sum);
     }
   // the 32 lane sums of this warp: (s, c) rows of 2C + 1 floats in the
   // (now empty) queue; lane q + 11 h adds lanes 16 h .. 16 h + 15 of
@@ -484,7 +502,7 @@ mk_real (RealMixArgs a)
   for (int k = 0; k < C; k++)
     {
       w[lane * RW + k] = sum.v[k];
-      w[lane * RW + C + k] = cmp.v[k];
+      w[lane * RW + C + k] = 0.f;
     }
   __syncwarp ();
   float S = 0.f, E = 0.f;
@@ -1169,7 +1187,7 @@ run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_
   const void *ptrs[] = {d_pos, d_x, d_y, m->kt.p, m->qpos.p, m->tab.p, m->xf.p, m->pq.p,
                         m->part_real.p, m->part_rec.p, m->selfbuf.p, m->status.p, m->sf.p,
                         m->rowm.p, m->rot.p, m->img_zf.p, m->img_wb.p, m->h_status, m->tyz.p,
-                        m->img.p, m->sq.p, m->cstart.p};
+                        m->img.p, m->sq.p, m->cstart.p, m->bpcnt.p};
   for (const void *p : ptrs) mix ((uint64_t) (uintptr_t) p);
   mix ((uint64_t) (uintptr_t) E);
   // a captured cudaEventRecord is only a dependency, not a record: around a
@@ -1239,14 +1257,13 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   const int np = c->np, C = NCOMP (c->version);
   const int ntab = (m->M[0] + 1) + (m->M[1] + 1) + (m->M[2] + 1);
   // the real-space sum: G warps per target; its hi + lo output is two
-  // combine chunks.  Fine work units balance best over the SMs (a wave
-  // model with dynamic CTA scheduling, 3 CTAs of 8 warps per SM: at N = 1000
-  // and 4096 the finest split needs the fewest rounds of 32-term batches),
-  // while every warp pays one reduction: 8 warps per target up to 2048
-  // particles, 4 above
+  // combine chunks.  Measured on one GB300 (FTS, phi 0.3, G = 1, 2, 4, 8):
+  // best G 8 at N = 1000, 4 at 4096, 2 at 16384, 1 at 32768 -- about 8K to
+  // 32K warps in all, enough to balance the SMs without many per-warp
+  // reductions
   m->nchunk_r = sys->rmin > 0.0 ? 3 : 2;       // + the clamp kernel's sums
   {
-    int g = np <= 2048 ? 8 : 4;
+    int g = np <= 1024 ? 8 : (np <= 4096 ? 4 : (np <= 16384 ? 2 : 1));
     const int ge = (int) env_double ("LIBSTOKES_GB300_REAL_G", 0.0);
     if (ge == 1 || ge == 2 || ge == 4 || ge == 8) g = ge;
     m->real_g = g;
@@ -1328,6 +1345,15 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       if ((e = m->sf.ensure (sizeof (float) * kgemm_sf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "structure factors");
       if ((e = m->img_zf.ensure (sizeof (float) * kgemm_zf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image ZF");
       if ((e = m->img_wb.ensure (sizeof (float) * kgemm_wb_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image WB");
+      if (m->bpcnt_n < m->plan.mtiles || !m->bpcnt.p)
+        {
+          if ((e = m->bpcnt.ensure (sizeof (unsigned) * m->plan.mtiles)) != cudaSuccess)
+            return cuda_fail (e, "GEMM counters");
+          if ((e = cudaMemsetAsync (m->bpcnt.p, 0, sizeof (unsigned) * m->plan.mtiles, st))
+              != cudaSuccess)
+            return cuda_fail (e, "GEMM counters");
+          m->bpcnt_n = m->plan.mtiles;
+        }
       m->plan.ZF = (float *) m->img_zf.p;
       m->plan.WB = (float *) m->img_wb.p;
       m->plan.sf = (float *) m->sf.p;
@@ -1510,6 +1536,13 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     cb.c = C;
     cb.y = d_y;
     const bool fused = m->nkh > 0 && m->tensor;
+    BpFinal fin;
+    fin.x = d_x;
+    fin.pr = (const float *) m->part_real.p;
+    fin.ncr = m->nchunk_r;
+    fin.S = (const double *) m->selfbuf.p;
+    fin.y = d_y;
+    fin.cnt = (unsigned *) m->bpcnt.p;
     // reciprocal space up to the k operators (tensor cores) or the SIMT sums;
     // then the real-space partials, the back-projection and the final sum
     if (fused)
@@ -1543,10 +1576,14 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     if (E) cudaEventRecord (E[2], st);
     if (fused
         && (e = launch_kspace_backward (c->version, m->plan, m->maps, (float *) m->part_rec.p,
-                                        (int *) m->status.p, st, c)) != cudaSuccess)
+                                        fin, (int *) m->status.p, st, c)) != cudaSuccess)
       return cuda_fail (e, "reciprocal space (tensor cores)");
-    mk_combine<<<(int) (((long long) np * C * CMB_LANES + 255) / 256), 256, 0, st>>> (cb);
-    kmark (c, st, "mk_combine");
+    // the tensor-core back-projection does the final sum itself
+    if (!fused)
+      {
+        mk_combine<<<(int) (((long long) np * C * CMB_LANES + 255) / 256), 256, 0, st>>> (cb);
+        kmark (c, st, "mk_combine");
+      }
     if (E) cudaEventRecord (E[3], st);
     if (m->tensor)
       cudaMemcpyAsync (m->h_status, m->status.p, sizeof (int), cudaMemcpyDeviceToHost, st);
@@ -1556,7 +1593,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   };
   int rs = run_mixed_sequence (c, m, d_pos, d_x, d_y, st, E, sequence);
   if (rs) return rs;
-  c->launches = (m->nkh == 0 ? 3 : (m->tensor ? 6 : 5)) + (m->nc[0] ? 1 : 0)
+  c->launches = (m->nkh == 0 ? 3 : 5) + (m->nc[0] ? 1 : 0)
                 + (sys->rmin > 0.0 ? 1 : 0);
   c->timed = timed;
   return STOKES_GPU_OK;
@@ -1580,7 +1617,7 @@ release_mixed (Ctx *c)
   MixedState *m = c->mixed;
   for (DevBuf *b : {&m->kt, &m->qpos, &m->tab, &m->xf, &m->pq, &m->part_real, &m->part_rec,
                     &m->selfbuf, &m->status, &m->sf, &m->rowm, &m->rot, &m->img_zf,
-                    &m->img_wb, &m->tyz, &m->img, &m->sq, &m->cstart})
+                    &m->img_wb, &m->tyz, &m->img, &m->sq, &m->cstart, &m->bpcnt})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
   if (m->gexec) cudaGraphExecDestroy (m->gexec);
