@@ -454,14 +454,17 @@ k_sfac_gemm (const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CU
 // per-k operators: W_k = P_k + i Q_k from the summed structure factors,
 // written into the image WB (each (row, m1) belongs to at most one k)
 // ---------------------------------------------------------------------------
-constexpr int KOP_K = 64;    // k vectors per CTA
-constexpr int KOP_G = 4;     // particle-slice groups per k
+constexpr int KOP_K = 32;    // k vectors per CTA
+constexpr int KOP_G = 8;     // particle-slice groups per k (one slice each up to 8 slices)
+static_assert (KOP_G == 8, "k_kop's image writes assume eight groups");
 
-// CTA of KOP_K x KOP_G threads: thread (kk, sg) sums the slices sg, sg + 4,
-// ... of the forward partials of k = blockIdx.x * KOP_K + kk (the loads of
-// neighbouring k are neighbouring rows, so they coalesce); the four sums meet
-// in shared memory; group 0 forms P_k and group 1 Q_k; then the four groups
-// write the (re | im row) x (hi | lo plane) entries of the image.
+// CTA of KOP_K x KOP_G threads: thread (kk, sg) sums the slices sg, sg + 8,
+// ... of the forward partials of k = blockIdx.x * KOP_K + kk (one slice per
+// thread up to eight slices, so its loads are all independent; loads of
+// neighbouring k are neighbouring rows, so they coalesce); the eight sums
+// meet in shared memory; group 0 forms P_k and group 1 Q_k; then the groups
+// write the (re | im row) x (hi | lo plane) entries of the image, each pair
+// of groups half of the components.
 template <int V>
 __global__ void __launch_bounds__ (KOP_K * KOP_G)
 k_kop (KGemm g, const MixK *kt, int nk, const float *sf)
@@ -503,9 +506,15 @@ k_kop (KGemm g, const MixK *kt, int nk, const float *sf)
 #pragma unroll
       for (int q = 0; q < C; q++)
         {
-          cs[q] = (s_v[0][2 * q][kk] + s_v[1][2 * q][kk]) + (s_v[2][2 * q][kk] + s_v[3][2 * q][kk]);
-          sn[q] = (s_v[0][2 * q + 1][kk] + s_v[1][2 * q + 1][kk])
-                  + (s_v[2][2 * q + 1][kk] + s_v[3][2 * q + 1][kk]);
+          float a = 0.f, b = 0.f;
+#pragma unroll
+          for (int h = 0; h < KOP_G; h++)
+            {
+              a += s_v[h][2 * q][kk];
+              b += s_v[h][2 * q + 1][kk];
+            }
+          cs[q] = a;
+          sn[q] = b;
         }
       const float e[3] = {K.ex, K.ey, K.ez};
       GenF<V, float> ga, gb;
@@ -530,12 +539,16 @@ k_kop (KGemm g, const MixK *kt, int nk, const float *sf)
     for (int q = 0; q < C; q++) s_v[sg][q][kk] = P.v[q];
   __syncthreads ();
   if (k >= nk) return;
-  // group sg: image row (m1, re) for sg even, (m1, im) for odd; plane sg / 2
-  const int part = sg & 1, plane = sg >> 1;
+  // group sg: image row (m1, re) for sg even, (m1, im) for odd; plane
+  // (sg / 2) % 2; groups 0-3 write the components q < C / 2, groups 4-7 the
+  // others
+  const int part = sg & 1, plane = (sg >> 1) & 1;
+  const int qa = (sg < 4) ? 0 : C / 2, qb = (sg < 4) ? C / 2 : C;
   float *img = g.WB + (size_t) plane * g.pWB;
 #pragma unroll
   for (int q = 0; q < C; q++)
     {
+      if (q < qa || q >= qb) continue;
       const float U = s_v[0][q][kk], Vv = s_v[1][q][kk];
       float2 hi, lo;
       split2 (part ? make_float2 (Vv, -U) : make_float2 (U, Vv), hi, lo);
@@ -639,27 +652,61 @@ k_bp_gemm (const __grid_constant__ CUtensorMap tmB, KGemm g, float *ypart, BpFin
   __threadfence ();
   const int nck = gridDim.y * gridDim.z;
   const size_t n = (size_t) np * C;
-  for (int e = tid; e < TM * C; e += NT)
+  // each thread owns EPT elements e = tid + NT u; the partials of all of
+  // them are loaded in batches of KB chunks before they are summed, so the
+  // L2 latency is paid once per batch, not once per load
+  constexpr int EPT = (TM * C + NT - 1) / NT, KB = 8;
+  size_t tt[EPT];
+  bool ok[EPT];
+#pragma unroll
+  for (int u = 0; u < EPT; u++)
     {
-      const int r = e / C, q = e - r * C, i = i0 + r;
-      if (i >= np) continue;
-      const size_t t = (size_t) i * C + q;
-      float sr = 0.f, cr = 0.f, sk = 0.f, ck = 0.f;
-      for (int k = 0; k < fin.ncr; k++)
-        {
-          const float v = __ldcg (fin.pr + (size_t) k * n + t) - cr;
-          const float u = sr + v;
-          cr = (u - sr) - v;
-          sr = u;
-        }
-      for (int k = 0; k < nck; k++)
-        {
-          const float v = __ldcg (ypart + (size_t) k * n + t) - ck;
-          const float u = sk + v;
-          ck = (u - sk) - v;
-          sk = u;
-        }
-      const double rs = ((double) sr - (double) cr) + 2.0 * ((double) sk - (double) ck);
+      const int e = tid + NT * u, r = e / C, i = i0 + r;
+      ok[u] = e < TM * C && i < np;
+      tt[u] = ok[u] ? (size_t) i * C + (e - r * C) : 0;
+    }
+  float sr[EPT], cr[EPT], sk[EPT], ck[EPT];
+#pragma unroll
+  for (int u = 0; u < EPT; u++) sr[u] = cr[u] = sk[u] = ck[u] = 0.f;
+  auto kahan = [] (float &s, float &c, float x) {
+    const float v = x - c;
+    const float w = s + v;
+    c = (w - s) - v;
+    s = w;
+  };
+  for (int k0 = 0; k0 < fin.ncr; k0 += KB)
+    {
+      float v[EPT][KB];
+#pragma unroll
+      for (int u = 0; u < EPT; u++)
+#pragma unroll
+        for (int b = 0; b < KB; b++)
+          v[u][b] = (ok[u] && k0 + b < fin.ncr) ? __ldcg (fin.pr + (size_t) (k0 + b) * n + tt[u]) : 0.f;
+#pragma unroll
+      for (int u = 0; u < EPT; u++)
+#pragma unroll
+        for (int b = 0; b < KB; b++) kahan (sr[u], cr[u], v[u][b]);
+    }
+  for (int k0 = 0; k0 < nck; k0 += KB)
+    {
+      float v[EPT][KB];
+#pragma unroll
+      for (int u = 0; u < EPT; u++)
+#pragma unroll
+        for (int b = 0; b < KB; b++)
+          v[u][b] = (ok[u] && k0 + b < nck) ? __ldcg (ypart + (size_t) (k0 + b) * n + tt[u]) : 0.f;
+#pragma unroll
+      for (int u = 0; u < EPT; u++)
+#pragma unroll
+        for (int b = 0; b < KB; b++) kahan (sk[u], ck[u], v[u][b]);
+    }
+#pragma unroll
+  for (int u = 0; u < EPT; u++)
+    {
+      if (!ok[u]) continue;
+      const size_t t = tt[u];
+      const int i = (int) (t / C), q = (int) (t - (size_t) i * C);
+      const double rs = ((double) sr[u] - (double) cr[u]) + 2.0 * ((double) sk[u] - (double) ck[u]);
       // the self block is diagonal for F and T and couples the five
       // stresslet components
       const int q0 = (q < 6) ? q : 6, nq = (q < 6) ? 1 : 5;

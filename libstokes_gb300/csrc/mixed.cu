@@ -106,7 +106,7 @@ struct PrepArgs {
 };
 
 constexpr int PREP_P = 32;       // particles per mk_prep CTA
-constexpr int PREP_ROWS = 16;    // table rows per mk_prep CTA
+constexpr int PREP_ROWS = 4;     // table rows per mk_prep CTA (one entry per thread)
 constexpr int PREP_CMAX = 11;    // components per particle at most
 
 // floor(v) mod 2^32 for |v| < 2^62: the 32-bit fixed-point coordinate, the
@@ -122,12 +122,13 @@ fixq (double v)
 // u_d is the particle's fractional coordinate on axis d as a 32-bit fixed
 // point q_d, so m u_d mod 1 is the exact integer product m q_d mod 2^32; on
 // a sheared lattice the flow-axis phase coordinate is u_x - (shift/lx) u_g.
-// With a ZF image (the tensor-core path) the threads of the flow-axis rows
-// m1 also write Z = t0[m1] x_q as TF32 hi/lo pairs in the forward GEMM's
-// sign pattern: image row (m1, re, q) = (Re Z, -Im Z), (m1, im, q) =
+// With a ZF image (the tensor-core path) the CTA also writes, for its
+// flow-axis rows m1, Z = t0[m1] x_q as TF32 hi/lo pairs in the forward
+// GEMM's sign pattern: image row (m1, re, q) = (Re Z, -Im Z), (m1, im, q) =
 // (Im Z, Re Z) at column pair j.
-// CTA (blockIdx.x, blockIdx.y): PREP_P particles x about PREP_ROWS table
-// rows; the few FP64 operations per particle are repeated by each row group.
+// CTA (blockIdx.x, blockIdx.y): PREP_P particles x PREP_ROWS table rows, one
+// entry per thread; the few FP64 operations per particle are repeated by
+// each row group.
 __global__ void __launch_bounds__ (128)
 mk_prep (PrepArgs a)
 {
@@ -174,40 +175,55 @@ mk_prep (PrepArgs a)
       s_q[0][t] = qu; s_q[1][t] = q1; s_q[2][t] = q2;
     }
   __syncthreads ();
-  // row group y takes rows y, y + G, y + 2 G, ... (G = gridDim.y), so the
-  // flow-axis rows, which also write ZF, spread over the groups
-  const int G = gridDim.y, nr = (a.ntab - (int) blockIdx.y + G - 1) / G;
-  for (int e = t; e < nr * PREP_P; e += blockDim.x)
-    {
-      const int row = blockIdx.y + (e / PREP_P) * G, jl = e % PREP_P, j = jb + jl;
-      if (j >= a.np) continue;
-      const int d = row < a.m0end ? 0 : (row < a.m1end ? 1 : 2);
-      const uint32_t m = (uint32_t) (row - (d == 0 ? 0 : (d == 1 ? a.m0end : a.m1end)));
-      const float2 ph = phase_of (a.rot, m * s_q[d][jl]);
-      a.tab[(size_t) row * a.np + j] = ph;
-      if (d != 0 && a.tyz)
-        {
-          float2 *t = a.tyz + (size_t) j * a.wyz + (d == 1 ? a.M1 : 2 * a.M1 + 1 + a.M2);
-          t[(int) m] = ph;
-          t[-(int) m] = make_float2 (ph.x, -ph.y);
-        }
-      if (d == 0 && a.zf)
-        for (int q = 0; q < a.c; q++)
+  // row group y takes rows y, y + G, y + 2 G, y + 3 G (G = gridDim.y), so the
+  // flow-axis rows, which also write ZF, spread over the groups; thread
+  // (rr, jl) computes entry (row rr of the group, particle jl)
+  __shared__ float2 s_ph[PREP_ROWS][PREP_P];
+  const int G = gridDim.y;
+  {
+    const int rr = t / PREP_P, jl = t % PREP_P, j = jb + jl;
+    const int row = (int) blockIdx.y + rr * G;
+    if (row < a.ntab && j < a.np)
+      {
+        const int d = row < a.m0end ? 0 : (row < a.m1end ? 1 : 2);
+        const uint32_t m = (uint32_t) (row - (d == 0 ? 0 : (d == 1 ? a.m0end : a.m1end)));
+        const float2 ph = phase_of (a.rot, m * s_q[d][jl]);
+        a.tab[(size_t) row * a.np + j] = ph;
+        if (d != 0 && a.tyz)
           {
-            const float xq = s_x[jl * a.c + q];
-            const float u = ph.x * xq, v = ph.y * xq;
-            for (int part = 0; part < 2; part++)
-              {
-                const float p0 = part ? v : u, p1 = part ? u : -v;
-                uint32_t h0, l0, h1, l1;
-                umma::split_tf32 (p0, h0, l0);
-                umma::split_tf32 (p1, h1, l1);
-                float2 *o = reinterpret_cast<float2 *> (
-                              a.zf + (((size_t) m * 2 + part) * a.c + q) * a.kf) + j;
-                o[0] = make_float2 (__uint_as_float (h0), __uint_as_float (h1));
-                o[a.zplane / 2] = make_float2 (__uint_as_float (l0), __uint_as_float (l1));
-              }
+            float2 *ty = a.tyz + (size_t) j * a.wyz + (d == 1 ? a.M1 : 2 * a.M1 + 1 + a.M2);
+            ty[(int) m] = ph;
+            ty[-(int) m] = make_float2 (ph.x, -ph.y);
           }
+        s_ph[rr][jl] = ph;
+      }
+  }
+  if (!a.zf) return;
+  __syncthreads ();
+  // Z = t0[m1] x_q as TF32 hi / lo pairs for the flow-axis rows of this
+  // group, one (row, particle, component) entry per thread at a time
+  int nz = 0;                                  // flow-axis rows of the group
+  while (nz < PREP_ROWS && (int) blockIdx.y + nz * G < a.m0end) nz++;
+  for (int e = t; e < nz * PREP_P * a.c; e += blockDim.x)
+    {
+      const int rr = e / (PREP_P * a.c), rem = e - rr * PREP_P * a.c;
+      const int jl = rem / a.c, q = rem - jl * a.c, j = jb + jl;
+      if (j >= a.np) continue;
+      const int m = (int) blockIdx.y + rr * G;
+      const float2 ph = s_ph[rr][jl];
+      const float xq = s_x[jl * a.c + q];
+      const float u = ph.x * xq, v = ph.y * xq;
+      for (int part = 0; part < 2; part++)
+        {
+          const float p0 = part ? v : u, p1 = part ? u : -v;
+          uint32_t h0, l0, h1, l1;
+          umma::split_tf32 (p0, h0, l0);
+          umma::split_tf32 (p1, h1, l1);
+          float2 *o = reinterpret_cast<float2 *> (
+                        a.zf + (((size_t) m * 2 + part) * a.c + q) * a.kf) + j;
+          o[0] = make_float2 (__uint_as_float (h0), __uint_as_float (h1));
+          o[a.zplane / 2] = make_float2 (__uint_as_float (l0), __uint_as_float (l1));
+        }
     }
 }
 
@@ -345,10 +361,10 @@ static_assert (31 + 32 * RG_MAXIMG <= RG_QCAP, "mk_real queue too small");
 // With lattice offsets (cutoff beyond half the box) each lane tests all
 // offsets of its source into a bit mask and one warp prefix sum places the
 // accepted ones.  Each lane sums its terms per component (a few tens at
-// most); the per-particle sum over lanes and warps is compensated: the 32
-// lane sums meet in shared memory with TwoSum (two lanes per component,
-// 16 lane sums each), then the G warps of the target, and the result is
-// written as the FP32 pair hi + lo, which the combine adds in FP64.
+// most), the 32 lane sums meet in a shuffle tree (pairwise summation), the
+// G warps of the target meet with TwoSum (error-free, the rounding errors
+// carried along), and the result is written as the FP32 pair hi + lo,
+// which the combine adds in FP64.
 template <int V>
 __global__ void __launch_bounds__ (RG_WARPS * 32, 3)
 mk_real (RealMixArgs a)
@@ -491,41 +507,17 @@ mk_real (RealMixArgs a)
         }
       if (lane < qn) mix_term<V> (a, q[lane], sum);
     }
-  // the 32 lane sums of this warp: (s, c) rows of 2C + 1 floats in the
-  // (now empty) queue; lane q + 11 h adds lanes 16 h .. 16 h + 15 of
-  // component q
-  __syncwarp ();
-  constexpr int RW = 2 * C + 1;
-  static_assert (32 * RW * 4 <= RG_QCAP * 16, "reduction rows exceed the queue");
-  float *w = reinterpret_cast<float *> (q);
+  // the 32 lane sums of this warp by a shuffle tree (pairwise summation)
 #pragma unroll
   for (int k = 0; k < C; k++)
     {
-      w[lane * RW + k] = sum.v[k];
-      w[lane * RW + C + k] = 0.f;
+      const float v = warp_sum (sum.v[k]);
+      if (lane == 0)
+        {
+          s_red[wib][0][k] = v;
+          s_red[wib][1][k] = 0.f;
+        }
     }
-  __syncwarp ();
-  float S = 0.f, E = 0.f;
-  const int comp = lane % C, half = lane / C;
-  if (lane < 2 * C)
-    for (int l = 16 * half; l < 16 * half + 16; l++)
-      {
-        float s2, e2;
-        two_sum (S, w[l * RW + comp], s2, e2);
-        S = s2;
-        E += e2 + w[l * RW + C + comp];
-      }
-  {
-    const float So = __shfl_down_sync (0xffffffffu, S, C);
-    const float Eo = __shfl_down_sync (0xffffffffu, E, C);
-    if (lane < C)
-      {
-        float s2, e2;
-        two_sum (S, So, s2, e2);
-        s_red[wib][0][lane] = s2;
-        s_red[wib][1][lane] = E + Eo + e2;
-      }
-  }
   __syncthreads ();
   // the G warps of the target: part 0 adds them and writes hi, lo
   if (live && part == 0 && lane < C)
