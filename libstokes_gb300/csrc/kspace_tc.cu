@@ -562,8 +562,7 @@ k_kop (KGemm g, const MixK *kt, int nk, const float *sf)
 // ---------------------------------------------------------------------------
 template <int V>
 __global__ void __launch_bounds__ (NT, 1)
-k_bp_gemm (const __grid_constant__ CUtensorMap tmB, KGemm g, float *ypart, BpFinal fin,
-           int *status)
+k_bp_gemm (const __grid_constant__ CUtensorMap tmB, KGemm g, float *ypart, int *status)
 {
   constexpr int C = NComp<V>::value;
   extern __shared__ unsigned char dsm[];
@@ -636,86 +635,6 @@ k_bp_gemm (const __grid_constant__ CUtensorMap tmB, KGemm g, float *ypart, BpFin
   umma::fence_before_sync ();
   __syncthreads ();
   if (warp == 0) umma::tmem_dealloc (tmem, TMEM_COLS);
-
-  // the last CTA of this particle tile adds up every partial of its
-  // particles (BpFinal); the others are done
-  __shared__ int s_last;
-  __threadfence ();                   // this CTA's partials, before its arrival
-  __syncthreads ();
-  if (tid == 0)
-    {
-      const unsigned total = gridDim.y * gridDim.z;
-      s_last = atomicAdd (fin.cnt + blockIdx.x, 1u) == total - 1u;
-    }
-  __syncthreads ();
-  if (!s_last) return;
-  __threadfence ();
-  const int nck = gridDim.y * gridDim.z;
-  const size_t n = (size_t) np * C;
-  // each thread owns EPT elements e = tid + NT u; the partials of all of
-  // them are loaded in batches of KB chunks before they are summed, so the
-  // L2 latency is paid once per batch, not once per load
-  constexpr int EPT = (TM * C + NT - 1) / NT, KB = 8;
-  size_t tt[EPT];
-  bool ok[EPT];
-#pragma unroll
-  for (int u = 0; u < EPT; u++)
-    {
-      const int e = tid + NT * u, r = e / C, i = i0 + r;
-      ok[u] = e < TM * C && i < np;
-      tt[u] = ok[u] ? (size_t) i * C + (e - r * C) : 0;
-    }
-  float sr[EPT], cr[EPT], sk[EPT], ck[EPT];
-#pragma unroll
-  for (int u = 0; u < EPT; u++) sr[u] = cr[u] = sk[u] = ck[u] = 0.f;
-  auto kahan = [] (float &s, float &c, float x) {
-    const float v = x - c;
-    const float w = s + v;
-    c = (w - s) - v;
-    s = w;
-  };
-  for (int k0 = 0; k0 < fin.ncr; k0 += KB)
-    {
-      float v[EPT][KB];
-#pragma unroll
-      for (int u = 0; u < EPT; u++)
-#pragma unroll
-        for (int b = 0; b < KB; b++)
-          v[u][b] = (ok[u] && k0 + b < fin.ncr) ? __ldcg (fin.pr + (size_t) (k0 + b) * n + tt[u]) : 0.f;
-#pragma unroll
-      for (int u = 0; u < EPT; u++)
-#pragma unroll
-        for (int b = 0; b < KB; b++) kahan (sr[u], cr[u], v[u][b]);
-    }
-  for (int k0 = 0; k0 < nck; k0 += KB)
-    {
-      float v[EPT][KB];
-#pragma unroll
-      for (int u = 0; u < EPT; u++)
-#pragma unroll
-        for (int b = 0; b < KB; b++)
-          v[u][b] = (ok[u] && k0 + b < nck) ? __ldcg (ypart + (size_t) (k0 + b) * n + tt[u]) : 0.f;
-#pragma unroll
-      for (int u = 0; u < EPT; u++)
-#pragma unroll
-        for (int b = 0; b < KB; b++) kahan (sk[u], ck[u], v[u][b]);
-    }
-#pragma unroll
-  for (int u = 0; u < EPT; u++)
-    {
-      if (!ok[u]) continue;
-      const size_t t = tt[u];
-      const int i = (int) (t / C), q = (int) (t - (size_t) i * C);
-      const double rs = ((double) sr[u] - (double) cr[u]) + 2.0 * ((double) sk[u] - (double) ck[u]);
-      // the self block is diagonal for F and T and couples the five
-      // stresslet components
-      const int q0 = (q < 6) ? q : 6, nq = (q < 6) ? 1 : 5;
-      const double *xi = fin.x + (size_t) C * i;
-      double self = 0.0;
-      for (int k = 0; k < nq; k++) self = fma (fin.S[q * C + q0 + k], xi[q0 + k], self);
-      fin.y[t] = self + rs;
-    }
-  if (tid == 0) fin.cnt[blockIdx.x] = 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -837,13 +756,13 @@ forward_v (const KGemm &g, const KMaps &mp, const MixK *kt, int nk, int *status,
 
 template <int V>
 static cudaError_t
-backward_v (const KGemm &g, const KMaps &mp, float *ypart, const BpFinal &fin, int *status,
-            cudaStream_t st, Ctx *prof)
+backward_v (const KGemm &g, const KMaps &mp, float *ypart, int *status, cudaStream_t st,
+            Ctx *prof)
 {
   cudaError_t e = gemm_attrs<V> ();
   if (e != cudaSuccess) return e;
   k_bp_gemm<V><<<dim3 (g.mtiles, g.ntile_b, g.ksplit), NT, SMEM_DYN, st>>> (mp.wb, g, ypart,
-                                                                            fin, status);
+                                                                            status);
   kmark (prof, st, "k_bp_gemm");
   return cudaGetLastError ();
 }
@@ -858,12 +777,12 @@ launch_kspace_forward (int version, const KGemm &g, const KMaps &maps, const Mix
 }
 
 cudaError_t
-launch_kspace_backward (int version, const KGemm &g, const KMaps &maps, float *ypart,
-                        const BpFinal &fin, int *status, cudaStream_t st, Ctx *prof)
+launch_kspace_backward (int version, const KGemm &g, const KMaps &maps, float *ypart, int *status,
+                        cudaStream_t st, Ctx *prof)
 {
-  if (version == 0) return backward_v<0> (g, maps, ypart, fin, status, st, prof);
-  if (version == 1) return backward_v<1> (g, maps, ypart, fin, status, st, prof);
-  return backward_v<2> (g, maps, ypart, fin, status, st, prof);
+  if (version == 0) return backward_v<0> (g, maps, ypart, status, st, prof);
+  if (version == 1) return backward_v<1> (g, maps, ypart, status, st, prof);
+  return backward_v<2> (g, maps, ypart, status, st, prof);
 }
 
 }  // namespace lsg

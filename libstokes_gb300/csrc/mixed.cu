@@ -73,8 +73,6 @@ struct MixedState {
   int real_g = 1;               // warps per target of mk_real
   int nc[3] = {0, 0, 0};        // cell list of mk_real (nc[0] == 0: no cells)
   DevBuf sq, cstart;
-  DevBuf bpcnt;                 // arrival counters of the backward GEMM's final sum
-  int bpcnt_n = 0;
 };
 
 constexpr int MX_WARPS = 8;      // warps per CTA in the mixed kernels
@@ -201,13 +199,14 @@ mk_prep (PrepArgs a)
   if (!a.zf) return;
   __syncthreads ();
   // Z = t0[m1] x_q as TF32 hi / lo pairs for the flow-axis rows of this
-  // group, one (row, particle, component) entry per thread at a time
+  // group, one (row, component, particle) entry per thread at a time (the
+  // particle fastest: neighbouring threads store neighbouring columns)
   int nz = 0;                                  // flow-axis rows of the group
   while (nz < PREP_ROWS && (int) blockIdx.y + nz * G < a.m0end) nz++;
   for (int e = t; e < nz * PREP_P * a.c; e += blockDim.x)
     {
       const int rr = e / (PREP_P * a.c), rem = e - rr * PREP_P * a.c;
-      const int jl = rem / a.c, q = rem - jl * a.c, j = jb + jl;
+      const int q = rem / PREP_P, jl = rem - q * PREP_P, j = jb + jl;
       if (j >= a.np) continue;
       const int m = (int) blockIdx.y + rr * G;
       const float2 ph = s_ph[rr][jl];
@@ -1179,7 +1178,7 @@ run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_
   const void *ptrs[] = {d_pos, d_x, d_y, m->kt.p, m->qpos.p, m->tab.p, m->xf.p, m->pq.p,
                         m->part_real.p, m->part_rec.p, m->selfbuf.p, m->status.p, m->sf.p,
                         m->rowm.p, m->rot.p, m->img_zf.p, m->img_wb.p, m->h_status, m->tyz.p,
-                        m->img.p, m->sq.p, m->cstart.p, m->bpcnt.p};
+                        m->img.p, m->sq.p, m->cstart.p};
   for (const void *p : ptrs) mix ((uint64_t) (uintptr_t) p);
   mix ((uint64_t) (uintptr_t) E);
   // a captured cudaEventRecord is only a dependency, not a record: around a
@@ -1337,15 +1336,6 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       if ((e = m->sf.ensure (sizeof (float) * kgemm_sf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "structure factors");
       if ((e = m->img_zf.ensure (sizeof (float) * kgemm_zf_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image ZF");
       if ((e = m->img_wb.ensure (sizeof (float) * kgemm_wb_floats (m->plan))) != cudaSuccess) return cuda_fail (e, "image WB");
-      if (m->bpcnt_n < m->plan.mtiles || !m->bpcnt.p)
-        {
-          if ((e = m->bpcnt.ensure (sizeof (unsigned) * m->plan.mtiles)) != cudaSuccess)
-            return cuda_fail (e, "GEMM counters");
-          if ((e = cudaMemsetAsync (m->bpcnt.p, 0, sizeof (unsigned) * m->plan.mtiles, st))
-              != cudaSuccess)
-            return cuda_fail (e, "GEMM counters");
-          m->bpcnt_n = m->plan.mtiles;
-        }
       m->plan.ZF = (float *) m->img_zf.p;
       m->plan.WB = (float *) m->img_wb.p;
       m->plan.sf = (float *) m->sf.p;
@@ -1528,13 +1518,6 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     cb.c = C;
     cb.y = d_y;
     const bool fused = m->nkh > 0 && m->tensor;
-    BpFinal fin;
-    fin.x = d_x;
-    fin.pr = (const float *) m->part_real.p;
-    fin.ncr = m->nchunk_r;
-    fin.S = (const double *) m->selfbuf.p;
-    fin.y = d_y;
-    fin.cnt = (unsigned *) m->bpcnt.p;
     // reciprocal space up to the k operators (tensor cores) or the SIMT sums;
     // then the real-space partials, the back-projection and the final sum
     if (fused)
@@ -1568,14 +1551,10 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     if (E) cudaEventRecord (E[2], st);
     if (fused
         && (e = launch_kspace_backward (c->version, m->plan, m->maps, (float *) m->part_rec.p,
-                                        fin, (int *) m->status.p, st, c)) != cudaSuccess)
+                                        (int *) m->status.p, st, c)) != cudaSuccess)
       return cuda_fail (e, "reciprocal space (tensor cores)");
-    // the tensor-core back-projection does the final sum itself
-    if (!fused)
-      {
-        mk_combine<<<(int) (((long long) np * C * CMB_LANES + 255) / 256), 256, 0, st>>> (cb);
-        kmark (c, st, "mk_combine");
-      }
+    mk_combine<<<(int) (((long long) np * C * CMB_LANES + 255) / 256), 256, 0, st>>> (cb);
+    kmark (c, st, "mk_combine");
     if (E) cudaEventRecord (E[3], st);
     if (m->tensor)
       cudaMemcpyAsync (m->h_status, m->status.p, sizeof (int), cudaMemcpyDeviceToHost, st);
@@ -1585,7 +1564,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   };
   int rs = run_mixed_sequence (c, m, d_pos, d_x, d_y, st, E, sequence);
   if (rs) return rs;
-  c->launches = (m->nkh == 0 ? 3 : 5) + (m->nc[0] ? 1 : 0)
+  c->launches = (m->nkh == 0 ? 3 : (m->tensor ? 6 : 5)) + (m->nc[0] ? 1 : 0)
                 + (sys->rmin > 0.0 ? 1 : 0);
   c->timed = timed;
   return STOKES_GPU_OK;
@@ -1609,7 +1588,7 @@ release_mixed (Ctx *c)
   MixedState *m = c->mixed;
   for (DevBuf *b : {&m->kt, &m->qpos, &m->tab, &m->xf, &m->pq, &m->part_real, &m->part_rec,
                     &m->selfbuf, &m->status, &m->sf, &m->rowm, &m->rot, &m->img_zf,
-                    &m->img_wb, &m->tyz, &m->img, &m->sq, &m->cstart, &m->bpcnt})
+                    &m->img_wb, &m->tyz, &m->img, &m->sq, &m->cstart})
     b->release ();
   if (m->h_status) cudaFreeHost (m->h_status);
   if (m->gexec) cudaGraphExecDestroy (m->gexec);

@@ -139,28 +139,12 @@ size_t kgemm_ypart_floats (const KGemm &g);   // partial y, [ksplit][ntile_b][np
 int kgemm_ypart_chunks (const KGemm &g);       // ksplit * ntile_b
 int kgemm_maps (const KGemm &g, float *sf, KMaps *m);   // 0 on success
 
-// The final sum of a product, done by the backward GEMM itself: the last CTA
-// to finish a 128-particle tile (an arrival counter per tile, reset by that
-// CTA) adds, for the tile's particles, the real-space partials, twice the
-// reciprocal partials (half k space) and the FP64 self term:
-//   y = S x + sum_r pr + 2 sum_k ypart,
-// FP32 partials summed with Kahan compensation in a fixed order, the final
-// combination in FP64.
-struct BpFinal {
-  const double *x;        // input vector, FP64 [np c]
-  const float *pr;        // real-space partials [ncr][np][c]
-  int ncr;
-  const double *S;        // self block of equal spheres, c x c
-  double *y;              // output [np c]
-  unsigned *cnt;          // arrival counters [mtiles], zero between products
-};
-
 // forward GEMM -> per-k operators (image WB); then the backward GEMM into
-// ypart and the final sum.  The image ZF is written beforehand by mk_prep.
+// ypart.  The image ZF is written beforehand by mk_prep.
 struct Ctx;
 cudaError_t launch_kspace_forward (int version, const KGemm &g, const KMaps &maps, const MixK *kt,
                                    int nk, int *status, cudaStream_t st, Ctx *prof);
 cudaError_t launch_kspace_backward (int version, const KGemm &g, const KMaps &maps, float *ypart,
-                                    const BpFinal &fin, int *status, cudaStream_t st, Ctx *prof);
+                                    int *status, cudaStream_t st, Ctx *prof);
 
 }  // namespace lsg
