@@ -942,7 +942,13 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
   // against FP64 is 2.92e-7 at 1e-8, 2.99e-7 at 3e-8, 3.03e-7 at 1e-7 --
   // FP32 rounding, not truncation, sets it -- and the cutoffs shrink)
   const double eps = env_double ("LIBSTOKES_GB300_MIXED_EPS", 3e-8);
-  bool images = env_double ("LIBSTOKES_GB300_MIXED_IMAGES", sys->version == 2 ? 1.0 : 0.0) != 0.0;
+  // FTS takes lattice images in real space except between 512 and 2048
+  // particles, where the minimum-image split is faster (measured, one GB300,
+  // phi 0.3: N = 1000 74-86 us per product against 86-90 us with images,
+  // the real-space sum 18-23 us against 33-39 us; N = 256 and 4096 faster
+  // with images: 53 against 61 us, 295 against 406 us)
+  const bool fts_images = sys->version == 2 && !(sys->np > 512 && sys->np < 2048);
+  bool images = env_double ("LIBSTOKES_GB300_MIXED_IMAGES", fts_images ? 1.0 : 0.0) != 0.0;
   double eta = env_double ("LIBSTOKES_GB300_MIXED_ETA",
                            images ? default_eta_images (sys->np) : default_eta (sys->np));
   const uint64_t fp = mix_fingerprint (sys, eta + (images ? 1000.0 : 0.0), eps);
@@ -1249,12 +1255,12 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
   const int ntab = (m->M[0] + 1) + (m->M[1] + 1) + (m->M[2] + 1);
   // the real-space sum: G warps per target; its hi + lo output is two
   // combine chunks.  Measured on one GB300 (FTS, phi 0.3, G = 1, 2, 4, 8):
-  // best G 8 at N = 1000, 4 at 4096, 2 at 16384, 1 at 32768 -- about 8K to
-  // 32K warps in all, enough to balance the SMs without many per-warp
-  // reductions
+  // best G 4 at N = 1000 (minimum-image split) and 4096, 2 at 16384, 1 at
+  // 32768 -- about 4K to 32K warps in all, enough to balance the SMs
+  // without many per-warp reductions
   m->nchunk_r = sys->rmin > 0.0 ? 3 : 2;       // + the clamp kernel's sums
   {
-    int g = np <= 1024 ? 8 : (np <= 4096 ? 4 : (np <= 16384 ? 2 : 1));
+    int g = np <= 512 ? 8 : (np <= 4096 ? 4 : (np <= 16384 ? 2 : 1));
     const int ge = (int) env_double ("LIBSTOKES_GB300_REAL_G", 0.0);
     if (ge == 1 || ge == 2 || ge == 4 || ge == 8) g = ge;
     m->real_g = g;
