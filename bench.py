@@ -534,9 +534,29 @@ def adjoint_measure(lib, abi, L):
     t0 = time.perf_counter()
     vjp()
     adj = time.perf_counter() - t0
+    dr64, db64 = dr.copy(), db.copy()
+    # mixed precision: the FP32 adjoint against the mixed forward product
+    s.set_precision(abi.MIXED)
+    for _ in range(3):
+        s.atimes(f)
+        vjp()
+    fw, aw = [], []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        s.atimes(f)
+        fw.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        vjp()
+        aw.append(time.perf_counter() - t0)
+    fwd_m, adj_m = float(np.median(fw)), float(np.median(aw))
+    err_r = float(np.linalg.norm(dr - dr64) / np.linalg.norm(dr64))
+    err_b = float(np.abs(db - db64).max() / np.abs(db64).max())
     s.close()
     return {"workload": w["name"], "precision": "fp64", "forward_s": fwd, "vjp_s": adj,
             "vjp_over_forward": adj / fwd, "outputs": "dL/dr (6144) and dL/dl (3)",
+            "mixed": {"forward_s": fwd_m, "vjp_s": adj_m, "vjp_over_forward": adj_m / fwd_m,
+                      "rel_err_dLdr_vs_fp64": err_r, "rel_err_dLdbox_vs_fp64": err_b,
+                      "timing": "median of 5 calls each, host buffers"},
             "timing": "wall clock around one call each, host buffers"}
 
 

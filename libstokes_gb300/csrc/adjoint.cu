@@ -530,6 +530,32 @@ stokes_gpu_vjp (struct stokes *sys, const double *g, const double *f, double *dL
     return set_error (STOKES_GPU_EINVAL, "box derivatives are defined without shear");
   struct stokes *const usr = sys;
   {
+    // mixed precision: the FP32 adjoint (adjoint_f32.cu) unless the system
+    // needs the FP64 one (shear, or no minimum-image split)
+    Ctx *cu = get_ctx (usr, true);
+    if (!cu) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+    if (cu->precision == STOKES_GPU_MIXED)
+      {
+        const int done = vjp_mixed (cu, usr, g, f, dLdr, dLdbox);
+        if (done < 0) return -done;
+        if (done == 1)
+          {
+            if (Lval)
+              {
+                // L = g . M f with the mixed product
+                const size_t n = (size_t) NCOMP (usr->version) * usr->np;
+                std::vector<double> y (n);
+                const int rc = stokes_gpu_atimes (usr, f, y.data ());
+                if (rc) return rc;
+                double v = 0.0;
+                for (size_t q = 0; q < n; q++) v += g[q] * y[q];
+                *Lval = v;
+              }
+            return STOKES_GPU_OK;
+          }
+      }
+  }
+  {
     const char *ev = getenv ("LIBSTOKES_GB300_VJP_ETA");
     const double eta = ev ? atof (ev) : 9.0;
     if (eta > 0.0) sys = adj_shadow (sys, eta);

@@ -139,6 +139,7 @@ free_ctx (Ctx *c)
   if (c->hpos) cudaFreeHost (c->hpos);
   cudaStreamDestroy (c->stream);
   release_mixed (c);
+  release_vjp_mixed (c);
   if (c->tuned) stokes_free (c->tuned);
   delete c;
 }

@@ -124,6 +124,11 @@ int atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_
 int atimes_open_f32_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                          cudaStream_t st, bool timed);
 void release_mixed (Ctx *c);
+// mixed-precision VJP (adjoint_f32.cu): 1 when it served the call, 0 when
+// the system needs the FP64 adjoint, -status on error
+int vjp_mixed (Ctx *c, const struct stokes *sys, const double *g, const double *f, double *dLdr,
+               double *dLdbox);
+void release_vjp_mixed (const Ctx *c);
 // after the stream of a mixed product was synchronised: STOKES_GPU_ETIMEOUT
 // (and the status word cleared) when a bounded wait of its tensor-core
 // kernels ran out, else STOKES_GPU_OK

@@ -123,3 +123,59 @@ def test_gradient_descent_fits_velocity_field(lib):
         step *= 2.0
     assert losses[-1] < 0.9 * losses[0], losses
     s.close()
+
+
+def _mixed_vjp_ran(lib, s):
+    from libstokes_gb300 import abi
+    return any(k.startswith("kva_") for k in abi.kernel_profile(lib, s.sp))
+
+
+@pytest.mark.parametrize("version,n,phi", [(0, 150, 0.08), (1, 150, 0.08)])
+def test_mixed_vjp_matches_oracle(lib, version, n, phi):
+    """The mixed-precision VJP (FP32 terms, its own split) against the CPU
+    oracle's FP64 gradient at libstokes' split: 1e-6 relative L2 on dL/dr,
+    1e-6 of the largest on dL/dbox."""
+    from libstokes_gb300 import MIXED, System
+    from libstokes_gb300.workloads import rsa_positions
+    from oracle.oracle import Oracle
+    import os
+    pos, L = rsa_positions(n, phi, seed=31 + version)
+    c = (3, 6)[version]
+    rng = np.random.default_rng(40 + version)
+    g = rng.standard_normal(c * n)
+    f = rng.standard_normal(c * n)
+    s = System(version, pos, (L, L, L))
+    s.set_precision(MIXED)
+    lib.stokes_gpu_kprof_begin(s.sp, 16)
+    Lg, dr, db = _vjp(lib, s, g, f)
+    assert _mixed_vjp_ran(lib, s)
+    o = Oracle(version, pos, (L, L, L))
+    o.set_split(o.xi_by_tratio(1.0), 1e-12)
+    o.set_threads(os.cpu_count() or 1)
+    Lo, dro, dbo = o.vjp(pos, g, f)
+    assert abs(Lg - Lo) < 1e-6 * abs(Lo)
+    assert rel_l2(dr, dro) < 1e-6, rel_l2(dr, dro)
+    assert np.abs(db - dbo).max() < 1e-6 * np.abs(dbo).max(), (db, dbo)
+    s.close()
+
+
+def test_mixed_vjp_ft_n2048_against_fp64(lib):
+    """FT, N = 2048, phi 0.25 (the differentiated workload): the mixed VJP
+    against the FP64 VJP at 1e-6 (dL/dr relative L2, dL/dbox of the largest)."""
+    from libstokes_gb300 import FP64, MIXED, System
+    from libstokes_gb300.workloads import rsa_positions
+    pos, L = rsa_positions(2048, 0.25, seed=42)
+    rng = np.random.default_rng(1)
+    g = rng.standard_normal(6 * 2048)
+    f = rng.standard_normal(6 * 2048)
+    s = System(1, pos, (L, L, L))
+    L64, dr64, db64 = _vjp(lib, s, g, f)
+    s.set_precision(MIXED)
+    lib.stokes_gpu_kprof_begin(s.sp, 16)
+    Lm, drm, dbm = _vjp(lib, s, g, f)
+    assert _mixed_vjp_ran(lib, s)
+    assert abs(Lm - L64) < 1e-6 * abs(L64)
+    assert rel_l2(drm, dr64) < 1e-6, rel_l2(drm, dr64)
+    assert np.abs(dbm - db64).max() < 1e-6 * np.abs(db64).max(), (dbm, db64)
+    s.set_precision(FP64)
+    s.close()
