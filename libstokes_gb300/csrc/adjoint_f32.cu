@@ -39,6 +39,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -137,7 +138,8 @@ struct VjpArgs {
   float L[3];
   float xi, xisp, rc2, rmin;
   uint4 *q;                 // [np] fixed-point x, y, z
-  float *gf;                // [np][2][VJ_CP]: g then f
+  float *gf;                // [np][2][VJ_CP]: g then f (per-pair gathers)
+  float *gcm;               // [2][c][np]: g then f, component-major (coalesced sums)
   float3 *p32;              // [np] FP32 positions as given (box derivative)
   float2 *tab;              // [(M0+1) + (M1+1) + (M2+1)][np]
   int M0, M1, M2;
@@ -150,6 +152,8 @@ struct VjpArgs {
   int nchunk;
   float *grad;              // [kchunks][np][3]
   int kchunks;
+  double *dldr;             // [np][3] the gradient (FP64)
+  double *blk;              // [blocks of kva_final][6]: box sums, phase sums
 };
 
 __device__ __forceinline__ uint32_t
@@ -171,8 +175,11 @@ kva_prep (VjpArgs a)
   a.p32[j] = make_float3 ((float) x, (float) y, (float) z);
   for (int c = 0; c < C; c++)
     {
-      a.gf[(size_t) j * 2 * VJ_CP + c] = (float) a.g[(size_t) C * j + c];
-      a.gf[(size_t) j * 2 * VJ_CP + VJ_CP + c] = (float) a.f[(size_t) C * j + c];
+      const float gv = (float) a.g[(size_t) C * j + c], fv = (float) a.f[(size_t) C * j + c];
+      a.gf[(size_t) j * 2 * VJ_CP + c] = gv;
+      a.gf[(size_t) j * 2 * VJ_CP + VJ_CP + c] = fv;
+      a.gcm[(size_t) c * a.np + j] = gv;
+      a.gcm[(size_t) (C + c) * a.np + j] = fv;
     }
   // phase tables, m >= 0 per axis
   const int Md[3] = {a.M0, a.M1, a.M2};
@@ -211,11 +218,10 @@ kva_sfac (VjpArgs a)
   for (int j = lane; j < a.np; j += 32)
     {
       const float2 ph = kphase (a, K, j);
-      const float *gj = a.gf + (size_t) j * 2 * VJ_CP;
 #pragma unroll
       for (int q = 0; q < C; q++)
         {
-          const float gv = gj[q], fv = gj[VJ_CP + q];
+          const float gv = a.gcm[(size_t) q * a.np + j], fv = a.gcm[(size_t) (C + q) * a.np + j];
           cf[q] = fmaf (ph.x, fv, cf[q]);
           sf[q] = fmaf (ph.y, fv, sf[q]);
           cg[q] = fmaf (ph.x, gv, cg[q]);
@@ -337,6 +343,7 @@ kva_bp (VjpArgs a)
         s_wu[e / (4 * C)][e % (4 * C)] = a.wu[(size_t) kb * 4 * C + e];
       for (int e = threadIdx.x; e < nt; e += BP_T) s_k[e] = a.kt[kb + e];
       __syncthreads ();
+#pragma unroll 4
       for (int t = 0; t < nt; t++)
         {
           const VjpK &K = s_k[t];
@@ -477,6 +484,50 @@ kva_real (VjpArgs a)
     }
 }
 
+// the gradient per particle in FP64 (real-space chunks, twice the half-space
+// reciprocal slices) and, per block, the sums of the real-space box terms
+// and of r_l,a dL_rec/dr_l,a (the phase scaling of the box derivative)
+constexpr int FIN_T = 256;
+
+__global__ void __launch_bounds__ (FIN_T)
+kva_final (VjpArgs a)
+{
+  __shared__ double s_b[6][FIN_T];
+  const int l = blockIdx.x * FIN_T + threadIdx.x;
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  if (l < a.np)
+    {
+      double gr[3] = {0, 0, 0}, rec[3] = {0, 0, 0};
+      for (int ch = 0; ch < a.nchunk; ch++)
+        {
+          const float *p = a.part + ((size_t) ch * a.np + l) * 6;
+          for (int k = 0; k < 3; k++)
+            {
+              gr[k] += p[k];
+              v[k] += p[3 + k];
+            }
+        }
+      if (a.nk > 0)
+        for (int kc = 0; kc < a.kchunks; kc++)
+          for (int k = 0; k < 3; k++) rec[k] += a.grad[((size_t) kc * a.np + l) * 3 + k];
+      for (int k = 0; k < 3; k++)
+        {
+          rec[k] *= 2.0;
+          a.dldr[3 * l + k] = -gr[k] + rec[k];
+          v[3 + k] = a.pos[3 * l + k] * rec[k];
+        }
+    }
+  for (int k = 0; k < 6; k++) s_b[k][threadIdx.x] = v[k];
+  __syncthreads ();
+  for (int h = FIN_T / 2; h > 0; h >>= 1)
+    {
+      if ((int) threadIdx.x < h)
+        for (int k = 0; k < 6; k++) s_b[k][threadIdx.x] += s_b[k][threadIdx.x + h];
+      __syncthreads ();
+    }
+  if (threadIdx.x < 6) a.blk[(size_t) blockIdx.x * 6 + threadIdx.x] = s_b[threadIdx.x][0];
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -486,7 +537,7 @@ struct VjpState {
   int M[3] = {0, 0, 0};
   int nk = 0;
   std::vector<VjpK> hk;
-  DevBuf q, gf, p32, tab, kt, wu, dbox, part, grad, rot, g, f, pos;
+  DevBuf q, gf, gcm, p32, tab, kt, wu, dbox, part, grad, rot, g, f, pos, dldr, blk;
 };
 
 std::mutex g_vjp_mu;
@@ -503,10 +554,18 @@ vjp_state (const Ctx *c)
   return s;
 }
 
+double
+vjp_eta ()
+{
+  const char *e = getenv ("LIBSTOKES_GB300_VJP_MIXED_ETA");   // read per call: sweeps
+  return e ? atof (e) : 10.0;
+}
+
 uint64_t
 vjp_key (const struct stokes *sys)
 {
-  const double v[5] = {sys->lx, sys->ly, sys->lz, (double) sys->np, (double) sys->version};
+  const double v[6] = {sys->lx, sys->ly, sys->lz, (double) sys->np, (double) sys->version,
+                       vjp_eta ()};
   uint64_t h = 1469598103934665603ull;
   const unsigned char *b = (const unsigned char *) v;
   for (size_t i = 0; i < sizeof v; i++) { h ^= b[i]; h *= 1099511628211ull; }
@@ -525,7 +584,7 @@ vjp_split (const struct stokes *sys, VjpState *s)
   const double lmax = std::max (sys->lx, std::max (sys->ly, sys->lz));
   const double lv = cbrt (sys->lx * sys->ly * sys->lz);
   // the smallest xi whose cutoff is below half the box, and at least
-  // eta = 10 (real and reciprocal work about equal at FT N = 2048)
+  // eta / V^(1/3)
   double xi = 6.0 / lv, rc = 0.0, kc = 0.0;
   for (int it = 0; it < 400; it++)
     {
@@ -534,9 +593,10 @@ vjp_split (const struct stokes *sys, VjpState *s)
       xi *= 1.02;
     }
   if (rc > 0.4999 * lmin || xi > 0.5) return false;
-  if (xi < 10.0 / lv && 10.0 / lv <= 0.5)
+  const double eta = vjp_eta ();
+  if (xi < eta / lv && eta / lv <= 0.5)
     {
-      xi = 10.0 / lv;
+      xi = eta / lv;
       lsg_ewald_cutoffs (xi, eps, lmin, lmax, &rc, &kc);
     }
   const double k0x = 2.0 * M_PI / sys->lx, k0y = 2.0 * M_PI / sys->ly, k0z = 2.0 * M_PI / sys->lz;
@@ -593,6 +653,9 @@ vjp_mixed_v (Ctx *c, const struct stokes *sys, VjpState *s, const double *g, con
   cudaError_t e = cudaSuccess;
   for (auto pr : {std::make_pair (&s->q, sizeof (uint4) * np),
                   std::make_pair (&s->gf, sizeof (float) * 2 * VJ_CP * np),
+                  std::make_pair (&s->gcm, sizeof (float) * 2 * C * np),
+                  std::make_pair (&s->dldr, sizeof (double) * 3 * np),
+                  std::make_pair (&s->blk, sizeof (double) * 6 * ((np + FIN_T - 1) / FIN_T)),
                   std::make_pair (&s->p32, sizeof (float3) * np),
                   std::make_pair (&s->tab, sizeof (float2) * (size_t) ntab * np),
                   std::make_pair (&s->kt, sizeof (VjpK) * std::max (nk, 1)),
@@ -648,6 +711,9 @@ vjp_mixed_v (Ctx *c, const struct stokes *sys, VjpState *s, const double *g, con
   a.rmin = (float) sys->rmin;
   a.q = (uint4 *) s->q.p;
   a.gf = (float *) s->gf.p;
+  a.gcm = (float *) s->gcm.p;
+  a.dldr = (double *) s->dldr.p;
+  a.blk = (double *) s->blk.p;
   a.p32 = (float3 *) s->p32.p;
   a.tab = (float2 *) s->tab.p;
   a.M0 = s->M[0]; a.M1 = s->M[1]; a.M2 = s->M[2];
@@ -673,43 +739,29 @@ vjp_mixed_v (Ctx *c, const struct stokes *sys, VjpState *s, const double *g, con
       kva_bp<V><<<dim3 ((np + BP_T - 1) / BP_T, kchunks), BP_T, 0, st>>> (a);
       kmark (c, st, "kva_bp");
     }
+  const int nblk = (np + FIN_T - 1) / FIN_T;
+  kva_final<<<nblk, FIN_T, 0, st>>> (a);
+  kmark (c, st, "kva_final");
   if ((e = cudaGetLastError ()) != cudaSuccess) return cuda_fail (e, "mixed VJP kernels");
-  std::vector<float> part ((size_t) nchunk * np * 6), grad ((size_t) kchunks * np * 3, 0.f),
-    db ((size_t) 3 * std::max (nk, 1), 0.f);
-  e = cudaMemcpyAsync (part.data (), s->part.p, sizeof (float) * part.size (),
-                       cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess && nk > 0)
-    e = cudaMemcpyAsync (grad.data (), s->grad.p, sizeof (float) * grad.size (),
+  std::vector<double> blk ((size_t) 6 * nblk);
+  std::vector<float> db ((size_t) 3 * std::max (nk, 1), 0.f);
+  e = cudaMemcpyAsync (dLdr, s->dldr.p, sizeof (double) * 3 * np, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync (blk.data (), s->blk.p, sizeof (double) * blk.size (),
                          cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && nk > 0 && dLdbox)
     e = cudaMemcpyAsync (db.data (), s->dbox.p, sizeof (float) * 3 * nk, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize (st);
   if (e != cudaSuccess) return cuda_fail (e, "mixed VJP results");
-  // FP64 sums on the host: dL/dr = - sum grad psi + 2 (half-space) reciprocal
-  double bx[3] = {0, 0, 0}, phase[3] = {0, 0, 0};
-  for (int l = 0; l < np; l++)
-    {
-      double gr[3] = {0, 0, 0}, rec[3] = {0, 0, 0};
-      for (int ch = 0; ch < nchunk; ch++)
-        {
-          const float *p = &part[((size_t) ch * np + l) * 6];
-          for (int k = 0; k < 3; k++)
-            {
-              gr[k] += p[k];
-              bx[k] += p[3 + k];
-            }
-        }
-      for (int kc = 0; kc < kchunks; kc++)
-        for (int k = 0; k < 3; k++) rec[k] += grad[((size_t) kc * np + l) * 3 + k];
-      for (int k = 0; k < 3; k++)
-        {
-          rec[k] *= 2.0;
-          dLdr[3 * l + k] = -gr[k] + rec[k];
-          phase[k] += sys->pos[3 * l + k] * rec[k];
-        }
-    }
   if (dLdbox)
     {
+      double bx[3] = {0, 0, 0}, phase[3] = {0, 0, 0};
+      for (int b = 0; b < nblk; b++)
+        for (int k = 0; k < 3; k++)
+          {
+            bx[k] += blk[(size_t) b * 6 + k];
+            phase[k] += blk[(size_t) b * 6 + 3 + k];
+          }
       const double L[3] = {sys->lx, sys->ly, sys->lz};
       for (int k = 0; k < 3; k++)
         {
@@ -718,7 +770,7 @@ vjp_mixed_v (Ctx *c, const struct stokes *sys, VjpState *s, const double *g, con
           dLdbox[k] = bx[k] + 2.0 * opd - phase[k] / L[k];
         }
     }
-  c->launches = 2 + (nk > 0 ? 2 : 0);
+  c->launches = 3 + (nk > 0 ? 2 : 0);
   return STOKES_GPU_OK;
 }
 
@@ -754,8 +806,8 @@ release_vjp_mixed (const Ctx *c)
         }
   }
   if (!s) return;
-  for (DevBuf *b : {&s->q, &s->gf, &s->p32, &s->tab, &s->kt, &s->wu, &s->dbox, &s->part,
-                    &s->grad, &s->rot, &s->g, &s->f, &s->pos})
+  for (DevBuf *b : {&s->q, &s->gf, &s->gcm, &s->p32, &s->tab, &s->kt, &s->wu, &s->dbox,
+                    &s->part, &s->grad, &s->rot, &s->g, &s->f, &s->pos, &s->dldr, &s->blk})
     b->release ();
   delete s;
 }
