@@ -200,43 +200,107 @@ kphase (const VjpArgs &a, const VjpK &K, int j)
                 tabm (t2, K.m3, a.np, j));
 }
 
+// e^{2 pi i p / 2^32} from the rotation table in shared memory (phase_of)
+__device__ __forceinline__ float2
+phase_s (const float4 *srot, uint32_t p)
+{
+  const uint32_t h = (p + (1u << 21)) >> 22;
+  const int32_t r = (int32_t) (p - (h << 22));
+  const float th = (float) r * 1.4629180792671596e-09f;
+  const float t2 = th * th;
+  const float sn = th * (1.0f - t2 * (1.0f / 6.0f));
+  const float dc = t2 * (0.5f - t2 * (1.0f / 24.0f));
+  const float4 e = srot[h & 1023u];
+  const float re = e.x + fmaf (-e.x, dc, fmaf (-e.y, sn, e.z));
+  const float im = e.y + fmaf (-e.y, dc, fmaf (e.x, sn, e.w));
+  return make_float2 (re, im);
+}
+
 // ---------------------------------------------------------------------------
-// reciprocal space: structure factors and operators, one warp per k
+// reciprocal space
 // ---------------------------------------------------------------------------
+constexpr int SF_T = 256;     // k vectors per CTA of kva_sfac (one per thread)
+constexpr int SF_P = 128;     // particles per slice
+
+// partial structure factors of one particle slice: thread = one k; the
+// slice's fixed-point positions and g, f sit in shared memory (read by every
+// thread alike), the phase e^{ik.r_j} is the exact fixed-point phase
+// m1 q_x + m2 q_y + m3 q_z mod 2^32 through the rotation table.
+// out: sfp[slice][4 c][nk] = (cos f, sin f, cos g, sin g) sums
 template <int V>
-__global__ void __launch_bounds__ (256)
-kva_sfac (VjpArgs a)
+__global__ void __launch_bounds__ (SF_T)
+kva_sfac (VjpArgs a, float *sfp)
 {
   constexpr int C = NComp<V>::value;
-  const int lane = threadIdx.x & 31;
-  const int k = blockIdx.x * 8 + (threadIdx.x >> 5);
+  __shared__ float4 s_rot[1024];
+  __shared__ uint4 s_q[SF_P];
+  __shared__ float s_x[SF_P][2 * C];
+  for (int e = threadIdx.x; e < 1024; e += SF_T) s_rot[e] = a.rot[e];
+  const int j0 = blockIdx.y * SF_P, nj = min (SF_P, a.np - j0);
+  for (int e = threadIdx.x; e < nj; e += SF_T) s_q[e] = a.q[j0 + e];
+  for (int e = threadIdx.x; e < nj * 2 * C; e += SF_T)
+    {
+      const int jl = e / (2 * C), c = e - jl * 2 * C;
+      s_x[jl][c] = a.gf[(size_t) (j0 + jl) * 2 * VJ_CP + (c < C ? c : VJ_CP + c - C)];
+    }
+  __syncthreads ();
+  const int k = blockIdx.x * SF_T + threadIdx.x;
   if (k >= a.nk) return;
   const VjpK K = a.kt[k];
+  const uint32_t m1 = (uint32_t) K.m1, m2 = (uint32_t) K.m2, m3 = (uint32_t) K.m3;
   float cf[C], sf[C], cg[C], sg[C];
 #pragma unroll
   for (int q = 0; q < C; q++) cf[q] = sf[q] = cg[q] = sg[q] = 0.f;
-  for (int j = lane; j < a.np; j += 32)
+  for (int jl = 0; jl < nj; jl++)
     {
-      const float2 ph = kphase (a, K, j);
+      const uint4 qj = s_q[jl];
+      const float2 ph = phase_s (s_rot, m1 * qj.x + m2 * qj.y + m3 * qj.z);
 #pragma unroll
       for (int q = 0; q < C; q++)
         {
-          const float gv = a.gcm[(size_t) q * a.np + j], fv = a.gcm[(size_t) (C + q) * a.np + j];
-          cf[q] = fmaf (ph.x, fv, cf[q]);
-          sf[q] = fmaf (ph.y, fv, sf[q]);
+          const float gv = s_x[jl][q], fv = s_x[jl][C + q];
           cg[q] = fmaf (ph.x, gv, cg[q]);
           sg[q] = fmaf (ph.y, gv, sg[q]);
+          cf[q] = fmaf (ph.x, fv, cf[q]);
+          sf[q] = fmaf (ph.y, fv, sf[q]);
         }
     }
+  float *o = sfp + (size_t) blockIdx.y * 4 * C * a.nk + k;
 #pragma unroll
   for (int q = 0; q < C; q++)
     {
-      cf[q] = warp_sum (cf[q]);
-      sf[q] = warp_sum (sf[q]);
-      cg[q] = warp_sum (cg[q]);
-      sg[q] = warp_sum (sg[q]);
+      o[(size_t) q * a.nk] = cf[q];
+      o[(size_t) (C + q) * a.nk] = sf[q];
+      o[(size_t) (2 * C + q) * a.nk] = cg[q];
+      o[(size_t) (3 * C + q) * a.nk] = sg[q];
     }
-  if (lane != 0) return;
+}
+
+// one thread per k: the slices' sums (fixed order), W = op S_f, U = op S_g,
+// and the op's box derivative Re conj(S_g) . (d op / d l_a) S_f
+template <int V>
+__global__ void __launch_bounds__ (128)
+kva_wu (VjpArgs a, const float *sfp, int nslices)
+{
+  constexpr int C = NComp<V>::value;
+  const int k = blockIdx.x * 128 + threadIdx.x;
+  if (k >= a.nk) return;
+  float cf[C], sf[C], cg[C], sg[C];
+#pragma unroll
+  for (int q = 0; q < C; q++) cf[q] = sf[q] = cg[q] = sg[q] = 0.f;
+  for (int sl = 0; sl < nslices; sl++)
+    {
+      const float *p = sfp + (size_t) sl * 4 * C * a.nk + k;
+#pragma unroll
+      for (int q = 0; q < C; q++)
+        {
+          cf[q] += p[(size_t) q * a.nk];
+          sf[q] += p[(size_t) (C + q) * a.nk];
+          cg[q] += p[(size_t) (2 * C + q) * a.nk];
+          sg[q] += p[(size_t) (3 * C + q) * a.nk];
+        }
+    }
+  const VjpK K = a.kt[k];
   const float e[3] = {K.ex, K.ey, K.ez};
   float *o = a.wu + (size_t) k * 4 * C;
   // W = (Bc + i Bs)(C + i S): re = Bc C - Bs S, im = Bc S + Bs C
@@ -300,14 +364,15 @@ kva_sfac (VjpArgs a)
   // Re conj(S_g) . dW = Cg . dP + Sg . dQ
   for (int c = 0; c < 3; c++)
     {
-      float s = 0.f;
+      float sacc = 0.f;
 #pragma unroll
-      for (int q = 0; q < C; q++) s = fmaf (cg[q], P.v[q].d[c], fmaf (sg[q], Q.v[q].d[c], s));
-      a.dbox[(size_t) 3 * k + c] = s;
+      for (int q = 0; q < C; q++) sacc = fmaf (cg[q], P.v[q].d[c], fmaf (sg[q], Q.v[q].d[c], sacc));
+      a.dbox[(size_t) 3 * k + c] = sacc;
     }
 }
 
-// per particle l and a slice of k: sum_k k Im[e^{-ik.r_l} (g_l . W_k + f_l . U_k)]
+// per particle l and a slice of k: sum_k k Im[e^{-ik.r_l} (g_l . W_k + f_l . U_k)],
+// the phase from the fixed-point position through the rotation table
 constexpr int BP_T = 128;     // particles per CTA
 constexpr int BP_KT = 64;     // k vectors staged per tile
 
@@ -316,8 +381,11 @@ __global__ void __launch_bounds__ (BP_T)
 kva_bp (VjpArgs a)
 {
   constexpr int C = NComp<V>::value;
+  __shared__ float4 s_rot[1024];
   __shared__ float s_wu[BP_KT][4 * C];
-  __shared__ VjpK s_k[BP_KT];
+  __shared__ int4 s_m[BP_KT];
+  __shared__ float4 s_kv[BP_KT];
+  for (int e = threadIdx.x; e < 1024; e += BP_T) s_rot[e] = a.rot[e];
   const int l = blockIdx.x * BP_T + threadIdx.x;
   const bool live = l < a.np;
   const int lc = live ? l : 0;
@@ -330,30 +398,27 @@ kva_bp (VjpArgs a)
       gl[q] = a.gf[(size_t) lc * 2 * VJ_CP + q];
       fl[q] = a.gf[(size_t) lc * 2 * VJ_CP + VJ_CP + q];
     }
-  const float2 *t0 = a.tab, *t1 = t0 + (size_t) (a.M0 + 1) * a.np,
-               *t2 = t1 + (size_t) (a.M1 + 1) * a.np;
+  const uint4 ql = a.q[lc];
   float gx = 0.f, gy = 0.f, gz = 0.f;
-  int pm1 = -1 << 30, pm2 = -1 << 30;
-  float2 p12 = make_float2 (1.f, 0.f);
   for (int kb = k0; kb < k1; kb += BP_KT)
     {
       const int nt = min (BP_KT, k1 - kb);
       __syncthreads ();
       for (int e = threadIdx.x; e < nt * 4 * C; e += BP_T)
         s_wu[e / (4 * C)][e % (4 * C)] = a.wu[(size_t) kb * 4 * C + e];
-      for (int e = threadIdx.x; e < nt; e += BP_T) s_k[e] = a.kt[kb + e];
+      for (int e = threadIdx.x; e < nt; e += BP_T)
+        {
+          const VjpK K = a.kt[kb + e];
+          s_m[e] = make_int4 (K.m1, K.m2, K.m3, 0);
+          s_kv[e] = make_float4 (K.kx, K.ky, K.kz, 0.f);
+        }
       __syncthreads ();
 #pragma unroll 4
       for (int t = 0; t < nt; t++)
         {
-          const VjpK &K = s_k[t];
-          if (K.m1 != pm1 || K.m2 != pm2)
-            {
-              p12 = cmulf (t0[(size_t) K.m1 * a.np + lc], tabm (t1, K.m2, a.np, lc));
-              pm1 = K.m1;
-              pm2 = K.m2;
-            }
-          const float2 ph = cmulf (p12, tabm (t2, K.m3, a.np, lc));
+          const int4 m = s_m[t];
+          const float2 ph = phase_s (s_rot, (uint32_t) m.x * ql.x + (uint32_t) m.y * ql.y
+                                              + (uint32_t) m.z * ql.z);
           float hr = 0.f, hi = 0.f;
 #pragma unroll
           for (int q = 0; q < C; q++)
@@ -363,9 +428,10 @@ kva_bp (VjpArgs a)
             }
           // Im[(cos - i sin)(hr + i hi)] = cos hi - sin hr
           const float im = ph.x * hi - ph.y * hr;
-          gx = fmaf (K.kx, im, gx);
-          gy = fmaf (K.ky, im, gy);
-          gz = fmaf (K.kz, im, gz);
+          const float4 kv = s_kv[t];
+          gx = fmaf (kv.x, im, gx);
+          gy = fmaf (kv.y, im, gy);
+          gz = fmaf (kv.z, im, gz);
         }
     }
   if (!live) return;
@@ -485,47 +551,52 @@ kva_real (VjpArgs a)
 }
 
 // the gradient per particle in FP64 (real-space chunks, twice the half-space
-// reciprocal slices) and, per block, the sums of the real-space box terms
-// and of r_l,a dL_rec/dr_l,a (the phase scaling of the box derivative)
+// reciprocal slices; one warp per particle, lanes over the chunks) and, per
+// block, the sums of the real-space box terms and of r_l,a dL_rec/dr_l,a
+// (the phase scaling of the box derivative)
 constexpr int FIN_T = 256;
+constexpr int FIN_P = FIN_T / 32;   // particles per block
 
 __global__ void __launch_bounds__ (FIN_T)
 kva_final (VjpArgs a)
 {
-  __shared__ double s_b[6][FIN_T];
-  const int l = blockIdx.x * FIN_T + threadIdx.x;
-  double v[6] = {0, 0, 0, 0, 0, 0};
+  __shared__ double s_b[FIN_P][6];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int l = blockIdx.x * FIN_P + w;
+  double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};      // grad psi, box, reciprocal
   if (l < a.np)
     {
-      double gr[3] = {0, 0, 0}, rec[3] = {0, 0, 0};
-      for (int ch = 0; ch < a.nchunk; ch++)
+      for (int ch = lane; ch < a.nchunk; ch += 32)
         {
           const float *p = a.part + ((size_t) ch * a.np + l) * 6;
-          for (int k = 0; k < 3; k++)
-            {
-              gr[k] += p[k];
-              v[k] += p[3 + k];
-            }
+          for (int k = 0; k < 6; k++) v[k] += p[k];
         }
       if (a.nk > 0)
-        for (int kc = 0; kc < a.kchunks; kc++)
-          for (int k = 0; k < 3; k++) rec[k] += a.grad[((size_t) kc * a.np + l) * 3 + k];
-      for (int k = 0; k < 3; k++)
-        {
-          rec[k] *= 2.0;
-          a.dldr[3 * l + k] = -gr[k] + rec[k];
-          v[3 + k] = a.pos[3 * l + k] * rec[k];
-        }
+        for (int kc = lane; kc < a.kchunks; kc += 32)
+          for (int k = 0; k < 3; k++) v[6 + k] += a.grad[((size_t) kc * a.np + l) * 3 + k];
     }
-  for (int k = 0; k < 6; k++) s_b[k][threadIdx.x] = v[k];
-  __syncthreads ();
-  for (int h = FIN_T / 2; h > 0; h >>= 1)
+  for (int k = 0; k < 9; k++)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync (0xffffffffu, v[k], o);
+  if (lane == 0)
     {
-      if ((int) threadIdx.x < h)
-        for (int k = 0; k < 6; k++) s_b[k][threadIdx.x] += s_b[k][threadIdx.x + h];
-      __syncthreads ();
+      double b[6] = {0, 0, 0, 0, 0, 0};
+      if (l < a.np)
+        for (int k = 0; k < 3; k++)
+          {
+            const double rec = 2.0 * v[6 + k];
+            a.dldr[3 * l + k] = -v[k] + rec;
+            b[k] = v[3 + k];
+            b[3 + k] = a.pos[3 * l + k] * rec;
+          }
+      for (int k = 0; k < 6; k++) s_b[w][k] = b[k];
     }
-  if (threadIdx.x < 6) a.blk[(size_t) blockIdx.x * 6 + threadIdx.x] = s_b[threadIdx.x][0];
+  __syncthreads ();
+  if (threadIdx.x < 6)
+    {
+      double t = 0.0;
+      for (int p = 0; p < FIN_P; p++) t += s_b[p][threadIdx.x];
+      a.blk[(size_t) blockIdx.x * 6 + threadIdx.x] = t;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -537,7 +608,7 @@ struct VjpState {
   int M[3] = {0, 0, 0};
   int nk = 0;
   std::vector<VjpK> hk;
-  DevBuf q, gf, gcm, p32, tab, kt, wu, dbox, part, grad, rot, g, f, pos, dldr, blk;
+  DevBuf q, gf, gcm, p32, tab, kt, wu, dbox, part, grad, rot, g, f, pos, dldr, blk, sfp;
 };
 
 std::mutex g_vjp_mu;
@@ -655,7 +726,9 @@ vjp_mixed_v (Ctx *c, const struct stokes *sys, VjpState *s, const double *g, con
                   std::make_pair (&s->gf, sizeof (float) * 2 * VJ_CP * np),
                   std::make_pair (&s->gcm, sizeof (float) * 2 * C * np),
                   std::make_pair (&s->dldr, sizeof (double) * 3 * np),
-                  std::make_pair (&s->blk, sizeof (double) * 6 * ((np + FIN_T - 1) / FIN_T)),
+                  std::make_pair (&s->blk, sizeof (double) * 6 * ((np + FIN_P - 1) / FIN_P)),
+                  std::make_pair (&s->sfp, sizeof (float) * 4 * C * (size_t) std::max (nk, 1)
+                                             * ((np + SF_P - 1) / SF_P)),
                   std::make_pair (&s->p32, sizeof (float3) * np),
                   std::make_pair (&s->tab, sizeof (float2) * (size_t) ntab * np),
                   std::make_pair (&s->kt, sizeof (VjpK) * std::max (nk, 1)),
@@ -734,12 +807,15 @@ vjp_mixed_v (Ctx *c, const struct stokes *sys, VjpState *s, const double *g, con
   kmark (c, st, "kva_real");
   if (nk > 0)
     {
-      kva_sfac<V><<<(nk + 7) / 8, 256, 0, st>>> (a);
+      const int nsl = (np + SF_P - 1) / SF_P;
+      kva_sfac<V><<<dim3 ((nk + SF_T - 1) / SF_T, nsl), SF_T, 0, st>>> (a, (float *) s->sfp.p);
       kmark (c, st, "kva_sfac");
+      kva_wu<V><<<(nk + 127) / 128, 128, 0, st>>> (a, (const float *) s->sfp.p, nsl);
+      kmark (c, st, "kva_wu");
       kva_bp<V><<<dim3 ((np + BP_T - 1) / BP_T, kchunks), BP_T, 0, st>>> (a);
       kmark (c, st, "kva_bp");
     }
-  const int nblk = (np + FIN_T - 1) / FIN_T;
+  const int nblk = (np + FIN_P - 1) / FIN_P;
   kva_final<<<nblk, FIN_T, 0, st>>> (a);
   kmark (c, st, "kva_final");
   if ((e = cudaGetLastError ()) != cudaSuccess) return cuda_fail (e, "mixed VJP kernels");
@@ -770,7 +846,7 @@ vjp_mixed_v (Ctx *c, const struct stokes *sys, VjpState *s, const double *g, con
           dLdbox[k] = bx[k] + 2.0 * opd - phase[k] / L[k];
         }
     }
-  c->launches = 3 + (nk > 0 ? 2 : 0);
+  c->launches = 3 + (nk > 0 ? 3 : 0);
   return STOKES_GPU_OK;
 }
 
@@ -807,7 +883,8 @@ release_vjp_mixed (const Ctx *c)
   }
   if (!s) return;
   for (DevBuf *b : {&s->q, &s->gf, &s->gcm, &s->p32, &s->tab, &s->kt, &s->wu, &s->dbox,
-                    &s->part, &s->grad, &s->rot, &s->g, &s->f, &s->pos, &s->dldr, &s->blk})
+                    &s->part, &s->grad, &s->rot, &s->g, &s->f, &s->pos, &s->dldr, &s->blk,
+                    &s->sfp})
     b->release ();
   delete s;
 }
