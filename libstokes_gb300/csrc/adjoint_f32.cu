@@ -225,16 +225,17 @@ constexpr int SF_P = 128;     // particles per slice
 // partial structure factors of one particle slice: thread = one k; the
 // slice's fixed-point positions and g, f sit in shared memory (read by every
 // thread alike), the phase e^{ik.r_j} is the exact fixed-point phase
-// m1 q_x + m2 q_y + m3 q_z mod 2^32 through phase_poly (no table: the lanes'
-// different k would collide in a shared table).
+// m1 q_x + m2 q_y + m3 q_z mod 2^32 through the rotation table.
 // out: sfp[slice][4 c][nk] = (cos f, sin f, cos g, sin g) sums
 template <int V>
 __global__ void __launch_bounds__ (SF_T)
 kva_sfac (VjpArgs a, float *sfp)
 {
   constexpr int C = NComp<V>::value;
+  __shared__ float4 s_rot[1024];
   __shared__ uint4 s_q[SF_P];
   __shared__ float s_x[SF_P][2 * C];
+  for (int e = threadIdx.x; e < 1024; e += SF_T) s_rot[e] = a.rot[e];
   const int j0 = blockIdx.y * SF_P, nj = min (SF_P, a.np - j0);
   for (int e = threadIdx.x; e < nj; e += SF_T) s_q[e] = a.q[j0 + e];
   for (int e = threadIdx.x; e < nj * 2 * C; e += SF_T)
@@ -253,7 +254,7 @@ kva_sfac (VjpArgs a, float *sfp)
   for (int jl = 0; jl < nj; jl++)
     {
       const uint4 qj = s_q[jl];
-      const float2 ph = phase_poly (m1 * qj.x + m2 * qj.y + m3 * qj.z);
+      const float2 ph = phase_s (s_rot, m1 * qj.x + m2 * qj.y + m3 * qj.z);
 #pragma unroll
       for (int q = 0; q < C; q++)
         {
@@ -374,14 +375,12 @@ kva_wu (VjpArgs a, const float *sfp, int nslices)
 // the phase from the fixed-point position through the rotation table
 constexpr int BP_T = 128;     // particles per CTA
 constexpr int BP_KT = 64;     // k vectors staged per tile
-constexpr int BP_MZ = 48;     // largest |m3| of the per-thread z-phase table
 
 template <int V>
 __global__ void __launch_bounds__ (BP_T)
 kva_bp (VjpArgs a)
 {
   constexpr int C = NComp<V>::value;
-  extern __shared__ float2 s_tz[];          // [BP_T][2 M2 + 1 | odd stride]
   __shared__ float4 s_rot[1024];
   __shared__ float s_wu[BP_KT][4 * C];
   __shared__ int4 s_m[BP_KT];
@@ -400,14 +399,6 @@ kva_bp (VjpArgs a)
       fl[q] = a.gf[(size_t) lc * 2 * VJ_CP + VJ_CP + q];
     }
   const uint4 ql = a.q[lc];
-  // this particle's z phases e^{2 pi i m3 u_z}, m3 = -M2 .. M2, in its own
-  // row (odd stride: the threads' rows fall in different banks)
-  const int zs = 2 * a.M2 + 2 - (2 * a.M2 + 1) % 2;
-  float2 *tz = s_tz + (size_t) threadIdx.x * zs + a.M2;
-  __syncthreads ();
-  for (int m = -a.M2; m <= a.M2; m++) tz[m] = phase_s (s_rot, (uint32_t) m * ql.z);
-  int pm1 = 1 << 30, pm2 = 1 << 30;
-  float2 p12 = make_float2 (1.f, 0.f);
   float gx = 0.f, gy = 0.f, gz = 0.f;
   for (int kb = k0; kb < k1; kb += BP_KT)
     {
@@ -426,13 +417,8 @@ kva_bp (VjpArgs a)
       for (int t = 0; t < nt; t++)
         {
           const int4 m = s_m[t];
-          if (m.x != pm1 || m.y != pm2)
-            {
-              p12 = phase_s (s_rot, (uint32_t) m.x * ql.x + (uint32_t) m.y * ql.y);
-              pm1 = m.x;
-              pm2 = m.y;
-            }
-          const float2 ph = cmulf (p12, tz[m.z]);
+          const float2 ph = phase_s (s_rot, (uint32_t) m.x * ql.x + (uint32_t) m.y * ql.y
+                                              + (uint32_t) m.z * ql.z);
           float hr = 0.f, hi = 0.f;
 #pragma unroll
           for (int q = 0; q < C; q++)
@@ -714,7 +700,6 @@ vjp_split (const struct stokes *sys, VjpState *s)
           M[1] = std::max (M[1], abs (m2));
           M[2] = std::max (M[2], abs (m3));
         }
-  if (M[2] > BP_MZ) return false;     // the back-projection's z-phase table
   s->xi = xi;
   s->rc = rc;
   s->kc = kc;
@@ -827,13 +812,7 @@ vjp_mixed_v (Ctx *c, const struct stokes *sys, VjpState *s, const double *g, con
       kmark (c, st, "kva_sfac");
       kva_wu<V><<<(nk + 127) / 128, 128, 0, st>>> (a, (const float *) s->sfp.p, nsl);
       kmark (c, st, "kva_wu");
-      const int zs = 2 * s->M[2] + 2 - (2 * s->M[2] + 1) % 2;
-      if ((e = cudaFuncSetAttribute (kva_bp<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int) (sizeof (float2) * BP_T * (2 * BP_MZ + 2))))
-          != cudaSuccess)
-        return cuda_fail (e, "mixed VJP shared memory");
-      kva_bp<V><<<dim3 ((np + BP_T - 1) / BP_T, kchunks), BP_T,
-                  sizeof (float2) * BP_T * zs, st>>> (a);
+      kva_bp<V><<<dim3 ((np + BP_T - 1) / BP_T, kchunks), BP_T, 0, st>>> (a);
       kmark (c, st, "kva_bp");
     }
   const int nblk = (np + FIN_P - 1) / FIN_P;
