@@ -608,6 +608,7 @@ struct VjpState {
   int M[3] = {0, 0, 0};
   int nk = 0;
   std::vector<VjpK> hk;
+  uint64_t uploaded = 0;        // split whose k table and rotations are on the device
   DevBuf q, gf, gcm, p32, tab, kt, wu, dbox, part, grad, rot, g, f, pos, dldr, blk, sfp;
 };
 
@@ -742,7 +743,9 @@ vjp_mixed_v (Ctx *c, const struct stokes *sys, VjpState *s, const double *g, con
                   std::make_pair (&s->pos, sizeof (double) * 3 * np)})
     if (e == cudaSuccess) e = pr.first->ensure (pr.second);
   if (e != cudaSuccess) return cuda_fail (e, "mixed VJP buffers");
-  // 1024 rotations e^{2 pi i h / 1024} as FP32 pairs hi + lo (phase_of)
+  // 1024 rotations e^{2 pi i h / 1024} as FP32 pairs hi + lo (phase_of) and
+  // the k table, when the split (or the buffers) changed
+  if (s->uploaded != (s->key ^ (uint64_t) (uintptr_t) s->kt.p))
   {
     std::vector<float> h (4 * 1024);
     for (int k = 0; k < 1024; k++)
@@ -756,16 +759,17 @@ vjp_mixed_v (Ctx *c, const struct stokes *sys, VjpState *s, const double *g, con
     e = cudaMemcpyAsync (s->rot.p, h.data (), sizeof (float) * h.size (), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && nk)
       e = cudaMemcpyAsync (s->kt.p, s->hk.data (), sizeof (VjpK) * nk, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync (s->pos.p, sys->pos, sizeof (double) * 3 * np, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync (s->g.p, g, sizeof (double) * n, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync (s->f.p, f, sizeof (double) * n, cudaMemcpyHostToDevice, st);
-    // the pinned-free host vectors above must stay valid until the copies end
+    // h is local: the copy must end before it goes away
     if (e == cudaSuccess) e = cudaStreamSynchronize (st);
-    if (e != cudaSuccess) return cuda_fail (e, "mixed VJP upload");
+    if (e != cudaSuccess) return cuda_fail (e, "mixed VJP tables");
+    s->uploaded = s->key ^ (uint64_t) (uintptr_t) s->kt.p;
   }
+  e = cudaMemcpyAsync (s->pos.p, sys->pos, sizeof (double) * 3 * np, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync (s->g.p, g, sizeof (double) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync (s->f.p, f, sizeof (double) * n, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail (e, "mixed VJP upload");
   VjpArgs a;
   memset (&a, 0, sizeof a);
   a.pos = (const double *) s->pos.p;
