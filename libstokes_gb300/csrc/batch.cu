@@ -449,6 +449,8 @@ namespace lsg {
 static double
 batch_eta (int np)
 {
+  const char *e = getenv ("LIBSTOKES_GB300_BATCH_ETA");   // read per set-up: sweeps
+  if (e && atof (e) > 0.0) return atof (e);
   if (np <= 256) return 8.0;
   if (np <= 1024) return 10.0;
   return 12.0;
