@@ -655,6 +655,11 @@ def batch_measure(lib, abi, L, nsys=None):
         lib.stokes_gpu_batch_stats(h, st.ctypes.data_as(dp))
         dev_ms.append(st[0])
     t_prod = (time.perf_counter() - t0) / reps
+    etas = []
+    for s in range(ns):
+        eta = C.c_double()
+        abi.check(lib.stokes_gpu_batch_split(h, s, C.byref(eta), None))
+        etas.append(eta.value)
     t0 = time.perf_counter()
     abi.check(lib.stokes_gpu_batch_bd(h, 1.0, 1e-3, w["n_cheb"], 20, None, None, 11,
                                       w["bd_steps"], None))
@@ -680,7 +685,8 @@ def batch_measure(lib, abi, L, nsys=None):
             "systems_per_s_product_plus_bd": ns / (t_prod + t_bd),
             "host_loop_product_ms_extrapolated": 1000.0 * t_loop,
             "batch_over_host_loop": t_loop / t_prod,
-            "autotuned": {"chunk_mult": st[1], "real_warps_per_cta": st[2]},
+            "autotuned": {"chunk_mult": st[1], "real_warps_per_cta": st[2],
+                          "eta_min": min(etas), "eta_max": max(etas)},
             "create_s": t_create, "first_product_with_autotune_s": t_tune,
             "k_vectors_total": st[3]}
 

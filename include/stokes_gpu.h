@@ -146,6 +146,9 @@ int stokes_gpu_batch_atimes (stokes_gpu_batch *b, const double *x, double *y);
 /* device ms of the last batch product, chosen real-space chunking and warps
  * per CTA, total k vectors (mixed) */
 int stokes_gpu_batch_stats (const stokes_gpu_batch *b, double *out4);
+/* mixed batches: the split of system s, eta = xi V^(1/3) and xi (the split
+ * is autotuned with the chunking on the first product) */
+int stokes_gpu_batch_split (const stokes_gpu_batch *b, int s, double *eta, double *xi);
 /* nsteps Brownian-dynamics mid-point steps of every system of the batch
  * (no repulsion, no imposed flow): f = sqrt(2 / (peclet dt)) z with
  * z = M^{-1/2} y by an n_cheb-term Chebyshev series on per-system bounds

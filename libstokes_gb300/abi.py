@@ -266,6 +266,7 @@ _SIGS = {
     "stokes_gpu_batch_set_positions": (C.c_int, [C.c_void_p, _dp]),
     "stokes_gpu_batch_atimes": (C.c_int, [C.c_void_p, _dp, _dp]),
     "stokes_gpu_batch_stats": (C.c_int, [C.c_void_p, _dp]),
+    "stokes_gpu_batch_split": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "stokes_gpu_batch_bd": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int, _dp,
                                       _dp, C.c_ulonglong, C.c_int, _dp]),
     "stokes_gpu_vjp": (C.c_int, [_SP, _dp, _dp, _dp, _dp, _dp]),

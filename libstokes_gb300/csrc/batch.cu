@@ -435,6 +435,9 @@ struct stokes_gpu_batch {
   lsg::DevBuf d_sys, d_cum, d_pos, d_x, d_y, d_qpos, d_tab, d_xf, d_kt, d_pq, d_pr, d_img;
   int tab_tot = 0, k_tot = 0, pq_tot = 0, pr_tot = 0;
   int chunk_mult = 1, real_wpb = 4;     // autotuned
+  // split: eta = xi V^(1/3) = eta_scale np^(1/6), the balance of real-space
+  // pairs (~ np^2 / eta^3) and k vectors (~ np eta^3); the scale is autotuned
+  double eta_scale = 1.6;
   bool tuned = false;
   // FP64: one stream per branch inside the capture
   std::vector<cudaStream_t> side;
@@ -446,14 +449,20 @@ struct stokes_gpu_batch {
 
 namespace lsg {
 
+// a fixed eta for every system (measurements of the split), else none
 static double
-batch_eta (int np)
+batch_eta_override ()
 {
   const char *e = getenv ("LIBSTOKES_GB300_BATCH_ETA");   // read per set-up: sweeps
-  if (e && atof (e) > 0.0) return atof (e);
-  if (np <= 256) return 8.0;
-  if (np <= 1024) return 10.0;
-  return 12.0;
+  return (e && atof (e) > 0.0) ? atof (e) : 0.0;
+}
+
+static double
+batch_eta (const stokes_gpu_batch *b, int np)
+{
+  const double o = batch_eta_override ();
+  if (o > 0.0) return o;
+  return b->eta_scale * pow ((double) np, 1.0 / 6.0);
 }
 
 // the mixed split, k list and descriptors of every system
@@ -483,7 +492,7 @@ batch_setup_mixed (stokes_gpu_batch *b)
       // size (FP32 loses digits to their cancellation when xi a grows);
       // small boxes then take lattice images in real space
       const double XI_CAP = 0.5;
-      const double xi = std::min (batch_eta (sys->np) / lv, XI_CAP);
+      const double xi = std::min (batch_eta (b, sys->np) / lv, XI_CAP);
       double rc = 0, kc = 0;
       lsg_ewald_cutoffs (xi, eps, lmin, lmax, &rc, &kc);
       (void) lmax;
@@ -725,35 +734,57 @@ batch_run (stokes_gpu_batch *b, float *ms)
   return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "batch product");
 }
 
-// time a few real-space chunkings and CTA sizes, keep the fastest
+// time a few splits, then real-space chunkings and CTA sizes, keep the fastest
 static int
 batch_autotune (stokes_gpu_batch *b)
 {
+  auto trial = [&] (bool setup, float *best_ms) -> int {
+    int rc = setup ? batch_setup_mixed (b) : STOKES_GPU_OK;
+    if (!rc) batch_chunks (b);
+    if (!rc) rc = batch_upload_mixed (b);
+    if (!rc) rc = batch_capture (b);
+    float t = 0.f, tmin = 1e30f;
+    for (int rep = 0; rep < 3 && !rc; rep++)
+      {
+        rc = batch_run (b, &t);
+        tmin = std::min (tmin, t);
+      }
+    *best_ms = tmin;
+    return rc;
+  };
+  int rc = STOKES_GPU_OK;
+  float t = 0.f, best = 1e30f;
+  b->chunk_mult = 1;
+  b->real_wpb = 4;
+  if (batch_eta_override () <= 0.0)
+    {
+      const double scales[4] = {1.2, 1.6, 2.0, 2.4};
+      double bs = b->eta_scale;
+      for (double sc : scales)
+        {
+          b->eta_scale = sc;
+          if ((rc = trial (true, &t))) return rc;
+          if (t < best) { best = t; bs = sc; }
+        }
+      b->eta_scale = bs;
+      if ((rc = batch_setup_mixed (b))) return rc;
+    }
   const int mults[3] = {1, 2, 4};
   const int wpbs[2] = {4, 8};
-  float best = 1e30f;
+  best = 1e30f;
   int bm = 1, bw = 4;
   for (int m : mults)
     for (int w : wpbs)
       {
         b->chunk_mult = m;
         b->real_wpb = w;
-        batch_chunks (b);
-        int rc = batch_upload_mixed (b);
-        if (!rc) rc = batch_capture (b);
-        if (rc) return rc;
-        float t = 0.f, tmin = 1e30f;
-        for (int rep = 0; rep < 3; rep++)
-          {
-            if ((rc = batch_run (b, &t))) return rc;
-            tmin = std::min (tmin, t);
-          }
-        if (tmin < best) { best = tmin; bm = m; bw = w; }
+        if ((rc = trial (false, &t))) return rc;
+        if (t < best) { best = t; bm = m; bw = w; }
       }
   b->chunk_mult = bm;
   b->real_wpb = bw;
   batch_chunks (b);
-  int rc = batch_upload_mixed (b);
+  rc = batch_upload_mixed (b);
   if (!rc) rc = batch_capture (b);
   b->tuned = true;
   return rc;
@@ -932,6 +963,21 @@ stokes_gpu_batch_stats (const stokes_gpu_batch *b, double *out4)
   out4[1] = b->chunk_mult;
   out4[2] = b->real_wpb;
   out4[3] = b->k_tot;
+  return STOKES_GPU_OK;
+}
+
+// the mixed batch's split: eta = xi V^(1/3) of system s (the scale times
+// np^(1/6), or the fixed override)
+int
+stokes_gpu_batch_split (const stokes_gpu_batch *b, int s, double *eta, double *xi)
+{
+  if (!b || s < 0 || s >= b->nsys) return set_error (STOKES_GPU_EINVAL, "bad batch system");
+  if (b->precision != STOKES_GPU_MIXED)
+    return set_error (STOKES_GPU_EINVAL, "only mixed batches re-split");
+  const struct stokes *sys = b->sys[s];
+  const double lv = cbrt (sys->lx * sys->ly * sys->lz);
+  if (eta) *eta = (double) b->h_sys[s].xi * lv;
+  if (xi) *xi = (double) b->h_sys[s].xi;
   return STOKES_GPU_OK;
 }
 
