@@ -88,6 +88,29 @@ cudaError_t launch_combine_fp64 (int version, const double *x, const double *par
                                  int np, double *y, cudaStream_t st);
 cudaError_t launch_matrix_fp64 (int version, int mode, const MatArgs &a, cudaStream_t st);
 constexpr int KTF_STRIDE = 12;   // floats per reciprocal vector of the FP32 builder
+
+// thread-per-pair split-precision dense builder (equal spheres, no shear, no
+// clamp) at its own split: the lattice images of each pair are enumerated
+// from the box, the reciprocal vectors form a half-space table with doubled
+// weights
+struct MatPairArgs {
+  const double *pos;
+  int np;
+  double *mat;
+  double lx, ly, lz, ilx, ily, ilz;    // box and its inverse
+  float lxh, lyh, lzh, lxl, lyl, lzl;  // box as hi + lo floats
+  float ilxf, ilyf, ilzf;
+  float rc, rc2, xi, xisp;
+  double xi64;                         // xi in FP64 (the diagonal blocks)
+  double self[3];                      // self_a, self_c, self_m of the split
+  const float *ktf;                    // [nk][KTF_STRIDE]
+  const float2 *phf;                   // [nk][np]
+  int nk;
+  const float *selfmo;                 // moments of the diagonal blocks
+};
+cudaError_t launch_matrix_self (int version, const MatPairArgs &a, const double *kt,
+                                float *selfmo, cudaStream_t st);
+cudaError_t launch_matrix_pairs (int version, const MatPairArgs &a, cudaStream_t st);
 cudaError_t launch_phase_f32 (const double *pos, const double *kt, int nk, int np, float2 *phf,
                               cudaStream_t st);
 cudaError_t launch_gemv_fp64 (int version, const double *mat, const double *x,

@@ -940,6 +940,212 @@ k_matrix_f32 (MatArgs a)
     }
 }
 
+// Thread-per-pair split-precision dense builder (equal spheres, no shear,
+// no clamp) at a split of its own, light in both spaces per pair.  A warp
+// holds one target i and 32 consecutive sources j; each thread owns the
+// moments of its pair, so there is no reduction.
+//  * real space: the minimum-image separation in FP64 becomes hi + lo
+//    floats, and the lattice images within rc are enumerated from the box
+//    (a slice in y, in z, then the x range), each one a term;
+//  * reciprocal space: the half-space table (weights doubled: the terms of k
+//    and -k are equal) with the FP32 phase table, (cos, sin)(k.r);
+//  * the C x C block goes out row by row through shared memory: each row of
+//    the warp's 32 blocks is C * 32 consecutive doubles, stored coalesced
+//    with streaming stores (the matrix is far larger than L2; the phase
+//    table stays there).
+// The diagonal blocks do not depend on the positions: the self term, the
+// particle's own lattice images and the reciprocal vectors at phase 1.  One
+// warp sums their moments in FP64 (the FP32 sum of about a hundred terms on
+// top of the self term loses a few 1e-7 of the entry), once per build.
+template <int V>
+__global__ void __launch_bounds__ (32)
+k_matrix_self (MatPairArgs a, const double *kt, float *selfmo)
+{
+  constexpr int NM = Moments<V>::N;
+  const int lane = threadIdx.x;
+  double mo[NM];
+#pragma unroll
+  for (int q = 0; q < NM; q++) mo[q] = 0.0;
+  if (lane == 0)
+    {
+      PairScalars<double> s;
+      s.xa = s.ya = a.self[0];
+      s.xc = s.yc = a.self[1];
+      s.xm = s.ym = s.zm = a.self[2];
+      s.yb = s.xg = s.yg = s.yh = 0.0;
+      const double e0[3] = {0.0, 0.0, 0.0};
+      moments_add<V, double> (e0, s, mo);
+    }
+  const double rc2 = (double) a.rc2;
+  const double xi = a.xi64, xisp = a.xi64 / sqrt (M_PI);
+  const int n1 = (int) ceil (sqrt (rc2) * a.ilx), n2 = (int) ceil (sqrt (rc2) * a.ily),
+            n3 = (int) ceil (sqrt (rc2) * a.ilz);
+  const int w1 = 2 * n1 + 1, w2 = 2 * n2 + 1, w3 = 2 * n3 + 1;
+  for (int t = lane; t < w1 * w2 * w3; t += 32)
+    {
+      const int b1 = t / (w2 * w3) - n1, b2 = (t / w3) % w2 - n2, b3 = t % w3 - n3;
+      const double rx = b1 * a.lx, ry = b2 * a.ly, rz = b3 * a.lz;
+      const double rr = rx * rx + ry * ry + rz * rz;
+      if (rr == 0.0 || rr > rc2) continue;
+      const double r = sqrt (rr), ri = 1.0 / r;
+      const double e[3] = {rx * ri, ry * ri, rz * ri};
+      PairScalars<double> s;
+      real_scalars_mono_ri<V, double> (xi, xisp, r, ri, s);
+      moments_add<V, double> (e, s, mo);
+    }
+  for (int k = lane; k < a.nk; k += 32)
+    {
+      const double *K = kt + KT_STRIDE * k;
+      const double e[3] = {K[KT_EX], K[KT_EY], K[KT_EZ]};
+      PairScalars<double> s;
+      s.xa = 0.0; s.ya = K[KT_YA];
+      s.yb = 0.0;
+      s.xc = 0.0; s.yc = K[KT_YC];
+      s.xg = 0.0; s.yg = 0.0;
+      s.yh = K[KT_YH];
+      s.xm = 0.0; s.ym = K[KT_YM]; s.zm = 0.0;
+      moments_add<V, double> (e, s, mo);
+    }
+#pragma unroll
+  for (int q = 0; q < NM; q++)
+    {
+      const double v = warp_sum (mo[q]);
+      if (lane == 0) selfmo[q] = (float) v;
+    }
+}
+
+template <int V>
+__global__ void __launch_bounds__ (128)
+k_matrix_pairs (MatPairArgs a)
+{
+  constexpr int C = NComp<V>::value;
+  constexpr int NM = Moments<V>::N;
+  __shared__ float s_row[4][32 * C];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int njt = (a.np + 31) >> 5;
+  const long long w = (long long) blockIdx.x * 4 + wib;
+  if (w >= (long long) a.np * njt) return;   // uniform over the warp
+  const int i = (int) (w / njt), j0 = (int) (w % njt) * 32;
+  const int j = j0 + lane;
+  const bool act = j < a.np;
+  const bool same = (i == j);
+  float mo[NM];
+#pragma unroll
+  for (int q = 0; q < NM; q++) mo[q] = 0.0f;
+  if (same)
+    {
+#pragma unroll
+      for (int q = 0; q < NM; q++) mo[q] = __ldg (a.selfmo + q);
+    }
+  else if (act)
+    {
+      double dx = a.pos[3 * j] - a.pos[3 * i];
+      double dy = a.pos[3 * j + 1] - a.pos[3 * i + 1];
+      double dz = a.pos[3 * j + 2] - a.pos[3 * i + 2];
+      dx -= a.lx * rint (dx * a.ilx);
+      dy -= a.ly * rint (dy * a.ily);
+      dz -= a.lz * rint (dz * a.ilz);
+      // a separation that is not inside the box after the minimum image
+      // (non-finite or huge coordinates) gives NaN blocks and bounded loops
+      if (!(fabs (dx) <= a.lx && fabs (dy) <= a.ly && fabs (dz) <= a.lz))
+        dx = dy = dz = nan ("");
+      const float hx = (float) dx, hy = (float) dy, hz = (float) dz;
+      const float lx = (float) (dx - (double) hx), ly = (float) (dy - (double) hy),
+                  lz = (float) (dz - (double) hz);
+      const float rc = a.rc, rc2 = a.rc2, xi = a.xi, xisp = a.xisp;
+      const int b2lo = (int) ceilf ((-rc - hy) * a.ilyf), b2hi = (int) floorf ((rc - hy) * a.ilyf);
+      // NaN: the conversions give 0 (one pass, NaN terms)
+      for (int b2 = b2lo; b2 <= b2hi; b2++)
+        {
+          const float fb2 = (float) b2;
+          const float ry = fmaf (fb2, a.lyh, hy) + fmaf (fb2, a.lyl, ly);
+          const float rem2 = rc2 - ry * ry;
+          if (rem2 < 0.0f) continue;
+          const float sy = sqrtf (rem2);
+          const int b3lo = (int) ceilf ((-sy - hz) * a.ilzf), b3hi = (int) floorf ((sy - hz) * a.ilzf);
+          for (int b3 = b3lo; b3 <= b3hi; b3++)
+            {
+              const float fb3 = (float) b3;
+              const float rz = fmaf (fb3, a.lzh, hz) + fmaf (fb3, a.lzl, lz);
+              const float rem3 = rem2 - rz * rz;
+              if (rem3 < 0.0f) continue;
+              const float sz = sqrtf (rem3);
+              const int b1lo = (int) ceilf ((-sz - hx) * a.ilxf),
+                        b1hi = (int) floorf ((sz - hx) * a.ilxf);
+              for (int b1 = b1lo; b1 <= b1hi; b1++)
+                {
+                  const float fb1 = (float) b1;
+                  const float rx = fmaf (fb1, a.lxh, hx) + fmaf (fb1, a.lxl, lx);
+                  const float rr = rx * rx + ry * ry + rz * rz;
+                  // the zero separation (the pair's own image 0, or a
+                  // distinct pair at identical positions) is skipped
+                  if (rr == 0.0f || rr > rc2) continue;
+                  const float ri = rsqrtf (rr);
+                  const float r = rr * ri;
+                  const float e[3] = {rx * ri, ry * ri, rz * ri};
+                  PairScalars<float> s;
+                  real_scalars_mono_ri<V, float> (xi, xisp, r, ri, s);
+                  moments_add<V, float> (e, s, mo);
+                }
+            }
+        }
+      const float2 *phi = a.phf + i, *phj = a.phf + j;
+      for (int k = 0; k < a.nk; k++)
+        {
+          const float *K = a.ktf + KTF_STRIDE * k;
+          const float2 pi_ = __ldg (phi + (size_t) k * a.np);
+          const float2 pj = __ldg (phj + (size_t) k * a.np);
+          const float cf = pj.x * pi_.x + pj.y * pi_.y;
+          const float sf = pj.x * pi_.y - pj.y * pi_.x;
+          const float e[3] = {__ldg (K), __ldg (K + 1), __ldg (K + 2)};
+          PairScalars<float> s;
+          s.xa = 0.0f; s.ya = cf * __ldg (K + 3);
+          s.yb = sf * __ldg (K + 4);
+          s.xc = 0.0f; s.yc = cf * __ldg (K + 5);
+          s.xg = 0.0f; s.yg = sf * __ldg (K + 6);
+          s.yh = cf * __ldg (K + 7);
+          s.xm = 0.0f; s.ym = cf * __ldg (K + 8); s.zm = 0.0f;
+          moments_add<V, float> (e, s, mo);
+        }
+    }
+  const size_t n = (size_t) C * a.np;
+  const int nval = C * min (32, a.np - j0);
+  float *sr = s_row[wib];
+  double *base = a.mat + (size_t) C * i * n + (size_t) C * j0;
+#pragma unroll
+  for (int row = 0; row < C; row++)
+    {
+#pragma unroll
+      for (int col = 0; col < C; col++)
+        sr[lane * C + col] = block_entry<V, float> (mo, row, col, same);
+      __syncwarp ();
+      double *dst = base + (size_t) row * n;
+      for (int t = lane; t < nval; t += 32) __stcs (dst + t, (double) sr[t]);
+      __syncwarp ();
+    }
+}
+
+cudaError_t
+launch_matrix_self (int version, const MatPairArgs &a, const double *kt, float *selfmo,
+                    cudaStream_t st)
+{
+  if (version == 0) k_matrix_self<0><<<1, 32, 0, st>>> (a, kt, selfmo);
+  else if (version == 1) k_matrix_self<1><<<1, 32, 0, st>>> (a, kt, selfmo);
+  else k_matrix_self<2><<<1, 32, 0, st>>> (a, kt, selfmo);
+  return cudaGetLastError ();
+}
+
+cudaError_t
+launch_matrix_pairs (int version, const MatPairArgs &a, cudaStream_t st)
+{
+  const long long nw = (long long) a.np * ((a.np + 31) / 32);
+  const int grid = (int) ((nw + 3) / 4);
+  if (version == 0) k_matrix_pairs<0><<<grid, 128, 0, st>>> (a);
+  else if (version == 1) k_matrix_pairs<1><<<grid, 128, 0, st>>> (a);
+  else k_matrix_pairs<2><<<grid, 128, 0, st>>> (a);
+  return cudaGetLastError ();
+}
+
 // dense y = M . z(x), one warp per row (z = extracted-form transform for FTS)
 __global__ void __launch_bounds__ (256)
 k_gemv (const double *mat, const double *z, int n, double *y)

@@ -141,6 +141,7 @@ free_ctx (Ctx *c)
   release_mixed (c);
   release_vjp_mixed (c);
   if (c->tuned) stokes_free (c->tuned);
+  if (c->dense) stokes_free (c->dense);
   delete c;
 }
 
@@ -483,6 +484,7 @@ prepare (Ctx *c, const struct stokes *sys, bool cube, int tables)
   if (!c->open && !cube && (sys->nr > 0) && (!sys->rlx || !sys->rly || !sys->rlz))
     return set_error (STOKES_GPU_EINVAL, "image table missing (stokes_set_xi not called?)");
   c->sys = sys;
+  c->cube = cube;
   c->version = sys->version;
   c->np = sys->np;
   c->mode = sys->slip ? MODE_SLIP : (sys->a ? MODE_POLY : MODE_MONO);
@@ -804,10 +806,150 @@ atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
   return STOKES_GPU_OK;
 }
 
+// ---- the thread-per-pair dense builder ---------------------------------------
+// The split-precision builder of equal spheres pays for every real-space
+// image and every reciprocal vector once per pair.  At xi = eta / V^(1/3)
+// with eta about 2 and the FP32 truncation eps = 3e-8, a pair holds about 30
+// images and 50 half-space vectors (the reference's split at its 1e-12
+// holds about 110 and 55 full-space ones).  LIBSTOKES_GB300_DENSE_ETA sets
+// eta (0: the warp-per-pair builder at the reference's split).  FTS takes
+// the G correction of the tuned FP64 split (g_correction), so that the
+// matrix is that of the reference's split.
+static double
+dense_eta ()
+{
+  static const double env = [] {
+    const char *s = getenv ("LIBSTOKES_GB300_DENSE_ETA");
+    return s ? atof (s) : -1.0;
+  }();
+  return env >= 0.0 ? env : 2.2;
+}
+
+static bool
+dense_pairs_apply (const Ctx *c, const struct stokes *sys)
+{
+  return dense_eta () > 0.0 && c->precision == STOKES_GPU_MIXED && !c->open && !c->cube
+         && c->mode == MODE_MONO && sys->periodic && sys->shear_mode == 0 && sys->rmin == 0.0
+         && sys->np > 0 && split_is_as_set (sys);
+}
+
+// the private copy at the dense split and its half-space tables
+static int
+dense_tables (Ctx *c, const struct stokes *sys, cudaStream_t st)
+{
+  const double eps = 3e-8;
+  const double eta = dense_eta ();
+  const double key[7] = {sys->lx, sys->ly, sys->lz, (double) sys->np, (double) sys->version,
+                         eta, sys->xi};
+  if (!c->dense || memcmp (c->dense_key, key, sizeof key) != 0)
+    {
+      if (c->dense) stokes_free (c->dense);
+      c->dense = nullptr;
+      struct stokes *sv = stokes_init ();
+      if (!sv) return set_error (STOKES_GPU_ENOMEM, "dense split");
+      sv->version = sys->version;
+      sv->periodic = 1;
+      stokes_set_np (sv, sys->np, sys->nm);
+      stokes_set_l (sv, sys->lx, sys->ly, sys->lz);
+      stokes_set_xi (sv, eta / cbrt (sys->lx * sys->ly * sys->lz), eps);
+      c->dense = sv;
+      memcpy (c->dense_key, key, sizeof key);
+      std::vector<double> full;
+      build_ktable (sv, full);
+      if (sys->version == 2) g_correction (sys, full);
+      // half space: the terms of k and -k are equal (cos even, sin odd with
+      // the odd moments), so keep one of each pair with doubled weights
+      const double k0[3] = {2.0 * M_PI / sys->lx, 2.0 * M_PI / sys->ly, 2.0 * M_PI / sys->lz};
+      c->h_dkt.clear ();
+      c->h_dktf.clear ();
+      const size_t nk = full.size () / KT_STRIDE;
+      for (size_t q = 0; q < nk; q++)
+        {
+          const double *row = &full[q * KT_STRIDE];
+          const long long m1 = llrint (row[KT_KX] / k0[0]), m2 = llrint (row[KT_KY] / k0[1]),
+                          m3 = llrint (row[KT_KZ] / k0[2]);
+          if (!(m1 > 0 || (m1 == 0 && (m2 > 0 || (m2 == 0 && m3 > 0))))) continue;
+          double h[KT_STRIDE];
+          memcpy (h, row, sizeof h);
+          for (int w : {KT_YA, KT_YB, KT_YC, KT_YG, KT_YH, KT_YM}) h[w] *= 2.0;
+          c->h_dkt.insert (c->h_dkt.end (), h, h + KT_STRIDE);
+          const int src[9] = {KT_EX, KT_EY, KT_EZ, KT_YA, KT_YB, KT_YC, KT_YG, KT_YH, KT_YM};
+          float f[KTF_STRIDE] = {0};
+          for (int w = 0; w < 9; w++) f[w] = (float) h[src[w]];
+          c->h_dktf.insert (c->h_dktf.end (), f, f + KTF_STRIDE);
+        }
+      c->dense_nk = (int) (c->h_dkt.size () / KT_STRIDE);
+    }
+  int rc = upload_if_changed (c->dkt, c->fp_dkt, c->h_dkt.data (),
+                              sizeof (double) * c->h_dkt.size (), st, "dense reciprocal table");
+  if (!rc)
+    rc = upload_if_changed (c->dktf, c->fp_dktf, c->h_dktf.data (),
+                            sizeof (float) * c->h_dktf.size (), st, "dense reciprocal table");
+  return rc;
+}
+
+static int
+matrix_pairs_dev (Ctx *c, const struct stokes *sys, const double *d_pos, double *d_mat,
+                  cudaStream_t st)
+{
+  int rc = dense_tables (c, sys, st);
+  if (rc) return rc;
+  const int np = c->np, nk = c->dense_nk;
+  const struct stokes *sv = c->dense;
+  cudaError_t e;
+  kmark (c, st, nullptr);
+  int launches = 0;
+  if (nk > 0)
+    {
+      if ((e = c->ph.ensure (sizeof (float2) * (size_t) nk * np)) != cudaSuccess)
+        return cuda_fail (e, "phase table");
+      if ((e = launch_phase_f32 (d_pos, (const double *) c->dkt.p, nk, np, (float2 *) c->ph.p,
+                                 st)) != cudaSuccess)
+        return cuda_fail (e, "phase kernel");
+      launches++;
+      kmark (c, st, "k_phase");
+    }
+  MatPairArgs a;
+  a.pos = d_pos;
+  a.np = np;
+  a.mat = d_mat;
+  a.lx = sys->lx; a.ly = sys->ly; a.lz = sys->lz;
+  a.ilx = 1.0 / sys->lx; a.ily = 1.0 / sys->ly; a.ilz = 1.0 / sys->lz;
+  a.lxh = (float) sys->lx; a.lyh = (float) sys->ly; a.lzh = (float) sys->lz;
+  a.lxl = (float) (sys->lx - (double) a.lxh);
+  a.lyl = (float) (sys->ly - (double) a.lyh);
+  a.lzl = (float) (sys->lz - (double) a.lzh);
+  a.ilxf = (float) a.ilx; a.ilyf = (float) a.ily; a.ilzf = (float) a.ilz;
+  a.rc2 = (float) sv->rmax2;
+  a.rc = sqrtf (a.rc2);
+  a.xi = (float) sv->xi;
+  a.xisp = (float) (sv->xi / sqrt (M_PI));
+  a.xi64 = sv->xi;
+  a.self[0] = sv->self_a;
+  a.self[1] = sv->self_c;
+  a.self[2] = sv->self_m;
+  a.ktf = (const float *) c->dktf.p;
+  a.phf = (const float2 *) c->ph.p;
+  a.nk = nk;
+  if ((e = c->dself.ensure (sizeof (float) * 80)) != cudaSuccess)
+    return cuda_fail (e, "diagonal moments");
+  a.selfmo = (const float *) c->dself.p;
+  if ((e = launch_matrix_self (c->version, a, (const double *) c->dkt.p, (float *) c->dself.p,
+                               st)) != cudaSuccess)
+    return cuda_fail (e, "matrix kernel");
+  launches++;
+  if ((e = launch_matrix_pairs (c->version, a, st)) != cudaSuccess)
+    return cuda_fail (e, "matrix kernel");
+  kmark (c, st, "k_matrix_pairs");
+  c->launches = launches + 1;
+  return STOKES_GPU_OK;
+}
+
 // dense matrix on device
 int
 matrix_dev (Ctx *c, const double *d_pos, double *d_mat, cudaStream_t st)
 {
+  if (c->sys && dense_pairs_apply (c, c->sys)) return matrix_pairs_dev (c, c->sys, d_pos, d_mat, st);
   const int np = c->np;
   cudaError_t e;
   if ((e = c->ph.ensure (sizeof (double2) * (size_t) (c->nk > 0 ? c->nk : 1) * np)) != cudaSuccess)

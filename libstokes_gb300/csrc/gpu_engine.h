@@ -70,6 +70,17 @@ struct Ctx {
 
   DevBuf openf;   // scratch of the mixed-precision free-space product
   DevBuf imgf;    // the images in FP32 (split-precision dense builder)
+  // the thread-per-pair dense builder's split: a private copy of the system
+  // at it, its key, the half-space tables (FP64 rows for the phases, floats
+  // for the terms) and their count
+  bool cube = false;   // the last prepare's image set is the _notbl cube
+  struct stokes *dense = nullptr;
+  double dense_key[7] = {0, 0, 0, 0, 0, 0, 0};
+  int dense_nk = 0;
+  std::vector<double> h_dkt;
+  std::vector<float> h_dktf;
+  DevBuf dkt, dktf, dself;
+  uint64_t fp_dkt = 0, fp_dktf = 0;
 
   // pinned, mapped mirror of sys->pos for the host entry points of the
   // mixed paths, whose kernels read the positions once
@@ -77,9 +88,10 @@ struct Ctx {
   const double *hpos_dev = nullptr;   // its device address
   size_t hpos_bytes = 0;
 
-  std::array<DevBuf *, 14> all_buffers ()
+  std::array<DevBuf *, 17> all_buffers ()
   {
-    return {&pos, &x, &y, &img, &kt, &pp, &ph, &sf, &yrec, &partial, &mat, &zbuf, &openf, &imgf};
+    return {&pos, &x, &y, &img, &kt, &pp, &ph, &sf, &yrec, &partial, &mat, &zbuf, &openf, &imgf,
+            &dkt, &dktf, &dself};
   }
 };
 
