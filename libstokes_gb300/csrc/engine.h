@@ -103,11 +103,14 @@ struct MatPairArgs {
   float rc, rc2, xi, xisp;
   double xi64;                         // xi in FP64 (the diagonal blocks)
   double self[3];                      // self_a, self_c, self_m of the split
-  const float *ktf;                    // [nk][KTF_STRIDE]
+  const float *kco;                    // [nk][matrix_kco_stride]: moments per unit phase
   const float2 *phf;                   // [nk][np]
   int nk;
   const float *selfmo;                 // moments of the diagonal blocks
 };
+int matrix_kco_stride (int version);
+cudaError_t launch_matrix_kco (int version, const double *kt, int nk, float *kco,
+                               cudaStream_t st);
 cudaError_t launch_matrix_self (int version, const MatPairArgs &a, const double *kt,
                                 float *selfmo, cudaStream_t st);
 cudaError_t launch_matrix_pairs (int version, const MatPairArgs &a, cudaStream_t st);

@@ -1014,21 +1014,71 @@ k_matrix_self (MatPairArgs a, const double *kt, float *selfmo)
     }
 }
 
+// moments that the sine part of a reciprocal term feeds (odd in e); the
+// cosine part feeds the others
+__host__ __device__ constexpr bool
+mo_odd (int q)
+{
+  return (q >= MO_B1 && q < MO_C0) || (q >= MO_G1 && q < MO_H2);
+}
+// moments that no reciprocal term reaches (their scalars vanish in k space)
+__host__ __device__ constexpr bool
+mo_kzero (int q)
+{
+  return (q >= MO_G1 && q < MO_G2) || (q >= MO_M2 && q < MO_M4B) || q == MO_M5;
+}
+template <int V> struct MoPad { static constexpr int N = (Moments<V>::N + 3) / 4 * 4; };
+
+// Per reciprocal vector of the half-space table, each moment at unit cosine
+// (even moments) or unit sine (odd moments): a pair's term is then
+// cf * kco[q] or sf * kco[q], one FMA per moment.
 template <int V>
-__global__ void __launch_bounds__ (128)
+__global__ void
+k_matrix_kco (const double *kt, int nk, float *kco)
+{
+  constexpr int NM = Moments<V>::N, NP = MoPad<V>::N;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nk) return;
+  const double *K = kt + KT_STRIDE * k;
+  const double e[3] = {K[KT_EX], K[KT_EY], K[KT_EZ]};
+  PairScalars<double> s;
+  s.xa = 0.0; s.ya = K[KT_YA];
+  s.yb = K[KT_YB];
+  s.xc = 0.0; s.yc = K[KT_YC];
+  s.xg = 0.0; s.yg = K[KT_YG];
+  s.yh = K[KT_YH];
+  s.xm = 0.0; s.ym = K[KT_YM]; s.zm = 0.0;
+  double mo[NM];
+#pragma unroll
+  for (int q = 0; q < NM; q++) mo[q] = 0.0;
+  moments_add<V, double> (e, s, mo);
+#pragma unroll
+  for (int q = 0; q < NP; q++) kco[(size_t) k * NP + q] = q < NM ? (float) mo[q] : 0.0f;
+}
+
+constexpr int MP_TI = 8;     // targets per CTA, one per warp
+constexpr int MP_KCH = 64;   // reciprocal vectors per shared-memory chunk
+
+// A CTA holds 8 targets i (one per warp) and 32 consecutive sources j (one
+// per lane).  M is built from the pairs j > i only: block (j, i) is block
+// (i, j) with the odd moments negated (e -> -e, sin -> -sin), so each thread
+// writes both.  Tiles wholly below the diagonal exit at once.
+template <int V>
+__global__ void __launch_bounds__ (256, 2)
 k_matrix_pairs (MatPairArgs a)
 {
   constexpr int C = NComp<V>::value;
-  constexpr int NM = Moments<V>::N;
-  __shared__ float s_row[4][32 * C];
+  constexpr int NM = Moments<V>::N, NP = MoPad<V>::N;
+  __shared__ float4 s_k4[MP_KCH * NP / 4];
+  __shared__ float s_row[MP_TI][32 * C];
+  __shared__ float s_tr[32][MP_TI * C + 1];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int njt = (a.np + 31) >> 5;
-  const long long w = (long long) blockIdx.x * 4 + wib;
-  if (w >= (long long) a.np * njt) return;   // uniform over the warp
-  const int i = (int) (w / njt), j0 = (int) (w % njt) * 32;
-  const int j = j0 + lane;
-  const bool act = j < a.np;
-  const bool same = (i == j);
+  const int i0 = blockIdx.y * MP_TI, j0 = blockIdx.x * 32;
+  if (j0 + 31 < i0) return;   // uniform over the CTA, before any barrier
+  const int i = i0 + wib, j = j0 + lane;
+  const bool iok = i < a.np, jok = j < a.np;
+  const bool same = iok && i == j;
+  const bool work = iok && jok && j > i;
   float mo[NM];
 #pragma unroll
   for (int q = 0; q < NM; q++) mo[q] = 0.0f;
@@ -1037,7 +1087,7 @@ k_matrix_pairs (MatPairArgs a)
 #pragma unroll
       for (int q = 0; q < NM; q++) mo[q] = __ldg (a.selfmo + q);
     }
-  else if (act)
+  else if (work)
     {
       double dx = a.pos[3 * j] - a.pos[3 * i];
       double dy = a.pos[3 * j + 1] - a.pos[3 * i + 1];
@@ -1077,8 +1127,8 @@ k_matrix_pairs (MatPairArgs a)
                   const float fb1 = (float) b1;
                   const float rx = fmaf (fb1, a.lxh, hx) + fmaf (fb1, a.lxl, lx);
                   const float rr = rx * rx + ry * ry + rz * rz;
-                  // the zero separation (the pair's own image 0, or a
-                  // distinct pair at identical positions) is skipped
+                  // the zero separation (distinct particles at identical
+                  // positions) is skipped
                   if (rr == 0.0f || rr > rc2) continue;
                   const float ri = rsqrtf (rr);
                   const float r = rr * ri;
@@ -1089,39 +1139,83 @@ k_matrix_pairs (MatPairArgs a)
                 }
             }
         }
-      const float2 *phi = a.phf + i, *phj = a.phf + j;
-      for (int k = 0; k < a.nk; k++)
-        {
-          const float *K = a.ktf + KTF_STRIDE * k;
-          const float2 pi_ = __ldg (phi + (size_t) k * a.np);
-          const float2 pj = __ldg (phj + (size_t) k * a.np);
-          const float cf = pj.x * pi_.x + pj.y * pi_.y;
-          const float sf = pj.x * pi_.y - pj.y * pi_.x;
-          const float e[3] = {__ldg (K), __ldg (K + 1), __ldg (K + 2)};
-          PairScalars<float> s;
-          s.xa = 0.0f; s.ya = cf * __ldg (K + 3);
-          s.yb = sf * __ldg (K + 4);
-          s.xc = 0.0f; s.yc = cf * __ldg (K + 5);
-          s.xg = 0.0f; s.yg = sf * __ldg (K + 6);
-          s.yh = cf * __ldg (K + 7);
-          s.xm = 0.0f; s.ym = cf * __ldg (K + 8); s.zm = 0.0f;
-          moments_add<V, float> (e, s, mo);
-        }
+    }
+  // reciprocal space, the coefficient table staged in chunks
+  const float2 *phi = a.phf + (iok ? i : 0), *phj = a.phf + (jok ? j : 0);
+  for (int kc = 0; kc < a.nk; kc += MP_KCH)
+    {
+      const int nkc = min (MP_KCH, a.nk - kc);
+      __syncthreads ();
+      const float4 *src = reinterpret_cast<const float4 *> (a.kco) + (size_t) kc * (NP / 4);
+      for (int t = threadIdx.x; t < nkc * (NP / 4); t += blockDim.x) s_k4[t] = __ldg (src + t);
+      __syncthreads ();
+      if (work)
+        for (int k = 0; k < nkc; k++)
+          {
+            const float2 pi_ = __ldg (phi + (size_t) (kc + k) * a.np);
+            const float2 pj = __ldg (phj + (size_t) (kc + k) * a.np);
+            const float cf = pj.x * pi_.x + pj.y * pi_.y;
+            const float sf = pj.x * pi_.y - pj.y * pi_.x;
+            const float4 *c4 = s_k4 + k * (NP / 4);
+#pragma unroll
+            for (int q4 = 0; q4 < NP / 4; q4++)
+              {
+                const float4 v = c4[q4];
+                const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                  {
+                    const int q = 4 * q4 + u;
+                    if (q < NM && !mo_kzero (q)) mo[q] = fmaf (mo_odd (q) ? sf : cf, vv[u], mo[q]);
+                  }
+              }
+          }
     }
   const size_t n = (size_t) C * a.np;
-  const int nval = C * min (32, a.np - j0);
-  float *sr = s_row[wib];
-  double *base = a.mat + (size_t) C * i * n + (size_t) C * j0;
+  // blocks (i, j), j >= i: this warp's row, lanes l0 .. l1 - 1, C * 32
+  // consecutive doubles per matrix row
+  {
+    const int l0 = max (0, i - j0), l1 = min (32, a.np - j0);
+    float *sr = s_row[wib];
+    if (iok && l1 > l0)   // uniform over the warp
+      {
+        double *base = a.mat + (size_t) C * i * n + (size_t) C * j0;
 #pragma unroll
-  for (int row = 0; row < C; row++)
+        for (int row = 0; row < C; row++)
+          {
+#pragma unroll
+            for (int col = 0; col < C; col++)
+              sr[lane * C + col] = block_entry<V, float> (mo, row, col, same);
+            __syncwarp ();
+            double *dst = base + (size_t) row * n;
+            for (int t = C * l0 + lane; t < C * l1; t += 32) __stcs (dst + t, (double) sr[t]);
+            __syncwarp ();
+          }
+      }
+  }
+  // blocks (j, i), j > i: rows C j + beta hold the CTA's targets side by side
+#pragma unroll
+  for (int q = 0; q < NM; q++)
+    if (mo_odd (q)) mo[q] = -mo[q];
+#pragma unroll
+  for (int beta = 0; beta < C; beta++)
     {
 #pragma unroll
-      for (int col = 0; col < C; col++)
-        sr[lane * C + col] = block_entry<V, float> (mo, row, col, same);
-      __syncwarp ();
-      double *dst = base + (size_t) row * n;
-      for (int t = lane; t < nval; t += 32) __stcs (dst + t, (double) sr[t]);
-      __syncwarp ();
+      for (int alpha = 0; alpha < C; alpha++)
+        s_tr[lane][wib * C + alpha] = block_entry<V, float> (mo, beta, alpha, false);
+      __syncthreads ();
+#pragma unroll
+      for (int rr = 0; rr < 32 / MP_TI; rr++)
+        {
+          const int jl = (32 / MP_TI) * wib + rr, jj = j0 + jl;
+          const int ni = min (min (MP_TI, jj - i0), a.np - i0);   // targets i < jj
+          if (jj < a.np && ni > 0)
+            {
+              double *dst = a.mat + ((size_t) C * jj + beta) * n + (size_t) C * i0;
+              for (int t = lane; t < C * ni; t += 32) __stcs (dst + t, (double) s_tr[jl][t]);
+            }
+        }
+      __syncthreads ();
     }
 }
 
@@ -1135,14 +1229,30 @@ launch_matrix_self (int version, const MatPairArgs &a, const double *kt, float *
   return cudaGetLastError ();
 }
 
+int
+matrix_kco_stride (int version)
+{
+  return version == 0 ? MoPad<0>::N : (version == 1 ? MoPad<1>::N : MoPad<2>::N);
+}
+
+cudaError_t
+launch_matrix_kco (int version, const double *kt, int nk, float *kco, cudaStream_t st)
+{
+  if (nk <= 0) return cudaSuccess;
+  const int g = (nk + 127) / 128;
+  if (version == 0) k_matrix_kco<0><<<g, 128, 0, st>>> (kt, nk, kco);
+  else if (version == 1) k_matrix_kco<1><<<g, 128, 0, st>>> (kt, nk, kco);
+  else k_matrix_kco<2><<<g, 128, 0, st>>> (kt, nk, kco);
+  return cudaGetLastError ();
+}
+
 cudaError_t
 launch_matrix_pairs (int version, const MatPairArgs &a, cudaStream_t st)
 {
-  const long long nw = (long long) a.np * ((a.np + 31) / 32);
-  const int grid = (int) ((nw + 3) / 4);
-  if (version == 0) k_matrix_pairs<0><<<grid, 128, 0, st>>> (a);
-  else if (version == 1) k_matrix_pairs<1><<<grid, 128, 0, st>>> (a);
-  else k_matrix_pairs<2><<<grid, 128, 0, st>>> (a);
+  const dim3 grid ((a.np + 31) / 32, (a.np + MP_TI - 1) / MP_TI);
+  if (version == 0) k_matrix_pairs<0><<<grid, 32 * MP_TI, 0, st>>> (a);
+  else if (version == 1) k_matrix_pairs<1><<<grid, 32 * MP_TI, 0, st>>> (a);
+  else k_matrix_pairs<2><<<grid, 32 * MP_TI, 0, st>>> (a);
   return cudaGetLastError ();
 }
 

@@ -809,9 +809,9 @@ atimes_host (struct stokes *sys, const double *x, double *y, bool cube)
 // ---- the thread-per-pair dense builder ---------------------------------------
 // The split-precision builder of equal spheres pays for every real-space
 // image and every reciprocal vector once per pair.  At xi = eta / V^(1/3)
-// with eta about 2 and the FP32 truncation eps = 3e-8, a pair holds about 30
-// images and 50 half-space vectors (the reference's split at its 1e-12
-// holds about 110 and 55 full-space ones).  LIBSTOKES_GB300_DENSE_ETA sets
+// with eta about 2 and libstokes' cutoff rule at eps = 1e-6, a pair holds
+// about 35 images and 125 half-space vectors (the reference's split at its
+// 1e-12 holds about 110 images).  LIBSTOKES_GB300_DENSE_ETA sets
 // eta (0: the warp-per-pair builder at the reference's split).  FTS takes
 // the G correction of the tuned FP64 split (g_correction), so that the
 // matrix is that of the reference's split.
@@ -837,7 +837,9 @@ dense_pairs_apply (const Ctx *c, const struct stokes *sys)
 static int
 dense_tables (Ctx *c, const struct stokes *sys, cudaStream_t st)
 {
-  const double eps = 3e-8;
+  // truncation: 1e-6 in libstokes' cutoff rule leaves about 7e-8 of the
+  // largest entry (measured against eps 1e-14 on the FP64 oracle)
+  const double eps = 1e-6;
   const double eta = dense_eta ();
   const double key[7] = {sys->lx, sys->ly, sys->lz, (double) sys->np, (double) sys->version,
                          eta, sys->xi};
@@ -861,7 +863,6 @@ dense_tables (Ctx *c, const struct stokes *sys, cudaStream_t st)
       // the odd moments), so keep one of each pair with doubled weights
       const double k0[3] = {2.0 * M_PI / sys->lx, 2.0 * M_PI / sys->ly, 2.0 * M_PI / sys->lz};
       c->h_dkt.clear ();
-      c->h_dktf.clear ();
       const size_t nk = full.size () / KT_STRIDE;
       for (size_t q = 0; q < nk; q++)
         {
@@ -873,19 +874,11 @@ dense_tables (Ctx *c, const struct stokes *sys, cudaStream_t st)
           memcpy (h, row, sizeof h);
           for (int w : {KT_YA, KT_YB, KT_YC, KT_YG, KT_YH, KT_YM}) h[w] *= 2.0;
           c->h_dkt.insert (c->h_dkt.end (), h, h + KT_STRIDE);
-          const int src[9] = {KT_EX, KT_EY, KT_EZ, KT_YA, KT_YB, KT_YC, KT_YG, KT_YH, KT_YM};
-          float f[KTF_STRIDE] = {0};
-          for (int w = 0; w < 9; w++) f[w] = (float) h[src[w]];
-          c->h_dktf.insert (c->h_dktf.end (), f, f + KTF_STRIDE);
         }
       c->dense_nk = (int) (c->h_dkt.size () / KT_STRIDE);
     }
-  int rc = upload_if_changed (c->dkt, c->fp_dkt, c->h_dkt.data (),
-                              sizeof (double) * c->h_dkt.size (), st, "dense reciprocal table");
-  if (!rc)
-    rc = upload_if_changed (c->dktf, c->fp_dktf, c->h_dktf.data (),
-                            sizeof (float) * c->h_dktf.size (), st, "dense reciprocal table");
-  return rc;
+  return upload_if_changed (c->dkt, c->fp_dkt, c->h_dkt.data (),
+                            sizeof (double) * c->h_dkt.size (), st, "dense reciprocal table");
 }
 
 static int
@@ -928,7 +921,14 @@ matrix_pairs_dev (Ctx *c, const struct stokes *sys, const double *d_pos, double 
   a.self[0] = sv->self_a;
   a.self[1] = sv->self_c;
   a.self[2] = sv->self_m;
-  a.ktf = (const float *) c->dktf.p;
+  if ((e = c->dktf.ensure (sizeof (float) * matrix_kco_stride (c->version)
+                           * (size_t) std::max (nk, 1))) != cudaSuccess)
+    return cuda_fail (e, "reciprocal coefficients");
+  if ((e = launch_matrix_kco (c->version, (const double *) c->dkt.p, nk, (float *) c->dktf.p,
+                              st)) != cudaSuccess)
+    return cuda_fail (e, "matrix kernel");
+  if (nk > 0) launches++;
+  a.kco = (const float *) c->dktf.p;
   a.phf = (const float2 *) c->ph.p;
   a.nk = nk;
   if ((e = c->dself.ensure (sizeof (float) * 80)) != cudaSuccess)

@@ -78,9 +78,8 @@ struct Ctx {
   double dense_key[7] = {0, 0, 0, 0, 0, 0, 0};
   int dense_nk = 0;
   std::vector<double> h_dkt;
-  std::vector<float> h_dktf;
-  DevBuf dkt, dktf, dself;
-  uint64_t fp_dkt = 0, fp_dktf = 0;
+  DevBuf dkt, dktf, dself;   // FP64 rows, moment coefficients, diagonal moments
+  uint64_t fp_dkt = 0;
 
   // pinned, mapped mirror of sys->pos for the host entry points of the
   // mixed paths, whose kernels read the positions once
