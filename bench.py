@@ -291,8 +291,10 @@ def matrix_measure(lib, abi, L, torch, dev, pos, Lbox):
     11000 FP64 = 968 MB) at the reference split, on device memory: device
     time (CUDA events on the builder's stream, after one warm-up build) and
     the achieved store bandwidth, against the measured HBM copy rate.  The
-    builder evaluates the same pair-image terms as the FP64 product, 121
-    tensor entries each, so its FP64 pipe, not HBM, bounds it."""
+    FP64 builder evaluates every pair-image term of the reference split in
+    FP64, so the FP64 pipe bounds it.  The split-precision builder
+    (k_matrix_pairs: FP32 terms at its own split, each unordered pair once,
+    both blocks stored) is bound by its FP32 issue rate."""
     w = WORKLOAD
     s = L.System(w["version"], pos, (Lbox,) * 3, tratio=w["tratio"], eps=w["eps"])
     n = (3, 6, 11)[w["version"]] * w["n"]
@@ -339,7 +341,7 @@ def matrix_measure(lib, abi, L, torch, dev, pos, Lbox):
             "mixed": {"ms": ms32, "achieved_gbs": nbytes / (ms32 * 1e-3) / 1e9,
                       "hbm_frac": (nbytes / (ms32 * 1e-3) / 1e9) / peak if peak else None,
                       "max_err_over_max_entry": err32,
-                      "precision": "FP32 terms, FP64 entries (k_matrix_f32)"},
+                      "precision": "FP32 terms, FP64 entries (k_matrix_pairs)"},
             "bound": "fp64-pipe: every pair-image term of the reference split "
                      "(xi = sqrt(pi)/L, eps 1e-12) builds an 11 x 11 block in FP64"}
 
