@@ -27,9 +27,10 @@ _ip = C.POINTER(C.c_int)
 
 
 def build_oracle(force: bool = False) -> str:
-    """Compile oracle/oracle_ewald.c, oracle_bd.c and oracle_adjoint.cpp into
-    liboracle.so."""
-    srcs = [os.path.join(HERE, f) for f in ("oracle_ewald.c", "oracle_bd.c", "oracle_adjoint.cpp")
+    """Compile oracle/oracle_ewald.c, oracle_bd.c, oracle_adjoint.cpp and
+    oracle_lub.c into liboracle.so."""
+    srcs = [os.path.join(HERE, f) for f in ("oracle_ewald.c", "oracle_bd.c", "oracle_adjoint.cpp",
+                                            "oracle_lub.c")
             if os.path.exists(os.path.join(HERE, f))]
     if (not force and os.path.exists(ORACLE_SO)
             and all(os.path.getmtime(ORACLE_SO) >= os.path.getmtime(s) for s in srcs)):
@@ -307,6 +308,45 @@ class Oracle(_Backend):
 
     def xi_by_tratio(self, tratio):
         return float(self._L.oracle_xi_by_tratio(*self.box, float(tratio)))
+
+
+def lub_res2b(s):
+    """The ten lubrication-form resistance functions at distance s
+    (oracle/oracle_lub.c, src/two-body-res.c:31)."""
+    L = Oracle.lib()
+    out = np.zeros(10)
+    L.oracle_lub_res2b.argtypes = [C.c_double, _dp]
+    L.oracle_lub_res2b(float(s), _d(out))
+    return out
+
+
+def lub_minv(version, s):
+    """(M^inf)^-1 of two spheres at distance s: F 4 values, FT 10."""
+    L = Oracle.lib()
+    out = np.zeros(10)
+    L.oracle_lub_minv.argtypes = [C.c_int, C.c_double, _dp]
+    L.oracle_lub_minv(int(version), float(s), _d(out))
+    return out[:4] if version == 0 else out
+
+
+def calc_lub(version, pos, box=None, u=None, lubmin2=0.0, lubmax=0.0, shear_mode=0,
+             shear_shift=0.0):
+    """f = L u for equal spheres (src/lub.c:164-575); box None: an open
+    system."""
+    L = Oracle.lib()
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    np_ = pos.shape[0]
+    c = 3 if version == 0 else 6
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    f = np.zeros(c * np_)
+    periodic = box is not None
+    lx, ly, lz = box if periodic else (0.0, 0.0, 0.0)
+    L.oracle_calc_lub.argtypes = ([C.c_int, C.c_int, _dp, C.c_int] + [C.c_double] * 3
+                                  + [C.c_int] + [C.c_double] * 3 + [_dp, _dp])
+    L.oracle_calc_lub(int(version), np_, _d(pos), 1 if periodic else 0, float(lx), float(ly),
+                      float(lz), int(shear_mode), float(shear_shift), float(lubmin2),
+                      float(lubmax), _d(u), _d(f))
+    return f
 
 
 class Reference(_Backend):

@@ -106,3 +106,28 @@ refbd_run (void *h, unsigned long seed, double peclet, double dt, int nsteps, in
   free_bd (BD, lj);
   return 0;
 }
+
+/* f = L u, the reference's lubrication correction (src/lub.c:164-575) at
+ * the given lubmin2 / lubmax; version 0 (F) or 1 (FT) from the system */
+#include "lub.h"
+void
+refbd_calc_lub (void *h, double lubmin2, double lubmax, const double *u, double *f)
+{
+  struct stokes *sys = h;
+  sys->lubmin2 = lubmin2;
+  sys->lubmax = lubmax;
+  if (sys->version == 0) calc_lub_3f (sys, u, f);
+  else if (sys->version == 1) calc_lub_3ft (sys, u, f);
+  else calc_lub_3fts (sys, u, f);
+}
+
+/* the reference's two-body lubrication-form functions and (M^inf)^-1 */
+#include "two-body-res.h"
+void ref_res2b (double s, double *res) { scalar_two_body_res (s, res); }
+void scalar_minv_f (double s, double *r);
+void scalar_minv_ft (double s, double *r);
+void ref_minv (int version, double s, double *r)
+{
+  if (version == 0) scalar_minv_f (s, r);
+  else scalar_minv_ft (s, r);
+}

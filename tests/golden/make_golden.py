@@ -248,6 +248,76 @@ def nonewald_fixtures() -> dict:
     return out
 
 
+# (name, version, n, phi, position seed, periodic, lubmin2, lubmax, shear (mode, shift))
+LUB_CASES = [
+    ("lub_f_periodic", 0, 40, 0.30, 61, True, 2.0001 ** 2, 3.0, (0, 0.0)),
+    ("lub_ft_periodic", 1, 30, 0.30, 62, True, 2.0001 ** 2, 3.5, (0, 0.0)),
+    ("lub_f_open", 0, 25, 0.25, 63, False, 0.0, 4.0, (0, 0.0)),
+    ("lub_ft_open", 1, 20, 0.25, 64, False, 2.001 ** 2, 3.2, (0, 0.0)),
+    ("lub_ft_nolimit", 1, 12, 0.20, 65, True, 0.0, 0.0, (0, 0.0)),
+    ("lub_f_small_box", 0, 6, 0.25, 66, True, 0.0, 3.0, (0, 0.0)),
+    ("lub_f_shear1", 0, 30, 0.30, 67, True, 2.0001 ** 2, 3.0, (1, 2.3)),
+    ("lub_ft_shear2", 1, 20, 0.30, 68, True, 2.0001 ** 2, 3.0, (2, -1.7)),
+]
+
+
+def lub_fixtures() -> dict:
+    """The reference's lubrication correction f = L u (src/lub.c:164-575,
+    equal spheres) on small systems, and its two-body functions
+    (src/two-body-res.c:31, src/f.c:183, src/ft.c:414) on a grid of s."""
+    import ctypes as C
+    so = os.path.join(ROOT, "oracle", "_ref", "libstokes_ref_bd.so")
+    lib = C.CDLL(so)
+    dp = C.POINTER(C.c_double)
+    d = lambda a: None if a is None else a.ctypes.data_as(dp)  # noqa: E731
+    lib.ref_new.restype = C.c_void_p
+    lib.ref_new.argtypes = [C.c_int, C.c_int, dp, C.c_double, C.c_double, C.c_double]
+    lib.ref_free.argtypes = [C.c_void_p]
+    lib.ref_set_periodic.argtypes = [C.c_void_p, C.c_int]
+    lib.ref_set_misc.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_double]
+    lib.refbd_calc_lub.argtypes = [C.c_void_p, C.c_double, C.c_double, dp, dp]
+    lib.ref_res2b.argtypes = [C.c_double, dp]
+    lib.ref_minv.argtypes = [C.c_int, C.c_double, dp]
+    out = {}
+    grid = np.concatenate([2.0 + np.logspace(-6, 0, 25), np.linspace(3.05, 12.0, 20)])
+    res = np.zeros((len(grid), 22))
+    minv = np.zeros((2, len(grid), 22))
+    for q, sv in enumerate(grid):
+        lib.ref_res2b(float(sv), d(res[q]))
+        for v in (0, 1):
+            lib.ref_minv(v, float(sv), d(minv[v, q]))
+    out["grid_s"] = grid
+    out["grid_res2b"] = res[:, :10]
+    out["grid_minv_f"] = minv[0, :, :4]
+    out["grid_minv_ft"] = minv[1, :, :10]
+    for name, ver, n, phi, pseed, periodic, lubmin2, lubmax, shear in LUB_CASES:
+        pos, L = rsa_positions(n, phi, seed=pseed)
+        c = (3, 6)[ver]
+        u = np.random.default_rng(pseed + 1000).standard_normal(c * n)
+        h = lib.ref_new(ver, n, d(pos), L, L, L)
+        if not periodic:
+            lib.ref_set_periodic(h, 0)
+        if shear[0]:
+            lib.ref_set_misc(h, 0.0, shear[0], shear[1])
+        f = np.zeros(c * n)
+        lib.refbd_calc_lub(h, lubmin2, lubmax, d(u), d(f))
+        lib.ref_free(h)
+        out[f"{name}_meta"] = np.array([ver, n, L, 1.0 if periodic else 0.0, lubmin2, lubmax,
+                                        shear[0], shear[1]])
+        out[f"{name}_pos"] = pos
+        out[f"{name}_u"] = u
+        out[f"{name}_f"] = f
+    return out
+
+
+def write_lub(ref_root: str | None = None):
+    """Only the lubrication fixtures (tests/golden/lub.npz)."""
+    ref_root = ref_root or os.environ.get("LIBSTOKES_REF")
+    if not ref_root or build_reference(ref_root) is None:
+        raise SystemExit("usage: make_golden.py <libstokes checkout> (or set LIBSTOKES_REF)")
+    np.savez_compressed(os.path.join(HERE, "lub.npz"), **lub_fixtures())
+
+
 def main(ref_root: str | None = None):
     """ref_root: the libstokes checkout (argument or $LIBSTOKES_REF)."""
     ref_root = ref_root or os.environ.get("LIBSTOKES_REF")
@@ -424,6 +494,9 @@ def main(ref_root: str | None = None):
     # ---- Brownian dynamics (the reference's brownian.c) -------------------
     np.savez_compressed(os.path.join(HERE, "bd.npz"),
                         **bd_fixtures(), **bd_fixtures(BD_OPEN_CASES, periodic=False))
+
+    # ---- lubrication (the reference's lub.c and two-body functions) -------
+    np.savez_compressed(os.path.join(HERE, "lub.npz"), **lub_fixtures())
 
     # ---- struct layouts of the Brownian-dynamics interface ---------------
     json.dump(bd_layouts(ref_root), open(os.path.join(HERE, "bd_layouts.json"), "w"), indent=1)

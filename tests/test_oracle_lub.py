@@ -1,0 +1,48 @@
+"""The lubrication oracle (oracle/oracle_lub.c) against the reference's own
+outputs (tests/golden/lub.npz, made by tests/golden/make_golden.py from the
+compiled reference): the ten lubrication-form two-body functions of
+src/two-body-res.c:31 (regenerated here from the Jeffrey-Onishi
+recurrences), the far-field inverses of src/f.c:183 and src/ft.c:414, and
+f = L u of src/lub.c:164-575 on periodic, open, sheared, small-box and
+unlimited-range systems."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def lub():
+    return np.load(os.path.join(HERE, "golden", "lub.npz"))
+
+
+def test_two_body_functions(lub):
+    from oracle.oracle import lub_minv, lub_res2b
+    for q, s in enumerate(lub["grid_s"]):
+        mine = lub_res2b(s)
+        ref = lub["grid_res2b"][q]
+        # a function can be small against its singular parts: scale by those
+        scale = np.maximum(np.abs(ref), 1e-3)
+        assert np.all(np.abs(mine - ref) <= 2e-12 * scale), (s, mine - ref)
+        assert np.allclose(lub_minv(0, s), lub["grid_minv_f"][q], rtol=1e-13, atol=1e-15)
+        assert np.allclose(lub_minv(1, s), lub["grid_minv_ft"][q], rtol=1e-13, atol=1e-15)
+
+
+CASES = ["lub_f_periodic", "lub_ft_periodic", "lub_f_open", "lub_ft_open", "lub_ft_nolimit",
+         "lub_f_small_box", "lub_f_shear1", "lub_ft_shear2"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_calc_lub(lub, name):
+    from oracle.oracle import calc_lub
+    ver, n, L, periodic, lubmin2, lubmax, mode, shift = lub[f"{name}_meta"]
+    f = calc_lub(int(ver), lub[f"{name}_pos"], (L, L, L) if periodic else None,
+                 lub[f"{name}_u"], lubmin2=lubmin2, lubmax=lubmax, shear_mode=int(mode),
+                 shear_shift=shift)
+    ref = lub[f"{name}_f"]
+    assert np.linalg.norm(ref) > 0.0
+    assert rel_l2(f, ref) < 1e-12, rel_l2(f, ref)
