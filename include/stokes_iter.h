@@ -74,10 +74,14 @@ void solve_mob_3fts_0 (struct stokes *sys, struct iter *iter, const double *f,
  *   STOKES_GPU_SOLVE_RES     A = M (the resistance problems of
  *                            src/ewald-3f*.c: M x = b)
  *   STOKES_GPU_SOLVE_MOB_FTS A (u,o,s) = (u,o,0) - M (0,0,s) (FTS only)
+ *   STOKES_GPU_SOLVE_MOB_LUB A = I + M L, L the lubrication correction of
+ *                            calc_lub_3f / calc_lub_3ft (F and FT, equal
+ *                            spheres; the operator of src/ewald-3f.c:411
+ *                            and src/ewald-3ft.c, b = M f)
  * b, x [n] host buffers, n = np * {3, 6, 11}; x holds the start vector on
  * entry.  restart <= 0 and max <= 0 take 20 and 2000.  iters and res (may
  * be NULL) receive the operator applications and |b - A x| / |b|. */
-enum { STOKES_GPU_SOLVE_RES = 0, STOKES_GPU_SOLVE_MOB_FTS = 1 };
+enum { STOKES_GPU_SOLVE_RES = 0, STOKES_GPU_SOLVE_MOB_FTS = 1, STOKES_GPU_SOLVE_MOB_LUB = 2 };
 int stokes_gpu_solve (struct stokes *sys, int op, const double *b, double *x, int restart,
                       int max, double eps, int *iters, double *res);
 

@@ -34,6 +34,7 @@ FP64 = 0
 MIXED = 1
 SOLVE_RES = 0
 SOLVE_MOB_FTS = 1
+SOLVE_MOB_LUB = 2
 
 
 class TrajFrame(C.Structure):
@@ -267,6 +268,13 @@ _SIGS = {
     "stokes_gpu_batch_atimes": (C.c_int, [C.c_void_p, _dp, _dp]),
     "stokes_gpu_batch_stats": (C.c_int, [C.c_void_p, _dp]),
     "stokes_gpu_batch_split": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
+    "stokes_gpu_lub": (C.c_int, [_SP, C.c_int, _dp, _dp]),
+    "stokes_gpu_lub_dev": (C.c_int, [_SP, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p]),
+    "stokes_gpu_lub_coefficients": (C.c_int, [_dp]),
+    "calc_lub_3f": (None, [_SP, _dp, _dp]),
+    "calc_lub_3ft": (None, [_SP, _dp, _dp]),
+    "calc_lub_3fts": (None, [_SP, _dp, _dp]),
     "stokes_gpu_batch_bd": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int, _dp,
                                       _dp, C.c_ulonglong, C.c_int, _dp]),
     "stokes_gpu_vjp": (C.c_int, [_SP, _dp, _dp, _dp, _dp, _dp]),

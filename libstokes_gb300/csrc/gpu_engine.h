@@ -110,6 +110,9 @@ void build_ktable (const struct stokes *sys, std::vector<double> &kt);
 void build_particles (const struct stokes *sys, int mode, std::vector<double> &pp,
                       bool open = false, const struct stokes *split = nullptr);
 int release_ctx (const struct stokes *sys);
+// f = L u on device buffers (lub.cu): version 0 (F) or 1 (FT)
+int lub_dev (const struct stokes *sys, int version, const double *d_pos, const double *d_u,
+             double *d_f, cudaStream_t st);
 // check sys and bring the context's device tables up to date.  tables: 1
 // builds the FP64 image and reciprocal tables of the FP64 product (the
 // tuned split where it applies), 2 those of the dense builder (the

@@ -775,6 +775,15 @@ solve_own (struct stokes *sys, int op, bool force_open, const double *b, double 
       k_fts_mob_out<<<grid_of (n), KT, 0, st>>> (np, in, out, out);
       return STOKES_GPU_OK;
     };
+  else if (op == STOKES_GPU_SOLVE_MOB_LUB)
+    // (I + M L) u: the lubricated mobility problem of src/ewald-3f.c:411-445
+    A = [&] (const double *in, double *out) -> int {
+      int r = lub_dev (sys, sys->version, d_pos, in, tmp, st);
+      if (!r) r = atimes_dev (c, d_pos, tmp, out, st, false);
+      if (r) return r;
+      k_vaxpby<<<grid_of (n), KT, 0, st>>> (n, 1.0, in, 1.0, out, out);
+      return STOKES_GPU_OK;
+    };
   else
     A = [&] (const double *in, double *out) -> int {
       return atimes_dev (c, d_pos, in, out, st, false);
@@ -795,6 +804,14 @@ solve_own (struct stokes *sys, int op, bool force_open, const double *b, double 
           int r = atimes_fp64_dev (c, d_pos, tmp64, out, st, false);
           if (r) return r;
           k_fts_mob_out<<<grid_of (n), KT, 0, st>>> (np, in, out, out);
+          return STOKES_GPU_OK;
+        };
+      else if (op == STOKES_GPU_SOLVE_MOB_LUB)
+        A64 = [&] (const double *in, double *out) -> int {
+          int r = lub_dev (sys, sys->version, d_pos, in, tmp64, st);
+          if (!r) r = atimes_fp64_dev (c, d_pos, tmp64, out, st, false);
+          if (r) return r;
+          k_vaxpby<<<grid_of (n), KT, 0, st>>> (n, 1.0, in, 1.0, out, out);
           return STOKES_GPU_OK;
         };
       else
@@ -1021,10 +1038,13 @@ stokes_gpu_solve (struct stokes *sys, int op, const double *b, double *x, int re
 {
   clear_error ();
   if (!sys || !b || !x) return set_error (STOKES_GPU_EINVAL, "NULL argument");
-  if (op != STOKES_GPU_SOLVE_RES && op != STOKES_GPU_SOLVE_MOB_FTS)
+  if (op != STOKES_GPU_SOLVE_RES && op != STOKES_GPU_SOLVE_MOB_FTS
+      && op != STOKES_GPU_SOLVE_MOB_LUB)
     return set_error (STOKES_GPU_EINVAL, "unknown problem %d", op);
   if (op == STOKES_GPU_SOLVE_MOB_FTS && sys->version != 2)
     return set_error (STOKES_GPU_EINVAL, "the FTS mobility problem needs version 2");
+  if (op == STOKES_GPU_SOLVE_MOB_LUB && sys->version > 1)
+    return set_error (STOKES_GPU_EINVAL, "the lubricated mobility problem serves F and FT");
   Settings S;
   if (restart > 0) S.m = restart;
   if (max > 0) S.max = max;

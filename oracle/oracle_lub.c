@@ -259,6 +259,14 @@ ol_init (void)
   ol_ready = 1;
 }
 
+/* the series coefficients, out[10 * 26] */
+void
+oracle_lub_coef (double *out)
+{
+  ol_init ();
+  memcpy (out, ol_coef, sizeof ol_coef);
+}
+
 /* res[10]: the lubrication-form resistance functions at distance s */
 void
 oracle_lub_res2b (double s, double *res)

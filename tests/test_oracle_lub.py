@@ -46,3 +46,27 @@ def test_calc_lub(lub, name):
     ref = lub[f"{name}_f"]
     assert np.linalg.norm(ref) > 0.0
     assert rel_l2(f, ref) < 1e-12, rel_l2(f, ref)
+
+
+def test_product_coefficients_match_the_oracle():
+    """The library's own host-side generation of the series coefficients
+    (double precision, libstokes_gb300/csrc/lub.cu) against the oracle's
+    (long double): no GPU needed."""
+    import ctypes as C
+    from libstokes_gb300 import abi
+    from oracle.oracle import Oracle
+    lib = abi.load()
+    mine = np.zeros(260)
+    assert lib.stokes_gpu_lub_coefficients(mine.ctypes.data_as(abi._dp)) == 0
+    L = Oracle.lib()
+    ref = np.zeros(260)
+    L.oracle_lub_coef.argtypes = [abi._dp]
+    L.oracle_lub_coef(ref.ctypes.data_as(abi._dp))
+    mine, ref = mine.reshape(10, 26), ref.reshape(10, 26)
+    # the terms are c_m / s^(2m) with s >= 2: compare each coefficient's
+    # contribution at contact (the difference of the two precisions is below
+    # 1e-15 there; in the coefficients it reaches 3e-11 of the largest, high
+    # orders of x11a, from the cancellation against the singular part)
+    for g in range(10):
+        for m in range(26):
+            assert abs(mine[g, m] - ref[g, m]) * 0.25 ** m <= 1e-15, (g, m)
