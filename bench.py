@@ -346,6 +346,71 @@ def matrix_measure(lib, abi, L, torch, dev, pos, Lbox):
                      "(xi = sqrt(pi)/L, eps 1e-12) builds an 11 x 11 block in FP64"}
 
 
+def lub_measure(lib, abi, L, torch, dev, reps: int = 20):
+    """Lubrication correction (calc_lub_3ft, src/lub.c:370) of FT, N = 1000,
+    phi 0.35 (rsa seed 71), lubmax 3, lubmin2 2.0001^2, FP64 on device
+    buffers: device time per application (CUDA events over `reps` after
+    three warm-ups), the close pairs it visits, and one lubricated mobility
+    solve (I + M L) u = M f (STOKES_GPU_SOLVE_MOB_LUB, mixed product with
+    FP64 refinement) against the CPU oracle's time for one application on
+    all host threads."""
+    from libstokes_gb300.workloads import rsa_positions
+    from oracle.oracle import calc_lub
+    n = 1000
+    pos, Lb = rsa_positions(n, 0.35, seed=71)
+    s = L.System(1, pos, (Lb,) * 3)
+    s.s.lubmin2 = 2.0001 ** 2
+    s.s.lubmax = 3.0
+    u = np.random.default_rng(72).standard_normal(6 * n)
+    d_pos = torch.tensor(pos, dtype=torch.float64, device=dev).contiguous()
+    d_u = torch.tensor(u, dtype=torch.float64, device=dev)
+    d_f = torch.empty_like(d_u)
+    st = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(st.cuda_stream)
+
+    def apply():
+        abi.check(lib.stokes_gpu_lub_dev(s.sp, 1, C.c_void_p(d_pos.data_ptr()),
+                                         C.c_void_p(d_u.data_ptr()), C.c_void_p(d_f.data_ptr()),
+                                         sp))
+    for _ in range(3):
+        apply()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        apply()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    f = d_f.cpu().numpy()
+    d = pos[None, :, :] - pos[:, None, :]
+    d -= Lb * np.rint(d / Lb)
+    r2 = (d ** 2).sum(-1)
+    close = int(((r2 > 0) & (r2 < 9.0)).sum())
+    t0 = time.perf_counter()
+    fo = calc_lub(1, pos, (Lb,) * 3, u, lubmin2=2.0001 ** 2, lubmax=3.0)
+    cpu_s = time.perf_counter() - t0
+    err = float(np.linalg.norm(f - fo) / np.linalg.norm(fo))
+    # the lubricated mobility problem with the mixed product
+    s.set_precision(abi.MIXED)
+    b = s.atimes(np.random.default_rng(73).standard_normal(6 * n))
+    x = np.zeros(6 * n)
+    it, res = C.c_int(), C.c_double()
+    t0 = time.perf_counter()
+    abi.check(lib.stokes_gpu_solve(s.sp, abi.SOLVE_MOB_LUB, b.ctypes.data_as(abi._dp),
+                                   x.ctypes.data_as(abi._dp), 30, 2000, 1e-10, C.byref(it),
+                                   C.byref(res)))
+    solve_s = time.perf_counter() - t0
+    s.close()
+    return {"workload": "lub_ft_n1000_phi0.35_lubmax3", "precision": "fp64",
+            "ms_per_application": ms, "applications_per_s": 1000.0 / ms,
+            "close_pairs_ordered": close, "rel_err_vs_oracle": err,
+            "solve_mob_lub": {"wall_s": solve_s, "applications": it.value, "residual": res.value,
+                              "precision": "mixed product, FP64 refinement"},
+            "cpu_baseline": {"applications_per_s": 1.0 / cpu_s, "cores": 1, "kind": "port",
+                             "sample": "one application of the oracle (oracle_calc_lub, serial)"}}
+
+
 def open_measure(lib, abi, L, torch, dev, pos, reps: int = 20):
     """Free-space FTS product (atimes_nonewald_3all, src/non-ewald.c:330-481)
     of the bench's N = 1000 spheres as an open system, FP64, device buffers:
@@ -1049,6 +1114,8 @@ def run_gpu(args):
         line["open"] = open_measure(lib, abi, L, torch, dev, pos)
     if not args.no_solve and not fp64:
         line["solve"] = solve_measure(lib, abi, L, torch, dev, pos, Lbox, ms)
+    if not args.no_lub:
+        line["lub"] = lub_measure(lib, abi, L, torch, dev)
     if not args.no_scale and not fp64:
         line["scale"] = scale_measure(lib, abi, L, torch, dev)
     if not args.no_bd:
@@ -1089,6 +1156,7 @@ def main():
                     help="skip the larger-N legs of the mixed product")
     ap.add_argument("--no-open", action="store_true",
                     help="skip the free-space (non-periodic) operator leg")
+    ap.add_argument("--no-lub", action="store_true", help="skip the lubrication leg")
     ap.add_argument("--n", type=int, default=None,
                     help="override N (smaller cases for profiler captures)")
     args = ap.parse_args()
