@@ -911,8 +911,13 @@ dropin_engine (struct BD_params *BD, const char *fn)
   if (sys->version < 0 || sys->version > 1)
     dropin_die (fn, "the device BD serves the F and FT versions");
   if (sys->np != sys->nm) dropin_die (fn, "the device BD serves systems without fixed particles");
-  if (BD->flag_lub || BD->flag_lub_B || BD->flag_mat)
-    dropin_die (fn, "lubrication and matrix noise are not on the device path");
+  // flag_lub: the velocities solve the lubricated mobility problem; the
+  // Brownian lubrication force (flag_lub_B) is never set by the reference's
+  // BD_params_init (its pair check is commented out, src/brownian.c:161-180)
+  if (BD->flag_lub_B || BD->flag_mat)
+    dropin_die (fn, "the lubrication noise and matrix noise are not on the device path");
+  if (BD->flag_lub && (sys->a || sys->slip))
+    dropin_die (fn, "lubrication serves equal spheres without slip");
   if (BD->n_minv <= 0) dropin_die (fn, "n_minv <= 0 (matrix noise) is not on the device path");
   if (BD->br || BD->bonds || BD->ev || BD->ang || BD->ev_dh || BD->cf)
     dropin_die (fn, "only EV_LJ among the interactions is on the device path");
@@ -1042,6 +1047,20 @@ dropin_overlap (stokes_gpu_bd *b, const double *d_pos, double rmin, const char *
 
 // q += h dQ/dt(q, o) (src/ode-quaternion.c:60-105 with the inverse of the
 // quaternion rate matrix written out)
+// the velocities of a drop-in step: u = M f, or with lubrication
+// u = (I + M L)^-1 M f (src/brownian.c:2420-2428 through solve_mix_3all)
+static int
+dropin_velocity (stokes_gpu_bd *b, struct BD_params *BD, const double *d_pos)
+{
+  if (!BD->flag_lub)
+    return bd_prod (b, d_pos, (const double *) b->f.p, (double *) b->u.p);
+  int it = 0;
+  const int rc = lub_mobility_dev (b->c, BD->sys, d_pos, (const double *) b->f.p,
+                                   (double *) b->u.p, b->c->stream, &it);
+  b->products += it + 1;
+  return rc;
+}
+
 static void
 quaternion_step (int nm, const double *o, double h, const double *q0, double *q)
 {
@@ -1161,7 +1180,7 @@ redo_scale:
     // 1: velocity at the current configuration, Euler half step from x
     const Flow fl = bd_flow (sys);
     check_rc (bd_forces (b, cur, fact), fn);
-    check_rc (bd_prod (b, cur, (const double *) b->f.p, (double *) b->u.p), fn);
+    check_rc (dropin_velocity (b, BD, cur), fn);
     k_bd_euler<<<gridn (nm), 256, 0, st>>> (nm, C, dx, (const double *) b->u.p, cur, fl,
                                             0.5 * dt_local, dmid);
     if (check && dropin_overlap (b, dmid, BD->rmin, fn) > 0)
@@ -1186,7 +1205,7 @@ redo_scale:
     check_rc (prepare (b->c, sys, false), fn);
     const Flow fm = bd_flow (sys);
     check_rc (bd_forces (b, dmid, fact), fn);
-    check_rc (bd_prod (b, dmid, (const double *) b->f.p, (double *) b->u.p), fn);
+    check_rc (dropin_velocity (b, BD, dmid), fn);
     k_bd_euler<<<gridn (nm), 256, 0, st>>> (nm, C, dx, (const double *) b->u.p, dmid, fm,
                                             dt_local, dnew);
     if (check && dropin_overlap (b, dnew, BD->rmin, fn) > 0)

@@ -110,6 +110,10 @@ void build_ktable (const struct stokes *sys, std::vector<double> &kt);
 void build_particles (const struct stokes *sys, int mode, std::vector<double> &pp,
                       bool open = false, const struct stokes *split = nullptr);
 int release_ctx (const struct stokes *sys);
+// u = (I + M L)^-1 M f on device buffers (krylov.cu), F and FT, the
+// context's product at positions d_pos, GMRES settings from sys->it
+int lub_mobility_dev (Ctx *c, struct stokes *sys, const double *d_pos, const double *d_f,
+                      double *d_u, cudaStream_t st, int *iters);
 // f = L u on device buffers (lub.cu): version 0 (F) or 1 (FT)
 int lub_dev (const struct stokes *sys, int version, const double *d_pos, const double *d_u,
              double *d_f, cudaStream_t st);

@@ -834,6 +834,37 @@ solve_own (struct stokes *sys, int op, bool force_open, const double *b, double 
   return rc;
 }
 
+// the lubricated mobility problem of a Brownian step, on device vectors in
+// the particle layout: d_u = (I + M L)^-1 M d_f at positions d_pos, the
+// product of the context as prepared, GMRES settings from sys->it, start 0
+// (src/ewald-3f.c:447-490, src/ewald-3ft.c)
+int
+lub_mobility_dev_impl (Ctx *c, struct stokes *sys, const double *d_pos, const double *d_f,
+                       double *d_u, cudaStream_t st, int *iters)
+{
+  const int n = NCOMP (sys->version) * sys->np;
+  Krylov &K = t_kry;
+  cudaError_t e;
+  if ((e = K.b.ensure (sizeof (double) * n)) != cudaSuccess
+      || (e = K.t.ensure (sizeof (double) * n)) != cudaSuccess)
+    return cuda_fail (e, "solve buffers");
+  double *b = (double *) K.b.p, *tmp = (double *) K.t.p;
+  int rc = atimes_dev (c, d_pos, d_f, b, st, false);
+  if (rc) return rc;
+  if ((e = cudaMemsetAsync (d_u, 0, sizeof (double) * n, st)) != cudaSuccess)
+    return cuda_fail (e, "solve start");
+  Apply A = [&] (const double *in, double *out) -> int {
+    int r = lub_dev (sys, sys->version, d_pos, in, tmp, st);
+    if (!r) r = atimes_dev (c, d_pos, tmp, out, st, false);
+    if (r) return r;
+    k_vaxpby<<<grid_of (n), KT, 0, st>>> (n, 1.0, in, 1.0, out, out);
+    return STOKES_GPU_OK;
+  };
+  const Settings S = settings_of (sys->it);
+  double res = 0.0;
+  return gmres_dev (n, b, d_u, A, S.m, S.max, S.eps, st, iters, &res, S.dbg);
+}
+
 // solve with a caller's host operator (vectors still on the device)
 int
 solve_foreign (int n, const double *b, double *x,
@@ -873,6 +904,15 @@ solve_foreign (int n, const double *b, double *x,
 }
 
 }  // namespace
+}  // namespace lsg
+
+namespace lsg {
+int
+lub_mobility_dev (Ctx *c, struct stokes *sys, const double *d_pos, const double *d_f,
+                  double *d_u, cudaStream_t st, int *iters)
+{
+  return lub_mobility_dev_impl (c, sys, d_pos, d_f, d_u, st, iters);
+}
 }  // namespace lsg
 
 using namespace lsg;

@@ -329,99 +329,160 @@ lub_apply (const double e[3], const double *sc, bool self, double w, const doubl
     }
 }
 
+// one pair image (separation d, source velocity uj) into the target's sums;
+// self: the particle's own image (both halves of the pair)
+template <int V>
+__device__ __forceinline__ void
+lub_pair (const LubArgs &a, const double d[3], const double *ui, const double *uj, bool self,
+          double *acc)
+{
+  constexpr int NF = V == 0 ? 4 : 10;
+  double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  if (r2 < a.lubmin2) r2 = a.lubmin2;
+  const double r = sqrt (r2), ri = 1.0 / r;
+  const double e[3] = {d[0] * ri, d[1] * ri, d[2] * ri};
+  double res[NF], inf[NF];
+  lub_res (r, NF, res);
+  lub_minv<V> (r, inf);
+  double s11[5], s12[5];
+  s11[0] = res[0] - inf[0];
+  s12[0] = res[1] - inf[1];
+  s11[1] = res[2] - inf[2];
+  s12[1] = res[3] - inf[3];
+  if (V == 1)
+    {
+      s11[2] = res[4] - inf[4];
+      s12[2] = res[5] - inf[5];
+      s11[3] = res[6] - inf[6];
+      s12[3] = res[7] - inf[7];
+      s11[4] = res[8] - inf[8];
+      s12[4] = res[9] - inf[9];
+    }
+  lub_apply<V> (e, s11, true, 1.0, ui, acc);
+  lub_apply<V> (e, s12, false, 1.0, uj, acc);
+  if (self)
+    {
+      const double me[3] = {-e[0], -e[1], -e[2]};
+      lub_apply<V> (me, s11, true, 1.0, ui, acc);
+      lub_apply<V> (me, s12, false, 1.0, ui, acc);
+    }
+}
+
+constexpr int LUB_QCAP = 64;
+
+// A warp per target i.  The lanes scan the sources in FP32 (the FP64 pipe of
+// this GPU is 1/64 of FP32) and queue the candidates; 32 queued candidates
+// are then evaluated in FP64 at once, one per lane.  With a periodic,
+// unsheared box and lubmax below half the box, a pair has at most one image
+// within lubmax: the candidate test is its minimum image (with a margin for
+// the FP32 rounding) and the evaluation takes that image alone, if the
+// reference's image cube holds it.  Otherwise every source is a candidate
+// (or those whose minimum image is within lubmax, unsheared) and its whole
+// image cube is walked in FP64.
 template <int V>
 __global__ void __launch_bounds__ (256)
 k_lub (LubArgs a)
 {
   constexpr int C = V == 0 ? 3 : 6;
-  constexpr int NF = V == 0 ? 4 : 10;
-  const int lane = threadIdx.x & 31;
-  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (i >= a.np) return;
+  __shared__ int s_q[8][LUB_QCAP];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int i = blockIdx.x * 8 + wib;
+  if (i >= a.np) return;   // uniform over the warp
+  int *q = s_q[wib];
   const double xi[3] = {a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]};
   double ui[C], acc[C];
 #pragma unroll
-  for (int q = 0; q < C; q++)
+  for (int k = 0; k < C; k++)
     {
-      ui[q] = a.u[C * i + q];
-      acc[q] = 0.0;
+      ui[k] = a.u[C * i + k];
+      acc[k] = 0.0;
     }
-  const bool reject = a.periodic && a.shear_mode == 0 && a.lubmax2 > 0.0;
-  for (int j = lane; j < a.np; j += 32)
+  const bool unsheared = a.periodic && a.shear_mode == 0;
+  const double lmin = fmin (a.lx, fmin (a.ly, a.lz));
+  const bool single = unsheared && a.lubmax2 > 0.0 && 4.0 * a.lubmax2 <= lmin * lmin;
+  const bool test = a.lubmax2 > 0.0 && (unsheared || !a.periodic);
+  const float cut2 = (float) a.lubmax2 * 1.0001f + 1e-6f;
+  const float lxf = (float) a.lx, lyf = (float) a.ly, lzf = (float) a.lz;
+  const float ilxf = 1.0f / lxf, ilyf = 1.0f / lyf, ilzf = 1.0f / lzf;
+  const unsigned lt = (1u << lane) - 1u;
+
+  auto evaluate = [&] (int j) {
+    double uj[C];
+#pragma unroll
+    for (int k = 0; k < C; k++) uj[k] = a.u[C * j + k];
+    const double r0[3] = {a.pos[3 * j] - xi[0], a.pos[3 * j + 1] - xi[1], a.pos[3 * j + 2] - xi[2]};
+    if (single)
+      {
+        // the one image within lubmax, if the reference's cube holds it
+        const double n0 = -rint (r0[0] / a.lx), n1 = -rint (r0[1] / a.ly),
+                     n2 = -rint (r0[2] / a.lz);
+        if (fabs (n0) > a.imx || fabs (n1) > a.imy || fabs (n2) > a.imz) return;
+        const double d[3] = {r0[0] + n0 * a.lx, r0[1] + n1 * a.ly, r0[2] + n2 * a.lz};
+        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (r2 == 0.0 || !(r2 < a.lubmax2)) return;
+        lub_pair<V> (a, d, ui, uj, j == i, acc);
+        return;
+      }
+    // the reference visits the pair once, from its lower index, with the
+    // image offsets o(n) of its loop (which need not be symmetric under a
+    // shift that accumulates): d = x_j + o - x_i for j > i, the negated
+    // separation x_j - o - x_i for j < i, and both signs for j == i
+    const double sg = (j >= i) ? 1.0 : -1.0;
+    for (int ix = -a.imx; ix <= a.imx; ix++)
+      {
+        double ox = a.lx * ix;
+        for (int iy = -a.imy; iy <= a.imy; iy++)
+          {
+            const double oy = a.ly * iy;
+            for (int iz = -a.imz; iz <= a.imz; iz++)
+              {
+                const double oz = a.lz * iz;
+                if (a.shear_mode == 1) ox += iy * a.shift;
+                else if (a.shear_mode == 2) ox += iz * a.shift;
+                const double d[3] = {r0[0] + sg * ox, r0[1] + sg * oy, r0[2] + sg * oz};
+                const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                if (r2 == 0.0 || (a.lubmax2 > 0.0 && !(r2 < a.lubmax2))) continue;
+                lub_pair<V> (a, d, ui, uj, j == i, acc);
+              }
+          }
+      }
+  };
+
+  int qn = 0;
+  for (int jb = 0; jb < a.np; jb += 32)
     {
-      const double pj[3] = {a.pos[3 * j], a.pos[3 * j + 1], a.pos[3 * j + 2]};
-      if (reject || (!a.periodic && a.lubmax2 > 0.0))
+      const int j = jb + lane;
+      bool cand = j < a.np;
+      if (cand && test)
         {
-          // the nearest image bounds every image from below
-          double d0 = pj[0] - xi[0], d1 = pj[1] - xi[1], d2 = pj[2] - xi[2];
+          // FP32 minimum-image distance (the box wrap only when periodic)
+          float dx = (float) (a.pos[3 * j] - xi[0]), dy = (float) (a.pos[3 * j + 1] - xi[1]),
+                dz = (float) (a.pos[3 * j + 2] - xi[2]);
           if (a.periodic)
             {
-              d0 -= a.lx * rint (d0 / a.lx);
-              d1 -= a.ly * rint (d1 / a.ly);
-              d2 -= a.lz * rint (d2 / a.lz);
+              dx -= lxf * rintf (dx * ilxf);
+              dy -= lyf * rintf (dy * ilyf);
+              dz -= lzf * rintf (dz * ilzf);
             }
-          if (!(d0 * d0 + d1 * d1 + d2 * d2 < a.lubmax2)) continue;
+          cand = dx * dx + dy * dy + dz * dz < cut2;
         }
-      double uj[C];
-#pragma unroll
-      for (int q = 0; q < C; q++) uj[q] = a.u[C * j + q];
-      // the reference visits the pair once, from its lower index, with the
-      // image offsets o(n) of its loop (which need not be symmetric under a
-      // shift that accumulates): d = x_j + o - x_i for j > i, the negated
-      // separation x_j - o - x_i for j < i, and both signs for j == i
-      const double sg = (j >= i) ? 1.0 : -1.0;
-      const double r0[3] = {pj[0] - xi[0], pj[1] - xi[1], pj[2] - xi[2]};
-      for (int ix = -a.imx; ix <= a.imx; ix++)
+      const unsigned b = __ballot_sync (0xffffffffu, cand);
+      if (cand) q[qn + __popc (b & lt)] = j;
+      qn += __popc (b);
+      __syncwarp ();
+      if (qn >= 32)
         {
-          double ox = a.lx * ix;
-          for (int iy = -a.imy; iy <= a.imy; iy++)
-            {
-              const double oy = a.ly * iy;
-              for (int iz = -a.imz; iz <= a.imz; iz++)
-                {
-                  const double oz = a.lz * iz;
-                  if (a.shear_mode == 1) ox += iy * a.shift;
-                  else if (a.shear_mode == 2) ox += iz * a.shift;
-                  const double d[3] = {r0[0] + sg * ox, r0[1] + sg * oy, r0[2] + sg * oz};
-                  double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-                  if (r2 == 0.0 || (a.lubmax2 > 0.0 && !(r2 < a.lubmax2))) continue;
-                  if (r2 < a.lubmin2) r2 = a.lubmin2;
-                  const double r = sqrt (r2);
-                  const double e[3] = {d[0] / r, d[1] / r, d[2] / r};
-                  double res[NF], inf[NF];
-                  lub_res (r, NF, res);
-                  lub_minv<V> (r, inf);
-                  double s11[5], s12[5];
-                  s11[0] = res[0] - inf[0];
-                  s12[0] = res[1] - inf[1];
-                  s11[1] = res[2] - inf[2];
-                  s12[1] = res[3] - inf[3];
-                  if (V == 1)
-                    {
-                      s11[2] = res[4] - inf[4];
-                      s12[2] = res[5] - inf[5];
-                      s11[3] = res[6] - inf[6];
-                      s12[3] = res[7] - inf[7];
-                      s11[4] = res[8] - inf[8];
-                      s12[4] = res[9] - inf[9];
-                    }
-                  lub_apply<V> (e, s11, true, 1.0, ui, acc);
-                  lub_apply<V> (e, s12, false, 1.0, uj, acc);
-                  if (j == i)
-                    {
-                      const double me[3] = {-e[0], -e[1], -e[2]};
-                      lub_apply<V> (me, s11, true, 1.0, ui, acc);
-                      lub_apply<V> (me, s12, false, 1.0, ui, acc);
-                    }
-                }
-            }
+          evaluate (q[qn - 32 + lane]);
+          qn -= 32;
+          __syncwarp ();
         }
     }
+  if (lane < qn) evaluate (q[lane]);
 #pragma unroll
-  for (int q = 0; q < C; q++)
+  for (int k = 0; k < C; k++)
     {
-      const double v = warp_sum (acc[q]);
-      if (lane == 0) a.f[C * i + q] = v;
+      const double v = warp_sum (acc[k]);
+      if (lane == 0) a.f[C * i + k] = v;
     }
 }
 
