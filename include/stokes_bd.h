@@ -149,8 +149,10 @@ int BD_get_n (struct stokes *sys);
 void BD_calc_FB (struct BD_params *BD, double *z);
 /* src/brownian.c:2352-2560 (scheme 0, F and FT, quaternions q when given,
  * constant force F/T, EV_LJ repulsion, imposed flow and shear, dt halving on
- * overlap when sys->rmin == 0 and BD->rmin > 0): one mid-point step with
- * noise from BD_calc_FB; returns the dt done.  The products run on the GPU
+ * overlap when sys->rmin == 0 and BD->rmin > 0; with BD->flag_lub the
+ * velocities solve (I + M L) u = M f on the device, GMRES settings from
+ * sys->it): one mid-point step with noise from BD_calc_FB; returns the dt
+ * done.  The products run on the GPU
  * in the precision set for sys (stokes_gpu_set_precision). */
 double BD_evolve_mid (double t, struct BD_params *BD, double *x, double *q, double dt);
 
