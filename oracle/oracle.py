@@ -311,22 +311,22 @@ class Oracle(_Backend):
 
 
 def lub_res2b(s):
-    """The ten lubrication-form resistance functions at distance s
+    """The 22 lubrication-form resistance functions at distance s
     (oracle/oracle_lub.c, src/two-body-res.c:31)."""
     L = Oracle.lib()
-    out = np.zeros(10)
+    out = np.zeros(22)
     L.oracle_lub_res2b.argtypes = [C.c_double, _dp]
     L.oracle_lub_res2b(float(s), _d(out))
     return out
 
 
 def lub_minv(version, s):
-    """(M^inf)^-1 of two spheres at distance s: F 4 values, FT 10."""
+    """(M^inf)^-1 of two spheres at distance s: F 4 values, FT 10, FTS 22."""
     L = Oracle.lib()
-    out = np.zeros(10)
+    out = np.zeros(22)
     L.oracle_lub_minv.argtypes = [C.c_int, C.c_double, _dp]
     L.oracle_lub_minv(int(version), float(s), _d(out))
-    return out[:4] if version == 0 else out
+    return out[:(4, 10, 22)[version]]
 
 
 def calc_lub(version, pos, box=None, u=None, lubmin2=0.0, lubmax=0.0, shear_mode=0,
@@ -336,7 +336,7 @@ def calc_lub(version, pos, box=None, u=None, lubmin2=0.0, lubmax=0.0, shear_mode
     L = Oracle.lib()
     pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
     np_ = pos.shape[0]
-    c = 3 if version == 0 else 6
+    c = (3, 6, 11)[version]
     u = np.ascontiguousarray(u, dtype=np.float64)
     f = np.zeros(c * np_)
     periodic = box is not None

@@ -126,8 +126,10 @@ refbd_calc_lub (void *h, double lubmin2, double lubmax, const double *u, double 
 void ref_res2b (double s, double *res) { scalar_two_body_res (s, res); }
 void scalar_minv_f (double s, double *r);
 void scalar_minv_ft (double s, double *r);
+void scalar_minv_fts (double s, double *r);
 void ref_minv (int version, double s, double *r)
 {
   if (version == 0) scalar_minv_f (s, r);
-  else scalar_minv_ft (s, r);
+  else if (version == 1) scalar_minv_ft (s, r);
+  else scalar_minv_fts (s, r);
 }

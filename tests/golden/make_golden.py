@@ -258,6 +258,9 @@ LUB_CASES = [
     ("lub_f_small_box", 0, 6, 0.25, 66, True, 0.0, 3.0, (0, 0.0)),
     ("lub_f_shear1", 0, 30, 0.30, 67, True, 2.0001 ** 2, 3.0, (1, 2.3)),
     ("lub_ft_shear2", 1, 20, 0.30, 68, True, 2.0001 ** 2, 3.0, (2, -1.7)),
+    ("lub_fts_periodic", 2, 24, 0.30, 69, True, 2.0001 ** 2, 3.0, (0, 0.0)),
+    ("lub_fts_open", 2, 15, 0.25, 70, False, 2.001 ** 2, 3.5, (0, 0.0)),
+    ("lub_fts_shear1", 2, 16, 0.30, 71, True, 2.0001 ** 2, 3.0, (1, 1.9)),
 ]
 
 
@@ -286,13 +289,17 @@ def lub_fixtures() -> dict:
         lib.ref_res2b(float(sv), d(res[q]))
         for v in (0, 1):
             lib.ref_minv(v, float(sv), d(minv[v, q]))
+    minv_fts = np.zeros((len(grid), 22))
+    for q, sv in enumerate(grid):
+        lib.ref_minv(2, float(sv), d(minv_fts[q]))
     out["grid_s"] = grid
-    out["grid_res2b"] = res[:, :10]
+    out["grid_res2b"] = res
     out["grid_minv_f"] = minv[0, :, :4]
     out["grid_minv_ft"] = minv[1, :, :10]
+    out["grid_minv_fts"] = minv_fts
     for name, ver, n, phi, pseed, periodic, lubmin2, lubmax, shear in LUB_CASES:
         pos, L = rsa_positions(n, phi, seed=pseed)
-        c = (3, 6)[ver]
+        c = (3, 6, 11)[ver]
         u = np.random.default_rng(pseed + 1000).standard_normal(c * n)
         h = lib.ref_new(ver, n, d(pos), L, L, L)
         if not periodic:
