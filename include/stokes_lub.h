@@ -6,8 +6,8 @@
  * sqrt(sys->lubmin2)) of the two-sphere resistance minus its far-field
  * part, with the lattice images of a periodic system in the cube
  * |n_x,y,z| <= lubmax / L + 1 (src/lub.c:129-157).  Errors (unequal radii,
- * slip, the FTS version) are reported as the other drop-in entry points
- * report them (stokes_gpu_last_error; exit unless the error mode is 1). */
+ * slip) are reported as the other drop-in entry points report them
+ * (stokes_gpu_last_error; exit unless the error mode is 1). */
 #ifndef STOKES_LUB_H
 #define STOKES_LUB_H
 
@@ -18,19 +18,21 @@ extern "C" {
 #endif
 
 /* src/lub.h: calc_lub_3f (u, f [np*3]), calc_lub_3ft (uo, ft [np*6]),
- * calc_lub_3fts (not built: reports an error, NaN output) */
+ * calc_lub_3fts (uoe, fts [np*11], the extracted 5-component stresslet and
+ * strain as in libstokes) */
 void calc_lub_3f (struct stokes *sys, const double *u, double *f);
 void calc_lub_3ft (struct stokes *sys, const double *uo, double *ft);
 void calc_lub_3fts (struct stokes *sys, const double *uoe, double *fts);
 
-/* status-returning forms: version 0 (F) or 1 (FT); host vectors, or device
- * vectors on the caller's stream (d_pos [np*3]) */
+/* status-returning forms: version 0 (F), 1 (FT) or 2 (FTS); host vectors,
+ * or device vectors on the caller's stream (d_pos [np*3]) */
 int stokes_gpu_lub (struct stokes *sys, int version, const double *u, double *f);
 int stokes_gpu_lub_dev (struct stokes *sys, int version, const double *d_pos,
                         const double *d_u, double *d_f, void *stream);
-/* the power-series coefficients of the ten lubrication-form functions
- * (x11a x12a y11a y12a y11b y12b x11c x12c y11c y12c; 26 each, out[260]),
- * generated on the host from the Jeffrey-Onishi recurrences */
+/* the power-series coefficients of the 22 lubrication-form functions
+ * (x11a x12a y11a y12a y11b y12b x11c x12c y11c y12c x11g x12g y11g y12g
+ * y11h y12h x11m x12m y11m y12m z11m z12m; 26 each, out[572]), generated on
+ * the host from the Jeffrey-Onishi recurrences */
 int stokes_gpu_lub_coefficients (double *out);
 
 #ifdef __cplusplus

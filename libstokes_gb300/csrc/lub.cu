@@ -1,5 +1,5 @@
-// lub.cu -- the lubrication correction f = L u for equal spheres, F and FT
-// (the drop-in for src/lub.c:164-575; FTS and unequal or slip spheres are
+// lub.cu -- the lubrication correction f = L u for equal spheres, F, FT and
+// FTS (the drop-in for src/lub.c:164-768; unequal or slip spheres are
 // refused), in FP64 on the device.
 //
 // L is the sum over close pairs (r < lubmax, images in the cube |n| <=
@@ -9,10 +9,11 @@
 // (src/two-body-res.c:31): a near-contact singular part in s1 = 1 - 4/s^2,
 // ln s1 and ln((s+2)/(s-2)) plus a power series in 1/s^2 truncated at
 // 1/s^50.  The series coefficients are generated here, at start-up, from
-// the Jeffrey & Onishi (1984) recurrences for the multipole coefficients of
-// two spheres (axisymmetric and asymmetric translation and rotation) and
-// the expansion of the singular part; (M^inf)^-1 is the closed-form inverse
-// of the Rotne-Prager two-sphere mobility.
+// the Jeffrey & Onishi (1984) and Jeffrey (1992) recurrences for the
+// multipole coefficients of two spheres (translation, rotation and
+// straining, azimuthal orders 0, 1, 2) and the expansion of the singular
+// part; (M^inf)^-1 is the closed-form inverse of the Rotne-Prager
+// two-sphere mobility.
 //
 // Each target i is one warp: the lanes take the sources j, reject those
 // whose minimum image is beyond lubmax (unsheared boxes), walk the image
@@ -40,7 +41,8 @@ namespace lsg {
 namespace {
 
 constexpr int JO_K = 51;                 // f_k up to k = 51
-constexpr int LUB_NF = 10;               // x11a x12a y11a y12a y11b y12b x11c x12c y11c y12c
+constexpr int LUB_NF = 22;   // x11a x12a y11a y12a y11b y12b x11c x12c y11c y12c x11g x12g
+                             // y11g y12g y11h y12h x11m x12m y11m y12m z11m z12m
 constexpr int LUB_NC = 26;
 
 // the multipole coefficients P, V, Q of one problem, n in [1, K + 1],
@@ -54,13 +56,13 @@ struct JO {
     if (n < 1 || n > JO_K + 1 || p < 0 || q < 0 || p > JO_K || q > JO_K) return 0.0;
     return T[at (n, p, q)];
   }
-  // f_k(1) = 2^k sum_q T_1,(k-q),q
-  void fk (const std::vector<double> &T, double scale, double *f) const
+  // f_k(1) = scale 2^k sum_q T_n,(k-q),q
+  void fk (const std::vector<double> &T, int n, double scale, double *f) const
   {
     for (int k = 0; k <= JO_K; k++)
       {
         double v = 0.0;
-        for (int q = 0; q <= k; q++) v += get (T, 1, k - q, q);
+        for (int q = 0; q <= k; q++) v += get (T, n, k - q, q);
         f[k] = scale * std::ldexp (v, k);
       }
   }
@@ -75,99 +77,83 @@ binom (int a, int b)
   return r;
 }
 
-// translation along the line of centres (X^A)
+// the recurrence of azimuthal order m (0: X, 1: Y, 2: Z functions) started
+// from a force-type (P = V = 1 at n0) or rotation-type (Q = 1 at n0)
+// singularity: Jeffrey & Onishi (1984) for m = 0, 1 written as one
+// expression in m, which at m = 2 gives Jeffrey's (1992) Z^M coefficients
 void
-jo_xa (JO &J)
+jo_family (JO &J, int m, int n0, bool rotation)
 {
-  J.P[JO::at (1, 0, 0)] = J.V[JO::at (1, 0, 0)] = 1.0;
-  for (int m = 1; m <= JO_K; m++)
-    for (int q = 0; q <= m; q++)
+  std::fill (J.P.begin (), J.P.end (), 0.0);
+  std::fill (J.V.begin (), J.V.end (), 0.0);
+  std::fill (J.Q.begin (), J.Q.end (), 0.0);
+  if (rotation) J.Q[JO::at (n0, 0, 0)] = 1.0;
+  else J.P[JO::at (n0, 0, 0)] = J.V[JO::at (n0, 0, 0)] = 1.0;
+  const double sg = m == 0 ? 1.0 : -1.0;
+  for (int lv = 1; lv <= JO_K; lv++)
+    for (int q = 0; q <= lv; q++)
       for (int n = 1; n <= JO_K + 1; n++)
         {
-          const int p = m - q;
-          double a = 0.0, b = 0.0;
-          for (int s = 1; s <= q; s++)
-            {
-              const double c = binom (n + s, n);
-              a += c * ((double) n * (2 * n + 1) * (2 * n * s - n - s + 2)
-                          / (2.0 * (n + 1) * (2 * s - 1) * (n + s)) * JO::get (J.P, s, q - s, p - n + 1)
-                        - (double) n * (2 * n - 1) / (2.0 * (n + 1)) * JO::get (J.P, s, q - s, p - n - 1)
-                        - (double) n * (4 * n * n - 1) / (2.0 * (n + 1) * (2 * s + 1))
-                            * JO::get (J.V, s, q - s - 2, p - n + 1));
-              b += c * JO::get (J.P, s, q - s, p - n - 1);
-            }
-          J.P[JO::at (n, p, q)] = a;
-          J.V[JO::at (n, p, q)] = a - 2.0 * n / ((n + 1.0) * (2 * n + 3)) * b;
-        }
-}
-
-// translation (rot = 0) or rotation (rot = 1) across the line of centres
-void
-jo_y (JO &J, int rot)
-{
-  if (rot) J.Q[JO::at (1, 0, 0)] = 1.0;
-  else J.P[JO::at (1, 0, 0)] = J.V[JO::at (1, 0, 0)] = 1.0;
-  for (int m = 1; m <= JO_K; m++)
-    for (int q = 0; q <= m; q++)
-      for (int n = 1; n <= JO_K + 1; n++)
-        {
-          const int p = m - q;
+          const int p = lv - q;
           double a = 0.0, bq = 0.0, bv = 0.0, qq = 0.0;
           for (int s = 1; s <= q; s++)
             {
-              const double c = binom (n + s, n + 1);
-              const double w = (3.0 * (n + s) - (double) (n * s + 1) * (2 * n * s - s - n + 2))
-                               / ((double) s * (n + s) * (2 * s - 1));
-              a += c * ((2.0 * n + 1) / (2.0 * (n + 1)) * w * JO::get (J.P, s, q - s, p - n + 1)
-                        + (double) n * (2 * n - 1) / (2.0 * (n + 1)) * JO::get (J.P, s, q - s, p - n - 1)
-                        + (double) n * (4 * n * n - 1) / (2.0 * (n + 1) * (2 * s + 1))
-                            * JO::get (J.V, s, q - s - 2, p - n + 1));
+              const double c = binom (n + s, n + m);
+              if (c == 0.0) continue;
+              const double X = 2.0 * n * s - n - s + 2;
+              const double A = sg * (2.0 * n + 1) * (n * s * X + m * m * (X - 3.0 * (n + s)))
+                               / (2.0 * (n + 1) * s * (n + s) * (2 * s - 1));
+              a += c * (A * JO::get (J.P, s, q - s, p - n + 1)
+                        + sg * (-(double) n * (2 * n - 1) / (2.0 * (n + 1))
+                                  * JO::get (J.P, s, q - s, p - n - 1)
+                                - (double) n * (4 * n * n - 1) / (2.0 * (n + 1) * (2 * s + 1))
+                                  * JO::get (J.V, s, q - s - 2, p - n + 1)));
               bq += c * JO::get (J.Q, s, q - s - 1, p - n + 1);
               bv += c * JO::get (J.P, s, q - s, p - n - 1);
               qq += c * ((double) s / (n + 1) * JO::get (J.Q, s, q - s - 1, p - n)
-                         - 3.0 / (2.0 * n * s * (n + 1)) * JO::get (J.P, s, q - s, p - n));
+                         - 3.0 * m / (2.0 * n * s * (n + 1)) * JO::get (J.P, s, q - s, p - n));
             }
-          const double pv = a - 2.0 * (4.0 * n * n - 1) / (3.0 * (n + 1)) * bq;
+          const double pv = a - 2.0 * m * (4.0 * n * n - 1) / (3.0 * (n + 1)) * bq;
           J.P[JO::at (n, p, q)] = pv;
-          J.V[JO::at (n, p, q)] = pv + 2.0 * n / ((n + 1.0) * (2 * n + 3)) * bv;
+          J.V[JO::at (n, p, q)] = pv - sg * 2.0 * n / ((n + 1.0) * (2 * n + 3)) * bv;
           J.Q[JO::at (n, p, q)] = qq;
         }
 }
 
-// rotation about the line of centres (X^C)
-void
-jo_xc (JO &J)
-{
-  J.Q[JO::at (1, 0, 0)] = 1.0;
-  for (int m = 1; m <= JO_K; m++)
-    for (int q = 0; q <= m; q++)
-      for (int n = 1; n <= JO_K + 1; n++)
-        {
-          const int p = m - q;
-          double v = 0.0;
-          for (int s = 1; s <= q; s++) v += binom (n + s, n + 1) * JO::get (J.Q, s, q - s - 1, p - n);
-          J.Q[JO::at (n, p, q)] = v;
-        }
-}
-
-// singular-part building blocks as series in u = 1/s
-enum { SB_L1, SB_L2, SB_IS1, SB_S1L1, SB_S1L2, SB_UIS1, SB_UL1, SB_UL2, SB_U, SB_ONE, SB_N };
+// singular-part building blocks as series in u = 1/s; s5 = s^2/4 - 1 and
+// S5L2M = s5 L2 - s (its 1/u terms cancel)
+enum { SB_L1, SB_L2, SB_IS1, SB_S1L1, SB_S1L2, SB_UIS1, SB_UL1, SB_UL2, SB_U, SB_ONE, SB_U2IS1,
+       SB_S5L1, SB_S5L2M, SB_N };
+enum { FA_XA, FA_YA, FA_YB, FA_XC, FA_YC, FA_XG, FA_YG, FA_YH, FA_XM, FA_YM, FA_ZM, FA_N };
 struct Term { int b; double c; };
-struct Form { int par, nt; Term t[4]; double esc; };
+struct Form { int par, M, nt; Term t[4]; double esc; int fam; };
 
-// libstokes' lubrication forms at lambda = 1: parity, singular part, and the
-// factor of the exact series (the SD scaling and sign of each function)
+// libstokes' lubrication forms at lambda = 1: parity, truncation, singular
+// part (the published lubrication constants), the factor of the exact series
+// (the SD scaling and sign of each function) and its family
 const Form kForms[LUB_NF] = {
-  {0, 3, {{SB_IS1, 0.25}, {SB_L1, -0.225}, {SB_S1L1, -3.0 / 112}}, 1.0},
-  {1, 4, {{SB_UIS1, -0.5}, {SB_L2, -0.225}, {SB_S1L2, -3.0 / 112}, {SB_U, -12.0 / 112}}, -1.0},
-  {0, 1, {{SB_L1, -1.0 / 6}}, 1.0},
-  {1, 1, {{SB_L2, -1.0 / 6}}, -1.0},
-  {1, 3, {{SB_L2, -2.0 / 12}, {SB_S1L2, -2.0 / 24}, {SB_U, -2.0 / 6}}, 2.0 / 3},
-  {0, 2, {{SB_L1, -2.0 / 12}, {SB_S1L1, -2.0 / 24}}, -2.0 / 3},
-  {0, 3, {{SB_L1, 4.0 / 12}, {SB_UL2, 4.0 / 6}, {SB_ONE, 4.0 / 3}}, 4.0 / 3},
-  {1, 3, {{SB_L2, 4.0 / 12}, {SB_UL1, 4.0 / 6}, {SB_U, -4.0 / 3}}, -4.0 / 3},
-  {0, 3, {{SB_L1, -4.0 / 15}, {SB_S1L1, -4.0 * 47 / 750}, {SB_ONE, 4.0 / 3}}, 4.0 / 3},
-  {1, 3, {{SB_L2, 4.0 / 60}, {SB_S1L2, 4.0 * 31 / 750}, {SB_U, 4.0 * 62 / 375}}, 4.0 / 3},
+  {0, 25, 3, {{SB_IS1, 0.25}, {SB_L1, -0.225}, {SB_S1L1, -3.0 / 112}}, 1.0, FA_XA},
+  {1, 24, 4, {{SB_UIS1, -0.5}, {SB_L2, -0.225}, {SB_S1L2, -3.0 / 112}, {SB_U, -12.0 / 112}}, -1.0, FA_XA},
+  {0, 25, 1, {{SB_L1, -1.0 / 6}}, 1.0, FA_YA},
+  {1, 24, 1, {{SB_L2, -1.0 / 6}}, -1.0, FA_YA},
+  {1, 24, 3, {{SB_L2, -2.0 / 12}, {SB_S1L2, -2.0 / 24}, {SB_U, -2.0 / 6}}, 2.0 / 3, FA_YB},
+  {0, 25, 2, {{SB_L1, -2.0 / 12}, {SB_S1L1, -2.0 / 24}}, -2.0 / 3, FA_YB},
+  {0, 25, 3, {{SB_L1, 4.0 / 12}, {SB_UL2, 4.0 / 6}, {SB_ONE, 4.0 / 3}}, 4.0 / 3, FA_XC},
+  {1, 24, 3, {{SB_L2, 4.0 / 12}, {SB_UL1, 4.0 / 6}, {SB_U, -4.0 / 3}}, -4.0 / 3, FA_XC},
+  {0, 25, 3, {{SB_L1, -4.0 / 15}, {SB_S1L1, -4.0 * 47 / 750}, {SB_ONE, 4.0 / 3}}, 4.0 / 3, FA_YC},
+  {1, 24, 3, {{SB_L2, 4.0 / 60}, {SB_S1L2, 4.0 * 31 / 750}, {SB_U, 4.0 * 62 / 375}}, 4.0 / 3, FA_YC},
+  {1, 24, 3, {{SB_UIS1, 0.5}, {SB_L2, 0.225}, {SB_S5L2M, 39.0 / 280}}, 2.0 / 3, FA_XG},
+  {0, 25, 3, {{SB_U2IS1, -1.0}, {SB_L1, 0.225}, {SB_S5L1, 39.0 / 280}}, -2.0 / 3, FA_XG},
+  {1, 24, 2, {{SB_L2, 1.0 / 12}, {SB_S5L2M, 1.0 / 24}}, 2.0 / 3, FA_YG},
+  {0, 25, 2, {{SB_L1, 1.0 / 12}, {SB_S5L1, 1.0 / 24}}, -2.0 / 3, FA_YG},
+  {0, 25, 2, {{SB_L1, -1.0 / 30}, {SB_S5L1, -137.0 / 1500}}, 4.0 / 3, FA_YH},
+  {1, 24, 2, {{SB_L2, 2.0 / 15}, {SB_S5L2M, 113.0 / 1500}}, 4.0 / 3, FA_YH},
+  {0, 25, 3, {{SB_U2IS1, 2.0 / 3}, {SB_L1, -0.15}, {SB_S5L1, -353.0 / 2520}}, 10.0 / 9, FA_XM},
+  {1, 24, 3, {{SB_UIS1, 1.0 / 3}, {SB_L2, 0.15}, {SB_S5L2M, 493.0 / 2520}}, 10.0 / 9, FA_XM},
+  {0, 25, 2, {{SB_L1, -2.0 / 15}, {SB_S5L1, -19.0 / 750}}, 10.0 / 9, FA_YM},
+  {1, 24, 2, {{SB_L2, 1.0 / 30}, {SB_S5L2M, 37.0 / 250}}, 10.0 / 9, FA_YM},
+  {0, 25, 1, {{SB_S5L1, 1.0 / 12}}, 10.0 / 9, FA_ZM},
+  {1, 24, 1, {{SB_S5L2M, 1.0 / 12}}, -10.0 / 9, FA_ZM},
 };
 
 struct LubCoef { double c[LUB_NF][LUB_NC]; };
@@ -175,30 +161,27 @@ struct LubCoef { double c[LUB_NF][LUB_NC]; };
 LubCoef
 make_coefficients ()
 {
-  double f[5][JO_K + 1];   // XA, YA, YB, XC, YC
-  {
-    JO J;
-    jo_xa (J);
-    J.fk (J.P, 1.0, f[0]);
-  }
-  {
-    JO J;
-    jo_y (J, 0);
-    J.fk (J.P, 1.0, f[1]);
-    J.fk (J.Q, 2.0, f[2]);
-  }
-  {
-    JO J;
-    jo_xc (J);
-    J.fk (J.Q, 1.0, f[3]);
-  }
-  {
-    JO J;
-    jo_y (J, 1);
-    J.fk (J.Q, 1.0, f[4]);
-  }
-  const int fam[LUB_NF] = {0, 0, 1, 1, 2, 2, 3, 3, 4, 4};
-  constexpr int NJ = JO_K + 2;
+  static double f[FA_N][JO_K + 1];
+  JO J;
+  jo_family (J, 0, 1, false);           // X^A, X^G (the n = 2 coefficients)
+  J.fk (J.P, 1, 1.0, f[FA_XA]);
+  J.fk (J.P, 2, 0.75, f[FA_XG]);
+  jo_family (J, 1, 1, false);           // Y^A, Y^B, Y^G
+  J.fk (J.P, 1, 1.0, f[FA_YA]);
+  J.fk (J.Q, 1, 2.0, f[FA_YB]);
+  J.fk (J.P, 2, 0.75, f[FA_YG]);
+  jo_family (J, 1, 1, true);            // Y^C, Y^H
+  J.fk (J.Q, 1, 1.0, f[FA_YC]);
+  J.fk (J.P, 2, -0.375, f[FA_YH]);
+  jo_family (J, 0, 1, true);            // X^C
+  J.fk (J.Q, 1, 1.0, f[FA_XC]);
+  jo_family (J, 0, 2, false);           // X^M
+  J.fk (J.P, 2, 1.0, f[FA_XM]);
+  jo_family (J, 1, 2, false);           // Y^M
+  J.fk (J.P, 2, 1.0, f[FA_YM]);
+  jo_family (J, 2, 2, false);           // Z^M
+  J.fk (J.P, 2, 1.0, f[FA_ZM]);
+  constexpr int NJ = JO_K + 3;
   static double blk[SB_N][NJ];
   memset (blk, 0, sizeof blk);
   for (int j = 0; j < NJ; j++)
@@ -217,6 +200,12 @@ make_coefficients ()
           blk[SB_UL1][j] = blk[SB_L1][j - 1];
           blk[SB_UL2][j] = blk[SB_L2][j - 1];
         }
+      if (j >= 2) blk[SB_U2IS1][j] = blk[SB_IS1][j - 2];
+      if (j + 2 < NJ)
+        {
+          blk[SB_S5L1][j] = blk[SB_L1][j + 2] / 4.0 - blk[SB_L1][j];
+          blk[SB_S5L2M][j] = blk[SB_L2][j + 2] / 4.0 - blk[SB_L2][j];
+        }
     }
   blk[SB_U][1] = 1.0;
   blk[SB_ONE][0] = 1.0;
@@ -225,11 +214,10 @@ make_coefficients ()
   for (int g = 0; g < LUB_NF; g++)
     {
       const Form &F = kForms[g];
-      const int M = F.par ? 24 : 25;
-      for (int m = 0; m <= M; m++)
+      for (int m = 0; m <= F.M; m++)
         {
           const int j = 2 * m + F.par;
-          double v = F.esc * std::ldexp (f[fam[g]][j], -j);
+          double v = F.esc * std::ldexp (f[F.fam][j], -j);
           for (int t = 0; t < F.nt; t++) v -= F.t[t].c * blk[F.t[t].b][j];
           C.c[g][m] = v;
         }
@@ -258,25 +246,87 @@ struct LubArgs {
 __device__ __forceinline__ void
 lub_res (double s, int nf, double *res)
 {
-  const double u = 1.0 / s, u2 = u * u, s1 = 1.0 - 4.0 * u2;
+  const double u = 1.0 / s, u2 = u * u, s1 = 1.0 - 4.0 * u2, s5 = 0.25 * s * s - 1.0;
   const double l1 = log (s1), l2 = log ((s + 2.0) / (s - 2.0));
-  const double bv[SB_N] = {l1, l2, 1.0 / s1, s1 * l1, s1 * l2, u / s1, u * l1, u * l2, u, 1.0};
+  const double bv[SB_N] = {l1,     l2, 1.0 / s1, s1 * l1,  s1 * l2, u / s1,      u * l1,
+                           u * l2, u,  1.0,      u2 / s1,  s5 * l1, s5 * l2 - s};
   for (int g = 0; g < nf; g++)
     {
       const Form &F = c_forms[g];
       double v = 0.0;
       for (int t = 0; t < F.nt; t++) v += F.t[t].c * bv[F.t[t].b];
       double p = 0.0;
-      for (int m = F.par ? 24 : 25; m >= 0; m--) p = fma (p, u2, c_lub[g][m]);
+      for (int m = F.M; m >= 0; m--) p = fma (p, u2, c_lub[g][m]);
       res[g] = v + (F.par ? p * u : p);
     }
 }
 
 // (M^inf)^-1 of two spheres, F (4 values) or FT (10 values)
+// FTS: the block form of the inverse of the Rotne-Prager two-sphere mobility
+// with stresslets, as rational functions of s (a computer-algebra inversion
+// of the two-sphere matrix at e = z, mode by mode)
+__device__ __noinline__ void
+lub_minv_fts (double s, double *r)
+{
+  double p[11];
+  p[0] = 1.0;
+#pragma unroll
+  for (int k = 1; k <= 10; k++) p[k] = p[k - 1] * s;
+  r[0] = (p[6]*(p[2]*(p[2]*(p[2]*(400.0*p[4] - 1500.0) - 5200.0) + 44160.0) - 57600.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(400.0*p[2] - 900.0) - 1800.0) - 800.0) + 45945.0) - 90600.0) + 55600.0) - 21120.0) + 2304.0);   /* xa11 */
+  r[1] = (p[3]*(p[2]*(p[2]*(p[2]*(p[4]*(400.0 - 600.0*p[2]) + 7500.0) - 40000.0) + 57600.0) - 11520.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(400.0*p[2] - 900.0) - 1800.0) - 800.0) + 45945.0) - 90600.0) + 55600.0) - 21120.0) + 2304.0);   /* xa12 */
+  r[2] = (p[6]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(1600.0*p[4] - 1200.0) - 22400.0) + 58880.0) - 90400.0) + 11200.0) - 43520.0) + 25600.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(1600.0*p[2] - 900.0) - 3600.0) - 22800.0) + 66360.0) - 112600.0) + 14880.0) - 16505.0) + 29624.0) + 2000.0) - 640.0) - 256.0);   /* ya11 */
+  r[3] = (p[3]*(p[4]*(p[2]*(p[2]*(p[2]*(p[2]*(p[4]*(-1200.0*p[2] - 800.0) + 16200.0) - 46400.0) + 57600.0) - 4760.0) + 16000.0) - 2560.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(1600.0*p[2] - 900.0) - 3600.0) - 22800.0) + 66360.0) - 112600.0) + 14880.0) - 16505.0) + 29624.0) + 2000.0) - 640.0) - 256.0);   /* ya12 */
+  r[4] = (p[7]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(-1200.0*p[2] - 1600.0) - 6400.0) + 12000.0) - 15200.0) - 19840.0) + 30720.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(1600.0*p[2] - 900.0) - 3600.0) - 22800.0) + 66360.0) - 112600.0) + 14880.0) - 16505.0) + 29624.0) + 2000.0) - 640.0) - 256.0);   /* yb11 */
+  r[5] = (p[4]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(1600.0*p[4] - 600.0) - 10800.0) + 49280.0) - 58700.0) + 14000.0) - 1600.0) - 2560.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(1600.0*p[2] - 900.0) - 3600.0) - 22800.0) + 66360.0) - 112600.0) + 14880.0) - 16505.0) + 29624.0) + 2000.0) - 640.0) - 256.0);   /* yb12 */
+  r[6] = (4.0*p[6])
+         / (3.0*p[6] - 3.0);   /* xc11 */
+  r[7] = (-4.0*p[3])
+         / (3.0*p[6] - 3.0);   /* xc12 */
+  r[8] = (p[6]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(6400.0*p[2] - 3600.0) - 9600.0) - 65600.0) + 251040.0) - 504400.0) + 31360.0) + 125440.0) + 4096.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(4800.0*p[2] - 2700.0) - 10800.0) - 68400.0) + 199080.0) - 337800.0) + 44640.0) - 49515.0) + 88872.0) + 6000.0) - 1920.0) - 768.0);   /* yc11 */
+  r[9] = (p[3]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[4]*(3200.0*p[2] + 1800.0) - 42400.0) + 322020.0) - 267800.0) + 800.0) + 14720.0) + 2048.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(4800.0*p[2] - 2700.0) - 10800.0) - 68400.0) + 199080.0) - 337800.0) + 44640.0) - 49515.0) + 88872.0) + 6000.0) - 1920.0) - 768.0);   /* yc12 */
+  r[10] = (p[7]*(p[2]*(p[2]*(1500.0*p[2] + 1600.0) - 18400.0) + 19200.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(400.0*p[2] - 900.0) - 1800.0) - 800.0) + 45945.0) - 90600.0) + 55600.0) - 21120.0) + 2304.0);   /* xg11 */
+  r[11] = (p[4]*(p[2]*(p[2]*(p[2]*(p[2]*(1600.0 - 1000.0*p[2]) - 3750.0) + 17000.0) - 20000.0) + 3840.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(400.0*p[2] - 900.0) - 1800.0) - 800.0) + 45945.0) - 90600.0) + 55600.0) - 21120.0) + 2304.0);   /* xg12 */
+  r[12] = (p[7]*(p[2]*(p[2]*(p[2]*(p[2]*(10800.0*p[2] - 12800.0) + 37700.0) - 4800.0) + 32000.0) - 12800.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(4800.0*p[2] - 2700.0) - 10800.0) - 68400.0) + 199080.0) - 337800.0) + 44640.0) - 49515.0) + 88872.0) + 6000.0) - 1920.0) - 768.0);   /* yg11 */
+  r[13] = (p[4]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(-6400.0*p[2] - 4500.0) + 25800.0) - 52800.0) + 6130.0) - 9000.0) - 800.0) + 1280.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(4800.0*p[2] - 2700.0) - 10800.0) - 68400.0) + 199080.0) - 337800.0) + 44640.0) - 49515.0) + 88872.0) + 6000.0) - 1920.0) - 768.0);   /* yg12 */
+  r[14] = (p[8]*(p[2]*(p[2]*(p[2]*(77500.0 - 9600.0*p[2]) - 20400.0) - 24800.0) + 14720.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(4800.0*p[2] - 2700.0) - 10800.0) - 68400.0) + 199080.0) - 337800.0) + 44640.0) - 49515.0) + 88872.0) + 6000.0) - 1920.0) - 768.0);   /* yh11 */
+  r[15] = (p[5]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(8000.0*p[2] - 4500.0) - 7200.0) - 51600.0) + 68850.0) - 7500.0) - 1200.0) + 960.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(4800.0*p[2] - 2700.0) - 10800.0) - 68400.0) + 199080.0) - 337800.0) + 44640.0) - 49515.0) + 88872.0) + 6000.0) - 1920.0) - 768.0);   /* yh12 */
+  r[16] = (p[8]*(p[2]*(p[2]*(p[2]*(4000.0*p[2] - 9000.0) - 3000.0) + 44000.0) - 38400.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(3600.0*p[2] - 8100.0) - 16200.0) - 7200.0) + 413505.0) - 815400.0) + 500400.0) - 190080.0) + 20736.0);   /* xm11 */
+  r[17] = (p[5]*(p[2]*(p[2]*(p[2]*(20000.0*p[2] - 70500.0) + 81000.0) - 58400.0) + 9600.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(3600.0*p[2] - 8100.0) - 16200.0) - 7200.0) + 413505.0) - 815400.0) + 500400.0) - 190080.0) + 20736.0);   /* xm12 */
+  r[18] = (p[8]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(16000.0*p[2] - 9000.0) - 36000.0) - 68000.0) - 15200.0) + 15000.0) - 41600.0) + 12800.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(14400.0*p[2] - 8100.0) - 32400.0) - 205200.0) + 597240.0) - 1013400.0) + 133920.0) - 148545.0) + 266616.0) + 18000.0) - 5760.0) - 2304.0);   /* ym11 */
+  r[19] = (p[5]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(150500.0 - 40000.0*p[2]) + 18000.0) - 103600.0) - 27150.0) - 10500.0) - 400.0) + 1600.0))
+         / (p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(p[2]*(14400.0*p[2] - 8100.0) - 32400.0) - 205200.0) + 597240.0) - 1013400.0) + 133920.0) - 148545.0) + 266616.0) + 18000.0) - 5760.0) - 2304.0);   /* ym12 */
+  r[20] = (10.0*p[10])
+         / (9.0*p[10] - 36.0);   /* zm11 */
+  r[21] = (-20.0*p[5])
+         / (9.0*p[10] - 36.0);   /* zm12 */
+}
+
 template <int V>
 __device__ __forceinline__ void
 lub_minv (double s, double *r)
 {
+  if (V == 2)
+    {
+      lub_minv_fts (s, r);
+      return;
+    }
   const double s2 = s * s, s3 = s2 * s, s6 = s3 * s3;
   const double dx = (2.0 * s3 - 3.0 * s2 + 2.0) * (2.0 * s3 + 3.0 * s2 - 2.0);
   r[0] = 4.0 * s6 / dx;
@@ -327,6 +377,35 @@ lub_apply (const double e[3], const double *sc, bool self, double w, const doubl
       y[d] += sg * Txe[d];
       y[3 + d] += yb * Fxe[d] + yc * T[d] + (xc - yc) * eT * e[d];
     }
+  if (V < 2) return;
+  // the stresslet couplings (src/fts.c:626-1023 in vector form, the
+  // extracted stresslet as S' = (2 sxx + syy, 2 syy + sxx, sxy, sxz, syz),
+  // S'zz = 0); the self block flips the force-from-stresslet coupling
+  const double xg = w * sc[5], yg = w * sc[6], yh = w * sc[7];
+  const double xm = w * sc[8], ym = w * sc[9], zm = w * sc[10];
+  const double S00 = 2.0 * x[6] + x[10], S11 = 2.0 * x[10] + x[6], S01 = x[7], S02 = x[8],
+               S12 = x[9];
+  const double Se[3] = {S00 * e[0] + S01 * e[1] + S02 * e[2], S01 * e[0] + S11 * e[1] + S12 * e[2],
+                        S02 * e[0] + S12 * e[1]};
+  const double eSe = e[0] * Se[0] + e[1] * Se[1] + e[2] * Se[2], trS = S00 + S11;
+  const double g1 = -xg / 3.0, g2 = yg, g3 = xg - 2.0 * yg;
+  const double m1 = 1.5 * xm - 2.0 * ym + 0.5 * zm, m2 = 0.5 * (zm - xm);
+  const double m3 = xm / 6.0 - 0.5 * zm, m4x2 = ym - zm, m5x2 = zm;
+  const double gu = g1 * trS + g3 * eSe, sgg = self ? -1.0 : 1.0;
+#pragma unroll
+  for (int d = 0; d < 3; d++) y[d] -= sgg * (gu * e[d] + 2.0 * g2 * Se[d]);
+  y[3] += 2.0 * yh * (e[1] * Se[2] - e[2] * Se[1]);
+  y[4] += 2.0 * yh * (e[2] * Se[0] - e[0] * Se[2]);
+  y[5] += 2.0 * yh * (e[0] * Se[1] - e[1] * Se[0]);
+  const double dE = g1 * eF + m2 * eSe + m3 * trS, eeE = g3 * eF + m1 * eSe + m2 * trS;
+  double Vv[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) Vv[d] = g2 * x[d] + yh * Txe[d] + m4x2 * Se[d];
+  y[6] += dE + eeE * e[0] * e[0] + 2.0 * e[0] * Vv[0] + m5x2 * S00;
+  y[7] += eeE * e[0] * e[1] + e[0] * Vv[1] + e[1] * Vv[0] + m5x2 * S01;
+  y[8] += eeE * e[0] * e[2] + e[0] * Vv[2] + e[2] * Vv[0] + m5x2 * S02;
+  y[9] += eeE * e[1] * e[2] + e[1] * Vv[2] + e[2] * Vv[1] + m5x2 * S12;
+  y[10] += dE + eeE * e[1] * e[1] + 2.0 * e[1] * Vv[1] + m5x2 * S11;
 }
 
 // one pair image (separation d, source velocity uj) into the target's sums;
@@ -336,7 +415,7 @@ __device__ __forceinline__ void
 lub_pair (const LubArgs &a, const double d[3], const double *ui, const double *uj, bool self,
           double *acc)
 {
-  constexpr int NF = V == 0 ? 4 : 10;
+  constexpr int NF = V == 0 ? 4 : (V == 1 ? 10 : 22);
   double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
   if (r2 < a.lubmin2) r2 = a.lubmin2;
   const double r = sqrt (r2), ri = 1.0 / r;
@@ -344,19 +423,14 @@ lub_pair (const LubArgs &a, const double d[3], const double *ui, const double *u
   double res[NF], inf[NF];
   lub_res (r, NF, res);
   lub_minv<V> (r, inf);
-  double s11[5], s12[5];
-  s11[0] = res[0] - inf[0];
-  s12[0] = res[1] - inf[1];
-  s11[1] = res[2] - inf[2];
-  s12[1] = res[3] - inf[3];
-  if (V == 1)
+  // (xa, ya[, yb, xc, yc[, xg, yg, yh, xm, ym, zm]]) of the self (11) and
+  // cross (12) blocks: the 11 and 12 entries of each function alternate
+  double s11[NF / 2], s12[NF / 2];
+#pragma unroll
+  for (int k = 0; k < NF / 2; k++)
     {
-      s11[2] = res[4] - inf[4];
-      s12[2] = res[5] - inf[5];
-      s11[3] = res[6] - inf[6];
-      s12[3] = res[7] - inf[7];
-      s11[4] = res[8] - inf[8];
-      s12[4] = res[9] - inf[9];
+      s11[k] = res[2 * k] - inf[2 * k];
+      s12[k] = res[2 * k + 1] - inf[2 * k + 1];
     }
   lub_apply<V> (e, s11, true, 1.0, ui, acc);
   lub_apply<V> (e, s12, false, 1.0, uj, acc);
@@ -383,7 +457,7 @@ template <int V>
 __global__ void __launch_bounds__ (256)
 k_lub (LubArgs a)
 {
-  constexpr int C = V == 0 ? 3 : 6;
+  constexpr int C = V == 0 ? 3 : (V == 1 ? 6 : 11);
   __shared__ int s_q[8][LUB_QCAP];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int i = blockIdx.x * 8 + wib;
@@ -511,8 +585,7 @@ lub_check (const struct stokes *sys, int version)
 {
   if (!sys) return set_error (STOKES_GPU_EINVAL, "NULL system");
   if (sys->np <= 0) return set_error (STOKES_GPU_EINVAL, "no particles");
-  if (version > 1)
-    return set_error (STOKES_GPU_EINVAL, "the FTS lubrication correction is not built");
+  if (version < 0 || version > 2) return set_error (STOKES_GPU_EINVAL, "version %d", version);
   if (sys->a || sys->slip)
     return set_error (STOKES_GPU_EINVAL,
                       "the lubrication correction serves equal spheres without slip");
@@ -557,7 +630,8 @@ lub_dev (const struct stokes *sys, int version, const double *d_pos, const doubl
   a.lubmax2 = sys->lubmax * sys->lubmax;
   const int grid = (sys->np + 7) / 8;
   if (version == 0) k_lub<0><<<grid, 256, 0, st>>> (a);
-  else k_lub<1><<<grid, 256, 0, st>>> (a);
+  else if (version == 1) k_lub<1><<<grid, 256, 0, st>>> (a);
+  else k_lub<2><<<grid, 256, 0, st>>> (a);
   cudaError_t e = cudaGetLastError ();
   return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "lubrication kernel");
 }
@@ -574,7 +648,7 @@ lub_host (struct stokes *sys, int version, const double *u, double *f)
   Ctx *c = get_ctx (sys, true);
   if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
   const int np = sys->np;
-  const size_t n = (size_t) (version == 0 ? 3 : 6) * np;
+  const size_t n = (size_t) (version == 0 ? 3 : (version == 1 ? 6 : 11)) * np;
   cudaError_t e;
   if ((e = c->pos.ensure (sizeof (double) * 3 * np)) != cudaSuccess
       || (e = c->x.ensure (sizeof (double) * n)) != cudaSuccess
@@ -614,10 +688,8 @@ calc_lub_3ft (struct stokes *sys, const double *uo, double *ft)
 void
 calc_lub_3fts (struct stokes *sys, const double *uoe, double *fts)
 {
-  (void) uoe;
-  clear_error ();
-  set_error (STOKES_GPU_EINVAL, "the FTS lubrication correction is not built");
-  dropin_failed ("calc_lub_3fts", fts, fts && sys ? 11 * (size_t) sys->np : 0);
+  if (lub_host (sys, 2, uoe, fts))
+    dropin_failed ("calc_lub_3fts", fts, fts && sys ? 11 * (size_t) sys->np : 0);
 }
 
 // the series coefficients (10 functions x 26, host memory; no GPU needed)

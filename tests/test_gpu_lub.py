@@ -1,9 +1,10 @@
-"""The lubrication correction on the GPU (calc_lub_3f / calc_lub_3ft,
-src/lub.c:164-575, equal spheres) against the reference's own outputs
+"""The lubrication correction on the GPU (calc_lub_3f / 3ft / 3fts,
+src/lub.c:164-768, equal spheres) against the reference's own outputs
 (tests/golden/lub.npz: periodic, open, sheared, small-box and
-unlimited-range systems) and against the oracle on a larger system; the
-refusals (unequal radii, FTS); and the lubricated mobility problem
-(I + M L) u = M f solved on the device against a dense solve."""
+unlimited-range systems) and against the oracle on larger systems; the
+refusals (unequal radii, a bad version, an image cube too large); and the
+lubricated mobility problem (I + M L) u = M f solved on the device against
+a dense solve."""
 import ctypes as C
 import os
 
@@ -15,7 +16,8 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 CASES = ["lub_f_periodic", "lub_ft_periodic", "lub_f_open", "lub_ft_open", "lub_ft_nolimit",
-         "lub_f_small_box", "lub_f_shear1", "lub_ft_shear2"]
+         "lub_f_small_box", "lub_f_shear1", "lub_ft_shear2", "lub_fts_periodic", "lub_fts_open",
+         "lub_fts_shear1"]
 
 
 @pytest.fixture(scope="module")
@@ -52,18 +54,18 @@ def test_lub_against_reference(lib, lub, name):
     from libstokes_gb300 import abi
     u = np.ascontiguousarray(lub[f"{name}_u"])
     g = np.zeros_like(u)
-    (lib.calc_lub_3f if ver == 0 else lib.calc_lub_3ft)(s.sp, u.ctypes.data_as(abi._dp),
-                                                        g.ctypes.data_as(abi._dp))
+    (lib.calc_lub_3f, lib.calc_lub_3ft, lib.calc_lub_3fts)[ver](s.sp, u.ctypes.data_as(abi._dp),
+                                                               g.ctypes.data_as(abi._dp))
     assert np.array_equal(f, g)
     s.close()
 
 
-@pytest.mark.parametrize("ver", [0, 1])
+@pytest.mark.parametrize("ver", [0, 1, 2])
 def test_lub_large_against_oracle(lib, ver):
     from libstokes_gb300.workloads import rsa_positions
     from oracle.oracle import calc_lub
     pos, L = rsa_positions(1000, 0.35, seed=71 + ver)
-    c = (3, 6)[ver]
+    c = (3, 6, 11)[ver]
     u = np.random.default_rng(72).standard_normal(c * 1000)
     s = _system(ver, pos, L, True, 2.0001 ** 2, 3.0)
     f = _calc(lib, s, ver, u)
@@ -88,9 +90,12 @@ def test_lub_refusals(lib):
     s = _system(2, pos, L, True, 0.0, 3.0)
     u = np.ones(220)
     f = np.zeros(220)
+    assert lib.stokes_gpu_lub(s.sp, 3, u.ctypes.data_as(abi._dp),
+                              f.ctypes.data_as(abi._dp)) == abi.STOKES_GPU_EINVAL
+    s.s.lubmax = 1e6                    # an image cube too large to walk
     assert lib.stokes_gpu_lub(s.sp, 2, u.ctypes.data_as(abi._dp),
                               f.ctypes.data_as(abi._dp)) == abi.STOKES_GPU_EINVAL
-    assert b"FTS" in lib.stokes_gpu_last_error_message()
+    assert b"boxes" in lib.stokes_gpu_last_error_message()
     s.close()
 
 
