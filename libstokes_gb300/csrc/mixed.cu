@@ -73,6 +73,12 @@ struct MixedState {
   int real_g = 1;               // warps per target of mk_real
   int nc[3] = {0, 0, 0};        // cell list of mk_real (nc[0] == 0: no cells)
   DevBuf sq, cstart;
+  // unequal radii: radii and their squares (FP32), the per-particle self
+  // terms at the split (FP64, [np][3]), for the split they were made at
+  bool poly = false;
+  double amax = 1.0;
+  DevBuf prad, pqa, pself;
+  uint64_t poly_fp = 0;
 };
 
 constexpr int MX_WARPS = 8;      // warps per CTA in the mixed kernels
@@ -301,9 +307,9 @@ min_image (const RealMixArgs &a, uint4 qi, uint4 qj, float &dx, float &dy, float
 // one pair term (source j at displacement d from the target) added to t;
 // pairs under the rmin clamp arrive here only when the clamp is applied in
 // place (clampfix = 0); otherwise mk_clamp takes them
-template <int V>
+template <int V, bool POLY>
 __device__ __forceinline__ void
-mix_term (const RealMixArgs &a, float4 d, GenU<V, float> &t)
+mix_term (const RealMixArgs &a, float4 d, float ai, GenU<V, float> &t)
 {
   const int j = __float_as_int (d.w);
   const float rr = d.x * d.x + d.y * d.y + d.z * d.z;
@@ -331,7 +337,12 @@ mix_term (const RealMixArgs &a, float4 d, GenU<V, float> &t)
   load_genf<V, float> (xj, g);
   const float e[3] = {d.x * ri, d.y * ri, d.z * ri};
   PairScalars<float> s;
-  real_scalars_mono_ri<V, float> (a.xi, a.xisp, r, ri, s);
+  if (POLY)
+    // unequal radii (rmin = 0): the SD-form scalars of the pair's radii,
+    // scaled by the target's (src/ewald.c:204-359, :383-420)
+    real_scalars_poly<V, float> (a.xi, a.xisp, r, ai, __ldg (a.rad + j), ai, s);
+  else
+    real_scalars_mono_ri<V, float> (a.xi, a.xisp, r, ri, s);
   pair_apply<V, float> (e, s, g, t);
 }
 
@@ -364,7 +375,7 @@ static_assert (31 + 32 * RG_MAXIMG <= RG_QCAP, "mk_real queue too small");
 // G warps of the target meet with TwoSum (error-free, the rounding errors
 // carried along), and the result is written as the FP32 pair hi + lo,
 // which the combine adds in FP64.
-template <int V>
+template <int V, bool POLY>
 __global__ void __launch_bounds__ (RG_WARPS * 32, 3)
 mk_real (RealMixArgs a)
 {
@@ -394,6 +405,7 @@ mk_real (RealMixArgs a)
     }
   GenU<V, float> sum;
   sum.zero ();
+  const float ai = (POLY && live) ? __ldg (a.rad + i) : 1.0f;
   float4 *q = s_q[wib];
   int qn = 0;
   const unsigned lt = (1u << lane) - 1u;
@@ -456,7 +468,7 @@ mk_real (RealMixArgs a)
               __syncwarp ();
               while (qn >= 32)
                 {
-                  mix_term<V> (a, q[qn - 32 + lane], sum);
+                  mix_term<V, POLY> (a, q[qn - 32 + lane], ai, sum);
                   qn -= 32;
                   __syncwarp ();
                 }
@@ -464,7 +476,7 @@ mk_real (RealMixArgs a)
         __syncwarp ();
         if (qn >= 32)
           {
-            mix_term<V> (a, q[qn - 32 + lane], sum);
+            mix_term<V, POLY> (a, q[qn - 32 + lane], ai, sum);
             qn -= 32;
             __syncwarp ();
           }
@@ -504,7 +516,7 @@ mk_real (RealMixArgs a)
                 }
             }
         }
-      if (lane < qn) mix_term<V> (a, q[lane], sum);
+      if (lane < qn) mix_term<V, POLY> (a, q[lane], ai, sum);
     }
   // the 32 lane sums of this warp by a shuffle tree (pairwise summation)
 #pragma unroll
@@ -803,6 +815,136 @@ mk_backproj (BpMixArgs a)
     }
 }
 
+// Unequal radii (SIMT).  The reciprocal weights of a pair depend on both
+// radii, linearly in the source's squared radius q_j (src/ewald.c:985-1025),
+// so each half-space k keeps four raw sums: C = sum_j cos(k.r_j) x_j, S with
+// sin, and Cq, Sq weighted by q_j.  The k table holds, for unequal radii,
+// ya = kexp (the A, B, C, H, M factor), yb = |k|, yc = |k|^2 and yg = the G
+// factor (-kexp on the split's own vectors, +2 kexp_ref of the reference's
+// split for its G term).
+template <int V>
+__global__ void __launch_bounds__ (MX_WARPS * 32)
+mk_sfac_poly (KMixArgs a, const float *qa)
+{
+  constexpr int C = NComp<V>::value;
+  const int lane = threadIdx.x & 31;
+  const int k = blockIdx.x * MX_WARPS + (threadIdx.x >> 5);
+  if (k >= a.nkh) return;
+  const MixK K = a.kt[k];
+  const float2 *t0 = a.tab, *t1 = a.tab + a.off1, *t2 = a.tab + a.off2;
+  float cs[C], sn[C], cq[C], sq[C];
+#pragma unroll
+  for (int q = 0; q < C; q++) cs[q] = sn[q] = cq[q] = sq[q] = 0.f;
+  for (int j = lane; j < a.np; j += 32)
+    {
+      const float2 ph = cmul (cmul (tab_get (t0, K.m1, a.np, j), tab_get (t1, K.m2, a.np, j)),
+                              tab_get (t2, K.m3, a.np, j));
+      const float *xj = a.xf + (size_t) cpad (C) * j;
+      const float w = __ldg (qa + j);
+#pragma unroll
+      for (int q = 0; q < C; q++)
+        {
+          const float v = xj[q], vq = w * v;
+          cs[q] = fmaf (ph.x, v, cs[q]);
+          sn[q] = fmaf (ph.y, v, sn[q]);
+          cq[q] = fmaf (ph.x, vq, cq[q]);
+          sq[q] = fmaf (ph.y, vq, sq[q]);
+        }
+    }
+#pragma unroll
+  for (int q = 0; q < C; q++)
+    {
+      cs[q] = warp_sum (cs[q]);
+      sn[q] = warp_sum (sn[q]);
+      cq[q] = warp_sum (cq[q]);
+      sq[q] = warp_sum (sq[q]);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < C; q++)
+      {
+        a.pq[(size_t) q * a.nkh + k] = cs[q];
+        a.pq[(size_t) (C + q) * a.nkh + k] = sn[q];
+        a.pq[(size_t) (2 * C + q) * a.nkh + k] = cq[q];
+        a.pq[(size_t) (3 * C + q) * a.nkh + k] = sq[q];
+      }
+}
+
+// one warp per (target i, k chunk): the target's weights (its radius a_i
+// scales the SD form, q_i = a_i^2 enters the Laplacian terms) applied to
+// v1 = c_i C + s_i S, v2 = s_i C - c_i S and to the q-weighted sums
+template <int V>
+__global__ void __launch_bounds__ (MX_WARPS * 32)
+mk_backproj_poly (BpMixArgs a, const float *rad)
+{
+  constexpr int C = NComp<V>::value;
+  __shared__ float2 s_t[MX_WARPS][3][MX_MTAB + 1];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long w = (long long) blockIdx.x * MX_WARPS + wib;
+  if (w >= (long long) a.np * a.nchunk) return;
+  const int i = (int) (w % a.np);
+  const int chunk = (int) (w / a.np);
+  const int Md[3] = {a.M0, a.M1, a.M2};
+  const size_t off[3] = {0, a.off1, a.off2};
+  for (int d = 0; d < 3; d++)
+    for (int m = lane; m <= Md[d]; m += 32)
+      s_t[wib][d][m] = a.tab[off[d] + (size_t) m * a.np + i];
+  __syncwarp ();
+  const float aa = __ldg (rad + i), qai = aa * aa, aa2 = aa * aa, aa3 = aa2 * aa;
+  const int k0 = (int) ((long long) a.nkh * chunk / a.nchunk);
+  const int k1 = (int) ((long long) a.nkh * (chunk + 1) / a.nchunk);
+  GenU<V, float> acc;
+  acc.zero ();
+  for (int k = k0 + lane; k < k1; k += 32)
+    {
+      const MixK K = a.kt[k];
+      float2 p0 = s_t[wib][0][K.m1 < 0 ? -K.m1 : K.m1];
+      float2 p1 = s_t[wib][1][K.m2 < 0 ? -K.m2 : K.m2];
+      float2 p2 = s_t[wib][2][K.m3 < 0 ? -K.m3 : K.m3];
+      if (K.m1 < 0) p0.y = -p0.y;
+      if (K.m2 < 0) p1.y = -p1.y;
+      if (K.m3 < 0) p2.y = -p2.y;
+      const float2 p = cmul (cmul (p0, p1), p2);
+      float t1[C], t2[C], u1[C], u2[C];
+#pragma unroll
+      for (int q = 0; q < C; q++)
+        {
+          const float Cc = a.pq[(size_t) q * a.nkh + k], Ss = a.pq[(size_t) (C + q) * a.nkh + k];
+          const float Cq = a.pq[(size_t) (2 * C + q) * a.nkh + k];
+          const float Sq = a.pq[(size_t) (3 * C + q) * a.nkh + k];
+          t1[q] = p.x * Cc + p.y * Ss;
+          t2[q] = p.y * Cc - p.x * Ss;
+          u1[q] = p.x * Cq + p.y * Sq;
+          u2[q] = p.y * Cq - p.x * Sq;
+        }
+      const float e[3] = {K.ex, K.ey, K.ez};
+      const float ax = K.ya, kn = K.yb, kk = K.yc, gx = K.yg;
+      const float ya0 = aa * 6.0f * (1.0f - kk * qai * (1.0f / 6.0f)) * ax;
+      const float ya1 = -aa * kk * ax;
+      const float yb = aa2 * 3.0f * kn * ax;
+      const float yc = aa3 * 1.5f * kk * ax;
+      const float yg0 = aa2 * 3.0f * (1.0f - kk * qai * 0.1f) * kn * gx;
+      const float yg1 = -aa2 * 0.5f * kk * kn * gx;
+      const float yh = aa3 * 1.5f * kk * ax;
+      const float ym0 = aa3 * 3.0f * (1.0f - kk * qai * 0.1f) * kk * ax;
+      const float ym1 = -aa3 * 0.3f * kk * kk * ax;
+      GenF<V, float> g1, g2, h1, h2;
+      load_genf<V, float> (t1, g1);
+      load_genf<V, float> (t2, g2);
+      load_genf<V, float> (u1, h1);
+      load_genf<V, float> (u2, h2);
+      recip_apply<V, float> (e, ya0, yb, yc, yg0, yh, ym0, g1, g2, acc);
+      recip_apply<V, float> (e, ya1, 0.0f, 0.0f, yg1, 0.0f, ym1, h1, h2, acc);
+    }
+  float *out = a.partial + ((size_t) chunk * a.np + i) * C;
+#pragma unroll
+  for (int q = 0; q < C; q++)
+    {
+      const float v = warp_sum (acc.v[q]);
+      if (lane == 0) out[q] = v;
+    }
+}
+
 // The self term of equal spheres as a C x C matrix: column q is the self
 // block applied to the unit vector of component q (one thread per column,
 // run once per split).
@@ -840,6 +982,7 @@ struct CombineArgs {
   const float *pk;      // reciprocal partials [nck][np c]
   int nck;
   const double *S;      // self block of equal spheres, c x c
+  const double *selfp;  // unequal radii: [np][3] factors of S's F, T, S parts (S unit)
   int np, c;
   double *y;            // output [np c]
 };
@@ -884,6 +1027,7 @@ mk_combine (CombineArgs a)
   const double *xi = a.x + (size_t) a.c * i;
   double self = 0.0;
   for (int k = 0; k < nq; k++) self = fma (a.S[q * a.c + q0 + k], xi[q0 + k], self);
+  if (a.selfp) self *= a.selfp[3 * i + (q < 3 ? 0 : (q < 6 ? 1 : 2))];
   a.y[t] = self + r;
 }
 
@@ -951,15 +1095,31 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
   bool images = env_double ("LIBSTOKES_GB300_MIXED_IMAGES", fts_images ? 1.0 : 0.0) != 0.0;
   double eta = env_double ("LIBSTOKES_GB300_MIXED_ETA",
                            images ? default_eta_images (sys->np) : default_eta (sys->np));
-  const uint64_t fp = mix_fingerprint (sys, eta + (images ? 1000.0 : 0.0), eps);
+  uint64_t fp = mix_fingerprint (sys, eta + (images ? 1000.0 : 0.0), eps);
+  const bool poly = c->mode == MODE_POLY;
+  double amax = 1.0;
+  if (poly)
+    {
+      // the radii enter the split (xi a_max <= 0.5) and every table
+      amax = 0.0;
+      for (int q = 0; q < sys->np; q++)
+        {
+          amax = std::max (amax, sys->a[q]);
+          uint64_t b;
+          memcpy (&b, &sys->a[q], sizeof b);
+          fp = (fp ^ b) * 1099511628211ull;
+        }
+    }
   if (fp == m->fp && m->kt.p) return STOKES_GPU_OK;
+  m->poly = poly;
+  m->amax = amax;
 
   const double lmin = fmin (sys->lx, fmin (sys->ly, sys->lz));
   const double lmax = fmax (sys->lx, fmax (sys->ly, sys->lz));
   const double lv = cbrt (sys->lx * sys->ly * sys->lz);
   // xi a <= 0.5 keeps the self, real and reciprocal parts of comparable size
   // (FP32 loses digits to their cancellation when xi a grows)
-  const double XI_CAP = 0.5;
+  const double XI_CAP = 0.5 / amax;
   double xi = std::min (eta / lv, XI_CAP), rc = 0, kc = 0;
   if (!images)
     {
@@ -1046,14 +1206,28 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
           memset (&r, 0, sizeof r);
           r.m1 = m1; r.m2 = m2; r.m3 = m3;
           r.ex = (float) (k1 / k); r.ey = (float) (k2 / k); r.ez = (float) (k3 / k);
-          r.ya = (float) (6.0 * (1.0 - kk / 3.0) * kexp);
-          r.yb = (float) (3.0 * k * kexp);
-          r.yc = (float) (1.5 * kk * kexp);
-          // G coupling with the sign that makes real + reciprocal independent
-          // of xi (the opposite of libstokes' src/ewald.c:1060-1066)
-          r.yg = (float) (-3.0 * (1.0 - 4.0 / 15.0 * kk) * k * kexp);
-          r.yh = (float) (1.5 * kk * kexp);
-          r.ym = (float) (3.0 * (1.0 - kk / 5.0) * kk * kexp);
+          if (poly)
+            {
+              // the per-k factors of the unequal-radius weights
+              // (mk_backproj_poly); G with the xi-independent sign
+              r.ya = (float) kexp;
+              r.yb = (float) k;
+              r.yc = (float) kk;
+              r.yg = (float) -kexp;
+              r.yh = r.ym = 0.f;
+            }
+          else
+            {
+              r.ya = (float) (6.0 * (1.0 - kk / 3.0) * kexp);
+              r.yb = (float) (3.0 * k * kexp);
+              r.yc = (float) (1.5 * kk * kexp);
+              // G coupling with the sign that makes real + reciprocal
+              // independent of xi (the opposite of libstokes'
+              // src/ewald.c:1060-1066)
+              r.yg = (float) (-3.0 * (1.0 - 4.0 / 15.0 * kk) * k * kexp);
+              r.yh = (float) (1.5 * kk * kexp);
+              r.ym = (float) (3.0 * (1.0 - kk / 5.0) * kk * kexp);
+            }
           m->h_k.push_back (r);
           M[0] = std::max (M[0], abs (m1));
           M[1] = std::max (M[1], abs (m2));
@@ -1091,7 +1265,16 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
               memset (&r, 0, sizeof r);
               r.m1 = m1; r.m2 = m2; r.m3 = m3;
               r.ex = (float) (k1 / k); r.ey = (float) (k2 / k); r.ez = (float) (k3 / k);
-              r.yg = (float) (2.0 * 3.0 * (1.0 - 4.0 / 15.0 * kk) * k * kexp);
+              if (poly)
+                {
+                  // the G factor alone (no A, B, C, H, M part)
+                  r.ya = 0.f;
+                  r.yb = (float) k;
+                  r.yc = (float) kk;
+                  r.yg = (float) (2.0 * kexp);
+                }
+              else
+                r.yg = (float) (2.0 * 3.0 * (1.0 - 4.0 / 15.0 * kk) * k * kexp);
               // the operator is linear in its coefficients, so a k vector of
               // the split's own list takes the term into its yg; each (m1,
               // m2, m3) then appears once, which the GEMM path relies on
@@ -1184,7 +1367,7 @@ run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_
   const void *ptrs[] = {d_pos, d_x, d_y, m->kt.p, m->qpos.p, m->tab.p, m->xf.p, m->pq.p,
                         m->part_real.p, m->part_rec.p, m->selfbuf.p, m->status.p, m->sf.p,
                         m->rowm.p, m->rot.p, m->img_zf.p, m->img_wb.p, m->h_status, m->tyz.p,
-                        m->img.p, m->sq.p, m->cstart.p};
+                        m->img.p, m->sq.p, m->cstart.p, m->prad.p, m->pqa.p, m->pself.p};
   for (const void *p : ptrs) mix ((uint64_t) (uintptr_t) p);
   mix ((uint64_t) (uintptr_t) E);
   // a captured cudaEventRecord is only a dependency, not a record: around a
@@ -1240,9 +1423,13 @@ int
 atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
                   cudaStream_t st, bool timed)
 {
-  if (c->mode != MODE_MONO)
+  if (c->mode == MODE_SLIP)
     return set_error (STOKES_GPU_EINVAL,
-                      "mixed precision serves equal spheres without slip; use STOKES_GPU_FP64");
+                      "mixed precision serves spheres without slip (libstokes' slip sum depends on "
+                      "its own xi); use STOKES_GPU_FP64");
+  if (c->mode == MODE_POLY && c->sys->rmin > 0.0)
+    return set_error (STOKES_GPU_EINVAL,
+                      "mixed precision with unequal radii needs rmin = 0; use STOKES_GPU_FP64");
   if (c->open)
     return set_error (STOKES_GPU_EINVAL,
                       "mixed precision serves periodic systems; the free-space operator runs in FP64");
@@ -1290,7 +1477,8 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     const char *ks = getenv ("LIBSTOKES_GB300_KSPACE");   // read per call: tests switch it
     m->plan = kgemm_plan (c->version, pt, (const int2 *) m->rowm.p, m->nrow);
     m->plan.stall = g_test_gemm_stall;
-    m->tensor = !(ks && strcmp (ks, "simt") == 0) && m->nkh > 0 && kgemm_fits (m->plan);
+    m->tensor = !(ks && strcmp (ks, "simt") == 0) && !m->poly && m->nkh > 0
+                && kgemm_fits (m->plan);
   }
   if (m->tensor)
     m->nchunk_k = kgemm_ypart_chunks (m->plan);
@@ -1351,20 +1539,54 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       m->plan.t.tyz = (const float2 *) m->tyz.p;
       m->plan.t.wyz = wyz;
     }
-  else if ((e = m->pq.ensure (sizeof (float) * 2 * C * (size_t) (m->nkh > 0 ? m->nkh : 1))) != cudaSuccess)
+  else if ((e = m->pq.ensure (sizeof (float) * (m->poly ? 4 : 2) * C
+                               * (size_t) (m->nkh > 0 ? m->nkh : 1))) != cudaSuccess)
     return cuda_fail (e, "pq");
   if ((e = m->part_real.ensure (sizeof (float) * (size_t) m->nchunk_r * np * C)) != cudaSuccess) return cuda_fail (e, "real partials");
   if ((e = m->part_rec.ensure (sizeof (float) * (size_t) m->nchunk_k * np * C)) != cudaSuccess) return cuda_fail (e, "k partials");
-  // the self block as a C x C matrix, rebuilt when the split changes
+  // the self block as a C x C matrix, rebuilt when the split changes; with
+  // unequal radii the unit block, scaled per particle by its self terms
   if (m->fp != m->self_fp || !m->selfbuf.p)
     {
       if ((e = m->selfbuf.ensure (sizeof (double) * C * C)) != cudaSuccess) return cuda_fail (e, "self");
       double *S = (double *) m->selfbuf.p;
-      if (c->version == 0) mk_selfmat<0><<<1, 32, 0, st>>> (m->selfc[0], m->selfc[1], m->selfc[2], S);
-      else if (c->version == 1) mk_selfmat<1><<<1, 32, 0, st>>> (m->selfc[0], m->selfc[1], m->selfc[2], S);
-      else mk_selfmat<2><<<1, 32, 0, st>>> (m->selfc[0], m->selfc[1], m->selfc[2], S);
+      const double s0 = m->poly ? 1.0 : m->selfc[0], s1 = m->poly ? 1.0 : m->selfc[1],
+                   s2 = m->poly ? 1.0 : m->selfc[2];
+      if (c->version == 0) mk_selfmat<0><<<1, 32, 0, st>>> (s0, s1, s2, S);
+      else if (c->version == 1) mk_selfmat<1><<<1, 32, 0, st>>> (s0, s1, s2, S);
+      else mk_selfmat<2><<<1, 32, 0, st>>> (s0, s1, s2, S);
       if ((e = cudaStreamSynchronize (st)) != cudaSuccess) return cuda_fail (e, "mixed self matrix");
       m->self_fp = m->fp;
+    }
+  if (m->poly && m->poly_fp != m->fp)
+    {
+      // radii, squared radii and the self terms at the split
+      // (src/ewald.c:579-642 with this split's xi)
+      std::vector<float> r ((size_t) np), q ((size_t) np);
+      std::vector<double> sf ((size_t) 3 * np);
+      const double xisp = m->xi / sqrt (M_PI), xi2 = m->xi * m->xi;
+      for (int i = 0; i < np; i++)
+        {
+          const double a = sys->a[i], a2 = a * a, a3 = a2 * a;
+          r[i] = (float) a;
+          q[i] = (float) a2;
+          sf[3 * i] = 1.0 - a * xisp * (6.0 - 40.0 / 3.0 * xi2 * a2);
+          sf[3 * i + 1] = 0.75 - a3 * xisp * xi2 * 10.0;
+          sf[3 * i + 2] = 0.9 - a3 * xisp * xi2 * (12.0 - 30.24 * xi2 * a2);
+        }
+      if ((e = m->prad.ensure (sizeof (float) * np)) != cudaSuccess
+          || (e = m->pqa.ensure (sizeof (float) * np)) != cudaSuccess
+          || (e = m->pself.ensure (sizeof (double) * 3 * np)) != cudaSuccess)
+        return cuda_fail (e, "particle tables");
+      e = cudaMemcpyAsync (m->prad.p, r.data (), sizeof (float) * np, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync (m->pqa.p, q.data (), sizeof (float) * np, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync (m->pself.p, sf.data (), sizeof (double) * 3 * np,
+                             cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize (st);
+      if (e != cudaSuccess) return cuda_fail (e, "particle tables");
+      m->poly_fp = m->fp;
     }
   // 1024 rotations e^{2 pi i h / 1024} as FP32 pairs hi + lo, made once
   if (!m->rot.p)
@@ -1455,7 +1677,8 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     ra.rmin = (float) sys->rmin;
     ra.xi = (float) m->xi;
     ra.xisp = (float) (m->xi / sqrt (M_PI));
-    ra.rad = nullptr; ra.slipa = nullptr;
+    ra.rad = m->poly ? (const float *) m->prad.p : nullptr;
+    ra.slipa = nullptr;
     ra.clampfix = sys->rmin > 0.0 ? 1 : 0;
     ra.rm2 = (float) (4.0 * sys->rmin * sys->rmin);
     ra.out_clamp = (float *) m->part_real.p + (size_t) 2 * np * C;
@@ -1484,9 +1707,15 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
             (uint4 *) m->sq.p);
           kmark (c, rs, "mk_cells");
         }
-      if (c->version == 0) mk_real<0><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
-      else if (c->version == 1) mk_real<1><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
-      else mk_real<2><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
+      if (m->poly)
+        {
+          if (c->version == 0) mk_real<0, true><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
+          else if (c->version == 1) mk_real<1, true><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
+          else mk_real<2, true><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
+        }
+      else if (c->version == 0) mk_real<0, false><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
+      else if (c->version == 1) mk_real<1, false><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
+      else mk_real<2, false><<<gr, RG_WARPS * 32, 0, rs>>> (ra);
       if (ra.clampfix)
         {
           const int gc = (np + 7) / 8;
@@ -1520,6 +1749,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     cb.pk = (const float *) m->part_rec.p;
     cb.nck = m->nchunk_k;
     cb.S = (const double *) m->selfbuf.p;
+    cb.selfp = m->poly ? (const double *) m->pself.p : nullptr;
     cb.np = np;
     cb.c = C;
     cb.y = d_y;
@@ -1531,6 +1761,18 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
         if ((e = launch_kspace_forward (c->version, m->plan, m->maps, ka.kt, m->nkh,
                                         (int *) m->status.p, st, c)) != cudaSuccess)
           return cuda_fail (e, "reciprocal space (tensor cores)");
+      }
+    else if (m->nkh > 0 && m->poly)
+      {
+        const float *qa = (const float *) m->pqa.p, *rad = (const float *) m->prad.p;
+        if (c->version == 0) mk_sfac_poly<0><<<gk, MX_WARPS * 32, 0, st>>> (ka, qa);
+        else if (c->version == 1) mk_sfac_poly<1><<<gk, MX_WARPS * 32, 0, st>>> (ka, qa);
+        else mk_sfac_poly<2><<<gk, MX_WARPS * 32, 0, st>>> (ka, qa);
+        kmark (c, st, "mk_sfac_poly");
+        if (c->version == 0) mk_backproj_poly<0><<<gb, MX_WARPS * 32, 0, st>>> (ba, rad);
+        else if (c->version == 1) mk_backproj_poly<1><<<gb, MX_WARPS * 32, 0, st>>> (ba, rad);
+        else mk_backproj_poly<2><<<gb, MX_WARPS * 32, 0, st>>> (ba, rad);
+        kmark (c, st, "mk_backproj_poly");
       }
     else if (m->nkh > 0)
       {

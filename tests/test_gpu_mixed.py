@@ -110,15 +110,63 @@ def test_mixed_unwrapped_positions(lib):
 
 
 def test_mixed_rejects_unsupported(lib):
+    """Slip, and unequal radii under the rmin clamp, stay on the FP64 path."""
     from libstokes_gb300 import MIXED, GPUError, System
     from libstokes_gb300.workloads import rsa_positions
     pos, L = rsa_positions(20, 0.2, seed=2)
     s = System(0, pos, (L, L, L))
-    s.set_radius(np.ones(20))
+    s.set_slip(np.full(20, 0.5))
     s.set_precision(MIXED)
     with pytest.raises(GPUError):
         s.atimes(np.ones(60))
     s.close()
+    s = System(0, pos, (L, L, L))
+    s.set_radius(np.full(20, 0.9))
+    s.set_misc(1.0)
+    s.set_precision(MIXED)
+    with pytest.raises(GPUError):
+        s.atimes(np.ones(60))
+    s.close()
+
+
+@pytest.mark.parametrize("version,n,phi", [(0, 200, 0.2), (1, 160, 0.25), (2, 120, 0.3),
+                                           (2, 1000, 0.3)])
+def test_mixed_unequal_radii(lib, version, n, phi):
+    """Unequal radii (0.6 to 1.0) on the mixed path (FP32 SD-form poly
+    scalars in real space, q-weighted structure factors in reciprocal space,
+    per-particle self terms) against the FP64 path, which the golden poly
+    cases pin to the reference at 1e-12; and the kernels that ran."""
+    from libstokes_gb300 import FP64, MIXED, System, abi
+    from libstokes_gb300.workloads import rsa_positions
+    pos, L = rsa_positions(n, phi, seed=50 + version)
+    a = np.random.default_rng(51 + version).uniform(0.6, 1.0, n)
+    x = np.random.default_rng(52).standard_normal((3, 6, 11)[version] * n)
+    s = System(version, pos, (L, L, L))
+    s.set_radius(a)
+    s.set_precision(FP64)
+    y64 = s.atimes(x)
+    s.set_precision(MIXED)
+    lib.stokes_gpu_kprof_begin(s.sp, 16)
+    ym = s.atimes(x)
+    names = abi.kernel_profile(lib, s.sp)
+    assert "mk_backproj_poly" in names, names
+    assert rel_l2(ym, y64) < TOL, rel_l2(ym, y64)
+    s.close()
+
+
+def test_mixed_unequal_radii_golden(lib, products):
+    """Against the reference's own products for unequal radii."""
+    from conftest import make_system
+    from libstokes_gb300 import MIXED
+    for name in ("r12_v0_poly", "r12_v1_poly", "r12_v2_poly"):
+        if name not in products:
+            continue
+        case = products[name]
+        s = make_system(case)
+        s.set_precision(MIXED)
+        y = s.atimes(case["x"])
+        assert rel_l2(y, case["y"]) < TOL, (name, rel_l2(y, case["y"]))
+        s.close()
 
 
 @pytest.mark.parametrize("version,n,phi", [(0, 200, 0.2), (1, 150, 0.25), (2, 120, 0.3)])
