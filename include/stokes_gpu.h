@@ -48,8 +48,9 @@ void stokes_gpu_set_error_mode (int mode);
 /* precision of the products of this system (default: STOKES_GPU_FP64, or
  * the value of the LIBSTOKES_GB300_PRECISION environment variable,
  * "fp64" or "mixed", at the first product of a system).  Mixed precision
- * (<= 1e-6 against FP64) serves periodic equal or unequal spheres without
- * slip (unequal ones with rmin = 0); other systems report an error in it. */
+ * (<= 1e-6 against FP64) serves open systems, and periodic equal or unequal
+ * spheres without slip (unequal ones with rmin = 0); other periodic systems
+ * report an error in it. */
 int stokes_gpu_set_precision (struct stokes *sys, int mode);
 int stokes_gpu_get_precision (const struct stokes *sys, int *mode);
 
