@@ -157,7 +157,11 @@ void stokes_unset_slip (struct stokes *sys);
  * y = M x for the Ewald-summed F/FT/FTS mobility, n = np*{3,6,11}.
  * x holds F | FT | FTS (stresslet as xx,xy,xz,yz,yy) per particle, y the
  * matching U | UO | UOE.  y is fully overwritten.  sys->cpu1/2/3 are set to
- * the GPU time (ms) of the whole product / real part / reciprocal part.
+ * the GPU time (ms) of the whole product / real part / the rest
+ * (cpu1 = cpu2 + cpu3, as in the reference).  In mixed precision the real
+ * part runs on a second stream beside the reciprocal part: cpu2 is its span
+ * there (as measured on the configuration's last launch outside its CUDA
+ * graph) and cpu3 the rest of the product's span.
  * On a device or input error the library prints the reason, records it for
  * stokes_gpu_last_error() and exits the process with status 1 -- the
  * reference's own behaviour on allocation failure (src/memory-check.h:22-25). */

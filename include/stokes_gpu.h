@@ -102,7 +102,9 @@ int stokes_gpu_matrix_dev (struct stokes *sys, const double *d_pos,
 int stokes_gpu_matvec_dev (int version, int np, const double *d_mat,
                            const double *d_x, double *d_y, void *stream);
 
-/* device milliseconds of the last product: total, real, reciprocal */
+/* device milliseconds of the last host-buffer product: total, real space,
+ * the rest (the real space runs beside the reciprocal part in mixed
+ * precision; the rest is then total - real) */
 int stokes_gpu_last_times (const struct stokes *sys, double *ms3);
 
 /* Profiling window for the device entry points: between begin and end, each

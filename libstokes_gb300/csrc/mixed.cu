@@ -1372,7 +1372,7 @@ run_mixed_sequence (Ctx *c, MixedState *m, const double *d_pos, const double *d_
   mix ((uint64_t) (uintptr_t) E);
   // a captured cudaEventRecord is only a dependency, not a record: around a
   // replay the start and end events are recorded on the stream itself, and
-  // the real / reciprocal split keeps the last direct launch's events
+  // the real-space span is the one of the configuration's last direct launch
   auto replay = [&] () -> int {
     if (E) cudaEventRecord (E[0], st);
     const cudaError_t le = cudaGraphLaunch (m->gexec, st);
@@ -1695,9 +1695,11 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       }
     const int tpc = RG_WARPS / m->real_g;
     const int gr = (np + tpc - 1) / tpc;
-    // concurrent with the reciprocal chain unless the launches are being
-    // timed one by one (then in order: reciprocal, real, combine)
-    const bool overlap = !E && !c->kprof_on && m->side;
+    // concurrent with the reciprocal chain unless a profiling window times
+    // the launches one by one (then in order: reciprocal, real, combine).
+    // The host call's own timing (E == c->ev) keeps the overlap and times
+    // the real space on the side stream
+    const bool overlap = (!E || E == c->ev) && !c->kprof_on && m->side;
     auto launch_real = [&] (cudaStream_t rs) {
       if (m->nc[0])
         {
@@ -1728,7 +1730,9 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       {
         cudaEventRecord (m->ev_fork, st);
         cudaStreamWaitEvent (m->side, m->ev_fork, 0);
+        if (E) cudaEventRecord (E[1], m->side);
         launch_real (m->side);
+        if (E) cudaEventRecord (E[2], m->side);
         cudaEventRecord (m->ev_join, m->side);
       }
 
@@ -1788,15 +1792,15 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     else
       cudaMemsetAsync (m->part_rec.p, 0, sizeof (float) * (size_t) m->nchunk_k * np * C, st);
     // the real-space partials must be complete before the combine
-    if (E) cudaEventRecord (E[1], st);
     if (overlap)
       cudaStreamWaitEvent (st, m->ev_join, 0);
     else
       {
+        if (E) cudaEventRecord (E[1], st);
         launch_real (st);
         kmark (c, st, "mk_real");
+        if (E) cudaEventRecord (E[2], st);
       }
-    if (E) cudaEventRecord (E[2], st);
     if (fused
         && (e = launch_kspace_backward (c->version, m->plan, m->maps, (float *) m->part_rec.p,
                                         (int *) m->status.p, st, c)) != cudaSuccess)

@@ -233,3 +233,23 @@ def test_tiny_systems(lib, version, n):
     assert np.abs(m32 - m64).max() / np.abs(m64).max() < 1e-6
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("n,phi", [(1000, 0.3), (3000, 0.3)])
+def test_timed_host_calls_overlap(lib, n, phi):
+    """The drop-in call times itself (sys->cpu1..3) with the real space on its
+    second stream: over direct launches, the graph capture and its replays,
+    with a new x each call, the product matches the FP64 path and the phase
+    times add up (total = real + rest, each positive)."""
+    a, b, _ = _pair(2, n, phi, seed=17)
+    rng = np.random.default_rng(18)
+    for call in range(6):
+        x = rng.standard_normal(11 * n)
+        y = b.atimes(x)
+        assert rel_l2(y, a.atimes(x)) < TOL, call
+        t = b.times()
+        assert t[0] > 0 and t[1] > 0 and t[2] > 0, (call, t)
+        assert abs(t[0] - t[1] - t[2]) < 1e-6 * t[0]
+        assert (b.s.cpu1, b.s.cpu2, b.s.cpu3) == tuple(t)
+    a.close()
+    b.close()
