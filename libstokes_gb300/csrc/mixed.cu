@@ -987,41 +987,55 @@ struct CombineArgs {
   double *y;            // output [np c]
 };
 
-constexpr int CMB_LANES = 4;    // threads per output element
+constexpr int CMB_OUT = 32;      // elements per CTA (one per lane)
+constexpr int CMB_WARPS = 8;     // chunk groups per element (one per warp)
+constexpr int CMB_BATCH = 4;     // loads in flight per thread
 
-// Four threads per element t = i c + q: lane l sums the chunks l, l + 4, ...
-// of both partial sets (Kahan-compensated FP32, all its loads in flight);
-// the lanes meet in FP64 through shuffles, and lane 0 adds the FP64 self
-// term (at most five FMAs: the self block is diagonal for F and T and
-// couples the five stresslet components).
-__global__ void __launch_bounds__ (256)
+// CTA of eight warps over the 32 consecutive elements t = i c + q of its
+// lanes: warp w sums the chunks w, w + 8, ... of the real-space partials
+// and, doubled (half k space; exact in FP32), of the reciprocal ones, so
+// each load instruction reads 32 consecutive elements of one chunk and up
+// to four loads per thread are in flight at once (TwoSum-compensated FP32).
+// The warps' (sum, compensation) pairs meet in shared memory; warp 0 adds
+// them in FP64 with the FP64 self term (at most five FMAs: the self block
+// is diagonal for F and T and couples the five stresslet components) and
+// writes 32 consecutive elements of y.
+__global__ void __launch_bounds__ (CMB_OUT * CMB_WARPS)
 mk_combine (CombineArgs a)
 {
+  __shared__ float2 s_p[CMB_WARPS][CMB_OUT];
   const int n = a.np * a.c;
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  const int t = g / CMB_LANES, l = g % CMB_LANES;
-  const int tt = t < n ? t : n - 1;        // the shuffles need every lane
-  float sr = 0.f, cr = 0.f, sk = 0.f, ck = 0.f;
-#pragma unroll 8
-  for (int k = l; k < a.ncr; k += CMB_LANES)
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int t = blockIdx.x * CMB_OUT + lane;
+  const int tt = t < n ? t : n - 1;
+  const int ntot = a.ncr + a.nck;
+  float sum = 0.f, comp = 0.f;
+  for (int k0 = w; k0 < ntot; k0 += CMB_BATCH * CMB_WARPS)
     {
-      const float v = a.pr[(size_t) k * n + tt] - cr;
-      const float u = sr + v;
-      cr = (u - sr) - v;
-      sr = u;
+      float v[CMB_BATCH];
+#pragma unroll
+      for (int u = 0; u < CMB_BATCH; u++)
+        {
+          const int k = k0 + u * CMB_WARPS;
+          v[u] = k < a.ncr ? a.pr[(size_t) k * n + tt]
+                 : (k < ntot ? 2.f * a.pk[(size_t) (k - a.ncr) * n + tt] : 0.f);
+        }
+#pragma unroll
+      for (int u = 0; u < CMB_BATCH; u++)
+        {
+          // TwoSum: sum + v = sn + e exactly
+          const float sn = sum + v[u];
+          const float bp = sn - sum;
+          comp += (sum - (sn - bp)) + (v[u] - bp);
+          sum = sn;
+        }
     }
-#pragma unroll 8
-  for (int k = l; k < a.nck; k += CMB_LANES)
-    {
-      const float v = a.pk[(size_t) k * n + tt] - ck;
-      const float u = sk + v;
-      ck = (u - sk) - v;
-      sk = u;
-    }
-  double r = ((double) sr - (double) cr) + 2.0 * ((double) sk - (double) ck);
-  r += __shfl_xor_sync (0xffffffffu, r, 1);
-  r += __shfl_xor_sync (0xffffffffu, r, 2);
-  if (l != 0 || t >= n) return;
+  s_p[w][lane] = make_float2 (sum, comp);
+  __syncthreads ();
+  if (w != 0 || t >= n) return;
+  double r = 0.0;
+#pragma unroll
+  for (int g = 0; g < CMB_WARPS; g++) r += (double) s_p[g][lane].x + (double) s_p[g][lane].y;
   const int i = t / a.c, q = t - i * a.c;
   const int q0 = (q < 6) ? q : 6, nq = (q < 6) ? 1 : 5;
   const double *xi = a.x + (size_t) a.c * i;
@@ -1726,14 +1740,24 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
           else mk_clamp<2><<<gc, 256, 0, rs>>> (ra);
         }
     };
+    // the real space depends on mk_prep only and joins before the combine;
+    // on the tensor-core path its launch is recorded after the forward
+    // GEMM's, so the GEMM takes the SMs first and the real-space CTAs fill
+    // what the chain leaves idle up to the back-projection (measured, one
+    // GB300: FTS N = 256 49 -> 39 us, FT N = 2048 123 -> 112 us, FTS
+    // N = 4096 295 -> 283 us, N = 1000 unchanged)
+    auto fork_real = [&] () {
+      cudaStreamWaitEvent (m->side, m->ev_fork, 0);
+      if (E) cudaEventRecord (E[1], m->side);
+      launch_real (m->side);
+      if (E) cudaEventRecord (E[2], m->side);
+      cudaEventRecord (m->ev_join, m->side);
+    };
+    const bool fused = m->nkh > 0 && m->tensor;
     if (overlap)
       {
         cudaEventRecord (m->ev_fork, st);
-        cudaStreamWaitEvent (m->side, m->ev_fork, 0);
-        if (E) cudaEventRecord (E[1], m->side);
-        launch_real (m->side);
-        if (E) cudaEventRecord (E[2], m->side);
-        cudaEventRecord (m->ev_join, m->side);
+        if (!fused) fork_real ();
       }
 
     KMixArgs ka;
@@ -1757,7 +1781,6 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
     cb.np = np;
     cb.c = C;
     cb.y = d_y;
-    const bool fused = m->nkh > 0 && m->tensor;
     // reciprocal space up to the k operators (tensor cores) or the SIMT sums;
     // then the real-space partials, the back-projection and the final sum
     if (fused)
@@ -1765,6 +1788,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
         if ((e = launch_kspace_forward (c->version, m->plan, m->maps, ka.kt, m->nkh,
                                         (int *) m->status.p, st, c)) != cudaSuccess)
           return cuda_fail (e, "reciprocal space (tensor cores)");
+        if (overlap) fork_real ();
       }
     else if (m->nkh > 0 && m->poly)
       {
@@ -1791,10 +1815,7 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
       }
     else
       cudaMemsetAsync (m->part_rec.p, 0, sizeof (float) * (size_t) m->nchunk_k * np * C, st);
-    // the real-space partials must be complete before the combine
-    if (overlap)
-      cudaStreamWaitEvent (st, m->ev_join, 0);
-    else
+    if (!overlap)
       {
         if (E) cudaEventRecord (E[1], st);
         launch_real (st);
@@ -1805,7 +1826,9 @@ atimes_mixed_dev (Ctx *c, const double *d_pos, const double *d_x, double *d_y,
         && (e = launch_kspace_backward (c->version, m->plan, m->maps, (float *) m->part_rec.p,
                                         (int *) m->status.p, st, c)) != cudaSuccess)
       return cuda_fail (e, "reciprocal space (tensor cores)");
-    mk_combine<<<(int) (((long long) np * C * CMB_LANES + 255) / 256), 256, 0, st>>> (cb);
+    // the real-space partials must be complete before the combine
+    if (overlap) cudaStreamWaitEvent (st, m->ev_join, 0);
+    mk_combine<<<(np * C + CMB_OUT - 1) / CMB_OUT, CMB_OUT * CMB_WARPS, 0, st>>> (cb);
     kmark (c, st, "mk_combine");
     if (E) cudaEventRecord (E[3], st);
     if (m->tensor)
