@@ -1068,21 +1068,32 @@ env_double (const char *name, double dflt)
   return s ? atof (s) : dflt;
 }
 
-// default split parameter eta = xi L by system size (see split_for)
+// default split parameter eta = xi V^(1/3), minimum image, by version and
+// system size.  Measured on one GB300 (FTS at phi 0.3, FT 0.25, F 0.2) with
+// the real space recorded after the forward GEMM; an eta below the smallest
+// minimum-image split is raised to it, so small values all time the same:
+//   FTS  N <= 512: 8 (N = 512 49.0 us against 52.5 with images at 10);
+//        N <= 4096: 10 (N = 4096 273 us against 283 with images at 11);
+//        above: 11 (N = 8192 726 us against 936 with images at 13)
+//   FT   N = 1025-8192: 9 (N = 4096 171 us against 233 at 12; N = 8192
+//        444 against 614 at 14)
+//   F    N = 1025-4096: 9 (N = 2048 69.6 us against 75.2 at 12); above 12
+//        (N = 16384 1131 us against 1189 at 9)
+//   N <= 1024: the time is flat over eta 7-11 for all three
 static double
-default_eta (int np)
+default_eta (int version, int np)
 {
   if (np <= 256) return 8.0;
+  if (version == 2) return np <= 512 ? 8.0 : (np <= 4096 ? 10.0 : 11.0);
   if (np <= 1024) return 10.0;
-  if (np <= 4096) return 12.0;
-  return 14.0;
+  if (version == 1) return np <= 8192 ? 9.0 : 10.0;
+  return np <= 4096 ? 9.0 : 12.0;
 }
 
-// FTS: the split may take lattice images in real space.  Measured (one
-// GB300): FTS N = 256 runs 53 us at eta 7 with images against 61 us at the
-// minimum-image eta (11.2); at N = 1000 eta 8-11 all run 86 us; at N = 4096
-// eta 11 is best either way.  F and FT keep the minimum-image split (images
-// measured slower for them).
+// eta when lattice images are asked for (LIBSTOKES_GB300_MIXED_IMAGES=1)
+// or the box is too small for a minimum-image cutoff (measured before the
+// real space moved behind the forward GEMM: FTS N = 256 53 us at eta 7
+// against 61 us at the minimum-image split of then)
 static double
 default_eta_images (int np)
 {
@@ -1100,15 +1111,14 @@ mixed_setup (Ctx *c, const struct stokes *sys, MixedState *m)
   // against FP64 is 2.92e-7 at 1e-8, 2.99e-7 at 3e-8, 3.03e-7 at 1e-7 --
   // FP32 rounding, not truncation, sets it -- and the cutoffs shrink)
   const double eps = env_double ("LIBSTOKES_GB300_MIXED_EPS", 3e-8);
-  // FTS takes lattice images in real space except between 512 and 2048
-  // particles, where the minimum-image split is faster (measured, one GB300,
-  // phi 0.3: N = 1000 74-86 us per product against 86-90 us with images,
-  // the real-space sum 18-23 us against 33-39 us; N = 256 and 4096 faster
-  // with images: 53 against 61 us, 295 against 406 us)
-  const bool fts_images = sys->version == 2 && !(sys->np > 512 && sys->np < 2048);
-  bool images = env_double ("LIBSTOKES_GB300_MIXED_IMAGES", fts_images ? 1.0 : 0.0) != 0.0;
+  // minimum image unless asked otherwise: with the real space overlapping
+  // the back-projection, lattice images were faster at no measured size
+  // (FTS N = 256-512 level at eta 8; N = 4096 283 against 273 us; N = 8192
+  // and 16384 level at eta 11, where the cutoff is below half the box)
+  bool images = env_double ("LIBSTOKES_GB300_MIXED_IMAGES", 0.0) != 0.0;
   double eta = env_double ("LIBSTOKES_GB300_MIXED_ETA",
-                           images ? default_eta_images (sys->np) : default_eta (sys->np));
+                           images ? default_eta_images (sys->np)
+                                  : default_eta (sys->version, sys->np));
   uint64_t fp = mix_fingerprint (sys, eta + (images ? 1000.0 : 0.0), eps);
   const bool poly = c->mode == MODE_POLY;
   double amax = 1.0;

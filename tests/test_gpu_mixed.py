@@ -253,3 +253,16 @@ def test_timed_host_calls_overlap(lib, n, phi):
         assert (b.s.cpu1, b.s.cpu2, b.s.cpu3) == tuple(t)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("version", [0, 1, 2])
+def test_lattice_images_on_request(lib, monkeypatch, version):
+    """The real space over lattice images (LIBSTOKES_GB300_MIXED_IMAGES=1, a
+    split whose cutoff exceeds half the box) against the FP64 path; the
+    default is the minimum-image split, images only for boxes too small."""
+    monkeypatch.setenv("LIBSTOKES_GB300_MIXED_IMAGES", "1")
+    monkeypatch.setenv("LIBSTOKES_GB300_MIXED_ETA", "6")
+    a, b, x = _pair(version, 300, 0.3, seed=23)
+    assert rel_l2(b.atimes(x), a.atimes(x)) < TOL
+    a.close()
+    b.close()
