@@ -141,17 +141,24 @@ void BD_params_free (struct BD_params *BD);
 double BD_params_get_fact (struct BD_params *BD, double dt);
 /* src/brownian.c:2033-2058: nm*3 (F) or nm*6 (FT, FTS) */
 int BD_get_n (struct stokes *sys);
-/* src/brownian.c:1545-1874, Chebyshev branch (n_minv > 0, no lubrication,
- * HI on, no fixed particles, equal or unequal spheres): z = M^{-1/2} y with
- * y ~ N(0,1) from BD->rng.  When eig_minv[0] == eig_minv[1] the bounds are
- * estimated first (20-step FP64 Lanczos on the device, in place of ARPACK)
- * and a_minv is fitted.  Unsupported branches exit with a message. */
+/* src/brownian.c:1545-1874, Chebyshev branch (n_minv > 0, HI on, no fixed
+ * particles, equal or unequal spheres): z = M^{-1/2} y with y ~ N(0,1) from
+ * BD->rng.  When eig_minv[0] == eig_minv[1] the bounds are estimated first
+ * (20-step FP64 Lanczos on the device, in place of ARPACK) and a_minv is
+ * fitted.  With BD->flag_lub_B (equal spheres without slip, n_lub > 0) the
+ * lubrication noise L^{1/2} y_lub is added, y_lub drawn after y: Chebyshev
+ * of sqrt on [eig_lub[0], eig_lub[1]] with the device lubrication operator,
+ * bounds by Lanczos when eig_lub[0] == eig_lub[1] (lower bound at least 0),
+ * re-estimated when |y.Ly - z.z| / y.Ly > BD->eps (src/brownian.c:1734-1849).
+ * Unsupported branches (the matrix forms n_minv <= 0, n_lub <= 0) exit with
+ * a message. */
 void BD_calc_FB (struct BD_params *BD, double *z);
 /* src/brownian.c:2352-2560 (scheme 0, F and FT, quaternions q when given,
  * constant force F/T, EV_LJ repulsion, imposed flow and shear, dt halving on
  * overlap when sys->rmin == 0 and BD->rmin > 0; with BD->flag_lub the
  * velocities solve (I + M L) u = M f on the device, GMRES settings from
- * sys->it): one mid-point step with noise from BD_calc_FB; returns the dt
+ * sys->it; BD->flag_lub_B adds the lubrication noise as in BD_calc_FB): one
+ * mid-point step with noise from BD_calc_FB; returns the dt
  * done.  The products run on the GPU
  * in the precision set for sys (stokes_gpu_set_precision). */
 double BD_evolve_mid (double t, struct BD_params *BD, double *x, double *q, double dt);

@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <vector>
 
@@ -32,6 +33,9 @@ namespace lsg {
 int cheb_clenshaw_dev (Ctx *c, const double *d_pos, int ncheb, const double *a, int n,
                        const double *d_y, double *d_z, double e0, double e1, cudaStream_t st,
                        DevBuf &work);
+int cheb_clenshaw_op (int ncheb, const double *a, int n, const double *d_y, double *d_z,
+                      double e0, double e1, cudaStream_t st, DevBuf &work,
+                      const std::function<int (const double *, double *)> &op);
 
 // ---------------------------------------------------------------------------
 // kernels
@@ -340,6 +344,14 @@ k_bd_copy (int n, const double *a, double *b)
   if (k < n) b[k] = a[k];
 }
 
+// y += x
+__global__ void
+k_bd_add (int n, const double *x, double *y)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) y[k] += x[k];
+}
+
 // z (particle order, zc per particle) -> product input (c per particle)
 __global__ void
 k_bd_zexpand (int np, int nm, int c, const double *z, double *x)
@@ -406,6 +418,7 @@ struct stokes_gpu_bd {
   int nm = 0, np = 0, C = 3, n = 0;   // n = BD_get_n (noise length)
   lsg::DevBuf x, xmid, y, z, f, u, fext, work, lan, tmp, dots, pos_fixed;
   lsg::DevBuf xnew, lje, ljr0, ovl;    // drop-in BD_evolve_mid
+  lsg::DevBuf lubv;                    // drop-in lubrication noise: y, z, L y
   bool lj_arrays = false;              // per-particle EV_LJ coefficients in lje, ljr0
   bool ref_lj = false;                 // drop-in: the reference's EV_LJ pair force
   double eig[2] = {0, 0};
@@ -490,22 +503,25 @@ tridiag_extreme (const std::vector<double> &al, const std::vector<double> &be, b
 
 static double f_invsqrt (double x) { return 1.0 / sqrt (x); }
 
-// FP64 Lanczos with full reorthogonalisation, m steps
+// FP64 Lanczos with full reorthogonalisation, m steps, for a symmetric
+// operator op on particle-ordered vectors of length b->n (start vector: a
+// device Gaussian of stream `stream`): the extreme Ritz values
 static int
-bd_lanczos (stokes_gpu_bd *b, const double *d_pos, int m, double lo_fac, double hi_fac)
+lanczos_extremes (stokes_gpu_bd *b, int m, unsigned long long stream,
+                  const std::function<int (const double *, double *)> &op, double *lmin,
+                  double *lmax)
 {
   cudaStream_t st = b->c->stream;
-  const int n = b->n, np = b->np, C = b->C, nx = C * np;
+  const int n = b->n;
   cudaError_t e;
   if ((e = b->lan.ensure (sizeof (double) * (size_t) (m + 1) * n)) != cudaSuccess)
     return cuda_fail (e, "Lanczos vectors");
   double *V = (double *) b->lan.p;
   double *w = (double *) b->f.p;            // scratch vector of length >= n
-  double *xin = (double *) b->tmp.p, *xout = xin + nx;
   double *dots = (double *) b->dots.p;
   std::vector<double> al, be (1, 0.0), h (m + 1);
   // start vector: device Gaussian, normalised
-  k_bd_gauss<<<gridn (n), 256, 0, st>>> (n, b->p.seed ^ 0x9e3779b97f4a7c15ull, 77ull, V);
+  k_bd_gauss<<<gridn (n), 256, 0, st>>> (n, b->p.seed ^ 0x9e3779b97f4a7c15ull, stream, V);
   cudaMemsetAsync (dots, 0, 2 * sizeof (double), st);
   k_bd_dot2<<<64, 256, 0, st>>> (n, V, V, V, V, dots);
   cudaMemcpyAsync (b->h_dots, dots, sizeof (double), cudaMemcpyDeviceToHost, st);
@@ -514,10 +530,8 @@ bd_lanczos (stokes_gpu_bd *b, const double *d_pos, int m, double lo_fac, double 
   for (int j = 0; j < m; j++)
     {
       double *vj = V + (size_t) j * n;
-      k_bd_zexpand<<<gridn (np), 256, 0, st>>> (np, b->nm, C, vj, xin);
-      int rc = bd_prod (b, d_pos, xin, xout);
+      int rc = op (vj, w);
       if (rc) return rc;
-      k_bd_zcompress<<<gridn (b->nm), 256, 0, st>>> (b->nm, C, xout, w);
       // two rounds of classical Gram-Schmidt against V[0..j]
       for (int pass = 0; pass < 2; pass++)
         {
@@ -538,7 +552,28 @@ bd_lanczos (stokes_gpu_bd *b, const double *d_pos, int m, double lo_fac, double 
       be.push_back (beta);
       k_bd_scale<<<gridn (n), 256, 0, st>>> (n, w, 1.0 / beta, V + (size_t) (j + 1) * n);
     }
-  const double lmin = tridiag_extreme (al, be, false), lmax = tridiag_extreme (al, be, true);
+  *lmin = tridiag_extreme (al, be, false);
+  *lmax = tridiag_extreme (al, be, true);
+  return STOKES_GPU_OK;
+}
+
+// bounds of the mobility's spectrum (Ritz extremes widened by lo_fac,
+// hi_fac) and the coefficients of 1/sqrt on them
+static int
+bd_lanczos (stokes_gpu_bd *b, const double *d_pos, int m, double lo_fac, double hi_fac)
+{
+  cudaStream_t st = b->c->stream;
+  const int np = b->np, C = b->C, nx = C * np;
+  double *xin = (double *) b->tmp.p, *xout = xin + nx;
+  double lmin = 0.0, lmax = 0.0;
+  int rc = lanczos_extremes (b, m, 77ull, [&] (const double *v, double *w) {
+    k_bd_zexpand<<<gridn (np), 256, 0, st>>> (np, b->nm, C, v, xin);
+    const int r = bd_prod (b, d_pos, xin, xout);
+    if (r) return r;
+    k_bd_zcompress<<<gridn (b->nm), 256, 0, st>>> (b->nm, C, xout, w);
+    return (int) STOKES_GPU_OK;
+  }, &lmin, &lmax);
+  if (rc) return rc;
   if (!(lmin > 0.0))
     return set_error (STOKES_GPU_EACCURACY, "mobility not positive definite (Ritz min %g)", lmin);
   b->eig[0] = lmin * lo_fac;
@@ -730,7 +765,8 @@ stokes_gpu_bd_destroy (stokes_gpu_bd *b)
   if (!b) return STOKES_GPU_OK;
   if (b->c) cudaStreamSynchronize (b->c->stream);
   for (DevBuf *d : {&b->x, &b->xmid, &b->y, &b->z, &b->f, &b->u, &b->fext, &b->work, &b->lan,
-                    &b->tmp, &b->dots, &b->pos_fixed, &b->xnew, &b->lje, &b->ljr0, &b->ovl})
+                    &b->tmp, &b->dots, &b->pos_fixed, &b->xnew, &b->lje, &b->ljr0, &b->ovl,
+                    &b->lubv})
     d->release ();
   if (b->h_dots) cudaFreeHost (b->h_dots);
   delete b;
@@ -911,12 +947,15 @@ dropin_engine (struct BD_params *BD, const char *fn)
   if (sys->version < 0 || sys->version > 1)
     dropin_die (fn, "the device BD serves the F and FT versions");
   if (sys->np != sys->nm) dropin_die (fn, "the device BD serves systems without fixed particles");
-  // flag_lub: the velocities solve the lubricated mobility problem; the
-  // Brownian lubrication force (flag_lub_B) is never set by the reference's
-  // BD_params_init (its pair check is commented out, src/brownian.c:161-180)
-  if (BD->flag_lub_B || BD->flag_mat)
-    dropin_die (fn, "the lubrication noise and matrix noise are not on the device path");
-  if (BD->flag_lub && (sys->a || sys->slip))
+  // flag_lub: the velocities solve the lubricated mobility problem.
+  // flag_lub_B adds the lubrication noise (the reference's BD_params_init
+  // leaves it 0, its pair check being commented out, src/brownian.c:161-180;
+  // a caller sets it): its Chebyshev form runs on the device, the matrix
+  // form (n_lub <= 0, LAPACK's Cholesky) does not
+  if (BD->flag_mat) dropin_die (fn, "the matrix noise is not on the device path");
+  if (BD->flag_lub_B && BD->n_lub <= 0)
+    dropin_die (fn, "the matrix form of the lubrication noise (n_lub <= 0) is not on the device path");
+  if ((BD->flag_lub || BD->flag_lub_B) && (sys->a || sys->slip))
     dropin_die (fn, "lubrication serves equal spheres without slip");
   if (BD->n_minv <= 0) dropin_die (fn, "n_minv <= 0 (matrix noise) is not on the device path");
   if (BD->br || BD->bonds || BD->ev || BD->ang || BD->ev_dh || BD->cf)
@@ -1026,6 +1065,74 @@ dropin_noise (stokes_gpu_bd *b, struct BD_params *BD, const double *d_pos, const
   b->last_err = err;
 }
 
+static double f_sqrt (double x) { return sqrt (x); }
+
+// BD_calc_FB's lubrication noise on the device, the Chebyshev form
+// (flag_lub_B, n_lub > 0; src/brownian.c:1734-1849): y_lub from BD->rng
+// after the mobility noise's draws, z_lub = L^{1/2} y_lub with L the
+// lubrication correction of the system (calc_lub_3f / 3ft at d_pos:
+// BD_atimes_lub_FU for equal spheres without fixed particles), added to the
+// noise in b->z.  The bounds of L are BD's own, estimated first when
+// eig_lub[0] == eig_lub[1] and again when |y.Ly - z.z| / y.Ly exceeds
+// BD->eps (chebyshev_error_Rsqrt), by FP64 Lanczos in place of ARPACK: the
+// Ritz extremes widened by (0.8, 1.05), the lower one at least 0 (L is
+// positive semi-definite; sqrt needs the interval in [0, inf)).  A system
+// with no pair within lubmax has L = 0 and gets z_lub = 0.
+static void
+dropin_lub_noise (stokes_gpu_bd *b, struct BD_params *BD, const double *d_pos, const char *fn)
+{
+  const int n = b->n;
+  cudaStream_t st = b->c->stream;
+  std::vector<double> y ((size_t) n);
+  for (double &v : y) v = KIrand_Gaussian (BD->rng);
+  if (BD->n_lub <= 0 || !BD->a_lub) dropin_die (fn, "the lubrication noise needs n_lub > 0");
+  cudaError_t e = b->lubv.ensure (sizeof (double) * 3 * (size_t) n);
+  if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+  double *d_y = (double *) b->lubv.p, *d_z = d_y + n, *d_ly = d_z + n;
+  e = cudaMemcpyAsync (d_y, y.data (), sizeof (double) * n, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) dropin_die (fn, cudaGetErrorString (e));
+  const struct stokes *sys = BD->sys;
+  const auto op = [&] (const double *in, double *out) {
+    return lub_dev (sys, sys->version, d_pos, in, out, st);
+  };
+  auto estimate = [&] () {
+    double lmin = 0.0, lmax = 0.0;
+    check_rc (lanczos_extremes (b, b->p.n_lanczos, 78ull, op, &lmin, &lmax), fn);
+    BD->eig_lub[0] = std::max (0.0, 0.8 * lmin);
+    BD->eig_lub[1] = 1.05 * lmax;
+    if (BD->eig_lub[1] > BD->eig_lub[0])
+      chebyshev_coef (BD->n_lub, f_sqrt, BD->eig_lub[0], BD->eig_lub[1], BD->a_lub);
+  };
+  auto error = [&] () {
+    check_rc (op (d_y, d_ly), fn);
+    double *d = (double *) b->dots.p;
+    cudaMemsetAsync (d, 0, 2 * sizeof (double), st);
+    k_bd_dot2<<<64, 256, 0, st>>> (n, d_y, d_ly, d_z, d_z, d);
+    cudaMemcpyAsync (b->h_dots, d, 2 * sizeof (double), cudaMemcpyDeviceToHost, st);
+    cudaError_t e2 = cudaStreamSynchronize (st);
+    if (e2 != cudaSuccess) dropin_die (fn, cudaGetErrorString (e2));
+    const double yy = b->h_dots[0], zz = b->h_dots[1];
+    if (!(yy > 0.0)) dropin_die (fn, "negative norm y.Ly of the lubrication noise");
+    return fabs (yy - zz) / yy;
+  };
+  auto evaluate = [&] () {
+    check_rc (cheb_clenshaw_op (BD->n_lub, BD->a_lub, n, d_y, d_z, BD->eig_lub[0],
+                                BD->eig_lub[1], st, b->work, op), fn);
+  };
+  if (BD->eig_lub[0] == BD->eig_lub[1]) estimate ();
+  // no positive spectrum: no pair within lubmax, L = 0
+  if (!(BD->eig_lub[1] > BD->eig_lub[0])) return;
+  evaluate ();
+  if (error () > BD->eps)
+    {
+      estimate ();
+      if (!(BD->eig_lub[1] > BD->eig_lub[0])) return;
+      evaluate ();
+      error ();
+    }
+  k_bd_add<<<gridn (n), 256, 0, st>>> (n, d_z, (double *) b->z.p);
+}
+
 static int
 dropin_overlap (stokes_gpu_bd *b, const double *d_pos, double rmin, const char *fn)
 {
@@ -1127,6 +1234,7 @@ BD_calc_FB (struct BD_params *BD, double *z)
   check_rc (prepare (b->c, sys, false), fn);
   upload (b->x, sys->pos, 3 * (size_t) sys->np, b->c->stream, fn);
   dropin_noise (b, BD, (const double *) b->x.p, fn);
+  if (BD->flag_lub_B) dropin_lub_noise (b, BD, (const double *) b->x.p, fn);
   std::vector<double> zp ((size_t) n);
   cudaError_t e = cudaMemcpyAsync (zp.data (), b->z.p, sizeof (double) * n,
                                    cudaMemcpyDeviceToHost, b->c->stream);
@@ -1175,6 +1283,7 @@ redo:
   check_rc (prepare (b->c, sys, false), fn);
 redo_fb:
   dropin_noise (b, BD, cur, fn);
+  if (BD->flag_lub_B) dropin_lub_noise (b, BD, cur, fn);
 redo_scale:
   {
     // 1: velocity at the current configuration, Euler half step from x

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <functional>
 #include <vector>
 
 #include "stokes_gpu.h"
@@ -26,12 +27,13 @@ k_clenshaw (int n, const double *x, const double *b1, const double *b0, const do
   if (k < n) out[k] = ca * x[k] + cb * b1[k] - b0[k] + cj * y[k];
 }
 
-// Clenshaw recurrence with every product on the device.  d_y, d_z: device
-// vectors of length n.  Scratch: 4 vectors of n on the context.
+// Clenshaw recurrence with every operator application on the device.  op
+// maps a device vector of length n to another (stream st).  d_y, d_z:
+// device vectors of length n.  Scratch: 4 vectors of n in work.
 int
-cheb_clenshaw_dev (Ctx *c, const double *d_pos, int ncheb, const double *a, int n,
-                   const double *d_y, double *d_z, double e0, double e1, cudaStream_t st,
-                   DevBuf &work)
+cheb_clenshaw_op (int ncheb, const double *a, int n, const double *d_y, double *d_z, double e0,
+                  double e1, cudaStream_t st, DevBuf &work,
+                  const std::function<int (const double *, double *)> &op)
 {
   cudaError_t e = work.ensure (sizeof (double) * 4 * (size_t) n);
   if (e != cudaSuccess) return cuda_fail (e, "Chebyshev work vectors");
@@ -46,18 +48,30 @@ cheb_clenshaw_dev (Ctx *c, const double *d_pos, int ncheb, const double *a, int 
     {
       double *bi2 = b[(i + 2) % 3], *bi1 = b[(i + 1) % 3], *bi0 = b[i % 3];
       const int j = ncheb - 1 - i;
-      int rc = atimes_dev (c, d_pos, bi1, x, st, false);
+      int rc = op (bi1, x);
       if (rc) return rc;
       k_clenshaw<<<grid, 256, 0, st>>> (n, x, bi1, bi0, d_y, 2.0 * da, 2.0 * db, a[j], bi2);
     }
   const int i = ncheb - 1;
   double *bi1 = b[(i + 1) % 3], *bi0 = b[i % 3];
-  int rc = atimes_dev (c, d_pos, bi1, x, st, false);
+  int rc = op (bi1, x);
   if (rc) return rc;
   k_clenshaw<<<grid, 256, 0, st>>> (n, x, bi1, bi0, d_y, da, db, a[0], d_z);
   e = cudaGetLastError ();
   if (e != cudaSuccess) return cuda_fail (e, "Clenshaw kernel");
   return STOKES_GPU_OK;
+}
+
+// the same with the context's mobility product at positions d_pos
+int
+cheb_clenshaw_dev (Ctx *c, const double *d_pos, int ncheb, const double *a, int n,
+                   const double *d_y, double *d_z, double e0, double e1, cudaStream_t st,
+                   DevBuf &work)
+{
+  return cheb_clenshaw_op (ncheb, a, n, d_y, d_z, e0, e1, st, work,
+                           [&] (const double *in, double *out) {
+                             return atimes_dev (c, d_pos, in, out, st, false);
+                           });
 }
 
 }  // namespace lsg

@@ -84,6 +84,41 @@ refbd_calc_fb (void *h, unsigned long seed, double peclet, int n_minv, double ei
   return BD_get_n (h);
 }
 
+/* z = BD_calc_FB with the lubrication noise (flag_lub_B = 1, the Chebyshev
+ * form n_lub > 0, src/brownian.c:1734-1849) at the given lubmin2 / lubmax.
+ * The bounds of L are preset (eig_lub[0] != eig_lub[1]: ARPACK is absent)
+ * and a_lub is fitted by the reference's chebyshev_coef of sqrt; bd_eps
+ * keeps both re-estimate branches off. */
+static double sqrt_fn (double x) { return sqrt (x); }
+int
+refbd_calc_fb_lub (void *h, unsigned long seed, double peclet, int n_minv, double eig0,
+                   double eig1, int n_lub, double eigl0, double eigl1, double bd_eps,
+                   double lubmin2, double lubmax, double *z)
+{
+  struct stokes *sys = h;
+  sys->lubmin2 = lubmin2;
+  sys->lubmax = lubmax;
+  const int nm = sys->nm;
+  double *Fb = calloc ((size_t) nm * 3, sizeof (double));
+  double *Tb = calloc ((size_t) nm * 3, sizeof (double));
+  double *Eb = calloc ((size_t) nm * 5, sizeof (double));
+  struct BD_params *BD = BD_params_init (sys, seed, Fb, Tb, Eb, NULL, NULL, NULL,
+                                         0 /* noHI */, 1 /* lub */, 0 /* mat */, 0.0 /* st */,
+                                         NULL, NULL, 1.0, NULL, NULL, NULL, NULL, NULL,
+                                         0 /* flag_Q */, peclet, bd_eps, n_minv, n_lub,
+                                         0 /* mid-point */, 0.0, 0.0, 1e-12);
+  BD->flag_lub_B = 1;
+  BD->eig_minv[0] = eig0;
+  BD->eig_minv[1] = eig1;
+  chebyshev_coef (n_minv, inv_sqrt, eig0, eig1, BD->a_minv);
+  BD->eig_lub[0] = eigl0;
+  BD->eig_lub[1] = eigl1;
+  chebyshev_coef (n_lub, sqrt_fn, eigl0, eigl1, BD->a_lub);
+  BD_calc_FB (BD, z);
+  free_bd (BD, NULL);
+  return BD_get_n (h);
+}
+
 /* nsteps BD_evolve_mid steps from time t0; x (nm*3) and q (nm*4 or NULL)
  * are advanced in place, x_traj[s] holds x after step s, dts[s] the dt done */
 int

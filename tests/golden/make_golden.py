@@ -264,6 +264,14 @@ LUB_CASES = [
 ]
 
 
+# BD_calc_FB with the lubrication noise (flag_lub_B = 1, Chebyshev form):
+# (name, version, N, phi, placement seed, lubmin2, lubmax, n_minv, n_lub, rng seed)
+LUBNOISE_CASES = [
+    ("lubnoise_f", 0, 30, 0.30, 91, 2.0001 ** 2, 3.0, 20, 20, 93),
+    ("lubnoise_ft", 1, 24, 0.30, 92, 2.0001 ** 2, 3.0, 20, 24, 94),
+]
+
+
 def lub_fixtures() -> dict:
     """The reference's lubrication correction f = L u (src/lub.c:164-575,
     equal spheres) on small systems, and its two-body functions
@@ -314,6 +322,44 @@ def lub_fixtures() -> dict:
         out[f"{name}_pos"] = pos
         out[f"{name}_u"] = u
         out[f"{name}_f"] = f
+    # the lubrication noise of BD_calc_FB: bounds of M and L from their dense
+    # matrices (ARPACK is absent), widened by (0.8, 1.05); BD->eps = 10 keeps
+    # the re-estimates off
+    lib.ref_xi_by_tratio.restype = C.c_double
+    lib.ref_xi_by_tratio.argtypes = [C.c_void_p, C.c_double]
+    lib.ref_set_split.argtypes = [C.c_void_p, C.c_double, C.c_double]
+    lib.ref_matrix.argtypes = [C.c_void_p, dp]
+    lib.refbd_calc_fb_lub.argtypes = [C.c_void_p, C.c_ulong, C.c_double, C.c_int, C.c_double,
+                                      C.c_double, C.c_int, C.c_double, C.c_double, C.c_double,
+                                      C.c_double, C.c_double, dp]
+    for name, ver, n, phi, pseed, lubmin2, lubmax, nminv, nlub, rseed in LUBNOISE_CASES:
+        pos, L = rsa_positions(n, phi, seed=pseed)
+        c = (3, 6)[ver]
+        h = lib.ref_new(ver, n, d(pos), L, L, L)
+        lib.ref_set_split(h, lib.ref_xi_by_tratio(h, 1.0), 1e-12)
+        M = np.zeros((c * n, c * n))
+        lib.ref_matrix(h, d(M))
+        ev = np.linalg.eigvalsh(0.5 * (M + M.T))
+        eig = np.array([0.8 * ev[0], 1.05 * ev[-1]])
+        Lm = np.zeros((c * n, c * n))
+        for k in range(c * n):
+            e = np.zeros(c * n)
+            e[k] = 1.0
+            col = np.zeros(c * n)
+            lib.refbd_calc_lub(h, lubmin2, lubmax, d(e), d(col))
+            Lm[:, k] = col
+        evl = np.linalg.eigvalsh(0.5 * (Lm + Lm.T))
+        eigl = np.array([0.8 * max(evl[0], 0.0), 1.05 * evl[-1]])
+        z = np.zeros(c * n)
+        lib.refbd_calc_fb_lub(h, rseed, 1.0, nminv, eig[0], eig[1], nlub, eigl[0], eigl[1], 10.0,
+                              lubmin2, lubmax, d(z))
+        lib.ref_free(h)
+        out[f"{name}_meta"] = np.array([ver, n, L, lubmin2, lubmax, nminv, nlub, rseed])
+        out[f"{name}_pos"] = pos
+        out[f"{name}_eig"] = eig
+        out[f"{name}_eigl"] = eigl
+        out[f"{name}_z"] = z
+        out[f"{name}_lev"] = np.array([evl[0], evl[-1]])
     return out
 
 
