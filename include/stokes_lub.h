@@ -29,6 +29,19 @@ void calc_lub_3fts (struct stokes *sys, const double *uoe, double *fts);
 int stokes_gpu_lub (struct stokes *sys, int version, const double *u, double *f);
 int stokes_gpu_lub_dev (struct stokes *sys, int version, const double *d_pos,
                         const double *d_u, double *d_f, void *stream);
+/* src/lub-matrix.c:76-507: the dense L, mat [n*n] row-major with
+ * n = np*{3, 6, 11}, fully overwritten; f = mat u equals calc_lub_3f / 3ft
+ * (u, f), and for FTS mat acts in libstokes' extracted form (as
+ * multiply_extmat_with_extvec_3fts, src/matrix.c:447-478, applies it).
+ * make_matrix_lub_3f / 3ft / 3fts are the drop-ins; the status-returning
+ * forms take the version, host memory or a device buffer on the caller's
+ * stream (d_pos [np*3], d_mat [n*n]). */
+void make_matrix_lub_3f (struct stokes *sys, double *mat);
+void make_matrix_lub_3ft (struct stokes *sys, double *mat);
+void make_matrix_lub_3fts (struct stokes *sys, double *mat);
+int stokes_gpu_lub_matrix (struct stokes *sys, int version, double *mat);
+int stokes_gpu_lub_matrix_dev (struct stokes *sys, int version, const double *d_pos,
+                               double *d_mat, void *stream);
 /* the power-series coefficients of the 22 lubrication-form functions
  * (x11a x12a y11a y12a y11b y12b x11c x12c y11c y12c x11g x12g y11g y12g
  * y11h y12h x11m x12m y11m y12m z11m z12m; 26 each, out[572]), generated on

@@ -275,6 +275,11 @@ _SIGS = {
     "calc_lub_3f": (None, [_SP, _dp, _dp]),
     "calc_lub_3ft": (None, [_SP, _dp, _dp]),
     "calc_lub_3fts": (None, [_SP, _dp, _dp]),
+    "make_matrix_lub_3f": (None, [_SP, _dp]),
+    "make_matrix_lub_3ft": (None, [_SP, _dp]),
+    "make_matrix_lub_3fts": (None, [_SP, _dp]),
+    "stokes_gpu_lub_matrix": (C.c_int, [_SP, C.c_int, _dp]),
+    "stokes_gpu_lub_matrix_dev": (C.c_int, [_SP, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "stokes_gpu_batch_bd": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int, _dp,
                                       _dp, C.c_ulonglong, C.c_int, _dp]),
     "stokes_gpu_vjp": (C.c_int, [_SP, _dp, _dp, _dp, _dp, _dp]),

@@ -410,28 +410,40 @@ lub_apply (const double e[3], const double *sc, bool self, double w, const doubl
 
 // one pair image (separation d, source velocity uj) into the target's sums;
 // self: the particle's own image (both halves of the pair)
+// the unit separation e and the scalars (xa, ya[, yb, xc, yc[, xg, yg, yh,
+// xm, ym, zm]]) of the self (11) and cross (12) blocks of one pair image:
+// lubrication form minus far-field part, r clamped at sqrt(lubmin2)
 template <int V>
 __device__ __forceinline__ void
-lub_pair (const LubArgs &a, const double d[3], const double *ui, const double *uj, bool self,
-          double *acc)
+lub_scalars (const LubArgs &a, const double d[3], double e[3], double *s11, double *s12)
 {
   constexpr int NF = V == 0 ? 4 : (V == 1 ? 10 : 22);
   double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
   if (r2 < a.lubmin2) r2 = a.lubmin2;
   const double r = sqrt (r2), ri = 1.0 / r;
-  const double e[3] = {d[0] * ri, d[1] * ri, d[2] * ri};
+  e[0] = d[0] * ri;
+  e[1] = d[1] * ri;
+  e[2] = d[2] * ri;
   double res[NF], inf[NF];
   lub_res (r, NF, res);
   lub_minv<V> (r, inf);
-  // (xa, ya[, yb, xc, yc[, xg, yg, yh, xm, ym, zm]]) of the self (11) and
-  // cross (12) blocks: the 11 and 12 entries of each function alternate
-  double s11[NF / 2], s12[NF / 2];
+  // the 11 and 12 entries of each function alternate
 #pragma unroll
   for (int k = 0; k < NF / 2; k++)
     {
       s11[k] = res[2 * k] - inf[2 * k];
       s12[k] = res[2 * k + 1] - inf[2 * k + 1];
     }
+}
+
+template <int V>
+__device__ __forceinline__ void
+lub_pair (const LubArgs &a, const double d[3], const double *ui, const double *uj, bool self,
+          double *acc)
+{
+  constexpr int NF = V == 0 ? 4 : (V == 1 ? 10 : 22);
+  double e[3], s11[NF / 2], s12[NF / 2];
+  lub_scalars<V> (a, d, e, s11, s12);
   lub_apply<V> (e, s11, true, 1.0, ui, acc);
   lub_apply<V> (e, s12, false, 1.0, uj, acc);
   if (self)
@@ -443,6 +455,96 @@ lub_pair (const LubArgs &a, const double d[3], const double *ui, const double *u
 }
 
 constexpr int LUB_QCAP = 64;
+
+// every pair image of (i, j) within lubmax that the reference visits, as
+// separation d = x_j(image) - x_i: fn (d).  single: the unsheared periodic
+// box with lubmax below half the box, where only the minimum image can be
+// within lubmax (taken if the reference's cube holds it).  Otherwise the
+// reference's cube: it visits the pair once, from its lower index, with the
+// image offsets o(n) of its loop (which need not be symmetric under a shift
+// that accumulates): d = x_j + o - x_i for j > i, the negated separation
+// x_j - o - x_i for j < i, and both signs for j == i (the caller's fn
+// handles the j == i pair as both halves)
+template <class Fn>
+__device__ __forceinline__ void
+lub_images (const LubArgs &a, int i, int j, const double xi[3], bool single, Fn &&fn)
+{
+  const double r0[3] = {a.pos[3 * j] - xi[0], a.pos[3 * j + 1] - xi[1], a.pos[3 * j + 2] - xi[2]};
+  if (single)
+    {
+      const double n0 = -rint (r0[0] / a.lx), n1 = -rint (r0[1] / a.ly), n2 = -rint (r0[2] / a.lz);
+      if (fabs (n0) > a.imx || fabs (n1) > a.imy || fabs (n2) > a.imz) return;
+      const double d[3] = {r0[0] + n0 * a.lx, r0[1] + n1 * a.ly, r0[2] + n2 * a.lz};
+      const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+      if (r2 == 0.0 || !(r2 < a.lubmax2)) return;
+      fn (d);
+      return;
+    }
+  const double sg = (j >= i) ? 1.0 : -1.0;
+  for (int ix = -a.imx; ix <= a.imx; ix++)
+    {
+      double ox = a.lx * ix;
+      for (int iy = -a.imy; iy <= a.imy; iy++)
+        {
+          const double oy = a.ly * iy;
+          for (int iz = -a.imz; iz <= a.imz; iz++)
+            {
+              const double oz = a.lz * iz;
+              if (a.shear_mode == 1) ox += iy * a.shift;
+              else if (a.shear_mode == 2) ox += iz * a.shift;
+              const double d[3] = {r0[0] + sg * ox, r0[1] + sg * oy, r0[2] + sg * oz};
+              const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+              if (r2 == 0.0 || (a.lubmax2 > 0.0 && !(r2 < a.lubmax2))) continue;
+              fn (d);
+            }
+        }
+    }
+}
+
+// the candidate scan of a warp over the sources: the lanes test the
+// sources in FP32 (minimum-image distance within lubmax, with a margin for
+// the rounding; every source when there is no such test) and queue them in
+// q; each full batch of 32 and the remainder go to batch (q, count)
+template <class Batch>
+__device__ __forceinline__ void
+lub_scan (const LubArgs &a, const double xi[3], bool test, int *q, Batch &&batch)
+{
+  const int lane = threadIdx.x & 31;
+  const float cut2 = (float) a.lubmax2 * 1.0001f + 1e-6f;
+  const float lxf = (float) a.lx, lyf = (float) a.ly, lzf = (float) a.lz;
+  const float ilxf = 1.0f / lxf, ilyf = 1.0f / lyf, ilzf = 1.0f / lzf;
+  const unsigned lt = (1u << lane) - 1u;
+  int qn = 0;
+  for (int jb = 0; jb < a.np; jb += 32)
+    {
+      const int j = jb + lane;
+      bool cand = j < a.np;
+      if (cand && test)
+        {
+          float dx = (float) (a.pos[3 * j] - xi[0]), dy = (float) (a.pos[3 * j + 1] - xi[1]),
+                dz = (float) (a.pos[3 * j + 2] - xi[2]);
+          if (a.periodic)
+            {
+              dx -= lxf * rintf (dx * ilxf);
+              dy -= lyf * rintf (dy * ilyf);
+              dz -= lzf * rintf (dz * ilzf);
+            }
+          cand = dx * dx + dy * dy + dz * dz < cut2;
+        }
+      const unsigned b = __ballot_sync (0xffffffffu, cand);
+      if (cand) q[qn + __popc (b & lt)] = j;
+      qn += __popc (b);
+      __syncwarp ();
+      if (qn >= 32)
+        {
+          batch (q + qn - 32, 32);
+          qn -= 32;
+          __syncwarp ();
+        }
+    }
+  if (qn > 0) batch (q, qn);
+  __syncwarp ();
+}
 
 // A warp per target i.  The lanes scan the sources in FP32 (the FP64 pipe of
 // this GPU is 1/64 of FP32) and queue the candidates; 32 queued candidates
@@ -475,88 +577,95 @@ k_lub (LubArgs a)
   const double lmin = fmin (a.lx, fmin (a.ly, a.lz));
   const bool single = unsheared && a.lubmax2 > 0.0 && 4.0 * a.lubmax2 <= lmin * lmin;
   const bool test = a.lubmax2 > 0.0 && (unsheared || !a.periodic);
-  const float cut2 = (float) a.lubmax2 * 1.0001f + 1e-6f;
-  const float lxf = (float) a.lx, lyf = (float) a.ly, lzf = (float) a.lz;
-  const float ilxf = 1.0f / lxf, ilyf = 1.0f / lyf, ilzf = 1.0f / lzf;
-  const unsigned lt = (1u << lane) - 1u;
-
-  auto evaluate = [&] (int j) {
+  // one queued candidate per lane, in FP64
+  lub_scan (a, xi, test, q, [&] (const int *qb, int count) {
+    if (lane >= count) return;
+    const int j = qb[lane];
     double uj[C];
 #pragma unroll
     for (int k = 0; k < C; k++) uj[k] = a.u[C * j + k];
-    const double r0[3] = {a.pos[3 * j] - xi[0], a.pos[3 * j + 1] - xi[1], a.pos[3 * j + 2] - xi[2]};
-    if (single)
-      {
-        // the one image within lubmax, if the reference's cube holds it
-        const double n0 = -rint (r0[0] / a.lx), n1 = -rint (r0[1] / a.ly),
-                     n2 = -rint (r0[2] / a.lz);
-        if (fabs (n0) > a.imx || fabs (n1) > a.imy || fabs (n2) > a.imz) return;
-        const double d[3] = {r0[0] + n0 * a.lx, r0[1] + n1 * a.ly, r0[2] + n2 * a.lz};
-        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        if (r2 == 0.0 || !(r2 < a.lubmax2)) return;
-        lub_pair<V> (a, d, ui, uj, j == i, acc);
-        return;
-      }
-    // the reference visits the pair once, from its lower index, with the
-    // image offsets o(n) of its loop (which need not be symmetric under a
-    // shift that accumulates): d = x_j + o - x_i for j > i, the negated
-    // separation x_j - o - x_i for j < i, and both signs for j == i
-    const double sg = (j >= i) ? 1.0 : -1.0;
-    for (int ix = -a.imx; ix <= a.imx; ix++)
-      {
-        double ox = a.lx * ix;
-        for (int iy = -a.imy; iy <= a.imy; iy++)
-          {
-            const double oy = a.ly * iy;
-            for (int iz = -a.imz; iz <= a.imz; iz++)
-              {
-                const double oz = a.lz * iz;
-                if (a.shear_mode == 1) ox += iy * a.shift;
-                else if (a.shear_mode == 2) ox += iz * a.shift;
-                const double d[3] = {r0[0] + sg * ox, r0[1] + sg * oy, r0[2] + sg * oz};
-                const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-                if (r2 == 0.0 || (a.lubmax2 > 0.0 && !(r2 < a.lubmax2))) continue;
-                lub_pair<V> (a, d, ui, uj, j == i, acc);
-              }
-          }
-      }
-  };
-
-  int qn = 0;
-  for (int jb = 0; jb < a.np; jb += 32)
-    {
-      const int j = jb + lane;
-      bool cand = j < a.np;
-      if (cand && test)
-        {
-          // FP32 minimum-image distance (the box wrap only when periodic)
-          float dx = (float) (a.pos[3 * j] - xi[0]), dy = (float) (a.pos[3 * j + 1] - xi[1]),
-                dz = (float) (a.pos[3 * j + 2] - xi[2]);
-          if (a.periodic)
-            {
-              dx -= lxf * rintf (dx * ilxf);
-              dy -= lyf * rintf (dy * ilyf);
-              dz -= lzf * rintf (dz * ilzf);
-            }
-          cand = dx * dx + dy * dy + dz * dz < cut2;
-        }
-      const unsigned b = __ballot_sync (0xffffffffu, cand);
-      if (cand) q[qn + __popc (b & lt)] = j;
-      qn += __popc (b);
-      __syncwarp ();
-      if (qn >= 32)
-        {
-          evaluate (q[qn - 32 + lane]);
-          qn -= 32;
-          __syncwarp ();
-        }
-    }
-  if (lane < qn) evaluate (q[lane]);
+    lub_images (a, i, j, xi, single,
+                [&] (const double d[3]) { lub_pair<V> (a, d, ui, uj, j == i, acc); });
+  });
 #pragma unroll
   for (int k = 0; k < C; k++)
     {
       const double v = warp_sum (acc[k]);
       if (lane == 0) a.f[C * i + k] = v;
+    }
+}
+
+// Dense L (src/lub-matrix.c:76-507), row block i per warp.  Candidates as
+// in k_lub, taken one at a time: lane b < C applies the pair's blocks to the
+// input t_b, so that it holds column b of the self and the cross block of
+// (i, j).  t_b is the unit vector e_b for F and FT; for FTS it is column b
+// of T^-1, T being the map through which libstokes' FTS matrices act on the
+// strain (2 E0 + E4, 2 E1, 2 E2, 2 E3, E0 + 2 E4; src/matrix.c:447-478), so
+// that M T = L.  The cross block is added into (i, j) at once and the self
+// block into (i, i) at the end: a warp writes only its own rows and one
+// candidate at a time, so no two threads write one entry.  The matrix is
+// cleared before the launch.
+template <int V>
+__global__ void __launch_bounds__ (256)
+k_lub_matrix (LubArgs a, double *mat)
+{
+  constexpr int C = V == 0 ? 3 : (V == 1 ? 6 : 11);
+  constexpr int NF = V == 0 ? 4 : (V == 1 ? 10 : 22);
+  __shared__ int s_q[8][LUB_QCAP];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int i = blockIdx.x * 8 + wib;
+  if (i >= a.np) return;   // uniform over the warp
+  int *q = s_q[wib];
+  const double xi[3] = {a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]};
+  const size_t n = (size_t) C * a.np;
+  double tb[C], sacc[C];
+#pragma unroll
+  for (int k = 0; k < C; k++)
+    {
+      tb[k] = (k == lane) ? 1.0 : 0.0;
+      sacc[k] = 0.0;
+    }
+  if constexpr (V == 2)
+    {
+      if (lane == 6) { tb[6] = 2.0 / 3.0; tb[C - 1] = -1.0 / 3.0; }
+      else if (lane == 10) { tb[6] = -1.0 / 3.0; tb[C - 1] = 2.0 / 3.0; }
+      else if (lane >= 7 && lane <= 9) tb[lane] = 0.5;
+    }
+  const bool unsheared = a.periodic && a.shear_mode == 0;
+  const double lmin = fmin (a.lx, fmin (a.ly, a.lz));
+  const bool single = unsheared && a.lubmax2 > 0.0 && 4.0 * a.lubmax2 <= lmin * lmin;
+  const bool test = a.lubmax2 > 0.0 && (unsheared || !a.periodic);
+  double *rows = mat + (size_t) C * i * n;
+  lub_scan (a, xi, test, q, [&] (const int *qb, int count) {
+    if (lane >= C) return;
+    for (int t = 0; t < count; t++)
+      {
+        const int j = qb[t];
+        double xacc[C];
+#pragma unroll
+        for (int k = 0; k < C; k++) xacc[k] = 0.0;
+        lub_images (a, i, j, xi, single, [&] (const double d[3]) {
+          double e[3], s11[NF / 2], s12[NF / 2];
+          lub_scalars<V> (a, d, e, s11, s12);
+          lub_apply<V> (e, s11, true, 1.0, tb, sacc);
+          lub_apply<V> (e, s12, false, 1.0, tb, xacc);
+          if (j == i)
+            {
+              const double me[3] = {-e[0], -e[1], -e[2]};
+              lub_apply<V> (me, s11, true, 1.0, tb, sacc);
+              lub_apply<V> (me, s12, false, 1.0, tb, xacc);
+            }
+        });
+        double *col = rows + (size_t) C * j + lane;
+#pragma unroll
+        for (int k = 0; k < C; k++) col[k * n] += xacc[k];
+      }
+  });
+  if (lane < C)
+    {
+      double *col = rows + (size_t) C * i + lane;
+#pragma unroll
+      for (int k = 0; k < C; k++) col[k * n] += sacc[k];
     }
 }
 
@@ -594,18 +703,16 @@ lub_check (const struct stokes *sys, int version)
   return STOKES_GPU_OK;
 }
 
-// f = L u on device buffers, version 0 (F, 3 per particle) or 1 (FT, 6)
-int
-lub_dev (const struct stokes *sys, int version, const double *d_pos, const double *d_u,
-         double *d_f, cudaStream_t st)
+// the kernels' arguments for sys (image cube of src/lub.c:129-157)
+static int
+lub_args (const struct stokes *sys, int version, const double *d_pos, LubArgs &a)
 {
   int rc = lub_check (sys, version);
   if (!rc) rc = lub_upload ();
   if (rc) return rc;
-  LubArgs a;
   a.pos = d_pos;
-  a.u = d_u;
-  a.f = d_f;
+  a.u = nullptr;
+  a.f = nullptr;
   a.np = sys->np;
   a.periodic = sys->periodic ? 1 : 0;
   a.lx = sys->lx;
@@ -614,7 +721,6 @@ lub_dev (const struct stokes *sys, int version, const double *d_pos, const doubl
   a.imx = a.imy = a.imz = 0;
   if (a.periodic)
     {
-      // the image cube of src/lub.c:129-157
       const double lm = sys->lubmax > 0.0 ? sys->lubmax : std::fmax (a.lx, std::fmax (a.ly, a.lz));
       // a cube of more than 33^3 images per pair is refused (the loop is
       // per pair and would run for minutes)
@@ -628,12 +734,71 @@ lub_dev (const struct stokes *sys, int version, const double *d_pos, const doubl
   a.shift = sys->shear_shift;
   a.lubmin2 = sys->lubmin2;
   a.lubmax2 = sys->lubmax * sys->lubmax;
+  return STOKES_GPU_OK;
+}
+
+// f = L u on device buffers, version 0 (F, 3 per particle), 1 (FT, 6) or 2
+int
+lub_dev (const struct stokes *sys, int version, const double *d_pos, const double *d_u,
+         double *d_f, cudaStream_t st)
+{
+  LubArgs a;
+  int rc = lub_args (sys, version, d_pos, a);
+  if (rc) return rc;
+  a.u = d_u;
+  a.f = d_f;
   const int grid = (sys->np + 7) / 8;
   if (version == 0) k_lub<0><<<grid, 256, 0, st>>> (a);
   else if (version == 1) k_lub<1><<<grid, 256, 0, st>>> (a);
   else k_lub<2><<<grid, 256, 0, st>>> (a);
   cudaError_t e = cudaGetLastError ();
   return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "lubrication kernel");
+}
+
+// the dense L on a device buffer d_mat [n n], n = np {3, 6, 11}, row-major
+// (FTS in libstokes' extracted form)
+static int
+lub_matrix_dev (const struct stokes *sys, int version, const double *d_pos, double *d_mat,
+                cudaStream_t st)
+{
+  LubArgs a;
+  int rc = lub_args (sys, version, d_pos, a);
+  if (rc) return rc;
+  const size_t n = (size_t) (version == 0 ? 3 : (version == 1 ? 6 : 11)) * sys->np;
+  cudaError_t e = cudaMemsetAsync (d_mat, 0, sizeof (double) * n * n, st);
+  if (e != cudaSuccess) return cuda_fail (e, "lubrication matrix");
+  const int grid = (sys->np + 7) / 8;
+  if (version == 0) k_lub_matrix<0><<<grid, 256, 0, st>>> (a, d_mat);
+  else if (version == 1) k_lub_matrix<1><<<grid, 256, 0, st>>> (a, d_mat);
+  else k_lub_matrix<2><<<grid, 256, 0, st>>> (a, d_mat);
+  e = cudaGetLastError ();
+  return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "lubrication matrix kernel");
+}
+
+// the dense L into host memory
+static int
+lub_matrix_host (struct stokes *sys, int version, double *mat)
+{
+  clear_error ();
+  if (!mat) return set_error (STOKES_GPU_EINVAL, "NULL matrix");
+  int rc = lub_check (sys, version);
+  if (rc) return rc;
+  if ((rc = check_positions (sys->pos, sys->np))) return rc;
+  Ctx *c = get_ctx (sys, true);
+  if (!c) return set_error (STOKES_GPU_ECUDA, "cannot create a CUDA stream");
+  const int np = sys->np;
+  const size_t n = (size_t) (version == 0 ? 3 : (version == 1 ? 6 : 11)) * np;
+  cudaError_t e;
+  if ((e = c->pos.ensure (sizeof (double) * 3 * np)) != cudaSuccess
+      || (e = c->mat.ensure (sizeof (double) * n * n)) != cudaSuccess)
+    return cuda_fail (e, "lubrication matrix buffers");
+  cudaMemcpyAsync (c->pos.p, sys->pos, sizeof (double) * 3 * np, cudaMemcpyHostToDevice,
+                   c->stream);
+  rc = lub_matrix_dev (sys, version, (const double *) c->pos.p, (double *) c->mat.p, c->stream);
+  if (rc) return rc;
+  e = cudaMemcpyAsync (mat, c->mat.p, sizeof (double) * n * n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize (c->stream);
+  return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "lubrication matrix");
 }
 
 // f = L u with host vectors
@@ -707,6 +872,44 @@ int
 stokes_gpu_lub (struct stokes *sys, int version, const double *u, double *f)
 {
   return lub_host (sys, version, u, f);
+}
+
+// src/lub-matrix.c:76 (make_matrix_lub_3f), :225 (3ft), :373 (3fts)
+void
+make_matrix_lub_3f (struct stokes *sys, double *mat)
+{
+  if (lub_matrix_host (sys, 0, mat))
+    dropin_failed ("make_matrix_lub_3f", mat, mat && sys ? 9 * (size_t) sys->np * sys->np : 0);
+}
+
+void
+make_matrix_lub_3ft (struct stokes *sys, double *mat)
+{
+  if (lub_matrix_host (sys, 1, mat))
+    dropin_failed ("make_matrix_lub_3ft", mat, mat && sys ? 36 * (size_t) sys->np * sys->np : 0);
+}
+
+void
+make_matrix_lub_3fts (struct stokes *sys, double *mat)
+{
+  if (lub_matrix_host (sys, 2, mat))
+    dropin_failed ("make_matrix_lub_3fts", mat,
+                   mat && sys ? 121 * (size_t) sys->np * sys->np : 0);
+}
+
+int
+stokes_gpu_lub_matrix (struct stokes *sys, int version, double *mat)
+{
+  return lub_matrix_host (sys, version, mat);
+}
+
+int
+stokes_gpu_lub_matrix_dev (struct stokes *sys, int version, const double *d_pos, double *d_mat,
+                           void *stream)
+{
+  clear_error ();
+  if (!d_pos || !d_mat) return set_error (STOKES_GPU_EINVAL, "NULL buffer");
+  return lub_matrix_dev (sys, version, d_pos, d_mat, (cudaStream_t) stream);
 }
 
 int

@@ -156,6 +156,20 @@ refbd_calc_lub (void *h, double lubmin2, double lubmax, const double *u, double 
   else calc_lub_3fts (sys, u, f);
 }
 
+/* the reference's dense lubrication matrix (src/lub-matrix.c:76-507) at
+ * the given lubmin2 / lubmax, n = np * {3, 6, 11} rows, row-major */
+#include "lub-matrix.h"
+void
+refbd_matrix_lub (void *h, double lubmin2, double lubmax, double *mat)
+{
+  struct stokes *sys = h;
+  sys->lubmin2 = lubmin2;
+  sys->lubmax = lubmax;
+  if (sys->version == 0) make_matrix_lub_3f (sys, mat);
+  else if (sys->version == 1) make_matrix_lub_3ft (sys, mat);
+  else make_matrix_lub_3fts (sys, mat);
+}
+
 /* the reference's two-body lubrication-form functions and (M^inf)^-1 */
 #include "two-body-res.h"
 void ref_res2b (double s, double *res) { scalar_two_body_res (s, res); }

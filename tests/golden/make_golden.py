@@ -272,10 +272,24 @@ LUBNOISE_CASES = [
 ]
 
 
+# the reference's dense lubrication matrices (src/lub-matrix.c):
+# (name, version, N, phi, placement seed, periodic, lubmin2, lubmax, shear)
+LUBMAT_CASES = [
+    ("lubmat_f_periodic", 0, 14, 0.30, 101, True, 2.0001 ** 2, 3.0, (0, 0.0)),
+    ("lubmat_ft_shear1", 1, 12, 0.30, 102, True, 2.0001 ** 2, 3.0, (1, 1.3)),
+    ("lubmat_ft_nolimit", 1, 8, 0.20, 106, True, 2.0001 ** 2, 0.0, (0, 0.0)),
+    ("lubmat_fts_periodic", 2, 10, 0.30, 103, True, 2.0001 ** 2, 3.0, (0, 0.0)),
+    ("lubmat_fts_open", 2, 10, 0.25, 104, False, 2.001 ** 2, 3.5, (0, 0.0)),
+    ("lubmat_fts_shear2", 2, 8, 0.30, 105, True, 2.0001 ** 2, 3.0, (2, -0.7)),
+]
+
+
 def lub_fixtures() -> dict:
     """The reference's lubrication correction f = L u (src/lub.c:164-575,
-    equal spheres) on small systems, and its two-body functions
-    (src/two-body-res.c:31, src/f.c:183, src/ft.c:414) on a grid of s."""
+    equal spheres) on small systems, its two-body functions
+    (src/two-body-res.c:31, src/f.c:183, src/ft.c:414) on a grid of s, the
+    lubrication noise of BD_calc_FB and the dense lubrication matrices
+    (src/lub-matrix.c)."""
     import ctypes as C
     so = os.path.join(ROOT, "oracle", "_ref", "libstokes_ref_bd.so")
     lib = C.CDLL(so)
@@ -360,6 +374,22 @@ def lub_fixtures() -> dict:
         out[f"{name}_eigl"] = eigl
         out[f"{name}_z"] = z
         out[f"{name}_lev"] = np.array([evl[0], evl[-1]])
+    lib.refbd_matrix_lub.argtypes = [C.c_void_p, C.c_double, C.c_double, dp]
+    for name, ver, n, phi, pseed, periodic, lubmin2, lubmax, shear in LUBMAT_CASES:
+        pos, L = rsa_positions(n, phi, seed=pseed)
+        c = (3, 6, 11)[ver]
+        h = lib.ref_new(ver, n, d(pos), L, L, L)
+        if not periodic:
+            lib.ref_set_periodic(h, 0)
+        if shear[0]:
+            lib.ref_set_misc(h, 0.0, shear[0], shear[1])
+        mat = np.zeros((c * n, c * n))
+        lib.refbd_matrix_lub(h, lubmin2, lubmax, d(mat))
+        lib.ref_free(h)
+        out[f"{name}_meta"] = np.array([ver, n, L, 1.0 if periodic else 0.0, lubmin2, lubmax,
+                                        shear[0], shear[1]])
+        out[f"{name}_pos"] = pos
+        out[f"{name}_mat"] = mat
     return out
 
 

@@ -1,4 +1,5 @@
-"""The lubrication correction on the GPU (calc_lub_3f / 3ft / 3fts,
+"""The lubrication correction on the GPU (calc_lub_3f / 3ft / 3fts and the
+dense matrices make_matrix_lub_3f / 3ft / 3fts,
 src/lub.c:164-768, equal spheres) against the reference's own outputs
 (tests/golden/lub.npz: periodic, open, sheared, small-box and
 unlimited-range systems) and against the oracle on larger systems; the
@@ -126,4 +127,65 @@ def test_lubricated_mobility_solve(lib, ver):
                               C.byref(res))
     assert rc == abi.STOKES_GPU_OK, lib.stokes_gpu_last_error_message()
     assert rel_l2(x, u_dense) < 1e-9, rel_l2(x, u_dense)
+    s.close()
+
+
+MAT_CASES = ["lubmat_f_periodic", "lubmat_ft_shear1", "lubmat_ft_nolimit", "lubmat_fts_periodic",
+             "lubmat_fts_open", "lubmat_fts_shear2"]
+
+
+@pytest.mark.parametrize("name", MAT_CASES)
+def test_lub_matrix_against_reference(lib, lub, name):
+    """The dense L (make_matrix_lub_3f / 3ft / 3fts, src/lub-matrix.c:76-507)
+    against the reference's own matrices: periodic, sheared (both modes),
+    open, unlimited range; FTS in the extracted form."""
+    from libstokes_gb300 import abi
+    ver, n, L, periodic, lubmin2, lubmax, mode, shift = lub[f"{name}_meta"]
+    ver, n = int(ver), int(n)
+    s = _system(ver, lub[f"{name}_pos"], L, periodic, lubmin2, lubmax, int(mode), shift)
+    want = lub[f"{name}_mat"]
+    mat = np.zeros_like(want)
+    assert lib.stokes_gpu_lub_matrix(s.sp, ver, mat.ctypes.data_as(abi._dp)) == abi.STOKES_GPU_OK
+    assert np.abs(mat - want).max() < 1e-12 * np.abs(want).max(), np.abs(mat - want).max()
+    m2 = np.full_like(want, 7.0)         # fully overwritten
+    (lib.make_matrix_lub_3f, lib.make_matrix_lub_3ft, lib.make_matrix_lub_3fts)[ver](
+        s.sp, m2.ctypes.data_as(abi._dp))
+    assert np.array_equal(mat, m2)
+    s.close()
+
+
+def _extract_map(n):
+    """T of libstokes' FTS matrices: mat (T x) = L x per particle
+    (src/matrix.c:447-478)."""
+    t = np.eye(11)
+    t[6:, 6:] = [[2, 0, 0, 0, 1], [0, 2, 0, 0, 0], [0, 0, 2, 0, 0], [0, 0, 0, 2, 0], [1, 0, 0, 0, 2]]
+    return np.kron(np.eye(n), t)
+
+
+@pytest.mark.parametrize("ver", [0, 1, 2])
+def test_lub_matrix_matches_operator(lib, ver):
+    """At N = 300: mat u (mat T u for FTS) equals L u from the device
+    operator, and the device-buffer entry gives the same matrix."""
+    import ctypes as C
+    import torch
+    from libstokes_gb300 import abi
+    from libstokes_gb300.workloads import rsa_positions
+    n = 300
+    c = (3, 6, 11)[ver]
+    pos, L = rsa_positions(n, 0.35, seed=111 + ver)
+    s = _system(ver, pos, L, True, 2.0001 ** 2, 3.0)
+    mat = np.zeros((c * n, c * n))
+    assert lib.stokes_gpu_lub_matrix(s.sp, ver, mat.ctypes.data_as(abi._dp)) == abi.STOKES_GPU_OK
+    u = np.random.default_rng(112).standard_normal(c * n)
+    f = _calc(lib, s, ver, u)
+    fm = mat @ (_extract_map(n) @ u if ver == 2 else u)
+    assert np.count_nonzero(f) > 0
+    assert rel_l2(fm, f) < 1e-12, rel_l2(fm, f)
+    d_pos = torch.tensor(pos, dtype=torch.float64, device="cuda").contiguous()
+    d_mat = torch.empty((c * n, c * n), dtype=torch.float64, device="cuda")
+    rc = lib.stokes_gpu_lub_matrix_dev(s.sp, ver, C.c_void_p(d_pos.data_ptr()),
+                                       C.c_void_p(d_mat.data_ptr()), None)
+    assert rc == abi.STOKES_GPU_OK
+    torch.cuda.synchronize()
+    assert np.array_equal(d_mat.cpu().numpy(), mat)
     s.close()
