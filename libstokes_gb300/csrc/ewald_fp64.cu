@@ -795,7 +795,7 @@ k_matrix_open (MatArgs a)
 // FP64 pipe of this GPU is 1/64 of FP32).  Separations r_j - r_i + image
 // are formed from hi + lo float pairs of both (the difference of the hi
 // parts is exact where it cancels, so a separation carries one FP32
-// rounding); the cutoff test runs on them (a candidate it misjudges lies at
+// rounding); the cutoff test runs on them (a candidate it misclassifies lies at
 // the cutoff, where its term is below the split's accuracy).  Reciprocal
 // phases and coefficients come from float copies of the FP64 tables.
 // Moments accumulate in FP32 per lane (about ten terms each at the
