@@ -3,8 +3,9 @@ outputs (tests/golden/lub.npz, made by tests/golden/make_golden.py from the
 compiled reference): the 22 lubrication-form two-body functions of
 src/two-body-res.c:31 (regenerated here from the Jeffrey-Onishi and Jeffrey
 recurrences), the far-field inverses of src/f.c:183, src/ft.c:414 and
-src/fts.c:1491, and f = L u of src/lub.c:164-768 (F, FT, FTS) on periodic,
-open, sheared, small-box and unlimited-range systems."""
+src/fts.c:1491, f = L u of src/lub.c:164-768 (F, FT, FTS) on periodic,
+open, sheared, small-box and unlimited-range systems, and the reference's
+dense lubrication matrices (src/lub-matrix.c) as that operator."""
 import os
 
 import numpy as np
@@ -49,6 +50,39 @@ def test_calc_lub(lub, name):
     ref = lub[f"{name}_f"]
     assert np.linalg.norm(ref) > 0.0
     assert rel_l2(f, ref) < 1e-12, rel_l2(f, ref)
+
+
+MAT_CASES = ["lubmat_f_periodic", "lubmat_ft_shear1", "lubmat_ft_nolimit", "lubmat_fts_periodic",
+             "lubmat_fts_open", "lubmat_fts_shear2"]
+
+
+@pytest.mark.parametrize("name", MAT_CASES)
+def test_dense_matrix_is_the_operator(lub, name):
+    """The reference's dense lubrication matrices (src/lub-matrix.c:76-507)
+    are the columns of the oracle's L for F and FT, and for FTS the oracle's
+    L in libstokes' extracted form, mat (T u) = L u with T per particle
+    (2 E0 + E4, 2 E1, 2 E2, 2 E3, E0 + 2 E4), src/matrix.c:447-478."""
+    from oracle.oracle import calc_lub
+    ver, n, L, periodic, lubmin2, lubmax, mode, shift = lub[f"{name}_meta"]
+    ver, n = int(ver), int(n)
+    c = (3, 6, 11)[ver]
+    want = lub[f"{name}_mat"]
+    cols = np.zeros_like(want)
+    for k in range(c * n):
+        e = np.zeros(c * n)
+        e[k] = 1.0
+        cols[:, k] = calc_lub(ver, lub[f"{name}_pos"], (L, L, L) if periodic else None, e,
+                              lubmin2=lubmin2, lubmax=lubmax, shear_mode=int(mode),
+                              shear_shift=shift)
+    if ver == 2:
+        t = np.eye(11)
+        t[6:, 6:] = [[2, 0, 0, 0, 1], [0, 2, 0, 0, 0], [0, 0, 2, 0, 0], [0, 0, 0, 2, 0],
+                     [1, 0, 0, 0, 2]]
+        got = want @ np.kron(np.eye(n), t)
+    else:
+        got = want
+    assert np.abs(want).max() > 0.0
+    assert np.abs(got - cols).max() < 1e-12 * np.abs(cols).max(), np.abs(got - cols).max()
 
 
 def test_product_coefficients_match_the_oracle():
