@@ -555,14 +555,16 @@ lub_scan (const LubArgs &a, const double xi[3], bool test, int *q, Batch &&batch
 // reference's image cube holds it.  Otherwise every source is a candidate
 // (or those whose minimum image is within lubmax, unsheared) and its whole
 // image cube is walked in FP64.
+constexpr int LUB_WPB = 4;   // warps per CTA of k_lub: N = 1000 fills all 152 SMs
+
 template <int V>
-__global__ void __launch_bounds__ (256)
+__global__ void __launch_bounds__ (LUB_WPB * 32, 2)
 k_lub (LubArgs a)
 {
   constexpr int C = V == 0 ? 3 : (V == 1 ? 6 : 11);
-  __shared__ int s_q[8][LUB_QCAP];
+  __shared__ int s_q[LUB_WPB][LUB_QCAP];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int i = blockIdx.x * 8 + wib;
+  const int i = blockIdx.x * LUB_WPB + wib;
   if (i >= a.np) return;   // uniform over the warp
   int *q = s_q[wib];
   const double xi[3] = {a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]};
@@ -747,10 +749,10 @@ lub_dev (const struct stokes *sys, int version, const double *d_pos, const doubl
   if (rc) return rc;
   a.u = d_u;
   a.f = d_f;
-  const int grid = (sys->np + 7) / 8;
-  if (version == 0) k_lub<0><<<grid, 256, 0, st>>> (a);
-  else if (version == 1) k_lub<1><<<grid, 256, 0, st>>> (a);
-  else k_lub<2><<<grid, 256, 0, st>>> (a);
+  const int grid = (sys->np + LUB_WPB - 1) / LUB_WPB;
+  if (version == 0) k_lub<0><<<grid, LUB_WPB * 32, 0, st>>> (a);
+  else if (version == 1) k_lub<1><<<grid, LUB_WPB * 32, 0, st>>> (a);
+  else k_lub<2><<<grid, LUB_WPB * 32, 0, st>>> (a);
   cudaError_t e = cudaGetLastError ();
   return e == cudaSuccess ? STOKES_GPU_OK : cuda_fail (e, "lubrication kernel");
 }
