@@ -4,8 +4,9 @@ compiled reference): the 22 lubrication-form two-body functions of
 src/two-body-res.c:31 (regenerated here from the Jeffrey-Onishi and Jeffrey
 recurrences), the far-field inverses of src/f.c:183, src/ft.c:414 and
 src/fts.c:1491, f = L u of src/lub.c:164-768 (F, FT, FTS) on periodic,
-open, sheared, small-box and unlimited-range systems, and the reference's
-dense lubrication matrices (src/lub-matrix.c) as that operator."""
+open, sheared, small-box and unlimited-range systems, the reference's
+dense lubrication matrices (src/lub-matrix.c) as that operator, and its
+lubrication noise (BD_calc_FB with flag_lub_B) recomposed from the oracle."""
 import os
 
 import numpy as np
@@ -107,3 +108,63 @@ def test_product_coefficients_match_the_oracle():
     for g in range(22):
         for m in range(26):
             assert abs(mine[g, m] - ref[g, m]) * 0.25 ** m <= 1e-15, (g, m)
+
+
+def _clenshaw(a, e0, e1, A, y):
+    """z = sum_k a_k T_k(A~) y by the reference's recurrence
+    (src/chebyshev.c:163-228), A dense."""
+    n = len(a)
+    da, db = 2.0 / (e1 - e0), -(e1 + e0) / (e1 - e0)
+    b = [np.zeros_like(y), np.zeros_like(y), np.zeros_like(y)]
+    for i in range(n - 1):
+        j = n - 1 - i
+        b[(i + 2) % 3] = 2.0 * da * (A @ b[(i + 1) % 3]) + 2.0 * db * b[(i + 1) % 3] \
+            - b[i % 3] + a[j] * y
+    i = n - 1
+    return da * (A @ b[(i + 1) % 3]) + db * b[(i + 1) % 3] - b[i % 3] + a[0] * y
+
+
+@pytest.mark.parametrize("name", ["lubnoise_f", "lubnoise_ft"])
+def test_lubrication_noise_fixture_recomposed(lib, lub, name):
+    """The reference's BD_calc_FB with flag_lub_B (src/brownian.c:1597-1871)
+    recomposed from the oracle: y then y_lub from the KIrand stream of the
+    seed, z = M^-1/2 y + L^1/2 y_lub by Chebyshev of the oracle's dense M
+    and L with the coefficients of the preset bounds, FT reordered to
+    [F part, T part]."""
+    import ctypes as C
+    from libstokes_gb300.abi import FUNC1
+    from oracle.oracle import Oracle, calc_lub
+    r = {k[len(name) + 1:]: lub[k] for k in lub.files if k.startswith(name + "_")}
+    ver, n, L, lubmin2, lubmax, nminv, nlub, seed = r["meta"]
+    ver, n, nminv, nlub, seed = int(ver), int(n), int(nminv), int(nlub), int(seed)
+    c = (3, 6)[ver]
+    pos = r["pos"]
+    o = Oracle(ver, pos, (L, L, L))
+    o.set_split(o.xi_by_tratio(1.0), 1e-12)
+    M = o.matrix()
+    Lm = np.zeros((c * n, c * n))
+    for k in range(c * n):
+        e = np.zeros(c * n)
+        e[k] = 1.0
+        Lm[:, k] = calc_lub(ver, pos, (L, L, L), e, lubmin2=lubmin2, lubmax=lubmax)
+    rng = lib.KIrand_init()
+    lib.KIrand_init_genrand(rng, seed)
+    y = np.array([lib.KIrand_Gaussian(rng) for _ in range(c * n)])
+    ylub = np.array([lib.KIrand_Gaussian(rng) for _ in range(c * n)])
+    lib.KIrand_free(rng)
+    fs = [FUNC1(lambda v: 1.0 / np.sqrt(v)), FUNC1(lambda v: np.sqrt(v))]
+    am = np.zeros(nminv)
+    al = np.zeros(nlub)
+    dp = C.POINTER(C.c_double)
+    lib.chebyshev_coef(nminv, fs[0], float(r["eig"][0]), float(r["eig"][1]), am.ctypes.data_as(dp))
+    lib.chebyshev_coef(nlub, fs[1], float(r["eigl"][0]), float(r["eigl"][1]),
+                       al.ctypes.data_as(dp))
+    zp = _clenshaw(am, r["eig"][0], r["eig"][1], M, y) \
+        + _clenshaw(al, r["eigl"][0], r["eigl"][1], Lm, ylub)
+    if ver == 1:
+        zp = np.concatenate([zp.reshape(n, 6)[:, :3].ravel(), zp.reshape(n, 6)[:, 3:].ravel()])
+    # the lubrication part is a large share: the check is not the mobility
+    # noise alone
+    assert np.linalg.norm(_clenshaw(al, r["eigl"][0], r["eigl"][1], Lm, ylub)) \
+        > 0.1 * np.linalg.norm(zp)
+    assert rel_l2(zp, r["z"]) < 1e-10, rel_l2(zp, r["z"])
